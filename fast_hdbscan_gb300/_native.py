@@ -1,0 +1,134 @@
+"""ctypes binding of libfhg.so (the C ABI declared in include/fhg.h).
+
+The library is built in-tree by ``fast_hdbscan_gb300.build`` and loaded from
+``fast_hdbscan_gb300/_lib/libfhg.so``.  There is no fallback: if the library
+or a CUDA device is missing, every engine call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libfhg.so")
+
+FHG_OK = 0
+FHG_ERR_INVALID = 1
+FHG_ERR_OOM = 2
+FHG_ERR_CUDA = 3
+FHG_ERR_NO_CONVERGENCE = 4
+FHG_ERR_UNSUPPORTED = 5
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_INT = ctypes.c_int
+_D = ctypes.c_double
+
+# name -> (restype, argtypes); kept in the order of include/fhg.h
+SIGNATURES = {
+    "fhg_last_error": (ctypes.c_char_p, []),
+    "fhg_abi_version": (_INT, []),
+    "fhg_index_build": (_INT, [_P, _I64, _I32, _P, ctypes.POINTER(_P)]),
+    "fhg_index_free": (_INT, [_P, _P]),
+    "fhg_index_shape": (_INT, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I32)]),
+    "fhg_index_knn": (_INT, [_P, _I32, _P, _P, _P]),
+    "fhg_index_boruvka": (_INT, [_P, _I32, _P, _P, _P, ctypes.POINTER(_I32), _P]),
+    "fhg_sort_mst": (_INT, [_P, _I64, _P, _P]),
+    "fhg_mst_to_linkage_tree": (_INT, [_P, _I64, _P, _P]),
+    "fhg_condense_tree": (_INT, [_P, _I64, _I64, _D, _P, _P, _P, _P, ctypes.POINTER(_I64), _P]),
+    "fhg_extract_eom_clusters": (_INT, [_P, _P, _P, _P, _I64, _D, _INT, _P,
+                                        ctypes.POINTER(_I64), _P]),
+    "fhg_label_points": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _I64, _P, _P, _P]),
+}
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+def load(path=LIB_PATH):
+    """Loads libfhg.so and binds every exported entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise EngineError(
+            f"{path} is missing: build the CUDA engine first "
+            "(python -c 'import fast_hdbscan_gb300.build as b; b.build()')")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc == FHG_OK:
+        return
+    msg = (load().fhg_last_error() or b"").decode(errors="replace")
+    if rc == FHG_ERR_INVALID:
+        raise ValueError(msg)
+    if rc == FHG_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if rc == FHG_ERR_OOM:
+        raise MemoryError(msg)
+    raise EngineError(f"fhg error {rc}: {msg}")
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise EngineError("the GB300 HDBSCAN engine needs a CUDA device")
+    return torch
+
+
+def stream_ptr():
+    return _P(_torch().cuda.current_stream().cuda_stream)
+
+
+def dptr(t):
+    """Device pointer of a contiguous CUDA tensor."""
+    assert t.is_cuda and t.is_contiguous()
+    return _P(t.data_ptr())
+
+
+def to_device(a, dtype):
+    torch = _torch()
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return torch.from_numpy(a).to("cuda", non_blocking=False)
+
+
+class Index:
+    """Owner of an fhg_index handle (the spatial index of a point set)."""
+
+    def __init__(self, X_dev):
+        self._handle = None
+        lib = load()
+        n, d = X_dev.shape
+        h = _P()
+        check(lib.fhg_index_build(dptr(X_dev), n, d, stream_ptr(), ctypes.byref(h)))
+        self._handle = h
+        self.n, self.d = int(n), int(d)
+
+    @property
+    def handle(self):
+        return self._handle
+
+    def close(self):
+        if self._handle is not None and _lib is not None:
+            _lib.fhg_index_free(self._handle, stream_ptr())
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,78 @@
+"""Builds libfhg.so (the CUDA engine behind include/fhg.h) in-tree.
+
+Every translation unit under csrc/ is compiled by nvcc for sm_103a only, in
+parallel, then linked into fast_hdbscan_gb300/_lib/libfhg.so.  Float
+contraction is off (--fmad=false) so that distance arithmetic rounds each
+multiply and add separately, matching the reference's float32 arithmetic.
+"""
+import concurrent.futures
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+OUT_DIR = os.path.join(HERE, "_lib")
+OBJ_DIR = os.path.join(OUT_DIR, "obj")
+LIB = os.path.join(OUT_DIR, "libfhg.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-fvisibility=hidden", "-I", INCLUDE]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False, ptxas_info=False):
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    headers = (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+               + glob.glob(os.path.join(INCLUDE, "*.h")))
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    for src in sources:
+        obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
+        if force or _stale(obj, [src] + headers + [__file__]):
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+            if ptxas_info:
+                cmd += ["-Xptxas", "-v"]
+            jobs.append((src, cmd))
+    if jobs:
+        workers = min(len(jobs), max(1, os.cpu_count() or 1))
+        with concurrent.futures.ThreadPoolExecutor(workers) as ex:
+            futs = {ex.submit(subprocess.run, cmd, capture_output=True, text=True): src
+                    for src, cmd in jobs}
+            failed = []
+            for f in concurrent.futures.as_completed(futs):
+                r = f.result()
+                if verbose or ptxas_info or r.returncode:
+                    sys.stderr.write(r.stdout + r.stderr)
+                if r.returncode:
+                    failed.append(futs[f])
+            if failed:
+                raise RuntimeError("nvcc failed for: " + ", ".join(failed))
+    objs = [os.path.join(OBJ_DIR, os.path.basename(s)[:-3] + ".o") for s in sources]
+    if force or jobs or _stale(LIB, objs):
+        tmp = LIB + ".tmp"
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+        subprocess.check_call(cmd)
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True, ptxas_info="--ptxas" in sys.argv))

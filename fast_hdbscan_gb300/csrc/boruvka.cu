@@ -1,0 +1,640 @@
+// Boruvka minimum spanning tree over mutual reachability, on the GPU.
+//
+// Replaces boruvka.py:474-647 (initialize_boruvka_from_knn,
+// update_component_vectors, boruvka_tree_query, merge_components,
+// parallel_boruvka).  Weights are squared float32 mutual-reachability
+// distances max(rdist(p, q), core2[p], core2[q]) until the final sqrt.
+//
+// Round 0 (boruvka.py:474): every point p links to its first kNN neighbour q
+// (position >= 1) with core2[p] >= core2[q], weight max(core2[p], rdist).
+// These links form a forest except for cycles through equal core distances;
+// the reference unions them in point order, so on every cycle the link of
+// the largest point index is the one it skips -- dropped here the same way.
+//
+// Round r >= 1: for every point, the best edge to another component by
+// (weight, caller index of the far end), found by a warp-cooperative walk of
+// the bucket tree that skips nodes lying wholly inside the point's own
+// component (node_comp, boruvka.py:98-124) and nodes beyond the component's
+// running bound (boruvka.py:182-186).  Each component keeps its minimum in a
+// 64-bit word (weight bits << 32 | min endpoint index) updated by atomicMin,
+// with a second 32-bit atomicMin on the max endpoint index: together the
+// total order (weight, min index, max index).  Under a total order two
+// components can only choose each other with the same edge; the edge is
+// then written once, oriented from the component whose lowest point index
+// is smaller -- the component the reference's merge loop visits first.
+// Components merge with a lock-free union-find; edges of a round are written
+// in order of each component's lowest point index (the reference's dict
+// insertion order).
+#include "mst.cuh"
+#include "primitives.cuh"
+#include "uf.cuh"
+
+namespace fhg {
+namespace {
+
+constexpr int kSW = 4;        // warps per block, search kernel
+constexpr int kStack = 64;
+constexpr int kMaxRounds = 64;
+constexpr int32_t kEmpty = -2;  // node_comp of a node with no points
+constexpr int32_t kMixed = -1;  // node_comp of a node spanning components
+
+__device__ __forceinline__ unsigned long long pack_key(float w, int32_t lo) {
+    return ((unsigned long long)__float_as_uint(w) << 32) | (uint32_t)lo;
+}
+__device__ __forceinline__ float key_weight(unsigned long long k) {
+    return __uint_as_float((uint32_t)(k >> 32));
+}
+
+// ------------------------------------------------------------- kNN to core
+__global__ void core_from_knn_kernel(int64_t n, int k, int ms, const float* __restrict__ knn_d_s,
+                                     float* __restrict__ core2) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    core2[p] = ms > 1 ? knn_d_s[p * k + k - 1] : 0.0f;
+}
+
+__global__ void outputs_kernel(int64_t n, int k, const int32_t* __restrict__ orig,
+                               const float* __restrict__ core2,
+                               const int32_t* __restrict__ knn_i_o, float* __restrict__ core_o,
+                               int32_t* __restrict__ nbr_o) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int64_t o = orig[p];
+    if (core_o) core_o[o] = __fsqrt_rn(core2[p]);
+    if (nbr_o)
+        for (int j = 1; j < k; ++j) nbr_o[o * (k - 1) + j - 1] = knn_i_o[o * k + j];
+}
+
+// ----------------------------------------------------------------- round 0
+__global__ void round0_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
+                              const float* __restrict__ knn_d, const float* __restrict__ core2,
+                              int32_t* __restrict__ target, float* __restrict__ w0,
+                              int* __restrict__ eq_flag) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float cp = core2[p];
+    int32_t t = -1;
+    float w = 0.0f;
+    for (int j = 1; j < k; ++j) {
+        int32_t q = knn_s[p * k + j];
+        if (q < 0) break;
+        float cq = core2[q];
+        if (cp >= cq) {
+            if (q != p) {
+                t = q;
+                w = fmaxf(cp, knn_d[p * k + j]);
+                if (cq == cp) atomicOr(eq_flag, 1);
+            }
+            break;
+        }
+    }
+    target[p] = t;
+    w0[p] = w;
+}
+
+__global__ void iota_kernel(int32_t* a, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (int32_t)i;
+}
+
+__global__ void union_targets_kernel(int32_t* par, const int32_t* __restrict__ target, int64_t n) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int32_t t = target[p];
+    if (t >= 0) uf_union(par, (int32_t)p, t);
+}
+
+__global__ void flatten_kernel(int32_t* par, int32_t* __restrict__ comp, int64_t n) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    comp[p] = uf_find(par, (int32_t)p);
+}
+
+// Functional-graph cycle detection by pointer doubling (only run when some
+// round-0 link joins two equal core distances).
+__global__ void cyc_init_kernel(int64_t n, const int32_t* __restrict__ target,
+                                const int32_t* __restrict__ orig, int32_t* nxt, int32_t* mx) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    nxt[p] = target[p] >= 0 ? target[p] : (int32_t)p;
+    mx[p] = orig[p];
+}
+__global__ void cyc_step_kernel(int64_t n, const int32_t* __restrict__ nxt,
+                                const int32_t* __restrict__ mx, int32_t* __restrict__ nxt2,
+                                int32_t* __restrict__ mx2) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int32_t q = nxt[p];
+    nxt2[p] = nxt[q];
+    mx2[p] = max(mx[p], mx[q]);
+}
+__global__ void cyc_drop_kernel(int64_t n, const int32_t* __restrict__ nxt,
+                                const int32_t* __restrict__ mx, const int32_t* __restrict__ orig,
+                                int32_t* __restrict__ target) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    if (target[p] >= 0 && mx[nxt[p]] == orig[p]) target[p] = -1;
+}
+
+__global__ void r0_flags_kernel(int64_t n, const int32_t* __restrict__ target,
+                                const int32_t* __restrict__ orig, uint32_t* __restrict__ flag) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    flag[orig[p]] = target[p] >= 0 ? 1u : 0u;
+}
+__global__ void r0_emit_kernel(int64_t n, const int32_t* __restrict__ target,
+                               const float* __restrict__ w0, const int32_t* __restrict__ orig,
+                               const uint32_t* __restrict__ pos, int32_t* __restrict__ src,
+                               int32_t* __restrict__ dst, float* __restrict__ w2) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int32_t t = target[p];
+    if (t < 0) return;
+    int32_t op = orig[p];
+    uint32_t i = pos[op];
+    src[i] = op;
+    dst[i] = orig[t];
+    w2[i] = w0[p];
+}
+
+__global__ void cmin_init_kernel(int64_t n, int32_t* cmin) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) cmin[p] = INT32_MAX;
+}
+__global__ void cmin_points_kernel(int64_t n, const int32_t* __restrict__ comp,
+                                   const int32_t* __restrict__ orig, int32_t* cmin) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) atomicMin(&cmin[comp[p]], orig[p]);
+}
+__global__ void rep_flags_kernel(int64_t n, const int32_t* __restrict__ comp,
+                                 uint32_t* __restrict__ flag) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) flag[p] = comp[p] == (int32_t)p ? 1u : 0u;
+}
+__global__ void compact_kernel(int64_t n, const uint32_t* __restrict__ flag,
+                               const uint32_t* __restrict__ pos, const int32_t* __restrict__ src,
+                               int32_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) out[pos[i]] = src ? src[i] : (int32_t)i;
+}
+
+// ---------------------------------------------------------- per round: nodes
+__global__ void node_comp_leaf_kernel(const int32_t* __restrict__ comp, int64_t n,
+                                      int64_t nleaves, int64_t slots, int32_t* __restrict__ nc) {
+    int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (leaf >= slots) return;
+    int64_t i = leaf * kLeaf + lane;
+    bool valid = leaf < nleaves && i < n;
+    int32_t c = valid ? comp[i] : 0;
+    int32_t c0 = __shfl_sync(kFull, c, 0);
+    bool same = __all_sync(kFull, !valid || c == c0);
+    if (lane == 0) nc[slots - 1 + leaf] = leaf >= nleaves ? kEmpty : (same ? c0 : kMixed);
+}
+__global__ void node_comp_level_kernel(int32_t* __restrict__ nc, int64_t first, int64_t count) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    int64_t node = first + t;
+    int32_t l = nc[2 * node + 1], r = nc[2 * node + 2];
+    nc[node] = l == kEmpty ? r : (r == kEmpty ? l : (l == r ? l : kMixed));
+}
+
+__global__ void reset_keys_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                  unsigned long long* keyA, uint32_t* keyB, int32_t* winner,
+                                  int32_t* par) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    int32_t c = reps[i];
+    keyA[c] = ~0ull;
+    keyB[c] = 0xffffffffu;
+    winner[c] = -1;
+    par[c] = c;
+}
+
+// ------------------------------------------------------- per round: search
+template <int P>
+__global__ void __launch_bounds__(kSW * 32) search_kernel(
+    IndexView ix, int k, const int32_t* __restrict__ knn_s, const float* __restrict__ knn_d,
+    const float* __restrict__ core2, const int32_t* __restrict__ comp,
+    const int32_t* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
+    int32_t* __restrict__ cand_q) {
+    __shared__ int32_t s_stack[kSW][kStack];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t leaf = (int64_t)blockIdx.x * kSW + warp;
+    if (leaf >= ix.nleaves) return;
+    const int64_t p = leaf * kLeaf + lane;
+    const bool valid = p < ix.n;
+    float q[P];
+    int32_t c = -3, op = 0;
+    float cp = 0.0f;
+    if (valid) {
+        load_pt<P>(ix.pts, p, q);
+        c = comp[p];
+        op = ix.orig[p];
+        cp = core2[p];
+    } else {
+#pragma unroll
+        for (int j = 0; j < P; ++j) q[j] = 0.0f;
+    }
+    float bw = INFINITY;
+    int32_t bq = -1, bo = INT32_MAX;
+    // Seed from the point's own kNN list (boruvka.py:474 uses the same lists).
+    if (valid) {
+        for (int j = 1; j < k; ++j) {
+            int32_t qs = knn_s[p * k + j];
+            if (qs < 0) break;
+            if (comp[qs] == c) continue;
+            float w = fmaxf(fmaxf(knn_d[p * k + j], cp), core2[qs]);
+            int32_t oq = ix.orig[qs];
+            if (w < bw || (w == bw && oq < bo)) {
+                bw = w;
+                bq = qs;
+                bo = oq;
+            }
+        }
+        if (bq >= 0) {
+            unsigned long long key = pack_key(bw, min(op, bo));
+            if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
+        }
+    }
+    float thr = bw;
+    if (valid) thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
+    bool active = valid && !(cp > thr);
+
+    float ctr[P];
+    {
+        float b[2 * P];
+        load_box<P>(ix.box, ix.slots - 1 + leaf, b);
+#pragma unroll
+        for (int j = 0; j < P; ++j) ctr[j] = 0.5f * (b[j] + b[P + j]);
+    }
+    int32_t* st = s_stack[warp];
+    int sp = 0;
+    if (__any_sync(kFull, active)) {
+        if (lane == 0) st[0] = 0;
+        sp = 1;
+    }
+    __syncwarp();
+    const int64_t first_leaf_node = ix.slots - 1;
+    while (sp > 0) {
+        --sp;
+        const int32_t node = st[sp];
+        __syncwarp();
+        const int32_t ncn = nc[node];
+        bool need = active && ncn != c && ncn != kEmpty;
+        if (need) {
+            float b[2 * P];
+            load_box<P>(ix.box, node, b);
+            need = box_lb<P>(b, q) <= thr;
+        }
+        if (!__any_sync(kFull, need)) continue;
+        if (node >= first_leaf_node) {
+            const int64_t base = (int64_t)(node - first_leaf_node) * kLeaf;
+            const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
+            float cc[P];
+            int32_t ccomp = -4, co = INT32_MAX;
+            float ccore = INFINITY;
+            if (lane < cnt) {
+                load_pt<P>(ix.pts, base + lane, cc);
+                ccomp = comp[base + lane];
+                co = ix.orig[base + lane];
+                ccore = core2[base + lane];
+            } else {
+#pragma unroll
+                for (int j = 0; j < P; ++j) cc[j] = 0.0f;
+            }
+            for (int t = 0; t < cnt; ++t) {
+                float x[P];
+#pragma unroll
+                for (int j = 0; j < P; ++j) x[j] = __shfl_sync(kFull, cc[j], t);
+                const int32_t tc = __shfl_sync(kFull, ccomp, t);
+                const int32_t to = __shfl_sync(kFull, co, t);
+                const float tk = __shfl_sync(kFull, ccore, t);
+                if (need && tc != c && tk <= thr) {
+                    float w = fmaxf(fmaxf(rdist_rn<P>(q, x), cp), tk);
+                    if (w < bw || (w == bw && to < bo)) {
+                        bw = w;
+                        bq = (int32_t)(base + t);
+                        bo = to;
+                        thr = fminf(thr, bw);
+                    }
+                }
+            }
+            if (active) {
+                thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
+                active = !(cp > thr);
+            }
+        } else {
+            const int32_t l = 2 * node + 1, r = l + 1;
+            float bl[2 * P], br[2 * P];
+            load_box<P>(ix.box, l, bl);
+            load_box<P>(ix.box, r, br);
+            const float ll = box_lb<P>(bl, ctr), lr = box_lb<P>(br, ctr);
+            const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
+            if (lane == 0) {
+                st[sp] = far;
+                st[sp + 1] = near;
+            }
+            sp += 2;
+            __syncwarp();
+        }
+    }
+    if (!valid) return;
+    cand_w[p] = bw;
+    cand_q[p] = bq;
+    if (bq >= 0) {
+        unsigned long long key = pack_key(bw, min(op, bo));
+        if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
+    }
+}
+
+__global__ void stage_b_kernel(int64_t n, const int32_t* __restrict__ comp,
+                               const int32_t* __restrict__ orig, const float* __restrict__ cand_w,
+                               const int32_t* __restrict__ cand_q,
+                               const unsigned long long* __restrict__ keyA, uint32_t* keyB) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int32_t q = cand_q[p];
+    if (q < 0) return;
+    int32_t c = comp[p], op = orig[p], oq = orig[q];
+    if (keyA[c] == pack_key(cand_w[p], min(op, oq))) atomicMin(&keyB[c], (uint32_t)max(op, oq));
+}
+__global__ void stage_c_kernel(int64_t n, const int32_t* __restrict__ comp,
+                               const int32_t* __restrict__ orig, const float* __restrict__ cand_w,
+                               const int32_t* __restrict__ cand_q,
+                               const unsigned long long* __restrict__ keyA,
+                               const uint32_t* __restrict__ keyB, int32_t* winner) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int32_t q = cand_q[p];
+    if (q < 0) return;
+    int32_t c = comp[p], op = orig[p], oq = orig[q];
+    if (keyA[c] == pack_key(cand_w[p], min(op, oq)) && keyB[c] == (uint32_t)max(op, oq))
+        winner[c] = (int32_t)p;
+}
+
+__global__ void select_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                              const int32_t* __restrict__ winner,
+                              const int32_t* __restrict__ cand_q,
+                              const int32_t* __restrict__ comp, int32_t* __restrict__ tgt,
+                              int* __restrict__ missing) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    int32_t c = reps[i], p = winner[c];
+    if (p < 0) {
+        tgt[c] = -1;
+        atomicOr(missing, 1);
+        return;
+    }
+    tgt[c] = comp[cand_q[p]];
+}
+
+__global__ void emit_flags_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                  const int32_t* __restrict__ tgt,
+                                  const int32_t* __restrict__ cmin, uint32_t* __restrict__ flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    int32_t c = reps[i], t = tgt[c];
+    if (t < 0) return;
+    bool mutual = tgt[t] == c;
+    if (!mutual || cmin[c] < cmin[t]) flag[cmin[c]] = 1u;
+}
+
+__global__ void emit_write_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                  const int32_t* __restrict__ tgt,
+                                  const int32_t* __restrict__ cmin,
+                                  const uint32_t* __restrict__ flag, const uint32_t* __restrict__ pos,
+                                  const int32_t* __restrict__ winner,
+                                  const int32_t* __restrict__ cand_q,
+                                  const float* __restrict__ cand_w,
+                                  const int32_t* __restrict__ orig, int64_t base,
+                                  int32_t* __restrict__ src, int32_t* __restrict__ dst,
+                                  float* __restrict__ w2) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    int32_t c = reps[i];
+    if (tgt[c] < 0 || !flag[cmin[c]]) return;
+    int32_t p = winner[c];
+    int64_t e = base + pos[cmin[c]];
+    src[e] = orig[p];
+    dst[e] = orig[cand_q[p]];
+    w2[e] = cand_w[p];
+}
+
+__global__ void emit_clear_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                  const int32_t* __restrict__ cmin, uint32_t* __restrict__ flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nrep) flag[cmin[reps[i]]] = 0u;
+}
+
+__global__ void union_reps_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                  const int32_t* __restrict__ tgt, int32_t* par) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    int32_t c = reps[i], t = tgt[c];
+    if (t >= 0) uf_union(par, c, t);
+}
+__global__ void relabel_points_kernel(int64_t n, int32_t* par, int32_t* __restrict__ comp) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) comp[p] = uf_find(par, comp[p]);
+}
+__global__ void merge_cmin_kernel(const int32_t* __restrict__ reps, int64_t nrep, int32_t* par,
+                                  int32_t* cmin, uint32_t* __restrict__ keep) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    int32_t c = reps[i];
+    int32_t r = uf_find(par, c);
+    keep[i] = r == c ? 1u : 0u;
+    if (r != c) atomicMin(&cmin[r], cmin[c]);
+}
+
+__global__ void finalize_edges_kernel(int64_t m, const int32_t* __restrict__ src,
+                                      const int32_t* __restrict__ dst,
+                                      const float* __restrict__ w2, double* __restrict__ edges) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    edges[3 * e + 0] = (double)src[e];
+    edges[3 * e + 1] = (double)dst[e];
+    edges[3 * e + 2] = __dsqrt_rn((double)w2[e]);
+}
+
+template <int P>
+int launch_search(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
+                  const float* core2, const int32_t* comp, const int32_t* nc,
+                  unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
+    search_kernel<P><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
+        view_of(ix), k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
+#define LAUNCH(kernel, count, ...)                                                   \
+    do {                                                                             \
+        if ((count) > 0) {                                                           \
+            kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);              \
+            FHG_CUDA(cudaGetLastError());                                            \
+        }                                                                            \
+    } while (0)
+
+}  // namespace
+
+int finalize_edges(const MstResult& r, double* edges, cudaStream_t s) {
+    LAUNCH(finalize_edges_kernel, r.m, r.m, r.src, r.dst, r.w2, edges);
+    return FHG_OK;
+}
+
+int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
+                float* core_o, int32_t* nbr_o) {
+    cudaStream_t s = ws.stream();
+    const int64_t n = ix.n;
+    const int k = min_samples > 1 ? min_samples + 1 : 2;
+    *out = MstResult();
+    if (k > 64) {
+        set_error("min_samples must be at most 63 (got %d)", min_samples);
+        return FHG_ERR_UNSUPPORTED;
+    }
+    const int64_t m_cap = n > 1 ? n - 1 : 1;
+    FHG_TRY(ws.alloc(&out->src, (size_t)m_cap));
+    FHG_TRY(ws.alloc(&out->dst, (size_t)m_cap));
+    FHG_TRY(ws.alloc(&out->w2, (size_t)m_cap));
+
+    float *knn_d, *core2, *knn_d_o = nullptr, *w0, *cand_w;
+    int32_t *knn_s, *knn_i_o = nullptr, *target, *par, *comp, *cmin, *reps, *reps2, *winner, *tgt,
+        *nc, *cand_q;
+    uint32_t *flag, *pos, *keyB, *cnt;
+    unsigned long long* keyA;
+    int* iflag;
+    FHG_TRY(ws.alloc(&knn_d, (size_t)(n * k)));
+    FHG_TRY(ws.alloc(&knn_s, (size_t)(n * k)));
+    if (nbr_o) {
+        FHG_TRY(ws.alloc(&knn_d_o, (size_t)(n * k)));
+        FHG_TRY(ws.alloc(&knn_i_o, (size_t)(n * k)));
+    }
+    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s));
+    FHG_TRY(ws.alloc(&core2, (size_t)n));
+    LAUNCH(core_from_knn_kernel, n, n, k, min_samples, knn_d, core2);
+    if (core_o || nbr_o) LAUNCH(outputs_kernel, n, n, k, ix.orig, core2, knn_i_o, core_o, nbr_o);
+    if (n < 2) return FHG_OK;
+
+    FHG_TRY(ws.alloc(&target, (size_t)n));
+    FHG_TRY(ws.alloc(&w0, (size_t)n));
+    FHG_TRY(ws.alloc(&par, (size_t)n));
+    FHG_TRY(ws.alloc(&comp, (size_t)n));
+    FHG_TRY(ws.alloc(&cmin, (size_t)n));
+    FHG_TRY(ws.alloc(&flag, (size_t)n));
+    FHG_TRY(ws.alloc(&pos, (size_t)n));
+    FHG_TRY(ws.alloc(&cnt, 2));
+    FHG_TRY(ws.alloc(&iflag, 2));
+    FHG_CUDA(cudaMemsetAsync(iflag, 0, 2 * sizeof(int), s));
+
+    // ---- round 0: kNN-seeded links (boruvka.py:474)
+    LAUNCH(round0_kernel, n, n, k, knn_s, knn_d, core2, target, w0, iflag);
+    int h_flag[2] = {0, 0};
+    FHG_CUDA(cudaMemcpyAsync(h_flag, iflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    if (h_flag[0]) {
+        int32_t *nxt, *mx, *nxt2, *mx2;
+        FHG_TRY(ws.alloc(&nxt, (size_t)n));
+        FHG_TRY(ws.alloc(&mx, (size_t)n));
+        FHG_TRY(ws.alloc(&nxt2, (size_t)n));
+        FHG_TRY(ws.alloc(&mx2, (size_t)n));
+        LAUNCH(cyc_init_kernel, n, n, target, ix.orig, nxt, mx);
+        int R = bits_for(n) + 1;
+        for (int r = 0; r < R; ++r) {
+            LAUNCH(cyc_step_kernel, n, n, nxt, mx, nxt2, mx2);
+            int32_t* t1 = nxt; nxt = nxt2; nxt2 = t1;
+            t1 = mx; mx = mx2; mx2 = t1;
+        }
+        LAUNCH(cyc_drop_kernel, n, n, nxt, mx, ix.orig, target);
+    }
+    LAUNCH(r0_flags_kernel, n, n, target, ix.orig, flag);
+    FHG_TRY(scan_exclusive_u32(ws, flag, pos, n, cnt));
+    LAUNCH(r0_emit_kernel, n, n, target, w0, ix.orig, pos, out->src, out->dst, out->w2);
+    uint32_t h_cnt = 0;
+    FHG_CUDA(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    LAUNCH(iota_kernel, n, par, n);
+    LAUNCH(union_targets_kernel, n, par, target, n);
+    LAUNCH(flatten_kernel, n, par, comp, n);
+    LAUNCH(cmin_init_kernel, n, n, cmin);
+    LAUNCH(cmin_points_kernel, n, n, comp, ix.orig, cmin);
+    FHG_CUDA(cudaStreamSynchronize(s));
+    int64_t m = h_cnt;
+
+    // representatives (component ids) in Morton order
+    FHG_TRY(ws.alloc(&reps, (size_t)n));
+    FHG_TRY(ws.alloc(&reps2, (size_t)n));
+    LAUNCH(rep_flags_kernel, n, n, comp, flag);
+    FHG_TRY(scan_exclusive_u32(ws, flag, pos, n, cnt));
+    LAUNCH(compact_kernel, n, n, flag, pos, (const int32_t*)nullptr, reps);
+    uint32_t h_ncomp = 0;
+    FHG_CUDA(cudaMemcpyAsync(&h_ncomp, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    int64_t ncomp = h_ncomp;
+
+    FHG_TRY(ws.alloc(&keyA, (size_t)n));
+    FHG_TRY(ws.alloc(&keyB, (size_t)n));
+    FHG_TRY(ws.alloc(&winner, (size_t)n));
+    FHG_TRY(ws.alloc(&tgt, (size_t)n));
+    FHG_TRY(ws.alloc(&nc, (size_t)ix.nnodes));
+    FHG_TRY(ws.alloc(&cand_w, (size_t)n));
+    FHG_TRY(ws.alloc(&cand_q, (size_t)n));
+    uint32_t* kpos;
+    FHG_TRY(ws.alloc(&kpos, (size_t)n));
+    FHG_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t) * n, s));
+
+    int rounds = 0;
+    while (ncomp > 1) {
+        if (rounds >= kMaxRounds) {
+            set_error("boruvka: no convergence after %d rounds (%lld components left)", rounds,
+                      (long long)ncomp);
+            return FHG_ERR_NO_CONVERGENCE;
+        }
+        // node_comp (boruvka.py:98-124), bottom-up
+        LAUNCH(node_comp_leaf_kernel, ix.slots * 32, comp, n, ix.nleaves, ix.slots, nc);
+        for (int64_t width = ix.slots / 2; width >= 1; width /= 2)
+            LAUNCH(node_comp_level_kernel, width, nc, width - 1, width);
+        LAUNCH(reset_keys_kernel, ncomp, reps, ncomp, keyA, keyB, winner, par);
+        FHG_TRY(ix.pad == 4 ? launch_search<4>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w,
+                                              cand_q, s)
+                            : launch_search<8>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w,
+                                              cand_q, s));
+        LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);
+        LAUNCH(stage_c_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB, winner);
+        FHG_CUDA(cudaMemsetAsync(iflag + 1, 0, sizeof(int), s));
+        LAUNCH(select_kernel, ncomp, reps, ncomp, winner, cand_q, comp, tgt, iflag + 1);
+        LAUNCH(emit_flags_kernel, ncomp, reps, ncomp, tgt, cmin, flag);
+        Workspace tmp(s);  // per-round scan scratch, released at the end of the round
+        FHG_TRY(scan_exclusive_u32(tmp, flag, pos, n, cnt));
+        LAUNCH(emit_write_kernel, ncomp, reps, ncomp, tgt, cmin, flag, pos, winner, cand_q, cand_w,
+               ix.orig, m, out->src, out->dst, out->w2);
+        LAUNCH(emit_clear_kernel, ncomp, reps, ncomp, cmin, flag);
+        LAUNCH(union_reps_kernel, ncomp, reps, ncomp, tgt, par);
+        LAUNCH(relabel_points_kernel, n, n, par, comp);
+        uint32_t* keep = pos;  // pos is free again after emit_write
+        LAUNCH(merge_cmin_kernel, ncomp, reps, ncomp, par, cmin, keep);
+        FHG_TRY(scan_exclusive_u32(tmp, keep, kpos, ncomp, cnt + 1));
+        LAUNCH(compact_kernel, ncomp, ncomp, keep, kpos, reps, reps2);
+        uint32_t h2[2] = {0, 0};
+        int h_missing = 0;
+        FHG_CUDA(cudaMemcpyAsync(h2, cnt, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaMemcpyAsync(&h_missing, iflag + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        int32_t* tr = reps; reps = reps2; reps2 = tr;
+        int64_t new_ncomp = h2[1];
+        int64_t added = h2[0];
+        if (h_missing || added != ncomp - new_ncomp) {
+            set_error("boruvka round %d: inconsistent merge (added %lld, components %lld -> %lld, "
+                      "missing=%d)", rounds, (long long)added, (long long)ncomp,
+                      (long long)new_ncomp, h_missing);
+            return FHG_ERR_NO_CONVERGENCE;
+        }
+        m += added;
+        ncomp = new_ncomp;
+        ++rounds;
+    }
+    out->m = m;
+    out->rounds = rounds;
+    return FHG_OK;
+}
+
+}  // namespace fhg

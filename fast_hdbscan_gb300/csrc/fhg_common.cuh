@@ -1,0 +1,106 @@
+// Shared helpers for the GB300 HDBSCAN engine (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fhg.h"
+
+namespace fhg {
+
+// Last error message of the calling host thread (read by fhg_last_error()).
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+// A status carried through the host driver code.  Device kernels never trap:
+// bounded loops report through a device status word instead.
+struct Status {
+    int code = FHG_OK;
+    bool ok() const { return code == FHG_OK; }
+};
+
+#define FHG_CUDA(expr)                                                                  \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            ::fhg::set_error("%s failed at %s:%d: %s", #expr, __FILE__, __LINE__,      \
+                             cudaGetErrorString(_e));                                   \
+            return (_e == cudaErrorMemoryAllocation) ? FHG_ERR_OOM : FHG_ERR_CUDA;      \
+        }                                                                               \
+    } while (0)
+
+#define FHG_TRY(expr)                      \
+    do {                                   \
+        int _s = (expr);                   \
+        if (_s != FHG_OK) return _s;       \
+    } while (0)
+
+// Stream-ordered scratch allocation.  Every buffer of a call is released on
+// the same stream when the Workspace goes out of scope.
+class Workspace {
+  public:
+    explicit Workspace(cudaStream_t s) : stream_(s) {}
+    ~Workspace() { release(); }
+    Workspace(const Workspace&) = delete;
+    Workspace& operator=(const Workspace&) = delete;
+
+    template <class T>
+    int alloc(T** out, size_t count) {
+        void* p = nullptr;
+        size_t bytes = count * sizeof(T);
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&p, bytes, stream_);
+        if (e != cudaSuccess) {
+            set_error("cudaMallocAsync(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? FHG_ERR_OOM : FHG_ERR_CUDA;
+        }
+        bufs_.push_back(p);
+        *out = static_cast<T*>(p);
+        return FHG_OK;
+    }
+    void release() {
+        for (size_t i = bufs_.size(); i-- > 0;) cudaFreeAsync(bufs_[i], stream_);
+        bufs_.clear();
+    }
+    cudaStream_t stream() const { return stream_; }
+
+  private:
+    cudaStream_t stream_;
+    std::vector<void*> bufs_;
+};
+
+inline unsigned grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffff) g = 0x7fffffff;
+    return (unsigned)g;
+}
+
+// Monotone float <-> uint32 for non-negative floats (including +inf).
+__host__ __device__ inline uint32_t fbits(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+__host__ __device__ inline float bitsf(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
+constexpr int kLeaf = 32;     // points per spatial bucket (one warp)
+constexpr unsigned kFull = 0xffffffffu;
+
+}  // namespace fhg

@@ -1,0 +1,101 @@
+// The spatial index shared by the kNN and Boruvka kernels.
+//
+// HBM layout (n points, p = 4 floats per point for d <= 4, 8 for d <= 8):
+//   pts   [n][p]  float32  points in Morton order, padded with zeros
+//   orig  [n]     int32    Morton position -> caller index
+//   rank  [n]     int32    caller index -> Morton position
+//   box   [nodes][2][p]    float32 lower / upper corner of every tree node
+// Buckets of kLeaf = 32 consecutive Morton positions are the leaves of an
+// implicit complete binary tree with `slots` (a power of two) leaf slots:
+// node i has children 2i+1 and 2i+2, and leaf slot s is node slots-1+s.
+// Slots past the last bucket carry an empty box (lo = +inf, hi = -inf).
+#pragma once
+#include "fhg_common.cuh"
+
+struct fhg_index {
+    int64_t n = 0;
+    int32_t d = 0;
+    int32_t pad = 4;
+    int64_t nleaves = 0, slots = 0, nnodes = 0;
+    float* pts = nullptr;
+    int32_t* orig = nullptr;
+    int32_t* rank = nullptr;
+    float* box = nullptr;
+};
+
+namespace fhg {
+
+struct IndexView {
+    int64_t n, nleaves, slots;
+    const float* __restrict__ pts;
+    const int32_t* __restrict__ orig;
+    const float* __restrict__ box;
+};
+
+inline IndexView view_of(const fhg_index& ix) {
+    return IndexView{ix.n, ix.nleaves, ix.slots, ix.pts, ix.orig, ix.box};
+}
+
+// Squared float32 distance with every multiply and add rounded separately,
+// in dimension order (the reference's rdist).
+template <int P>
+__device__ __forceinline__ float rdist_rn(const float* a, const float* b) {
+    float r = 0.0f;
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+        float df = __fsub_rn(a[j], b[j]);
+        r = __fadd_rn(r, __fmul_rn(df, df));
+    }
+    return r;
+}
+
+// Squared distance from a point to a box (the reference's
+// point_to_node_lower_bound_rdist); never exceeds rdist_rn to any point
+// inside the box.
+template <int P>
+__device__ __forceinline__ float box_lb(const float* __restrict__ box, const float* q) {
+    float r = 0.0f;
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+        float lo = box[j], hi = box[P + j];
+        float dlo = lo > q[j] ? __fsub_rn(lo, q[j]) : 0.0f;
+        float dhi = q[j] > hi ? __fsub_rn(q[j], hi) : 0.0f;
+        float dd = __fadd_rn(dlo, dhi);
+        r = __fadd_rn(r, __fmul_rn(dd, dd));
+    }
+    return r;
+}
+
+template <int P>
+__device__ __forceinline__ void load_pt(const float* __restrict__ pts, int64_t i, float* out) {
+    if (P == 4) {
+        float4 v = __ldg(reinterpret_cast<const float4*>(pts) + i);
+        out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+    } else {
+        const float4* p4 = reinterpret_cast<const float4*>(pts) + 2 * i;
+        float4 a = __ldg(p4), b = __ldg(p4 + 1);
+        out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+        out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+    }
+}
+
+template <int P>
+__device__ __forceinline__ void load_box(const float* __restrict__ box, int64_t node, float* out) {
+    const float4* b4 = reinterpret_cast<const float4*>(box + node * 2 * P);
+#pragma unroll
+    for (int j = 0; j < 2 * P / 4; ++j) {
+        float4 v = __ldg(b4 + j);
+        out[4 * j] = v.x; out[4 * j + 1] = v.y; out[4 * j + 2] = v.z; out[4 * j + 3] = v.w;
+    }
+}
+
+int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index** out);
+int index_free(fhg_index* ix, cudaStream_t s);
+
+// kNN over the index.  Outputs (all nullable):
+//   d_s/i_s : rows in Morton order, neighbour ids as Morton positions
+//   d_o/i_o : rows in caller order, neighbour ids as caller indices
+int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
+              cudaStream_t s);
+
+}  // namespace fhg

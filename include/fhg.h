@@ -1,0 +1,113 @@
+/*
+ * fhg.h -- C ABI of the GB300-native HDBSCAN engine (libfhg.so, sm_103a).
+ *
+ * The reference (fast_hdbscan 0.3.2) is a Python + Numba library; its
+ * "plugin API" is the Python signatures of the functions on the fit path.
+ * Each entry point below replaces one of those functions (cited as
+ * reference-file:line).  A Python binding (ctypes) or any other FFI passes
+ * plain device pointers, sizes and a cudaStream_t given as void*.
+ *
+ * Conventions
+ *   - All array arguments named *_dev are device pointers; *_host are host.
+ *   - Indices of points are positions in the caller's input (the reference's
+ *     numbering), never an internal permutation.
+ *   - Every call is stream-ordered on `stream` (NULL = legacy default stream)
+ *     and returns an FHG_* status; FHG_OK = 0.  fhg_last_error() returns a
+ *     message for the calling thread's last failure.
+ *   - Scratch memory is taken with cudaMallocAsync on `stream` and released
+ *     on the same stream before the call returns.
+ *   - Ties are broken by a total order on point indices: kNN lists by
+ *     (distance, index); a Boruvka component's outgoing edge by
+ *     (weight, min endpoint, max endpoint).  On tie-free input this yields the
+ *     reference's core distances, kNN lists and MST weight multiset exactly.
+ */
+#ifndef FHG_H
+#define FHG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FHG_OK 0
+#define FHG_ERR_INVALID 1        /* bad argument (maps to ValueError)            */
+#define FHG_ERR_OOM 2            /* device allocation failed                     */
+#define FHG_ERR_CUDA 3           /* a CUDA runtime call failed                   */
+#define FHG_ERR_NO_CONVERGENCE 4 /* a bounded device loop hit its iteration cap  */
+#define FHG_ERR_UNSUPPORTED 5    /* valid but not implemented (NotImplementedError) */
+
+/* Message for the calling thread's most recent failure ("" if none). */
+const char* fhg_last_error(void);
+/* ABI version of this library (bumped when a signature changes). */
+int fhg_abi_version(void);
+
+/* Opaque spatial index: points sorted along a Morton curve into buckets of
+ * 32 with a complete binary tree of bounding boxes over the buckets. */
+typedef struct fhg_index fhg_index;
+
+/* Replaces numba_kdtree.py:478 build_kdtree(data, leaf_size=40).
+ * X_dev: n x d float32, row-major, caller order.  1 <= d <= 8. */
+int fhg_index_build(const float* X_dev, int64_t n, int32_t d, void* stream, fhg_index** out);
+/* Releases an index built by fhg_index_build. */
+int fhg_index_free(fhg_index* index, void* stream);
+/* Number of points and dimensions of an index. */
+int fhg_index_shape(const fhg_index* index, int64_t* n, int32_t* d);
+
+/* Replaces numba_kdtree.py:765 parallel_tree_query(tree, tree.data, k,
+ * output_rdist=True): for every point its k nearest points (itself included)
+ * by squared float32 distance, ascending.  rdist_dev: n x k float32,
+ * idx_dev: n x k int32, rows in caller order.  1 <= k <= 64; entries past the
+ * n-th neighbour are (+inf, -1). */
+int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t* idx_dev,
+                  void* stream);
+
+/* Replaces boruvka.py:542 parallel_boruvka(tree, n_threads, min_samples,
+ * sample_weights=None, reproducible=False): the minimum spanning tree of the
+ * mutual-reachability graph.
+ *   edges_dev     (n-1) x 3 float64: src, dst, sqrt(weight), in Boruvka order
+ *                 (round by round; within a round by each component's lowest
+ *                 point index), src inside the component that chose the edge.
+ *   neighbors_dev n x max(min_samples,1) int32: kNN without the point itself
+ *                 (neighbors[:, 1:] of the k = min_samples + 1 query).
+ *   core_dev      n float32: sqrt of the squared core distance.
+ *   n_rounds_host optional: Boruvka rounds after the kNN-seeded round. */
+int fhg_index_boruvka(fhg_index* index, int32_t min_samples, double* edges_dev,
+                      int32_t* neighbors_dev, float* core_dev, int32_t* n_rounds_host,
+                      void* stream);
+
+/* Replaces the np.lexsort((mst[:,1], mst[:,0], mst[:,2])) of hdbscan.py:511:
+ * rows of an m x 3 float64 edge list ordered by (weight, src, dst). */
+int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream);
+
+/* Replaces cluster_trees.py:65 mst_to_linkage_tree(sorted_mst): m x 4 float64
+ * rows [max(root_l, root_r), min(root_l, root_r), weight, size]. */
+int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, double* linkage_dev,
+                            void* stream);
+
+/* Replaces cluster_trees.py:205 condense_tree(hierarchy, min_cluster_size,
+ * max_cluster_size) for unit sample weights.  Output buffers hold 2*m rows;
+ * *n_rows_host receives the row count.  Rows come in the reference's order. */
+int fhg_condense_tree(const double* linkage_dev, int64_t m, int64_t min_cluster_size,
+                      double max_cluster_size, int64_t* parent_dev, int64_t* child_dev,
+                      float* lambda_dev, float* child_size_dev, int64_t* n_rows_host,
+                      void* stream);
+
+/* Replaces cluster_trees.py:724 extract_eom_clusters(condensed_tree,
+ * cluster_tree, max_cluster_size, allow_single_cluster).  sel_dev holds up
+ * to `rows` ids; *n_sel_host receives the count (reference order). */
+int fhg_extract_eom_clusters(const int64_t* parent_dev, const int64_t* child_dev,
+                             const float* lambda_dev, const float* child_size_dev,
+                             int64_t rows, double max_cluster_size, int allow_single_cluster,
+                             int64_t* sel_dev, int64_t* n_sel_host, void* stream);
+
+/* Replaces cluster_trees.py:944 get_cluster_label_vector and :1011
+ * get_point_membership_strength_vector (cluster_selection_epsilon as given). */
+int fhg_label_points(const int64_t* parent_dev, const int64_t* child_dev,
+                     const float* lambda_dev, const float* child_size_dev, int64_t rows,
+                     const int64_t* sel_dev, int64_t n_sel, double epsilon, int64_t n_samples,
+                     int64_t* labels_dev, float* probs_dev, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FHG_H */

@@ -1,0 +1,96 @@
+/*
+ * CPU oracle for the fast_hdbscan fit path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference algorithm (fast_hdbscan 0.3.2,
+ * Python + Numba), statement for statement, used by the tests as the checker
+ * for the CUDA engine and by the benchmark as the timed CPU baseline.  It is
+ * never linked into, or called by, the product library.
+ *
+ * Two tie-breaking modes:
+ *   mode 0 ("reference"): exactly the reference's tie behaviour with its
+ *          parallel loops run sequentially (first-found-wins in KD-tree
+ *          traversal order, lowest point index wins inside a component).
+ *          Pinned bit-for-bit against fixtures produced by the reference.
+ *   mode 1 ("canonical"): every tie is broken by a total order on point
+ *          indices -- kNN by (distance, index), a point's Boruvka candidate by
+ *          (weight, index), a component's edge by (weight, min idx, max idx).
+ *          The result does not depend on the spatial index, and is what the
+ *          GPU engine reproduces bit for bit.
+ * On tie-free input both modes give the same core distances and the same MST
+ * weight multiset; they can differ only in which of several equal-weight MST
+ * edges is kept.
+ */
+#ifndef FHG_ORACLE_H
+#define FHG_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_kdtree orc_kdtree;
+
+/* numba_kdtree.py:478 build_kdtree */
+orc_kdtree* orc_build_kdtree(const float* X, int64_t n, int64_t d, int64_t leaf_size);
+void orc_free_kdtree(orc_kdtree* t);
+int64_t orc_kdtree_n_nodes(const orc_kdtree* t);
+void orc_kdtree_arrays(const orc_kdtree* t, int64_t* idx_array, int64_t* idx_start,
+                       int64_t* idx_end, uint8_t* is_leaf, float* node_bounds);
+
+/* numba_kdtree.py:765 parallel_tree_query(tree, tree.data, k, output_rdist=True) */
+void orc_tree_query(const orc_kdtree* t, int64_t k, int mode, int nthreads,
+                    float* rdist, int32_t* idx);
+
+/* boruvka.py:542 parallel_boruvka: returns number of edges written to
+ * edges[(n-1)*3] (src, dst, sqrt weight), neighbors[n*ms], core[n]. */
+int64_t orc_parallel_boruvka(const orc_kdtree* t, int64_t min_samples, int mode,
+                             int nthreads, double* edges, int32_t* neighbors,
+                             float* core, int64_t* n_rounds);
+
+/* hdbscan.py:511 lexsort by (weight, src, dst) */
+void orc_sort_mst(const double* mst, int64_t m, double* out);
+/* cluster_trees.py:65 mst_to_linkage_tree */
+void orc_mst_to_linkage_tree(const double* sorted_mst, int64_t m, double* out);
+/* cluster_trees.py:205 condense_tree; returns number of rows.  Buffers must
+ * hold 2*m rows. */
+int64_t orc_condense_tree(const double* linkage, int64_t m, int64_t min_cluster_size,
+                          double max_cluster_size, int64_t* parent, int64_t* child,
+                          float* lambda_val, float* child_size);
+/* cluster_trees.py:774 simplify_hierarchy (in place); returns kept rows */
+int64_t orc_simplify_hierarchy(int64_t* parent, int64_t* child, float* lambda_val,
+                               float* child_size, int64_t rows, double threshold);
+/* cluster_trees.py:724 extract_eom_clusters; returns count written to sel */
+int64_t orc_extract_eom_clusters(const int64_t* parent, const int64_t* child,
+                                 const float* lambda_val, const float* child_size,
+                                 int64_t rows, double max_cluster_size,
+                                 int allow_single_cluster, int64_t* sel);
+/* cluster_trees.py:369 cluster_tree_leaves */
+int64_t orc_cluster_tree_leaves(const int64_t* parent, const int64_t* child,
+                                const float* child_size, int64_t rows, int64_t n_points,
+                                int64_t* sel);
+/* cluster_trees.py:834 cluster_epsilon_search */
+int64_t orc_cluster_epsilon_search(const int64_t* parent, const int64_t* child,
+                                   const float* lambda_val, const float* child_size,
+                                   int64_t rows, const int64_t* clusters, int64_t n_clusters,
+                                   double min_epsilon, int64_t* out);
+/* cluster_trees.py:944 get_cluster_label_vector; returns 0, or -1 where the
+ * reference would raise (a KeyError on an unselected root cluster). */
+int orc_get_cluster_label_vector(const int64_t* parent, const int64_t* child,
+                                 const float* lambda_val, int64_t rows,
+                                 const int64_t* clusters, int64_t n_clusters,
+                                 double epsilon, int64_t n_samples, int64_t* labels);
+/* cluster_trees.py:1011 get_point_membership_strength_vector */
+void orc_get_point_membership_strength_vector(const int64_t* parent, const int64_t* child,
+                                              const float* lambda_val,
+                                              const float* child_size, int64_t rows,
+                                              const int64_t* clusters, int64_t n_clusters,
+                                              const int64_t* labels, int64_t n_samples,
+                                              float* probs);
+/* cluster_trees.py:906 get_cluster_labelling_at_cut */
+void orc_get_cluster_labelling_at_cut(const double* linkage, int64_t m, double cut,
+                                      int64_t min_cluster_size, int64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

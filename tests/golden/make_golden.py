@@ -1,0 +1,161 @@
+"""Generate golden HDBSCAN fixtures from the unmodified fast_hdbscan reference.
+
+The reference (fast_hdbscan 0.3.2, pure Python + Numba) is imported from a
+checkout given by ``--reference`` (default: the read-only copy mounted in the
+build container) with ``numba_shim/`` first on ``sys.path``: the shim turns
+``@njit`` into a no-op and ``prange`` into ``range``, so the reference runs its
+own code unmodified as plain Python, with its parallel loops sequential.
+
+Each case writes ``<name>.npz`` beside this script holding the float32 input,
+the parameters and every intermediate of the fit path:
+
+  knn_rdist, knn_idx         parallel_tree_query(tree, data, k=ms+1, output_rdist=True)
+  core                        sqrt of the k-th squared kNN distance (float32)
+  mst_raw                     compute_minimum_spanning_tree edges, unsorted
+  sorted_mst, linkage         clusters_from_spanning_tree outputs
+  ct_parent/child/lambda/size the CondensedTree namedtuple
+  selected                    the selected cluster ids
+  labels, probabilities       final outputs
+  kd_*                        the reference KD-tree arrays (small cases only)
+
+Run:  python tests/golden/make_golden.py [--only NAME ...]
+"""
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(HERE, "numba_shim"))
+sys.path.insert(0, REPO)
+
+from fast_hdbscan_gb300 import synthetic  # noqa: E402
+
+
+def _blobs200():
+    from sklearn.datasets import make_blobs
+    from sklearn.preprocessing import StandardScaler
+    from sklearn.utils import shuffle
+
+    X, y = make_blobs(n_samples=200, random_state=10)
+    X, y = shuffle(X, y, random_state=7)
+    return StandardScaler().fit_transform(X)
+
+
+def _rand(seed, n, d):
+    np.random.seed(seed)
+    return np.random.rand(n, d)
+
+
+def _one_d():
+    np.random.seed(42)
+    return np.concatenate(
+        [np.random.normal(0, 0.1, 50), np.random.normal(5, 0.1, 50)]
+    ).reshape(-1, 1)
+
+
+CASES = {
+    # name: (data factory, fit kwargs)
+    "ka150": (lambda: _rand(0, 150, 2), dict(min_cluster_size=5)),
+    "ka150_eps": (lambda: _rand(0, 150, 2),
+                  dict(min_cluster_size=5, cluster_selection_epsilon=0.2)),
+    "blobs200": (_blobs200, dict(min_cluster_size=5)),
+    "blobs200_ms1": (_blobs200, dict(min_cluster_size=5, min_samples=1)),
+    "blobs200_leaf": (_blobs200, dict(min_cluster_size=5, cluster_selection_method="leaf")),
+    "blobs200_maxcs": (_blobs200, dict(min_cluster_size=5, max_cluster_size=30)),
+    "blobs200_single": (_blobs200, dict(min_cluster_size=5, allow_single_cluster=True)),
+    "blobs200_persist": (_blobs200, dict(min_cluster_size=5, cluster_selection_persistence=0.5)),
+    "blobs2d_2k": (lambda: synthetic.blobs_2d(2000, seed=10),
+                   dict(min_samples=10, min_cluster_size=50)),
+    "blobs2d_20k": (lambda: synthetic.blobs_2d(20000, seed=0),
+                    dict(min_samples=10, min_cluster_size=50)),
+    "umap5d_5k": (lambda: synthetic.umap_like(5000, seed=11),
+                  dict(min_samples=10, min_cluster_size=25)),
+    "vd3d_5k": (lambda: synthetic.varying_density(5000, seed=12),
+                dict(min_samples=15, min_cluster_size=25)),
+    "vd3d_20k": (lambda: synthetic.varying_density(20000, seed=13),
+                 dict(min_samples=15, min_cluster_size=50)),
+    "edge_two": (lambda: np.array([[0.0, 0.0], [0.1, 0.0]]), dict(min_cluster_size=2)),
+    "edge_dups": (lambda: np.full((50, 3), 1.0), dict(min_cluster_size=5)),
+    "edge_1d": (_one_d, dict(min_cluster_size=10)),
+    "edge_highms": (lambda: _rand(42, 20, 2), dict(min_cluster_size=5, min_samples=18)),
+    "edge_mcs_gt_n": (lambda: _rand(42, 10, 2), dict(min_cluster_size=100)),
+}
+
+
+def run_case(name, factory, kwargs, ref):
+    from fast_hdbscan.hdbscan import fast_hdbscan, compute_minimum_spanning_tree
+    from fast_hdbscan.numba_kdtree import build_kdtree, parallel_tree_query
+    from fast_hdbscan.cluster_trees import (
+        cluster_tree_from_condensed_tree, extract_eom_clusters)
+
+    X = np.ascontiguousarray(factory(), dtype=np.float32)
+    kwargs = dict(kwargs)
+    kwargs.setdefault("min_samples", None)  # the HDBSCAN estimator's default
+    mcs = kwargs.get("min_cluster_size", 5)
+    ms = kwargs.get("min_samples") or mcs
+    t0 = time.time()
+    out = {"X": X, "min_samples": np.int64(ms), "min_cluster_size": np.int64(mcs)}
+    for key in ("cluster_selection_epsilon", "cluster_selection_persistence",
+                "max_cluster_size"):
+        out[key] = np.float64(kwargs.get(key, np.inf if key == "max_cluster_size" else 0.0))
+    out["allow_single_cluster"] = np.bool_(kwargs.get("allow_single_cluster", False))
+    out["cluster_selection_method"] = np.array(kwargs.get("cluster_selection_method", "eom"))
+
+    if X.shape[0] >= 2:
+        tree = build_kdtree(X)
+        k = ms + 1 if ms > 1 else 2
+        k = min(k, X.shape[0])
+        rd, idx = parallel_tree_query(tree, tree.data, k=k, output_rdist=True)
+        out["knn_rdist"], out["knn_idx"] = rd, idx
+        if X.shape[0] <= 5000:
+            out["kd_idx_array"] = tree.idx_array
+            out["kd_idx_start"] = tree.idx_start
+            out["kd_idx_end"] = tree.idx_end
+            out["kd_is_leaf"] = tree.is_leaf
+            out["kd_node_bounds"] = tree.node_bounds
+        mst_raw, nbrs, core = compute_minimum_spanning_tree(X, min_samples=ms)
+        out["mst_raw"] = mst_raw
+        out["core"] = core
+        out["neighbors"] = nbrs
+
+    res = fast_hdbscan(X, return_trees=True, **kwargs)
+    labels, probs, linkage, ct, smst, nbrs2, core2 = res
+    out["labels"] = np.asarray(labels)
+    out["probabilities"] = np.asarray(probs)
+    out["linkage"] = np.asarray(linkage)
+    out["sorted_mst"] = np.asarray(smst)
+    if hasattr(ct, "parent") and not isinstance(ct, np.ndarray):
+        out["ct_parent"] = np.asarray(ct.parent)
+        out["ct_child"] = np.asarray(ct.child)
+        out["ct_lambda"] = np.asarray(ct.lambda_val)
+        out["ct_size"] = np.asarray(ct.child_size)
+        if len(ct.parent) > 0:
+            cl_tree = cluster_tree_from_condensed_tree(ct)
+            out["selected_eom"] = np.asarray(extract_eom_clusters(
+                ct, cl_tree, max_cluster_size=kwargs.get("max_cluster_size", np.inf),
+                allow_single_cluster=kwargs.get("allow_single_cluster", False)))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(f"{name}: n={X.shape[0]} d={X.shape[1]} ms={ms} mcs={mcs} "
+          f"clusters={len(set(out['labels'].tolist()) - {-1})} "
+          f"noise={(out['labels'] == -1).sum()} ({time.time() - t0:.1f}s)")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", nargs="*")
+    args = ap.parse_args()
+    sys.path.insert(1, args.reference)
+    import fast_hdbscan  # noqa: F401
+    for name, (factory, kwargs) in CASES.items():
+        if args.only and name not in args.only:
+            continue
+        run_case(name, factory, kwargs, args.reference)
+
+
+if __name__ == "__main__":
+    main()
