@@ -1,0 +1,12 @@
+"""GB300-native HDBSCAN engine behind fast_hdbscan's API (Euclidean fit path).
+
+    from fast_hdbscan_gb300 import HDBSCAN
+    labels = HDBSCAN(min_cluster_size=50, min_samples=10).fit_predict(X)
+
+Every stage (spatial index, kNN core distances, Boruvka MST, linkage tree,
+condensed tree, cluster selection, labels) runs as hand-written sm_103a CUDA
+kernels in libfhg.so, called through the C ABI of include/fhg.h.
+"""
+from .hdbscan import HDBSCAN, fast_hdbscan  # noqa: F401
+
+__all__ = ["HDBSCAN", "fast_hdbscan"]

@@ -40,6 +40,11 @@ SIGNATURES = {
     "fhg_extract_eom_clusters": (_INT, [_P, _P, _P, _P, _I64, _D, _INT, _P,
                                         ctypes.POINTER(_I64), _P]),
     "fhg_label_points": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _I64, _P, _P, _P]),
+    "fhg_cluster_tree_leaves": (_INT, [_P, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), _P]),
+    "fhg_membership_strengths": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "fhg_hdbscan_fit": (_INT, [_P, _I64, _I32, _I32, _I64, _I32, _D, _INT, _D, _D,
+                               _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_I64),
+                               _P, _P, _P, ctypes.POINTER(_I64), _P]),
 }
 
 _lib = None
@@ -104,6 +109,28 @@ def to_device(a, dtype):
     torch = _torch()
     a = np.ascontiguousarray(a, dtype=dtype)
     return torch.from_numpy(a).to("cuda", non_blocking=False)
+
+
+def empty(shape, dtype):
+    """Uninitialised CUDA tensor with a numpy dtype."""
+    torch = _torch()
+    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+           np.dtype(np.int32): torch.int32, np.dtype(np.int64): torch.int64}[np.dtype(dtype)]
+    if isinstance(shape, int):
+        shape = (shape,)
+    shape = tuple(max(int(s), 0) for s in shape)
+    n = int(np.prod(shape)) if shape else 1
+    if n == 0:  # keep a valid device pointer for zero-size outputs
+        return torch.empty((1,), dtype=tdt, device="cuda")[:0].reshape(shape)
+    return torch.empty(shape, dtype=tdt, device="cuda")
+
+
+def vptr(t):
+    """Device pointer of a contiguous CUDA tensor, or NULL for None."""
+    if t is None:
+        return _P()
+    assert t.is_cuda and t.is_contiguous()
+    return _P(t.data_ptr())
 
 
 class Index:

@@ -46,14 +46,16 @@ __device__ __forceinline__ float key_weight(unsigned long long k) {
 }
 
 // ------------------------------------------------------------- kNN to core
-__global__ void core_from_knn_kernel(int64_t n, int k, int ms, const float* __restrict__ knn_d_s,
-                                     float* __restrict__ core2) {
+// core2 = squared distance to the k-th neighbour (itself included); +inf when
+// there are fewer than k points, 0 for min_samples <= 1 (boruvka.py:581-601).
+__global__ void core_from_knn_kernel(int64_t n, int kk, int k, int ms,
+                                     const float* __restrict__ knn_d_s, float* __restrict__ core2) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    core2[p] = ms > 1 ? knn_d_s[p * k + k - 1] : 0.0f;
+    core2[p] = ms <= 1 ? 0.0f : (k > kk ? INFINITY : knn_d_s[p * kk + kk - 1]);
 }
 
-__global__ void outputs_kernel(int64_t n, int k, const int32_t* __restrict__ orig,
+__global__ void outputs_kernel(int64_t n, int kk, int k, const int32_t* __restrict__ orig,
                                const float* __restrict__ core2,
                                const int32_t* __restrict__ knn_i_o, float* __restrict__ core_o,
                                int32_t* __restrict__ nbr_o) {
@@ -62,7 +64,8 @@ __global__ void outputs_kernel(int64_t n, int k, const int32_t* __restrict__ ori
     int64_t o = orig[p];
     if (core_o) core_o[o] = __fsqrt_rn(core2[p]);
     if (nbr_o)
-        for (int j = 1; j < k; ++j) nbr_o[o * (k - 1) + j - 1] = knn_i_o[o * k + j];
+        for (int j = 1; j < k; ++j)
+            nbr_o[o * (k - 1) + j - 1] = j < kk ? knn_i_o[o * kk + j] : -1;
 }
 
 // ----------------------------------------------------------------- round 0
@@ -487,7 +490,8 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
                 float* core_o, int32_t* nbr_o) {
     cudaStream_t s = ws.stream();
     const int64_t n = ix.n;
-    const int k = min_samples > 1 ? min_samples + 1 : 2;
+    const int kq = min_samples > 1 ? min_samples + 1 : 2;  // the reference's k
+    const int k = (int)(kq < n ? kq : n);                  // neighbours that exist
     *out = MstResult();
     if (k > 64) {
         set_error("min_samples must be at most 63 (got %d)", min_samples);
@@ -512,8 +516,9 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     }
     FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s));
     FHG_TRY(ws.alloc(&core2, (size_t)n));
-    LAUNCH(core_from_knn_kernel, n, n, k, min_samples, knn_d, core2);
-    if (core_o || nbr_o) LAUNCH(outputs_kernel, n, n, k, ix.orig, core2, knn_i_o, core_o, nbr_o);
+    LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2);
+    if (core_o || nbr_o)
+        LAUNCH(outputs_kernel, n, n, k, kq, ix.orig, core2, knn_i_o, core_o, nbr_o);
     if (n < 2) return FHG_OK;
 
     FHG_TRY(ws.alloc(&target, (size_t)n));

@@ -3,6 +3,9 @@
 
 #include "index.cuh"
 #include "mst.cuh"
+#include "trees.cuh"
+
+#include <initializer_list>
 
 namespace fhg {
 
@@ -86,4 +89,264 @@ FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples, double* edg
         return FHG_ERR_NO_CONVERGENCE;
     }
     return FHG_OK;
+}
+
+// ------------------------------------------------------------- tree passes
+namespace {
+
+__global__ void widen_sel_kernel(int64_t k, const int32_t* __restrict__ a, int64_t* __restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k) b[i] = a[i];
+}
+__global__ void narrow_sel_kernel(int64_t k, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k) b[i] = (int32_t)a[i];
+}
+__global__ void fill_labels_kernel(int64_t n, int64_t* __restrict__ labels, float* __restrict__ probs) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        labels[i] = -1;
+        probs[i] = 0.0f;
+    }
+}
+
+int check_ptrs(const char* fn, std::initializer_list<const void*> ps) {
+    for (const void* p : ps)
+        if (!p) {
+            set_error("%s: null pointer argument", fn);
+            return FHG_ERR_INVALID;
+        }
+    return FHG_OK;
+}
+
+}  // namespace
+
+FHG_API int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream) {
+    if (m <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_sort_mst", {mst_dev, sorted_dev}));
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    int32_t *src, *dst;
+    double* w;
+    FHG_TRY(split_mst_f64(ws, mst_dev, m, &src, &dst, &w));
+    Linkage lk;
+    FHG_TRY(sort_and_link(ws, m + 1, src, dst, w, nullptr, &lk));
+    return sorted_mst_to_f64(lk, sorted_dev, s);
+}
+
+FHG_API int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, double* linkage_dev,
+                                    void* stream) {
+    if (m <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_mst_to_linkage_tree", {sorted_mst_dev, linkage_dev}));
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    int32_t *src, *dst;
+    double* w;
+    FHG_TRY(split_mst_f64(ws, sorted_mst_dev, m, &src, &dst, &w));
+    Linkage lk;
+    FHG_TRY(sort_and_link(ws, m + 1, src, dst, w, nullptr, &lk, /*presorted=*/true));
+    return linkage_to_f64(lk, linkage_dev, s);
+}
+
+FHG_API int fhg_condense_tree(const double* linkage_dev, int64_t m, int64_t min_cluster_size,
+                              double max_cluster_size, int64_t* parent_dev, int64_t* child_dev,
+                              float* lambda_dev, float* child_size_dev, int64_t* n_rows_host,
+                              void* stream) {
+    FHG_TRY(check_ptrs("fhg_condense_tree", {n_rows_host}));
+    *n_rows_host = 0;
+    if (m <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_condense_tree",
+                       {linkage_dev, parent_dev, child_dev, lambda_dev, child_size_dev}));
+    if (min_cluster_size <= 0) {
+        set_error("min_cluster_size must be a positive integer");
+        return FHG_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    Linkage lk;
+    FHG_TRY(linkage_from_f64(ws, linkage_dev, m, &lk));
+    Condensed ct;
+    FHG_TRY(condense_tree(ws, lk, min_cluster_size, max_cluster_size, &ct));
+    FHG_TRY(condensed_to_arrays(ct, parent_dev, child_dev, lambda_dev, child_size_dev, s));
+    *n_rows_host = ct.rows;
+    return FHG_OK;
+}
+
+FHG_API int fhg_extract_eom_clusters(const int64_t* parent_dev, const int64_t* child_dev,
+                                     const float* lambda_dev, const float* child_size_dev,
+                                     int64_t rows, double max_cluster_size,
+                                     int allow_single_cluster, int64_t* sel_dev,
+                                     int64_t* n_sel_host, void* stream) {
+    FHG_TRY(check_ptrs("fhg_extract_eom_clusters", {n_sel_host}));
+    *n_sel_host = 0;
+    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_extract_eom_clusters",
+                       {parent_dev, child_dev, lambda_dev, child_size_dev, sel_dev}));
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    Condensed ct;
+    FHG_TRY(condensed_from_arrays(ws, parent_dev, child_dev, lambda_dev, child_size_dev, rows, &ct));
+    int32_t* sel;
+    FHG_TRY(ws.alloc(&sel, (size_t)ct.n_clusters));
+    int64_t k = 0;
+    FHG_TRY(select_eom(ws, ct, max_cluster_size, allow_single_cluster != 0, sel, &k));
+    if (k > 0) {
+        widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, sel, sel_dev);
+        FHG_CUDA(cudaGetLastError());
+    }
+    *n_sel_host = k;
+    return FHG_OK;
+}
+
+FHG_API int fhg_label_points(const int64_t* parent_dev, const int64_t* child_dev,
+                             const float* lambda_dev, const float* child_size_dev, int64_t rows,
+                             const int64_t* sel_dev, int64_t n_sel, double epsilon,
+                             int64_t n_samples, int64_t* labels_dev, float* probs_dev,
+                             void* stream) {
+    if (n_samples <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_label_points", {labels_dev, probs_dev}));
+    cudaStream_t s = as_stream(stream);
+    if (rows <= 0 || n_sel <= 0) {
+        fill_labels_kernel<<<grid_for(n_samples, 256), 256, 0, s>>>(n_samples, labels_dev, probs_dev);
+        FHG_CUDA(cudaGetLastError());
+        return FHG_OK;
+    }
+    FHG_TRY(check_ptrs("fhg_label_points", {parent_dev, child_dev, lambda_dev, child_size_dev,
+                                            sel_dev}));
+    Workspace ws(s);
+    Condensed ct;
+    FHG_TRY(condensed_from_arrays(ws, parent_dev, child_dev, lambda_dev, child_size_dev, rows, &ct));
+    if (ct.n != n_samples) {
+        set_error("fhg_label_points: n_samples (%lld) must equal the root label (%lld)",
+                  (long long)n_samples, (long long)ct.n);
+        return FHG_ERR_INVALID;
+    }
+    int32_t* sel;
+    FHG_TRY(ws.alloc(&sel, (size_t)n_sel));
+    narrow_sel_kernel<<<grid_for(n_sel, 256), 256, 0, s>>>(n_sel, sel_dev, sel);
+    FHG_CUDA(cudaGetLastError());
+    return label_points(ws, ct, sel, n_sel, epsilon, labels_dev, probs_dev);
+}
+
+FHG_API int fhg_cluster_tree_leaves(const int64_t* parent_dev, const int64_t* child_dev,
+                                    const float* lambda_dev, const float* child_size_dev,
+                                    int64_t rows, int64_t* sel_dev, int64_t* n_sel_host,
+                                    void* stream) {
+    FHG_TRY(check_ptrs("fhg_cluster_tree_leaves", {n_sel_host}));
+    *n_sel_host = 0;
+    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_cluster_tree_leaves",
+                       {parent_dev, child_dev, lambda_dev, child_size_dev, sel_dev}));
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    Condensed ct;
+    FHG_TRY(condensed_from_arrays(ws, parent_dev, child_dev, lambda_dev, child_size_dev, rows, &ct));
+    int32_t* sel;
+    FHG_TRY(ws.alloc(&sel, (size_t)ct.n_clusters));
+    int64_t k = 0;
+    FHG_TRY(select_leaf(ws, ct, sel, &k));
+    if (k > 0) {
+        widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, sel, sel_dev);
+        FHG_CUDA(cudaGetLastError());
+    }
+    *n_sel_host = k;
+    return FHG_OK;
+}
+
+FHG_API int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* child_dev,
+                                     const float* lambda_dev, const float* child_size_dev,
+                                     int64_t rows, const int64_t* sel_dev, int64_t n_sel,
+                                     const int64_t* labels_dev, int64_t n_samples,
+                                     float* probs_dev, void* stream) {
+    if (n_samples <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_membership_strengths", {labels_dev, probs_dev}));
+    cudaStream_t s = as_stream(stream);
+    FHG_CUDA(cudaMemsetAsync(probs_dev, 0, sizeof(float) * n_samples, s));
+    if (rows <= 0 || n_sel <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_membership_strengths",
+                       {parent_dev, child_dev, lambda_dev, child_size_dev, sel_dev}));
+    Workspace ws(s);
+    Condensed ct;
+    FHG_TRY(condensed_from_arrays(ws, parent_dev, child_dev, lambda_dev, child_size_dev, rows, &ct));
+    if (ct.n > n_samples) {
+        set_error("fhg_membership_strengths: labels hold %lld points, the tree %lld",
+                  (long long)n_samples, (long long)ct.n);
+        return FHG_ERR_INVALID;
+    }
+    int32_t* sel;
+    FHG_TRY(ws.alloc(&sel, (size_t)n_sel));
+    narrow_sel_kernel<<<grid_for(n_sel, 256), 256, 0, s>>>(n_sel, sel_dev, sel);
+    FHG_CUDA(cudaGetLastError());
+    return membership_strengths(ws, ct, sel, n_sel, labels_dev, probs_dev);
+}
+
+// ---------------------------------------------------------------- fused fit
+FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                            int64_t min_cluster_size, int32_t selection_method,
+                            double max_cluster_size, int allow_single_cluster, double epsilon,
+                            double persistence, int64_t* labels_dev, float* probs_dev,
+                            double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+                            int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+                            int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
+                            int64_t* selected_dev, int64_t* n_selected_host, void* stream) {
+    FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev, labels_dev, probs_dev}));
+    if (min_samples < 1 || min_cluster_size < 1) {
+        set_error("Min samples and min cluster size must be positive integers!");
+        return FHG_ERR_INVALID;
+    }
+    if (selection_method != 0 && selection_method != 1) {
+        set_error("Invalid cluster_selection_method %d", selection_method);
+        return FHG_ERR_INVALID;
+    }
+    if (epsilon > 0.0 || persistence > 0.0) {
+        set_error("cluster_selection_epsilon/persistence are not implemented on the GPU yet");
+        return FHG_ERR_UNSUPPORTED;
+    }
+    if (n < 2) {
+        set_error("fhg_hdbscan_fit needs at least two points");
+        return FHG_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    fhg_index* ix = nullptr;
+    FHG_TRY(index_build(X_dev, n, d, s, &ix));
+    struct IndexGuard {
+        fhg_index* p;
+        cudaStream_t s;
+        ~IndexGuard() { index_free(p, s); }
+    } guard{ix, s};
+    MstResult mst;
+    FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev));
+    if (mst.m != n - 1) {
+        set_error("boruvka: spanning forest has %lld edges for %lld points", (long long)mst.m,
+                  (long long)n);
+        return FHG_ERR_NO_CONVERGENCE;
+    }
+    Linkage lk;
+    FHG_TRY(sort_and_link(ws, n, mst.src, mst.dst, nullptr, mst.w2, &lk));
+    if (mst_dev) FHG_TRY(sorted_mst_to_f64(lk, mst_dev, s));
+    if (linkage_dev) FHG_TRY(linkage_to_f64(lk, linkage_dev, s));
+    Condensed ct;
+    // hdbscan.py:521: the fit path condenses without max_cluster_size; only
+    // the EOM selection reads it.
+    FHG_TRY(condense_tree(ws, lk, min_cluster_size, INFINITY, &ct));
+    if (ct_rows_host) *ct_rows_host = ct.rows;
+    if (ct_parent_dev && ct_child_dev && ct_lambda_dev && ct_size_dev)
+        FHG_TRY(condensed_to_arrays(ct, ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, s));
+    int32_t* sel;
+    FHG_TRY(ws.alloc(&sel, (size_t)(ct.n_clusters > 0 ? ct.n_clusters : 1)));
+    int64_t k = 0;
+    if (selection_method == 0) FHG_TRY(select_eom(ws, ct, max_cluster_size, allow_single_cluster != 0, sel, &k));
+    else FHG_TRY(select_leaf(ws, ct, sel, &k));
+    if (n_selected_host) *n_selected_host = k;
+    if (selected_dev && k > 0) {
+        widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, sel, selected_dev);
+        FHG_CUDA(cudaGetLastError());
+    }
+    if (k == 0 || ct.rows == 0) {
+        fill_labels_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, labels_dev, probs_dev);
+        FHG_CUDA(cudaGetLastError());
+        return FHG_OK;
+    }
+    return label_points(ws, ct, sel, k, epsilon, labels_dev, probs_dev);
 }

@@ -1,0 +1,282 @@
+// MST sort (hdbscan.py:511) and single-linkage tree (cluster_trees.py:65).
+//
+// The reference builds the linkage tree with a sequential union-find over
+// the sorted edges: edge i merges the current roots of its two endpoints
+// into node n + i.  Here the same tree is built by rank-halving divide and
+// conquer, level-synchronously:
+//   For an interval of sorted ranks [a, a+s), every endpoint carries the id
+//   of its component's root node at time a.  The lower half [a, a+s/2) is
+//   contracted by a lock-free union-find over those ids; each contracted
+//   component's new root is node n + (largest rank in it), and every endpoint
+//   of the upper half [a+s/2, a+s) that was touched is relabelled to that
+//   node.  Then both halves recurse with s/2.  After the last level every
+//   edge holds the roots at its own time: exactly the reference's
+//   (left, right) children.
+// An id can be an endpoint label in at most one interval per level (a root
+// touched by an interval is no longer a root in any later interval), so one
+// global parent array serves every interval of a level at once.  Work is
+// O(n log n), depth O(log^2 n), whatever the height of the dendrogram.
+#include "primitives.cuh"
+#include "trees.cuh"
+#include "uf.cuh"
+
+namespace fhg {
+namespace {
+
+__device__ __forceinline__ uint64_t f64_key(double x) {
+    if (x == 0.0) x = 0.0;  // -0.0 sorts with +0.0, as np.lexsort compares values
+    uint64_t b = (uint64_t)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void iota_kernel(int32_t* a, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (int32_t)i;
+}
+__global__ void gather_key32_kernel(const int32_t* __restrict__ v, const int32_t* __restrict__ perm,
+                                    uint32_t* __restrict__ keys, int64_t m) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) keys[i] = (uint32_t)v[perm[i]];
+}
+__global__ void gather_wkey_kernel(const double* __restrict__ w, const float* __restrict__ w2,
+                                   const int32_t* __restrict__ perm, uint64_t* __restrict__ k64,
+                                   uint32_t* __restrict__ k32, int64_t m) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    if (w) k64[i] = f64_key(w[perm[i]]);
+    else k32[i] = __float_as_uint(w2[perm[i]]);  // non-negative: bits are monotone
+}
+__global__ void apply_perm_kernel(const int32_t* __restrict__ perm, const int32_t* __restrict__ src,
+                                  const int32_t* __restrict__ dst, const double* __restrict__ w,
+                                  const float* __restrict__ w2, int32_t* __restrict__ ssrc,
+                                  int32_t* __restrict__ sdst, double* __restrict__ sw,
+                                  int32_t* __restrict__ A, int32_t* __restrict__ B, int64_t m) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    int32_t e = perm[i];
+    ssrc[i] = A[i] = src[e];
+    sdst[i] = B[i] = dst[e];
+    sw[i] = w ? w[e] : __dsqrt_rn((double)w2[e]);
+}
+__global__ void node_init_kernel(int64_t nodes, int64_t n, int32_t* stamp, int32_t* claim,
+                                 int32_t* sz) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nodes) return;
+    stamp[i] = -1;
+    claim[i] = -1;
+    sz[i] = i < n ? 1 : 0;
+}
+
+__device__ __forceinline__ bool in_low(int64_t i, int64_t s, int64_t half) {
+    return (i & (s - 1)) < half;
+}
+
+__global__ void lvl_init_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
+                                const int32_t* __restrict__ B, int32_t* P, int32_t* stamp,
+                                int32_t* M, int32_t* SUM, int lev) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !in_low(i, s, half)) return;
+    int32_t a = A[i], b = B[i];
+    P[a] = a; stamp[a] = lev; M[a] = -1; SUM[a] = 0;
+    P[b] = b; stamp[b] = lev; M[b] = -1; SUM[b] = 0;
+}
+__global__ void lvl_union_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
+                                 const int32_t* __restrict__ B, int32_t* P) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !in_low(i, s, half)) return;
+    uf_union(P, A[i], B[i]);
+}
+__global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
+                                  const int32_t* __restrict__ B, int32_t* P, int32_t* M,
+                                  int32_t* SUM, const int32_t* __restrict__ SZ, int32_t* claim,
+                                  int lev) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !in_low(i, s, half)) return;
+    int32_t a = A[i], b = B[i];
+    int32_t r = uf_find(P, a);
+    atomicMax(&M[r], (int32_t)i);
+    if (atomicExch(&claim[a], lev) != lev) atomicAdd(&SUM[r], SZ[a]);
+    if (atomicExch(&claim[b], lev) != lev) atomicAdd(&SUM[r], SZ[b]);
+}
+__global__ void lvl_size_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
+                                const int32_t* __restrict__ A, int32_t* P,
+                                const int32_t* __restrict__ M, const int32_t* __restrict__ SUM,
+                                int32_t* SZ) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !in_low(i, s, half)) return;
+    int32_t r = uf_find(P, A[i]);
+    if (M[r] == (int32_t)i) SZ[n + i] = SUM[r];
+}
+__global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n, int32_t* A,
+                                   int32_t* B, int32_t* P, const int32_t* __restrict__ M,
+                                   const int32_t* __restrict__ stamp, int lev) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || in_low(i, s, half)) return;
+    int32_t a = A[i], b = B[i];
+    if (stamp[a] == lev) A[i] = (int32_t)(n + M[uf_find(P, a)]);
+    if (stamp[b] == lev) B[i] = (int32_t)(n + M[uf_find(P, b)]);
+}
+__global__ void linkage_rows_kernel(int64_t m, int64_t n, const int32_t* __restrict__ A,
+                                    const int32_t* __restrict__ B, int32_t* SZ,
+                                    int32_t* __restrict__ left, int32_t* __restrict__ right) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    int32_t a = A[i], b = B[i];
+    left[i] = max(a, b);
+    right[i] = min(a, b);
+    SZ[n + i] = SZ[a] + SZ[b];
+}
+
+__global__ void linkage_f64_kernel(int64_t m, const int32_t* __restrict__ left,
+                                   const int32_t* __restrict__ right, const double* __restrict__ w,
+                                   const int32_t* __restrict__ sz, int64_t n,
+                                   double* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    out[4 * i + 0] = (double)left[i];
+    out[4 * i + 1] = (double)right[i];
+    out[4 * i + 2] = w[i];
+    out[4 * i + 3] = (double)sz[n + i];
+}
+__global__ void sorted_mst_f64_kernel(int64_t m, const int32_t* __restrict__ ssrc,
+                                      const int32_t* __restrict__ sdst,
+                                      const double* __restrict__ w, double* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    out[3 * i + 0] = (double)ssrc[i];
+    out[3 * i + 1] = (double)sdst[i];
+    out[3 * i + 2] = w[i];
+}
+
+#define LAUNCH(kernel, count, ...)                                          \
+    do {                                                                    \
+        if ((count) > 0) {                                                  \
+            kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);     \
+            FHG_CUDA(cudaGetLastError());                                   \
+        }                                                                   \
+    } while (0)
+
+}  // namespace
+
+int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* dst,
+                  const double* w, const float* w2, Linkage* out, bool presorted) {
+    cudaStream_t s = ws.stream();
+    const int64_t m = n - 1;
+    *out = Linkage();
+    out->n = n;
+    out->m = m > 0 ? m : 0;
+    const int64_t nodes = n + (m > 0 ? m : 0);
+    FHG_TRY(ws.alloc(&out->size, (size_t)nodes));
+    int32_t *P, *stamp, *claim, *M, *SUM;
+    FHG_TRY(ws.alloc(&P, (size_t)nodes));
+    FHG_TRY(ws.alloc(&stamp, (size_t)nodes));
+    FHG_TRY(ws.alloc(&claim, (size_t)nodes));
+    FHG_TRY(ws.alloc(&M, (size_t)nodes));
+    FHG_TRY(ws.alloc(&SUM, (size_t)nodes));
+    LAUNCH(node_init_kernel, nodes, nodes, n, stamp, claim, out->size);
+    if (m <= 0) return FHG_OK;
+
+    // ---- sort by (weight, src, dst): stable LSD over dst, src, weight
+    int32_t* perm;
+    uint32_t* k32;
+    uint64_t* k64 = nullptr;
+    FHG_TRY(ws.alloc(&perm, (size_t)m));
+    FHG_TRY(ws.alloc(&k32, (size_t)m));
+    if (w) FHG_TRY(ws.alloc(&k64, (size_t)m));
+    LAUNCH(iota_kernel, m, perm, m);
+    const int ibits = bits_for(n);
+    if (!presorted) {
+        Workspace tmp(s);
+        LAUNCH(gather_key32_kernel, m, dst, perm, k32, m);
+        FHG_TRY(radix_sort_u32(tmp, k32, perm, m, 0, ibits));
+        LAUNCH(gather_key32_kernel, m, src, perm, k32, m);
+        FHG_TRY(radix_sort_u32(tmp, k32, perm, m, 0, ibits));
+        LAUNCH(gather_wkey_kernel, m, w, w2, perm, k64, k32, m);
+        if (w) FHG_TRY(radix_sort_u64(tmp, k64, perm, m, 0, 64));
+        else FHG_TRY(radix_sort_u32(tmp, k32, perm, m, 0, 32));
+    }
+    int32_t *A, *B;
+    FHG_TRY(ws.alloc(&out->ssrc, (size_t)m));
+    FHG_TRY(ws.alloc(&out->sdst, (size_t)m));
+    FHG_TRY(ws.alloc(&out->w, (size_t)m));
+    FHG_TRY(ws.alloc(&A, (size_t)m));
+    FHG_TRY(ws.alloc(&B, (size_t)m));
+    LAUNCH(apply_perm_kernel, m, perm, src, dst, w, w2, out->ssrc, out->sdst, out->w, A, B, m);
+
+    // ---- rank-halving contraction
+    int64_t S = 1;
+    while (S < m) S *= 2;
+    int lev = 0;
+    for (int64_t sz = S; sz >= 2; sz /= 2, ++lev) {
+        const int64_t half = sz / 2;
+        LAUNCH(lvl_init_kernel, m, m, sz, half, A, B, P, stamp, M, SUM, lev);
+        LAUNCH(lvl_union_kernel, m, m, sz, half, A, B, P);
+        LAUNCH(lvl_reduce_kernel, m, m, sz, half, A, B, P, M, SUM, out->size, claim, lev);
+        LAUNCH(lvl_size_kernel, m, m, sz, half, n, A, P, M, SUM, out->size);
+        LAUNCH(lvl_relabel_kernel, m, m, sz, half, n, A, B, P, M, stamp, lev);
+    }
+    FHG_TRY(ws.alloc(&out->left, (size_t)m));
+    FHG_TRY(ws.alloc(&out->right, (size_t)m));
+    LAUNCH(linkage_rows_kernel, m, m, n, A, B, out->size, out->left, out->right);
+    return FHG_OK;
+}
+
+namespace {
+__global__ void split_mst_kernel(int64_t m, const double* __restrict__ mst, int32_t* __restrict__ src,
+                                 int32_t* __restrict__ dst, double* __restrict__ w) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    src[i] = (int32_t)mst[3 * i + 0];
+    dst[i] = (int32_t)mst[3 * i + 1];
+    w[i] = mst[3 * i + 2];
+}
+__global__ void split_linkage_kernel(int64_t m, int64_t n, const double* __restrict__ lk,
+                                     int32_t* __restrict__ left, int32_t* __restrict__ right,
+                                     double* __restrict__ w, int32_t* __restrict__ size) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    left[i] = (int32_t)lk[4 * i + 0];
+    right[i] = (int32_t)lk[4 * i + 1];
+    w[i] = lk[4 * i + 2];
+    size[n + i] = (int32_t)lk[4 * i + 3];
+}
+}  // namespace
+
+int split_mst_f64(Workspace& ws, const double* mst, int64_t m, int32_t** src, int32_t** dst,
+                  double** w) {
+    cudaStream_t s = ws.stream();
+    FHG_TRY(ws.alloc(src, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(dst, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(w, (size_t)(m > 0 ? m : 1)));
+    LAUNCH(split_mst_kernel, m, m, mst, *src, *dst, *w);
+    return FHG_OK;
+}
+
+int linkage_from_f64(Workspace& ws, const double* lk, int64_t m, Linkage* out) {
+    cudaStream_t s = ws.stream();
+    *out = Linkage();
+    const int64_t n = m + 1;
+    out->n = n;
+    out->m = m;
+    FHG_TRY(ws.alloc(&out->size, (size_t)(n + m)));
+    FHG_TRY(ws.alloc(&out->left, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&out->right, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&out->w, (size_t)(m > 0 ? m : 1)));
+    int32_t *stamp, *claim;
+    FHG_TRY(ws.alloc(&stamp, (size_t)(n + m)));
+    FHG_TRY(ws.alloc(&claim, (size_t)(n + m)));
+    LAUNCH(node_init_kernel, n + m, n + m, n, stamp, claim, out->size);
+    LAUNCH(split_linkage_kernel, m, m, n, lk, out->left, out->right, out->w, out->size);
+    return FHG_OK;
+}
+
+int linkage_to_f64(const Linkage& lk, double* out, cudaStream_t s) {
+    LAUNCH(linkage_f64_kernel, lk.m, lk.m, lk.left, lk.right, lk.w, lk.size, lk.n, out);
+    return FHG_OK;
+}
+int sorted_mst_to_f64(const Linkage& lk, double* out, cudaStream_t s) {
+    LAUNCH(sorted_mst_f64_kernel, lk.m, lk.m, lk.ssrc, lk.sdst, lk.w, out);
+    return FHG_OK;
+}
+
+}  // namespace fhg

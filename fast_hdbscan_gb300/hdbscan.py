@@ -1,0 +1,424 @@
+"""Drop-in for fast_hdbscan/hdbscan.py on the Euclidean fit path.
+
+``HDBSCAN(...).fit`` / ``fit_predict``, ``fast_hdbscan``,
+``compute_minimum_spanning_tree`` and ``clusters_from_spanning_tree`` keep the
+reference's signatures, validation, error types and return conventions; the
+work runs in the GB300 engine (libfhg.so) with no CPU fallback.  Paths the
+reference routes elsewhere (non-Euclidean metrics, precomputed graphs,
+Kruskal back-ends, semi-supervised selection, sample weights) raise
+NotImplementedError.
+"""
+import ctypes
+import numbers
+from collections import namedtuple
+
+import numpy as np
+
+from . import _native
+from .boruvka import parallel_boruvka
+from .cluster_trees import (
+    CondensedTree,
+    cluster_tree_from_condensed_tree,
+    cluster_tree_leaves,
+    condense_tree,
+    extract_eom_clusters,
+    get_cluster_label_vector,
+    get_point_membership_strength_vector,
+    mst_to_linkage_tree,
+    sort_mst,
+)
+from .numba_kdtree import build_kdtree
+
+try:  # scikit-learn is optional: the estimator mirrors its protocol either way
+    from sklearn.base import BaseEstimator as _BaseEstimator
+    from sklearn.base import ClusterMixin as _ClusterMixin
+    from sklearn.utils import check_array as _sk_check_array
+
+    _HAVE_SKLEARN = True
+except ImportError:  # pragma: no cover - exercised where sklearn is absent
+    _HAVE_SKLEARN = False
+
+    class _BaseEstimator:
+        def get_params(self, deep=True):
+            import inspect
+
+            sig = inspect.signature(type(self).__init__)
+            return {k: getattr(self, k) for k in sig.parameters if k != "self"}
+
+        def set_params(self, **params):
+            for k, v in params.items():
+                setattr(self, k, v)
+            return self
+
+    class _ClusterMixin:
+        def fit_predict(self, X, y=None, **kwargs):
+            self.fit(X, y=y, **kwargs)
+            return self.labels_
+
+    _sk_check_array = None
+
+
+def check_array(X, ensure_all_finite=True, dtype="numeric"):
+    """sklearn.utils.check_array for dense 2-D numeric input."""
+    if _HAVE_SKLEARN:
+        return _sk_check_array(X, ensure_all_finite=ensure_all_finite)
+    if X is None:
+        raise ValueError("Expected 2D array, got None")
+    if isinstance(X, str):
+        raise ValueError(f"Expected 2D array, got scalar array instead:\narray={X}.")
+    arr = np.asarray(X)
+    if arr.dtype.kind not in "biuf":
+        try:
+            arr = arr.astype(np.float64)
+        except (TypeError, ValueError) as e:
+            raise ValueError(f"could not convert input to float: {e}") from None
+    if arr.ndim != 2:
+        raise ValueError(f"Expected 2D array, got {arr.ndim}D array instead")
+    if arr.dtype.kind in "biu":
+        arr = arr.astype(np.float64)
+    if ensure_all_finite and not np.all(np.isfinite(arr)):
+        raise ValueError("Input contains NaN or infinity.")
+    return arr
+
+
+def _check_sample_weight(sample_weight, X, dtype):
+    """hdbscan.py:43 simplified check (shape and non-zero)."""
+    n = X.shape[0]
+    if isinstance(sample_weight, numbers.Number):
+        return np.full(n, sample_weight, dtype=dtype)
+    sw = np.asarray(sample_weight, dtype=dtype)
+    if sw.ndim != 1:
+        raise ValueError(f"Sample weights must be 1D array or scalar, got {sw.ndim}D array.")
+    if sw.shape != (n,):
+        raise ValueError(f"sample_weight.shape == {sw.shape}, expected {(n,)}!")
+    if np.all(sw == 0):
+        raise ValueError("Sample weights must contain at least one non-zero number.")
+    return sw
+
+
+def to_numpy_rec_array(named_tuple_tree):
+    """hdbscan.py:93."""
+    if isinstance(named_tuple_tree, np.ndarray) and named_tuple_tree.dtype.names is not None:
+        return named_tuple_tree
+    size = named_tuple_tree.parent.shape[0]
+    result = np.empty(size, dtype=[("parent", np.intp), ("child", np.intp),
+                                   ("lambda_val", float), ("child_size", np.float32)])
+    result["parent"] = named_tuple_tree.parent
+    result["child"] = named_tuple_tree.child
+    result["lambda_val"] = named_tuple_tree.lambda_val
+    result["child_size"] = named_tuple_tree.child_size
+    return result
+
+
+def remap_condensed_tree(tree, internal_to_raw, outliers):
+    """hdbscan.py:119: re-insert non-finite rows at lambda 0 under the root."""
+    finite_count = len(internal_to_raw)
+    outlier_count = len(outliers)
+    for i, (parent, child, lambda_val, child_size) in enumerate(tree):
+        child = internal_to_raw[child] if child < finite_count else child + outlier_count
+        tree[i] = (parent + outlier_count, child, lambda_val, child_size)
+    root = tree[0][0]
+    outlier_tree = np.array([(root, o, 0, 1) for o in outliers],
+                            dtype=[("parent", np.intp), ("child", np.intp),
+                                   ("lambda_val", float), ("child_size", np.intp)])
+    return np.append(outlier_tree, tree)
+
+
+def remap_single_linkage_tree(tree, internal_to_raw, outliers):
+    """hdbscan.py:161: non-finite rows join last at infinite distance."""
+    finite_count = len(internal_to_raw)
+    outlier_count = len(outliers)
+    for i, (left, right, distance, size) in enumerate(tree):
+        tree[i, 0] = internal_to_raw[left] if left < finite_count else left + outlier_count
+        tree[i, 1] = internal_to_raw[right] if right < finite_count else right + outlier_count
+    outlier_tree = np.zeros((len(outliers), 4))
+    last_cluster_id = tree[tree.shape[0] - 1][0:2].max()
+    last_cluster_size = tree[tree.shape[0] - 1][3]
+    for i, outlier in enumerate(outliers):
+        outlier_tree[i] = (outlier, last_cluster_id + 1, np.inf, last_cluster_size + 1)
+        last_cluster_id += 1
+        last_cluster_size += 1
+    return np.vstack([tree, outlier_tree])
+
+
+def _validate_params(min_samples, min_cluster_size, cluster_selection_epsilon,
+                     cluster_selection_persistence):
+    """hdbscan.py:254-275."""
+    if ((not (np.issubdtype(type(min_samples), np.integer) or min_samples is None))
+            or not np.issubdtype(type(min_cluster_size), np.integer)
+            or (min_samples is not None and min_samples <= 0)
+            or min_cluster_size <= 0):
+        raise ValueError("Min samples and min cluster size must be positive integers!")
+    if (not np.issubdtype(type(cluster_selection_epsilon), np.floating)
+            or cluster_selection_epsilon < 0.0):
+        raise ValueError("Cluster selection epsilon must be a positive floating point number!")
+    if (not np.issubdtype(type(cluster_selection_persistence), np.floating)
+            or cluster_selection_persistence < 0.0):
+        raise ValueError(
+            "Cluster selection persistence must be a positive floating point number!")
+
+
+def _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data=None,
+                        cannot_link=None, cannot_link_groups=None):
+    if metric != "euclidean":
+        raise NotImplementedError(f"metric={metric!r} is outside the GPU engine's Euclidean path")
+    if algorithm not in ("boruvka", "kruskal"):
+        raise ValueError("algorithm must be 'boruvka' or 'kruskal'. Got: %s" % algorithm)
+    if algorithm != "boruvka":
+        raise NotImplementedError("algorithm='kruskal' is outside the GPU engine's Boruvka path")
+    if cannot_link is not None or cannot_link_groups is not None:
+        raise ValueError("cannot_link constraints are only supported with algorithm='kruskal'. "
+                         "Got algorithm='boruvka'.")
+    if sample_weights is not None:
+        raise NotImplementedError("sample_weights are not supported by the GPU engine yet")
+    if semi_supervised:
+        raise NotImplementedError("semi-supervised selection is outside the GPU engine's path")
+    if data is not None and data.shape[1] > 8:
+        raise NotImplementedError(
+            f"{data.shape[1]}-dimensional data: the GPU spatial path supports up to 8 dimensions")
+
+
+def _degenerate(n, return_trees):
+    """hdbscan.py:278-304 (fewer than two points)."""
+    labels = np.full(n, -1, dtype=np.intp)
+    probabilities = np.zeros(n, dtype=np.float64)
+    single_linkage_tree = np.zeros((0, 4), dtype=np.float64)
+    condensed_tree = np.zeros(0, dtype=[("parent", np.intp), ("child", np.intp),
+                                        ("lambda_val", np.float64), ("child_size", np.intp)])
+    mst = np.zeros((0, 3), dtype=np.float64)
+    neighbors = np.zeros((n, 0), dtype=np.intp)
+    core_distances = np.full(n, np.inf, dtype=np.float64)
+    result = (labels, probabilities, single_linkage_tree, condensed_tree, mst, neighbors,
+              core_distances)
+    return result[: (None if return_trees else 2)]
+
+
+FitResult = namedtuple("FitResult", ["labels", "probabilities", "linkage", "condensed",
+                                     "sorted_mst", "neighbors", "core_distances", "selected"])
+
+
+def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
+            max_cluster_size=np.inf, allow_single_cluster=False, cluster_selection_epsilon=0.0,
+            cluster_selection_persistence=0.0, return_trees=True):
+    """One call of fhg_hdbscan_fit: every stage on the GPU, outputs copied back.
+
+    X may be a NumPy array, a CPU torch tensor (pinned for asynchronous
+    copies) or a CUDA tensor; it is used as float32."""
+    torch = _native._torch()
+    if isinstance(X, torch.Tensor):
+        Xd = X.to(device="cuda", dtype=torch.float32, non_blocking=True).contiguous()
+    else:
+        Xd = _native.to_device(np.ascontiguousarray(X, dtype=np.float32), np.float32)
+    n, d = Xd.shape
+    ms = min_cluster_size if min_samples is None else min_samples
+    kcols = ms if ms > 1 else 1
+    method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
+    if method is None:
+        raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+    E = _native.empty
+    labels, probs = E(n, np.int64), E(n, np.float32)
+    trees = return_trees
+    mst = E((n - 1, 3), np.float64) if trees else None
+    linkage = E((n - 1, 4), np.float64) if trees else None
+    ctp, ctc = (E(2 * n, np.int64), E(2 * n, np.int64)) if trees else (None, None)
+    ctl, cts = (E(2 * n, np.float32), E(2 * n, np.float32)) if trees else (None, None)
+    nbrs = E((n, kcols), np.int32) if trees else None
+    core = E(n, np.float32) if trees else None
+    sel = E(n, np.int64)
+    rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
+    V = _native.vptr
+    rc = _native.load().fhg_hdbscan_fit(
+        V(Xd), n, d, int(ms), int(min_cluster_size), method, float(max_cluster_size),
+        int(bool(allow_single_cluster)), float(cluster_selection_epsilon),
+        float(cluster_selection_persistence), V(labels), V(probs), V(mst), V(linkage), V(ctp),
+        V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
+        _native.stream_ptr())
+    if rc == _native.FHG_ERR_INVALID and "KeyError" in _native.load().fhg_last_error().decode():
+        raise KeyError(_native.load().fhg_last_error().decode())
+    _native.check(rc)
+    r, k = rows.value, nsel.value
+    outs = [labels, probs, sel[:k]]
+    if trees:
+        outs += [mst, linkage, ctp[:r], ctc[:r], ctl[:r], cts[:r], nbrs, core]
+    host = [t.to("cpu", non_blocking=True) for t in outs]
+    torch.cuda.current_stream().synchronize()
+    host = [h.numpy() for h in host]
+    labels_h = host[0].astype(np.intp, copy=False)
+    if not trees:
+        return FitResult(labels_h, host[1], None, None, None, None, None, host[2])
+    ct = CondensedTree(host[5], host[6], host[7], host[8])
+    return FitResult(labels_h, host[1], host[4], ct, host[3], host[9], host[10], host[2])
+
+
+def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc",
+                 min_samples=10, min_cluster_size=10, cluster_selection_method="eom",
+                 max_cluster_size=np.inf, allow_single_cluster=False,
+                 cluster_selection_epsilon=0.0, cluster_selection_persistence=0.0,
+                 sample_weights=None, reproducible=False, return_trees=False,
+                 metric="euclidean", algorithm="boruvka", knn_k=None, cannot_link=None,
+                 validate_cannot_link=True, cannot_link_groups=None, metric_kwds=None):
+    """hdbscan.py:199 fast_hdbscan on the GPU engine."""
+    if metric == "euclidean":
+        data = check_array(data)
+        if sample_weights is not None:
+            sample_weights = _check_sample_weight(sample_weights, data, dtype=np.float32)
+    elif metric != "precomputed":
+        data = check_array(data)
+    if semi_supervised:
+        if data_labels is None:
+            raise ValueError("data_labels must not be None when semi_supervised is set to True!")
+        if ss_algorithm not in ["bc", "bc_simple"]:
+            raise ValueError(f"Invalid ss_algorithm {ss_algorithm}")
+    _validate_params(min_samples, min_cluster_size, cluster_selection_epsilon,
+                     cluster_selection_persistence)
+    if cluster_selection_method not in ("eom", "leaf"):
+        raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+    if data.shape[0] < 2:
+        return _degenerate(data.shape[0], return_trees)
+    _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data, cannot_link,
+                        cannot_link_groups)
+    fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
+                 max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
+                 cluster_selection_persistence, return_trees=return_trees)
+    result = (fr.labels, fr.probabilities, fr.linkage, fr.condensed, fr.sorted_mst,
+              fr.neighbors, fr.core_distances)
+    return result[: (None if return_trees else 2)]
+
+
+def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, reproducible=False,
+                                  metric="euclidean", algorithm="boruvka", knn_k=None,
+                                  cannot_link=None, validate_cannot_link=True,
+                                  cannot_link_groups=None, metric_kwds=None):
+    """hdbscan.py:339: (mst float64[n-1, 3] in Boruvka order, neighbors, core)."""
+    if algorithm not in ("boruvka", "kruskal"):
+        raise ValueError("algorithm must be 'boruvka' or 'kruskal'. Got: %s" % algorithm)
+    if cannot_link is not None and cannot_link_groups is not None:
+        raise ValueError("cannot_link and cannot_link_groups are mutually exclusive. "
+                         "Provide one or the other, not both.")
+    data = check_array(data)
+    _unsupported_routes(metric, algorithm, sample_weights, False, data, cannot_link,
+                        cannot_link_groups)
+    tree = build_kdtree(data)
+    return parallel_boruvka(tree, 1, min_samples=min_samples)
+
+
+def clusters_from_spanning_tree(minimum_spanning_tree, data_labels=None, semi_supervised=False,
+                                ss_algorithm="bc", min_cluster_size=10,
+                                cluster_selection_method="eom", max_cluster_size=np.inf,
+                                allow_single_cluster=False, cluster_selection_epsilon=0.0,
+                                cluster_selection_persistence=0.0, sample_weights=None):
+    """hdbscan.py:497: labels, probabilities, linkage, condensed tree, sorted MST."""
+    if semi_supervised or sample_weights is not None:
+        raise NotImplementedError("semi-supervised and weighted selection are not on the GPU path")
+    n_points = minimum_spanning_tree.shape[0] + 1
+    sorted_mst = sort_mst(minimum_spanning_tree)
+    linkage_tree = mst_to_linkage_tree(sorted_mst)
+    condensed_tree = condense_tree(linkage_tree, min_cluster_size=min_cluster_size)
+    if cluster_selection_persistence > 0.0 and len(condensed_tree.parent) > 0:
+        from .cluster_trees import simplify_hierarchy
+
+        condensed_tree = simplify_hierarchy(condensed_tree, cluster_selection_persistence)
+    cluster_tree = cluster_tree_from_condensed_tree(condensed_tree)
+    if cluster_selection_method == "eom":
+        selected_clusters = extract_eom_clusters(condensed_tree, cluster_tree,
+                                                 max_cluster_size=max_cluster_size,
+                                                 allow_single_cluster=allow_single_cluster)
+    elif cluster_selection_method == "leaf":
+        if cluster_tree.parent.shape[0] == 0:
+            selected_clusters = np.empty(0, dtype=np.int64)
+        else:
+            selected_clusters = cluster_tree_leaves(cluster_tree, n_points)
+    else:
+        raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+    if len(selected_clusters) > 1 and cluster_selection_epsilon > 0.0:
+        from .cluster_trees import cluster_epsilon_search
+
+        selected_clusters = cluster_epsilon_search(selected_clusters, cluster_tree,
+                                                   min_epsilon=cluster_selection_epsilon)
+    clusters = get_cluster_label_vector(condensed_tree, selected_clusters,
+                                        cluster_selection_epsilon, n_samples=n_points)
+    membership_strengths = get_point_membership_strength_vector(condensed_tree,
+                                                                selected_clusters, clusters)
+    return clusters, membership_strengths, linkage_tree, condensed_tree, sorted_mst
+
+
+class HDBSCAN(_ClusterMixin, _BaseEstimator):
+    """hdbscan.py:577 HDBSCAN estimator, fitted by the GB300 engine.
+
+    Same parameters and attributes as the reference (labels_, probabilities_,
+    _single_linkage_tree, _condensed_tree, _min_spanning_tree, _neighbors,
+    _core_distances)."""
+
+    def __init__(self, *, min_cluster_size=5, min_samples=None, cluster_selection_method="eom",
+                 allow_single_cluster=False, max_cluster_size=np.inf,
+                 cluster_selection_epsilon=0.0, cluster_selection_persistence=0.0,
+                 semi_supervised=False, ss_algorithm="bc", reproducible=False,
+                 metric="euclidean", algorithm="boruvka", knn_k=None, cannot_link=None,
+                 validate_cannot_link=True, cannot_link_groups=None, metric_kwds=None):
+        self.min_cluster_size = min_cluster_size
+        self.min_samples = min_samples
+        self.cluster_selection_method = cluster_selection_method
+        self.allow_single_cluster = allow_single_cluster
+        self.max_cluster_size = max_cluster_size
+        self.cluster_selection_epsilon = cluster_selection_epsilon
+        self.cluster_selection_persistence = cluster_selection_persistence
+        self.semi_supervised = semi_supervised
+        self.ss_algorithm = ss_algorithm
+        self.reproducible = reproducible
+        self.metric = metric
+        self.algorithm = algorithm
+        self.knn_k = knn_k
+        self.cannot_link = cannot_link
+        self.validate_cannot_link = validate_cannot_link
+        self.cannot_link_groups = cannot_link_groups
+        self.metric_kwds = metric_kwds
+
+    def fit(self, X, y=None, sample_weight=None, **fit_params):
+        """hdbscan.py:686: validation, non-finite row filter, GPU fit, remap."""
+        if self.metric == "precomputed" or self.semi_supervised:
+            raise NotImplementedError("precomputed and semi-supervised fits are not on the GPU path")
+        X = check_array(X, ensure_all_finite=False)
+        self._raw_data = X
+        if sample_weight is not None:
+            sample_weight = _check_sample_weight(sample_weight, X, dtype=np.float32)
+        self._all_finite = bool(np.all(np.isfinite(X)))
+        if not self._all_finite:
+            finite_index = np.where(np.isfinite(X).sum(axis=1) == X.shape[1])[0]
+            clean_data = X[finite_index]
+            sample_weight = sample_weight[finite_index] if sample_weight is not None else None
+            internal_to_raw = {x: y for x, y in zip(range(len(finite_index)), finite_index)}
+            outliers = list(set(range(X.shape[0])) - set(finite_index))
+        else:
+            clean_data = X
+        kwargs = self.get_params()
+        (self.labels_, self.probabilities_, self._single_linkage_tree, self._condensed_tree,
+         self._min_spanning_tree, self._neighbors, self._core_distances) = fast_hdbscan(
+            clean_data, None, return_trees=True, sample_weights=sample_weight, **kwargs)
+        self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
+        if not self._all_finite:
+            self._condensed_tree = remap_condensed_tree(self._condensed_tree, internal_to_raw,
+                                                        outliers)
+            self._single_linkage_tree = remap_single_linkage_tree(self._single_linkage_tree,
+                                                                  internal_to_raw, outliers)
+            new_labels = np.full(X.shape[0], -1)
+            new_labels[finite_index] = self.labels_
+            self.labels_ = new_labels
+            new_probabilities = np.zeros(X.shape[0])
+            new_probabilities[finite_index] = self.probabilities_
+            self.probabilities_ = new_probabilities
+        return self
+
+    def fit_predict(self, X, y=None, **kwargs):
+        self.fit(X, y=y, **kwargs)
+        return self.labels_
+
+    def dbscan_clustering(self, epsilon):
+        """hdbscan.py:824."""
+        if not hasattr(self, "_single_linkage_tree"):
+            raise AttributeError("You first need to fit the HDBSCAN model before picking a "
+                                 "DBSCAN clustering")
+        from .cluster_trees import get_cluster_labelling_at_cut
+
+        return get_cluster_labelling_at_cut(
+            self._single_linkage_tree, epsilon,
+            self.min_samples if self.min_samples is not None else self.min_cluster_size)

@@ -107,6 +107,38 @@ int fhg_label_points(const int64_t* parent_dev, const int64_t* child_dev,
                      const int64_t* sel_dev, int64_t n_sel, double epsilon, int64_t n_samples,
                      int64_t* labels_dev, float* probs_dev, void* stream);
 
+/* Replaces cluster_trees.py:369 cluster_tree_leaves(cluster_tree, n_points)
+ * applied to cluster_tree_from_condensed_tree (:672) of the given rows:
+ * leaf clusters in increasing id order.  sel_dev holds up to `rows` ids. */
+int fhg_cluster_tree_leaves(const int64_t* parent_dev, const int64_t* child_dev,
+                            const float* lambda_dev, const float* child_size_dev, int64_t rows,
+                            int64_t* sel_dev, int64_t* n_sel_host, void* stream);
+
+/* Replaces cluster_trees.py:1011 get_point_membership_strength_vector(tree,
+ * clusters, labels) for caller-given labels (int64[n_samples]). */
+int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* child_dev,
+                             const float* lambda_dev, const float* child_size_dev, int64_t rows,
+                             const int64_t* sel_dev, int64_t n_sel, const int64_t* labels_dev,
+                             int64_t n_samples, float* probs_dev, void* stream);
+
+/* The whole fit of hdbscan.py:686 HDBSCAN.fit / :199 fast_hdbscan on device
+ * data (Euclidean, no sample weights): spatial index, kNN core distances,
+ * Boruvka MST and the tree passes, with every intermediate kept in HBM.
+ *   selection_method: 0 = "eom", 1 = "leaf".
+ *   Required outputs: labels_dev (int64[n]), probs_dev (float32[n]).
+ *   Optional outputs (NULL to skip): mst_dev ((n-1) x 3 float64, sorted as
+ *   in hdbscan.py:511), linkage_dev ((n-1) x 4), ct_* (condensed tree, room
+ *   for 2n rows; *ct_rows_host = rows), neighbors_dev (n x max(ms, 1)),
+ *   core_dev (n), selected_dev (room for n ids; *n_selected_host = count). */
+int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                    int64_t min_cluster_size, int32_t selection_method, double max_cluster_size,
+                    int allow_single_cluster, double epsilon, double persistence,
+                    int64_t* labels_dev, float* probs_dev, double* mst_dev, double* linkage_dev,
+                    int64_t* ct_parent_dev, int64_t* ct_child_dev, float* ct_lambda_dev,
+                    float* ct_size_dev, int64_t* ct_rows_host, int32_t* neighbors_dev,
+                    float* core_dev, int64_t* selected_dev, int64_t* n_selected_host,
+                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif
