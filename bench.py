@@ -1,0 +1,344 @@
+#!/usr/bin/env python
+"""HDBSCAN fit throughput on GB300: points/s for one full fit.
+
+Workload: the 10M x 3-D varying-density set (200 Gaussians, std
+log-normal(0, 1), centres U[-100, 100]^3), min_samples=15,
+min_cluster_size=500, seeded synthetic data.  A step is one complete fit
+(spatial index, kNN core distances, Boruvka MST, linkage tree, condensed
+tree, EOM selection, labels and membership strengths).
+
+  value  device-resident: X already in HBM, every output left in HBM.
+  e2e    HDBSCAN(...).fit(X) from pinned host memory, all fitted attributes
+         (labels_, probabilities_, trees, neighbours, core distances) read
+         back to host inside the timed region.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, OpenMP over the reference's parallel loops) on all host cores, on
+a bounded sample of the same workload per step.
+
+Multi-GPU: one process per GPU, each fitting its own independent dataset
+(the fit does not shard without a per-round exchange): weak scaling,
+replicas only.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "HDBSCAN fit points/s at 10M x 3-D (varying density, min_samples=15)"
+WORKLOAD = dict(workload="varying_density_10M_3d", n=10_000_000, d=3, min_samples=15,
+                min_cluster_size=500, seed=3,
+                generator="200 Gaussians, std lognormal(0,1), centres U[-100,100]^3")
+CPU_SAMPLE_N = 1_000_000
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="points (testing only)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_data(n, seed):
+    from fast_hdbscan_gb300 import synthetic
+
+    return synthetic.varying_density(n, seed=seed)
+
+
+# --------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- gb300 arm
+def algorithmic_bytes(stage, n, k, d_pad, rounds, comps):
+    """Minimum HBM bytes per launch of each timed kernel (fixed formulas)."""
+    if stage == "knn":
+        # read every point once (padded float4 + caller index), write the
+        # kNN rows (squared distance + index) in Morton order
+        return n * (4 * d_pad + 4) + n * k * 8
+    if stage == "boruvka_search":
+        # per round: kNN seed rows (index + distance + neighbour component),
+        # each point's coordinates, core, component and index, its candidate
+        # (weight + index), and one 8-byte component key per component
+        per_round = n * k * 12 + n * (4 * d_pad + 4 + 4 + 4 + 8) + 8 * comps / max(rounds, 1)
+        return per_round
+    return None
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from fast_hdbscan_gb300 import _native, build as engine_build
+    from fast_hdbscan_gb300.hdbscan import HDBSCAN
+
+    engine_build.build()
+    lib = _native.load()
+    lib.fhg_launch_count.restype = ctypes.c_uint64
+    lib.fhg_profile_enable.argtypes = [ctypes.c_int]
+    lib.fhg_profile_report.argtypes = [ctypes.c_char_p, ctypes.c_int64]
+
+    n = args.n
+    ms, mcs = WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"]
+    Xh = make_data(n, WORKLOAD["seed"] + rank)
+    d = Xh.shape[1]
+    Xd = torch.from_numpy(Xh).cuda()
+    E = _native.empty
+    labels, probs = E(n, np.int64), E(n, np.float32)
+    mst, linkage = E((n - 1, 3), np.float64), E((n - 1, 4), np.float64)
+    ctp, ctc, ctl, cts = (E(2 * n, np.int64), E(2 * n, np.int64), E(2 * n, np.float32),
+                          E(2 * n, np.float32))
+    nbrs, core, sel = E((n, ms), np.int32), E(n, np.float32), E(n, np.int64)
+    rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
+    V = _native.vptr
+    stream = torch.cuda.current_stream()
+
+    def step():
+        _native.check(lib.fhg_hdbscan_fit(
+            V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, V(labels), V(probs), V(mst),
+            V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core),
+            V(sel), ctypes.byref(nsel), _native.stream_ptr()))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    lib.fhg_profile_report(None, 0)  # drop warm-up records
+    lib.fhg_profile_enable(1)
+    launches0 = lib.fhg_launch_count()
+    with ClockSampler(local) as clocks:
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        barrier()
+    launches = lib.fhg_launch_count() - launches0
+    lib.fhg_profile_enable(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.fhg_profile_report(buf, len(buf))
+    stages = json.loads(buf.value.decode() or "{}")
+    ms_step = ev0.elapsed_time(ev1) / args.steps
+    t = torch.tensor([ms_step], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_step_max = float(t.item())
+    value = n * world / (ms_step_max / 1e3)
+    clock_info = clocks.summary()
+
+    # per-stage share and the dominant kernel's roofline
+    total_stage = sum(v[0] for v in stages.values()) or 1.0
+    kernel_stages = {k: v for k, v in stages.items() if k in ("knn", "boruvka_search")}
+    dom = max(kernel_stages, key=lambda k: kernel_stages[k][0]) if kernel_stages else None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    roofline = None
+    rounds = max(1, stages.get("boruvka_search", [0, 1])[1] // max(args.steps, 1))
+    if dom:
+        tot_ms, cnt = kernel_stages[dom]
+        per_launch_ms = tot_ms / cnt
+        alg = algorithmic_bytes(dom, n, ms + 1, 4 if d <= 4 else 8, rounds, n)
+        achieved = alg / (per_launch_ms / 1e3) / 1e9
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            tj = json.load(open(tpath))
+            ent = tj.get(dom)
+            if ent:
+                traffic = ent["dram_bytes_per_point"] * n
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak,
+                    "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 5),
+                    "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                    "ms_per_launch": round(per_launch_ms, 4)}
+
+    # e2e through the public estimator, pinned host input, outputs to host
+    e2e = None
+    if not args.no_e2e:
+        Xp = torch.from_numpy(Xh).pin_memory()
+        est = HDBSCAN(min_cluster_size=mcs, min_samples=ms)
+        est.fit(Xp)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            est.fit(Xp)
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        tt = torch.tensor([e2e_s], device="cuda")
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+        rows_out = est._condensed_tree.shape[0]
+        d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 24 + n * ms * 4 + n * 4)
+        e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",
+               "h2d_bytes_per_step": int(n * d * 4), "d2h_bytes_per_step": int(d2h),
+               "s_per_step": round(e2e_s, 4)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(args.cpu_sample)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 1), "unit": "points/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step_max, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator of the benchmark workload)",
+            "config": {**{k: v for k, v in WORKLOAD.items() if k != "n"}, "n": n,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs and working set (several GB) larger than the 129 MB L2"},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": int(launches),
+            "clocks": clock_info,
+            "stages_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in stages.items()},
+            "stage_share": {k: round(v[0] / total_stage, 4) for k, v in stages.items()},
+            "boruvka_rounds": rounds,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------- CPU baseline
+def _oracle_fit_time(n, nthreads):
+    from oracle import oracle as O
+
+    X = make_data(n, WORKLOAD["seed"])
+    t0 = time.perf_counter()
+    O.fit(X, WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"], mode=0, nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline_sample(n_sample):
+    cores = os.cpu_count() or 1
+    t = _oracle_fit_time(n_sample, cores)
+    return {"value": round(n_sample / t, 1), "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": f"{n_sample} points of the same generator, one fit, {t:.2f} s",
+            "what": "C/OpenMP restatement of the reference fit path (oracle/), reference "
+                    "tie mode; numba is not installed on this machine"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n_sample = args.cpu_sample
+    for _ in range(args.warmup):
+        _oracle_fit_time(n_sample, cores)
+    times = [_oracle_fit_time(n_sample, cores) for _ in range(args.steps)]
+    s = sum(times) / len(times)
+    value = n_sample / s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "points/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(s * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator of the benchmark workload)",
+        "config": {**{k: v for k, v in WORKLOAD.items() if k != "n"}, "n": n_sample,
+                   "sample_of_n": WORKLOAD["n"]},
+        "cpu_baseline": {"value": round(value, 1), "unit": "points/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{n_sample}-point sample of the workload per step"},
+        "e2e": {"value": round(value, 1), "unit": "points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

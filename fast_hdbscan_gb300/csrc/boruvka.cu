@@ -29,6 +29,8 @@
 #include "primitives.cuh"
 #include "uf.cuh"
 
+#include <memory>
+
 namespace fhg {
 namespace {
 
@@ -465,6 +467,7 @@ template <int P>
 int launch_search(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
                   const float* core2, const int32_t* comp, const int32_t* nc,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
+    ::fhg::note_launch();
     search_kernel<P><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
         view_of(ix), k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q);
     FHG_CUDA(cudaGetLastError());
@@ -474,6 +477,7 @@ int launch_search(const fhg_index& ix, int k, const int32_t* knn_s, const float*
 #define LAUNCH(kernel, count, ...)                                                   \
     do {                                                                             \
         if ((count) > 0) {                                                           \
+            ::fhg::note_launch(); \
             kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);              \
             FHG_CUDA(cudaGetLastError());                                            \
         }                                                                            \
@@ -533,6 +537,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_CUDA(cudaMemsetAsync(iflag, 0, 2 * sizeof(int), s));
 
     // ---- round 0: kNN-seeded links (boruvka.py:474)
+    std::unique_ptr<Stage> r0_stage(new Stage(s, "boruvka_round0"));
     LAUNCH(round0_kernel, n, n, k, knn_s, knn_d, core2, target, w0, iflag);
     int h_flag[2] = {0, 0};
     FHG_CUDA(cudaMemcpyAsync(h_flag, iflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -573,6 +578,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     LAUNCH(compact_kernel, n, n, flag, pos, (const int32_t*)nullptr, reps);
     uint32_t h_ncomp = 0;
     FHG_CUDA(cudaMemcpyAsync(&h_ncomp, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    r0_stage.reset();
     FHG_CUDA(cudaStreamSynchronize(s));
     int64_t ncomp = h_ncomp;
 
@@ -594,15 +600,21 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
                       (long long)ncomp);
             return FHG_ERR_NO_CONVERGENCE;
         }
-        // node_comp (boruvka.py:98-124), bottom-up
-        LAUNCH(node_comp_leaf_kernel, ix.slots * 32, comp, n, ix.nleaves, ix.slots, nc);
-        for (int64_t width = ix.slots / 2; width >= 1; width /= 2)
-            LAUNCH(node_comp_level_kernel, width, nc, width - 1, width);
-        LAUNCH(reset_keys_kernel, ncomp, reps, ncomp, keyA, keyB, winner, par);
-        FHG_TRY(ix.pad == 4 ? launch_search<4>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w,
-                                              cand_q, s)
-                            : launch_search<8>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w,
-                                              cand_q, s));
+        {  // node_comp (boruvka.py:98-124), bottom-up
+            Stage stage(s, "boruvka_nodes");
+            LAUNCH(node_comp_leaf_kernel, ix.slots * 32, comp, n, ix.nleaves, ix.slots, nc);
+            for (int64_t width = ix.slots / 2; width >= 1; width /= 2)
+                LAUNCH(node_comp_level_kernel, width, nc, width - 1, width);
+            LAUNCH(reset_keys_kernel, ncomp, reps, ncomp, keyA, keyB, winner, par);
+        }
+        {
+            Stage stage(s, "boruvka_search");
+            FHG_TRY(ix.pad == 4 ? launch_search<4>(ix, k, knn_s, knn_d, core2, comp, nc, keyA,
+                                                  cand_w, cand_q, s)
+                                : launch_search<8>(ix, k, knn_s, knn_d, core2, comp, nc, keyA,
+                                                  cand_w, cand_q, s));
+        }
+        Stage merge_stage(s, "boruvka_merge");
         LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);
         LAUNCH(stage_c_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB, winner);
         FHG_CUDA(cudaMemsetAsync(iflag + 1, 0, sizeof(int), s));

@@ -1,5 +1,8 @@
 // extern "C" entry points of libfhg.so (declared in include/fhg.h).
+#include <atomic>
 #include <cstdarg>
+#include <map>
+#include <mutex>
 
 #include "index.cuh"
 #include "mst.cuh"
@@ -23,6 +26,41 @@ const char* last_error() { return g_last_error.c_str(); }
 
 int finalize_edges(const MstResult& r, double* edges, cudaStream_t s);
 
+// ---------------------------------------------------------------- tracing
+static std::atomic<uint64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+struct StageRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
+std::vector<StageRec> g_prof;
+}  // namespace
+
+Stage::Stage(cudaStream_t s, const char* name) : s_(s), name_(name) {
+    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    if (cudaEventCreate(&a_) != cudaSuccess) {
+        a_ = nullptr;
+        return;
+    }
+    cudaEventRecord(a_, s_);
+}
+
+Stage::~Stage() {
+    if (!a_) return;
+    cudaEvent_t b;
+    if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a_);
+        return;
+    }
+    cudaEventRecord(b, s_);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof.push_back(StageRec{name_, a_, b});
+}
+
 }  // namespace fhg
 
 using namespace fhg;
@@ -33,6 +71,52 @@ static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStre
 
 FHG_API const char* fhg_last_error(void) { return last_error(); }
 FHG_API int fhg_abi_version(void) { return 1; }
+
+FHG_API uint64_t fhg_launch_count(void) { return g_launches.load(); }
+
+FHG_API int fhg_profile_enable(int on) {
+    g_prof_on.store(on != 0);
+    return FHG_OK;
+}
+
+FHG_API int fhg_profile_report(char* buf, int64_t cap) {
+    std::vector<StageRec> recs;
+    {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        recs.swap(g_prof);
+    }
+    std::map<std::string, std::pair<double, int64_t>> agg;
+    int rc = FHG_OK;
+    for (auto& r : recs) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) {
+            set_error("profile: event timing failed");
+            rc = FHG_ERR_CUDA;
+        }
+        auto& e = agg[r.name];
+        e.first += ms;
+        e.second += 1;
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    std::string out = "{";
+    bool first = true;
+    for (auto& kv : agg) {
+        char item[256];
+        snprintf(item, sizeof item, "%s\"%s\": [%.6f, %lld]", first ? "" : ", ", kv.first.c_str(),
+                 kv.second.first, (long long)kv.second.second);
+        out += item;
+        first = false;
+    }
+    out += "}";
+    if (buf && cap > 0) {
+        size_t n = out.size() < (size_t)(cap - 1) ? out.size() : (size_t)(cap - 1);
+        memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    }
+    return rc;
+}
 
 FHG_API int fhg_index_build(const float* X_dev, int64_t n, int32_t d, void* stream,
                             fhg_index** out) {
@@ -92,7 +176,8 @@ FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples, double* edg
 }
 
 // ------------------------------------------------------------- tree passes
-namespace {
+namespace fhg {
+namespace capi {
 
 __global__ void widen_sel_kernel(int64_t k, const int32_t* __restrict__ a, int64_t* __restrict__ b) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,7 +204,9 @@ int check_ptrs(const char* fn, std::initializer_list<const void*> ps) {
     return FHG_OK;
 }
 
-}  // namespace
+}  // namespace capi
+}  // namespace fhg
+using namespace fhg::capi;
 
 FHG_API int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream) {
     if (m <= 0) return FHG_OK;
@@ -191,6 +278,7 @@ FHG_API int fhg_extract_eom_clusters(const int64_t* parent_dev, const int64_t* c
     int64_t k = 0;
     FHG_TRY(select_eom(ws, ct, max_cluster_size, allow_single_cluster != 0, sel, &k));
     if (k > 0) {
+        ::fhg::note_launch();
         widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, sel, sel_dev);
         FHG_CUDA(cudaGetLastError());
     }
@@ -207,6 +295,7 @@ FHG_API int fhg_label_points(const int64_t* parent_dev, const int64_t* child_dev
     FHG_TRY(check_ptrs("fhg_label_points", {labels_dev, probs_dev}));
     cudaStream_t s = as_stream(stream);
     if (rows <= 0 || n_sel <= 0) {
+        ::fhg::note_launch();
         fill_labels_kernel<<<grid_for(n_samples, 256), 256, 0, s>>>(n_samples, labels_dev, probs_dev);
         FHG_CUDA(cudaGetLastError());
         return FHG_OK;
@@ -223,6 +312,7 @@ FHG_API int fhg_label_points(const int64_t* parent_dev, const int64_t* child_dev
     }
     int32_t* sel;
     FHG_TRY(ws.alloc(&sel, (size_t)n_sel));
+    ::fhg::note_launch();
     narrow_sel_kernel<<<grid_for(n_sel, 256), 256, 0, s>>>(n_sel, sel_dev, sel);
     FHG_CUDA(cudaGetLastError());
     return label_points(ws, ct, sel, n_sel, epsilon, labels_dev, probs_dev);
@@ -246,6 +336,7 @@ FHG_API int fhg_cluster_tree_leaves(const int64_t* parent_dev, const int64_t* ch
     int64_t k = 0;
     FHG_TRY(select_leaf(ws, ct, sel, &k));
     if (k > 0) {
+        ::fhg::note_launch();
         widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, sel, sel_dev);
         FHG_CUDA(cudaGetLastError());
     }
@@ -275,6 +366,7 @@ FHG_API int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* c
     }
     int32_t* sel;
     FHG_TRY(ws.alloc(&sel, (size_t)n_sel));
+    ::fhg::note_launch();
     narrow_sel_kernel<<<grid_for(n_sel, 256), 256, 0, s>>>(n_sel, sel_dev, sel);
     FHG_CUDA(cudaGetLastError());
     return membership_strengths(ws, ct, sel, n_sel, labels_dev, probs_dev);
@@ -324,8 +416,11 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     }
     Linkage lk;
     FHG_TRY(sort_and_link(ws, n, mst.src, mst.dst, nullptr, mst.w2, &lk));
-    if (mst_dev) FHG_TRY(sorted_mst_to_f64(lk, mst_dev, s));
-    if (linkage_dev) FHG_TRY(linkage_to_f64(lk, linkage_dev, s));
+    {
+        Stage stage(s, "outputs");
+        if (mst_dev) FHG_TRY(sorted_mst_to_f64(lk, mst_dev, s));
+        if (linkage_dev) FHG_TRY(linkage_to_f64(lk, linkage_dev, s));
+    }
     Condensed ct;
     // hdbscan.py:521: the fit path condenses without max_cluster_size; only
     // the EOM selection reads it.
@@ -340,10 +435,12 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     else FHG_TRY(select_leaf(ws, ct, sel, &k));
     if (n_selected_host) *n_selected_host = k;
     if (selected_dev && k > 0) {
+        ::fhg::note_launch();
         widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, sel, selected_dev);
         FHG_CUDA(cudaGetLastError());
     }
     if (k == 0 || ct.rows == 0) {
+        ::fhg::note_launch();
         fill_labels_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, labels_dev, probs_dev);
         FHG_CUDA(cudaGetLastError());
         return FHG_OK;

@@ -280,6 +280,7 @@ __global__ void condensed_out_kernel(int64_t rows, const int32_t* __restrict__ p
 #define LAUNCH(kernel, count, ...)                                          \
     do {                                                                    \
         if ((count) > 0) {                                                  \
+            ::fhg::note_launch(); \
             kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);     \
             FHG_CUDA(cudaGetLastError());                                   \
         }                                                                   \
@@ -300,6 +301,7 @@ int condense_tree(Workspace& ws, const Linkage& lk, int64_t mcs, double max_cs, 
     *out = Condensed();
     out->n = n;
     if (m <= 0) return FHG_OK;
+    Stage stage(s, "condense");
     const int64_t nodes = n + m;
 
     int8_t *kase, *cont, *birth, *side, *emit_part;

@@ -16,6 +16,24 @@ namespace fhg {
 void set_error(const char* fmt, ...);
 const char* last_error();
 
+// Counts every kernel launch made by the library (read by fhg_launch_count).
+void note_launch();
+
+// Per-stage timer: when profiling is on (fhg_profile_enable), records a pair
+// of CUDA events on the stage's stream; fhg_profile_report sums them by name.
+class Stage {
+  public:
+    Stage(cudaStream_t s, const char* name);
+    ~Stage();
+    Stage(const Stage&) = delete;
+    Stage& operator=(const Stage&) = delete;
+
+  private:
+    cudaStream_t s_;
+    const char* name_;
+    cudaEvent_t a_ = nullptr;
+};
+
 // A status carried through the host driver code.  Device kernels never trap:
 // bounded loops report through a device status word instead.
 struct Status {

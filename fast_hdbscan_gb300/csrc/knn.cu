@@ -142,6 +142,7 @@ template <int P, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
                cudaStream_t s) {
     unsigned g = grid_for(ix.nleaves, kKnnWarps);
+    ::fhg::note_launch();
     knn_kernel<P, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
@@ -168,6 +169,7 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
         set_error("knn: distance and index outputs must be given together");
         return FHG_ERR_INVALID;
     }
+    Stage stage(s, "knn");
     return ix.pad == 4 ? dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, s)
                        : dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, s);
 }

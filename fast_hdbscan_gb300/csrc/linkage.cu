@@ -151,6 +151,7 @@ __global__ void sorted_mst_f64_kernel(int64_t m, const int32_t* __restrict__ ssr
 #define LAUNCH(kernel, count, ...)                                          \
     do {                                                                    \
         if ((count) > 0) {                                                  \
+            ::fhg::note_launch(); \
             kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);     \
             FHG_CUDA(cudaGetLastError());                                   \
         }                                                                   \
@@ -186,6 +187,7 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     LAUNCH(iota_kernel, m, perm, m);
     const int ibits = bits_for(n);
     if (!presorted) {
+        Stage stage(s, "mst_sort");
         Workspace tmp(s);
         LAUNCH(gather_key32_kernel, m, dst, perm, k32, m);
         FHG_TRY(radix_sort_u32(tmp, k32, perm, m, 0, ibits));
@@ -204,6 +206,7 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     LAUNCH(apply_perm_kernel, m, perm, src, dst, w, w2, out->ssrc, out->sdst, out->w, A, B, m);
 
     // ---- rank-halving contraction
+    Stage stage(s, "linkage");
     int64_t S = 1;
     while (S < m) S *= 2;
     int lev = 0;

@@ -82,15 +82,18 @@ int scan_exclusive(Workspace& ws, const T* in, T* out, int64_t n, T* total) {
     }
     int64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles == 1) {
+        ::fhg::note_launch();
         scan_tile_kernel<T><<<1, kScanThreads, 0, s>>>(in, out, total, n);
         FHG_CUDA(cudaGetLastError());
         return FHG_OK;
     }
     T* sums;
     FHG_TRY(ws.alloc(&sums, (size_t)tiles));
+    ::fhg::note_launch();
     scan_tile_kernel<T><<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, sums, n);
     FHG_CUDA(cudaGetLastError());
     FHG_TRY(scan_exclusive<T>(ws, sums, sums, tiles, total));
+    ::fhg::note_launch();
     scan_add_kernel<T><<<grid_for(n, 256), 256, 0, s>>>(out, sums, n);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
@@ -190,9 +193,11 @@ int radix_sort(Workspace& ws, K* keys, int32_t* vals, int64_t n, int begin_bit, 
     K *ka = keys, *kb = kalt;
     int32_t *va = vals, *vb = valt;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
+        ::fhg::note_launch();
         rs_hist_kernel<K><<<(unsigned)tiles, kRsThreads, 0, s>>>(ka, n, shift, hist, tiles);
         FHG_CUDA(cudaGetLastError());
         FHG_TRY(scan_exclusive<uint32_t>(ws, hist, hist, 256 * tiles, nullptr));
+        ::fhg::note_launch();
         rs_scatter_kernel<K><<<(unsigned)tiles, kRsThreads, 0, s>>>(ka, va, kb, vb, n, shift,
                                                                    hist, tiles);
         FHG_CUDA(cudaGetLastError());
@@ -231,6 +236,7 @@ int radix_sort_u32(Workspace& ws, uint32_t* keys, int32_t* vals, int64_t n, int 
 }
 int fill_iota_i32(int32_t* p, int64_t n, cudaStream_t s) {
     if (n <= 0) return FHG_OK;
+    ::fhg::note_launch();
     iota_kernel<<<grid_for(n, 256), 256, 0, s>>>(p, n);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;

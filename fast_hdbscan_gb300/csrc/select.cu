@@ -365,6 +365,7 @@ __global__ void fill_i32_kernel(int32_t* a, int64_t n, int32_t v) {
 #define LAUNCH(kernel, count, ...)                                          \
     do {                                                                    \
         if ((count) > 0) {                                                  \
+            ::fhg::note_launch(); \
             kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);     \
             FHG_CUDA(cudaGetLastError());                                   \
         }                                                                   \
@@ -473,6 +474,7 @@ int select_eom(Workspace& ws, const Condensed& ct, double max_cs, bool allow_sin
     cudaStream_t s = ws.stream();
     *n_sel = 0;
     if (ct.rows == 0) return FHG_OK;
+    Stage stage(s, "select");
     Prepared P;
     FHG_TRY(prepare(ws, ct, &P));
     const int64_t C = P.C;
@@ -491,6 +493,7 @@ int select_eom(Workspace& ws, const Condensed& ct, double max_cs, bool allow_sin
     FHG_TRY(ws.alloc(&chose, (size_t)C));
     FHG_TRY(ws.alloc(&blocked, (size_t)C));
     FHG_TRY(ws.alloc(&nsel_dev, 1));
+    ::fhg::note_launch();
     eom_kernel<<<1, kEomThreads, 0, s>>>(C, P.cpar, P.nsize, P.in_tree, P.score, P.cstart, P.ccnt,
                                          P.corder, ct.csize, ct.child, ct.n, max_cs,
                                          allow_single ? 1 : 0, depth, depth2, jmp, jmp2, dcount,
@@ -511,6 +514,7 @@ int select_leaf(Workspace& ws, const Condensed& ct, int32_t* sel, int64_t* n_sel
     int64_t* nsel_dev;
     FHG_TRY(ws.alloc(&flags, (size_t)P.C));
     FHG_TRY(ws.alloc(&nsel_dev, 1));
+    ::fhg::note_launch();
     leaf_kernel<<<1, kEomThreads, 0, s>>>(P.C, ct.n, P.cpar, P.in_tree, flags, sel, nsel_dev);
     FHG_CUDA(cudaGetLastError());
     FHG_CUDA(cudaMemcpyAsync(n_sel, nsel_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -522,6 +526,7 @@ int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t
                  double eps, int64_t* labels, float* probs) {
     cudaStream_t s = ws.stream();
     const int64_t n = ct.n, rows = ct.rows, C = ct.n_clusters;
+    Stage stage(s, "labels");
     FHG_CUDA(cudaMemsetAsync(probs, 0, sizeof(float) * n, s));
     if (rows == 0 || n_sel == 0) {
         LAUNCH(fill_i64_kernel, n, labels, n, (int64_t)-1);

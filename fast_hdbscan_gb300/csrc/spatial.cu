@@ -142,10 +142,12 @@ __global__ void level_box_kernel(float* __restrict__ box, int64_t first, int64_t
 template <int P>
 int build_boxes(fhg_index* ix, cudaStream_t s) {
     unsigned g = grid_for(ix->slots * 32, 256);
+    ::fhg::note_launch();
     leaf_box_kernel<P><<<g, 256, 0, s>>>(ix->pts, ix->n, ix->nleaves, ix->slots, ix->box);
     FHG_CUDA(cudaGetLastError());
     for (int64_t width = ix->slots / 2; width >= 1; width /= 2) {
         int64_t first = width - 1;
+        ::fhg::note_launch();
         level_box_kernel<P><<<grid_for(width, 256), 256, 0, s>>>(ix->box, first, width);
         FHG_CUDA(cudaGetLastError());
     }
@@ -182,6 +184,7 @@ int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index*
         set_error("index_build: n must be below 2^31");
         return FHG_ERR_INVALID;
     }
+    Stage stage(s, "index_build");
     fhg_index* ix = new fhg_index();
     ix->n = n;
     ix->d = d;
@@ -204,9 +207,12 @@ int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index*
         if (rc == FHG_OK) rc = ws.alloc(&bb, 16);
         if (rc == FHG_OK) rc = ws.alloc(&keys, (size_t)n);
         if (rc == FHG_OK) {
+            ::fhg::note_launch();
             bbox_partial_kernel<<<nb, kBBThreads, 0, s>>>(X, n, d, partial);
+            ::fhg::note_launch();
             bbox_final_kernel<<<1, 32, 0, s>>>(partial, nb, bb);
             int bits = std::min(63 / d, 31);
+            ::fhg::note_launch();
             morton_kernel<<<grid_for(n, 256), 256, 0, s>>>(X, n, d, bb, bits, keys, ix->orig);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
@@ -217,6 +223,7 @@ int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index*
             }
         }
         if (rc == FHG_OK) {
+            ::fhg::note_launch();
             gather_points_kernel<<<grid_for(n, 256), 256, 0, s>>>(X, n, d, ix->pad, ix->orig,
                                                                   ix->pts, ix->rank);
             cudaError_t e = cudaGetLastError();

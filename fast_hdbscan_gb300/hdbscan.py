@@ -81,6 +81,22 @@ def check_array(X, ensure_all_finite=True, dtype="numeric"):
     return arr
 
 
+def _is_tensor(X):
+    mod = type(X).__module__
+    return mod.startswith("torch") and hasattr(X, "is_cuda")
+
+
+def _tensor_input(X):
+    """A 2-D float32 CUDA copy of a torch tensor (asynchronous from pinned
+    host memory) and whether every value is finite (checked on the device)."""
+    import torch
+
+    if X.dim() != 2:
+        raise ValueError(f"Expected 2D array, got {X.dim()}D array instead")
+    Xd = X.to(device="cuda", dtype=torch.float32, non_blocking=True).contiguous()
+    return Xd, bool(torch.isfinite(Xd).all().item())
+
+
 def _check_sample_weight(sample_weight, X, dtype):
     """hdbscan.py:43 simplified check (shape and non-zero)."""
     n = X.shape[0]
@@ -257,8 +273,11 @@ def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc
                  sample_weights=None, reproducible=False, return_trees=False,
                  metric="euclidean", algorithm="boruvka", knn_k=None, cannot_link=None,
                  validate_cannot_link=True, cannot_link_groups=None, metric_kwds=None):
-    """hdbscan.py:199 fast_hdbscan on the GPU engine."""
-    if metric == "euclidean":
+    """hdbscan.py:199 fast_hdbscan on the GPU engine.  Besides NumPy input,
+    `data` may be a torch tensor (CUDA, or pinned host memory) of finite values."""
+    if _is_tensor(data):
+        pass
+    elif metric == "euclidean":
         data = check_array(data)
         if sample_weights is not None:
             sample_weights = _check_sample_weight(sample_weights, data, dtype=np.float32)
@@ -377,6 +396,18 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
         """hdbscan.py:686: validation, non-finite row filter, GPU fit, remap."""
         if self.metric == "precomputed" or self.semi_supervised:
             raise NotImplementedError("precomputed and semi-supervised fits are not on the GPU path")
+        if _is_tensor(X):
+            Xd, finite = _tensor_input(X)
+            if finite and sample_weight is None:
+                self._raw_data = X
+                self._all_finite = True
+                kwargs = self.get_params()
+                (self.labels_, self.probabilities_, self._single_linkage_tree,
+                 self._condensed_tree, self._min_spanning_tree, self._neighbors,
+                 self._core_distances) = fast_hdbscan(Xd, None, return_trees=True, **kwargs)
+                self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
+                return self
+            X = Xd.cpu().numpy()
         X = check_array(X, ensure_all_finite=False)
         self._raw_data = X
         if sample_weight is not None:

@@ -41,6 +41,15 @@ const char* fhg_last_error(void);
 /* ABI version of this library (bumped when a signature changes). */
 int fhg_abi_version(void);
 
+/* Tracing (no counterpart in the reference, whose benchmark harness times
+ * whole calls with perf_counter).  fhg_launch_count: kernels launched by this
+ * library since load.  fhg_profile_enable(1): every stage records a pair of
+ * CUDA events on its stream.  fhg_profile_report: waits for those events and
+ * writes {"stage": [total_ms, count], ...} as JSON into buf, then clears them. */
+uint64_t fhg_launch_count(void);
+int fhg_profile_enable(int on);
+int fhg_profile_report(char* buf, int64_t cap);
+
 /* Opaque spatial index: points sorted along a Morton curve into buckets of
  * 32 with a complete binary tree of bounding boxes over the buckets. */
 typedef struct fhg_index fhg_index;
