@@ -58,53 +58,65 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
         bs[j] = -1;
     }
 
+    // Candidates of one bucket: lane t holds candidate t, broadcast by shuffle.
+    auto scan_leaf = [&](int64_t lf, bool need) {
+        const int64_t base = lf * kLeaf;
+        const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
+        float c[P];
+        int32_t co = INT32_MAX;
+        if (lane < cnt) {
+            load_pt<P>(ix.pts, base + lane, c);
+            co = __ldg(ix.orig + base + lane);
+        } else {
+#pragma unroll
+            for (int j = 0; j < P; ++j) c[j] = 0.0f;
+        }
+        for (int t = 0; t < cnt; ++t) {
+            float cc[P];
+#pragma unroll
+            for (int j = 0; j < P; ++j) cc[j] = __shfl_sync(kFull, c[j], t);
+            const int32_t o = __shfl_sync(kFull, co, t);
+            const float dd = rdist_rn<P>(q, cc);
+            if (need && (dd < bd[K - 1] || (dd == bd[K - 1] && o < bo[K - 1]))) {
+                bd[K - 1] = dd;
+                bo[K - 1] = o;
+                bs[K - 1] = (int32_t)(base + t);
+#pragma unroll
+                for (int j = K - 1; j > 0; --j) {
+                    const bool sw = bd[j] < bd[j - 1] || (bd[j] == bd[j - 1] && bo[j] < bo[j - 1]);
+                    if (sw) {
+                        float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
+                        int32_t ti = bo[j]; bo[j] = bo[j - 1]; bo[j - 1] = ti;
+                        ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
+                    }
+                }
+            }
+        }
+    };
+
+    // Seed with the warp's own bucket (it holds the queries themselves), so
+    // that the walk below starts with a tight k-th distance; the walk then
+    // skips this bucket.
+    scan_leaf(leaf, valid);
+
     int32_t* st = s_stack[warp];
     int sp = 1;
     if (lane == 0) st[0] = 0;
     __syncwarp();
     const int64_t first_leaf_node = ix.slots - 1;
+    const int64_t home_node = first_leaf_node + leaf;
     while (sp > 0) {
         --sp;
         const int32_t node = st[sp];
         __syncwarp();
+        if (node == home_node) continue;
         float b[2 * P];
         load_box<P>(ix.box, node, b);
         const float lb = box_lb<P>(b, q);
         const bool need = valid && lb <= bd[K - 1];
         if (!__any_sync(kFull, need)) continue;
         if (node >= first_leaf_node) {
-            const int64_t base = (int64_t)(node - first_leaf_node) * kLeaf;
-            const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
-            float c[P];
-            int32_t co = INT32_MAX;
-            if (lane < cnt) {
-                load_pt<P>(ix.pts, base + lane, c);
-                co = __ldg(ix.orig + base + lane);
-            } else {
-#pragma unroll
-                for (int j = 0; j < P; ++j) c[j] = 0.0f;
-            }
-            for (int t = 0; t < cnt; ++t) {
-                float cc[P];
-#pragma unroll
-                for (int j = 0; j < P; ++j) cc[j] = __shfl_sync(kFull, c[j], t);
-                const int32_t o = __shfl_sync(kFull, co, t);
-                const float dd = rdist_rn<P>(q, cc);
-                if (need && (dd < bd[K - 1] || (dd == bd[K - 1] && o < bo[K - 1]))) {
-                    bd[K - 1] = dd;
-                    bo[K - 1] = o;
-                    bs[K - 1] = (int32_t)(base + t);
-#pragma unroll
-                    for (int j = K - 1; j > 0; --j) {
-                        const bool sw = bd[j] < bd[j - 1] || (bd[j] == bd[j - 1] && bo[j] < bo[j - 1]);
-                        if (sw) {
-                            float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
-                            int32_t ti = bo[j]; bo[j] = bo[j - 1]; bo[j - 1] = ti;
-                            ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
-                        }
-                    }
-                }
-            }
+            scan_leaf(node - first_leaf_node, need);
         } else {
             const int32_t l = 2 * node + 1, r = l + 1;
             float bl[2 * P], br[2 * P];
