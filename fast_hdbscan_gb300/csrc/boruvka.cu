@@ -217,29 +217,43 @@ __global__ void reset_keys_kernel(const int32_t* __restrict__ reps, int64_t nrep
 }
 
 // ------------------------------------------------------- per round: search
-template <int P>
+// One warp per bucket of 32 query points, as in the kNN kernel.  A node is
+// entered when some lane's point lies outside the node's single component
+// (node_comp) and within that lane's threshold -- the smaller of its own best
+// weight and its component's running best (boruvka.py:182-191).  Candidates
+// of a leaf are staged in shared memory; a candidate in the query's own
+// component, or with a core distance above the threshold, costs one compare.
+template <int DIM, int SP>
 __global__ void __launch_bounds__(kSW * 32) search_kernel(
     IndexView ix, int k, const int32_t* __restrict__ knn_s, const float* __restrict__ knn_d,
     const float* __restrict__ core2, const int32_t* __restrict__ comp,
     const int32_t* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
     int32_t* __restrict__ cand_q) {
     __shared__ int32_t s_stack[kSW][kStack];
+    __shared__ float4 s_xyz[kSW][32 * (SP / 4)];
+    __shared__ int2 s_cc[kSW][32];      // (component, core bits)
+    __shared__ int32_t s_orig[kSW][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t leaf = (int64_t)blockIdx.x * kSW + warp;
     if (leaf >= ix.nleaves) return;
     const int64_t p = leaf * kLeaf + lane;
     const bool valid = p < ix.n;
-    float q[P];
+    float q[DIM];
     int32_t c = -3, op = 0;
     float cp = 0.0f;
-    if (valid) {
-        load_pt<P>(ix.pts, p, q);
-        c = comp[p];
-        op = ix.orig[p];
-        cp = core2[p];
-    } else {
+    {
+        float t[SP];
+        if (valid) {
+            load_pt<SP>(ix.pts, p, t);
+            c = comp[p];
+            op = ix.orig[p];
+            cp = core2[p];
+        } else {
 #pragma unroll
-        for (int j = 0; j < P; ++j) q[j] = 0.0f;
+            for (int j = 0; j < SP; ++j) t[j] = 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) q[j] = t[j];
     }
     float bw = INFINITY;
     int32_t bq = -1, bo = INT32_MAX;
@@ -266,58 +280,42 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     if (valid) thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
     bool active = valid && !(cp > thr);
 
-    float ctr[P];
+    float ctr[DIM];
     {
-        float b[2 * P];
-        load_box<P>(ix.box, ix.slots - 1 + leaf, b);
+        float b[2 * SP];
+        load_box<SP>(ix.box, ix.slots - 1 + leaf, b);
 #pragma unroll
-        for (int j = 0; j < P; ++j) ctr[j] = 0.5f * (b[j] + b[P + j]);
+        for (int j = 0; j < DIM; ++j) ctr[j] = 0.5f * (b[j] + b[SP + j]);
     }
-    int32_t* st = s_stack[warp];
-    int sp = 0;
-    if (__any_sync(kFull, active)) {
-        if (lane == 0) st[0] = 0;
-        sp = 1;
-    }
-    __syncwarp();
-    const int64_t first_leaf_node = ix.slots - 1;
-    while (sp > 0) {
-        --sp;
-        const int32_t node = st[sp];
-        __syncwarp();
-        const int32_t ncn = nc[node];
-        bool need = active && ncn != c && ncn != kEmpty;
-        if (need) {
-            float b[2 * P];
-            load_box<P>(ix.box, node, b);
-            need = box_lb<P>(b, q) <= thr;
+    float4* xyz = s_xyz[warp];
+    int2* cc = s_cc[warp];
+    int32_t* co = s_orig[warp];
+
+    auto scan_leaf = [&](int64_t lf, bool need) {
+        const int64_t base = lf * kLeaf;
+        const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
+        if (lane < cnt) {
+            const float4* src = reinterpret_cast<const float4*>(ix.pts) + (base + lane) * (SP / 4);
+#pragma unroll
+            for (int h = 0; h < SP / 4; ++h) xyz[lane * (SP / 4) + h] = __ldg(src + h);
+            cc[lane] = make_int2(comp[base + lane], __float_as_int(core2[base + lane]));
+            co[lane] = ix.orig[base + lane];
         }
-        if (!__any_sync(kFull, need)) continue;
-        if (node >= first_leaf_node) {
-            const int64_t base = (int64_t)(node - first_leaf_node) * kLeaf;
-            const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
-            float cc[P];
-            int32_t ccomp = -4, co = INT32_MAX;
-            float ccore = INFINITY;
-            if (lane < cnt) {
-                load_pt<P>(ix.pts, base + lane, cc);
-                ccomp = comp[base + lane];
-                co = ix.orig[base + lane];
-                ccore = core2[base + lane];
-            } else {
+        __syncwarp();
+        for (int t = 0; t < cnt; ++t) {
+            const int2 tcc = cc[t];
+            const float tk = __int_as_float(tcc.y);
+            if (need && tcc.x != c && tk <= thr) {
+                float x[SP];
 #pragma unroll
-                for (int j = 0; j < P; ++j) cc[j] = 0.0f;
-            }
-            for (int t = 0; t < cnt; ++t) {
-                float x[P];
-#pragma unroll
-                for (int j = 0; j < P; ++j) x[j] = __shfl_sync(kFull, cc[j], t);
-                const int32_t tc = __shfl_sync(kFull, ccomp, t);
-                const int32_t to = __shfl_sync(kFull, co, t);
-                const float tk = __shfl_sync(kFull, ccore, t);
-                if (need && tc != c && tk <= thr) {
-                    float w = fmaxf(fmaxf(rdist_rn<P>(q, x), cp), tk);
-                    if (w < bw || (w == bw && to < bo)) {
+                for (int h = 0; h < SP / 4; ++h) {
+                    float4 v = xyz[t * (SP / 4) + h];
+                    x[4 * h] = v.x; x[4 * h + 1] = v.y; x[4 * h + 2] = v.z; x[4 * h + 3] = v.w;
+                }
+                const float w = fmaxf(fmaxf(rdist_rn<DIM>(q, x), cp), tk);
+                if (w <= bw) {
+                    const int32_t to = co[t];
+                    if (w < bw || to < bo) {
                         bw = w;
                         bq = (int32_t)(base + t);
                         bo = to;
@@ -325,24 +323,60 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
                     }
                 }
             }
-            if (active) {
-                thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
-                active = !(cp > thr);
-            }
-        } else {
-            const int32_t l = 2 * node + 1, r = l + 1;
-            float bl[2 * P], br[2 * P];
-            load_box<P>(ix.box, l, bl);
-            load_box<P>(ix.box, r, br);
-            const float ll = box_lb<P>(bl, ctr), lr = box_lb<P>(br, ctr);
-            const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
-            if (lane == 0) {
-                st[sp] = far;
-                st[sp + 1] = near;
-            }
-            sp += 2;
-            __syncwarp();
         }
+        __syncwarp();
+        if (active) {
+            thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
+            active = !(cp > thr);
+        }
+    };
+
+    const int64_t first_leaf_node = ix.slots - 1;
+    const int64_t home_node = first_leaf_node + leaf;
+    // A home bucket spanning several components holds the nearest candidates.
+    const int32_t home_nc = nc[home_node];
+    const bool home_first = home_nc == kMixed;
+    if (home_first && __any_sync(kFull, active)) scan_leaf(leaf, active);
+
+    // Walk up from the home bucket to the root, searching the sibling subtree
+    // at every ancestor (nearest subtrees first).
+    int32_t* st = s_stack[warp];
+    int64_t x = home_node;
+    while (x > 0) {
+        const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+        int sp = 1;
+        if (lane == 0) st[0] = sib;
+        __syncwarp();
+        while (sp > 0) {
+            --sp;
+            const int32_t node = st[sp];
+            __syncwarp();
+            const int32_t ncn = nc[node];
+            bool need = active && ncn != c && ncn != kEmpty;
+            if (need) {
+                float b[2 * SP];
+                load_box<SP>(ix.box, node, b);
+                need = box_lb_n<DIM, SP>(b, q) <= thr;
+            }
+            if (!__any_sync(kFull, need)) continue;
+            if (node >= first_leaf_node) {
+                scan_leaf(node - first_leaf_node, need);
+            } else {
+                const int32_t l = 2 * node + 1, r = l + 1;
+                float bl[2 * SP], br[2 * SP];
+                load_box<SP>(ix.box, l, bl);
+                load_box<SP>(ix.box, r, br);
+                const float ll = box_lb_n<DIM, SP>(bl, ctr), lr = box_lb_n<DIM, SP>(br, ctr);
+                const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
+                if (lane == 0) {
+                    st[sp] = far;
+                    st[sp + 1] = near;
+                }
+                sp += 2;
+                __syncwarp();
+            }
+        }
+        x = (x - 1) >> 1;
     }
     if (!valid) return;
     cand_w[p] = bw;
@@ -463,15 +497,31 @@ __global__ void finalize_edges_kernel(int64_t m, const int32_t* __restrict__ src
     edges[3 * e + 2] = __dsqrt_rn((double)w2[e]);
 }
 
-template <int P>
+template <int DIM>
 int launch_search(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
                   const float* core2, const int32_t* comp, const int32_t* nc,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
+    constexpr int SP = DIM <= 4 ? 4 : 8;
     ::fhg::note_launch();
-    search_kernel<P><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
+    search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
         view_of(ix), k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
+}
+
+int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
+                 const float* core2, const int32_t* comp, const int32_t* nc,
+                 unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
+    switch (ix.d) {
+        case 1: return launch_search<1>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 2: return launch_search<2>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 3: return launch_search<3>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 4: return launch_search<4>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 5: return launch_search<5>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 6: return launch_search<6>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 7: return launch_search<7>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        default: return launch_search<8>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+    }
 }
 
 #define LAUNCH(kernel, count, ...)                                                   \
@@ -609,10 +659,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         }
         {
             Stage stage(s, "boruvka_search");
-            FHG_TRY(ix.pad == 4 ? launch_search<4>(ix, k, knn_s, knn_d, core2, comp, nc, keyA,
-                                                  cand_w, cand_q, s)
-                                : launch_search<8>(ix, k, knn_s, knn_d, core2, comp, nc, keyA,
-                                                  cand_w, cand_q, s));
+            FHG_TRY(search_round(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s));
         }
         Stage merge_stage(s, "boruvka_merge");
         LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);

@@ -66,6 +66,22 @@ __device__ __forceinline__ float box_lb(const float* __restrict__ box, const flo
     return r;
 }
 
+// box_lb over the first DIM coordinates of a box stored with SP floats per
+// corner (padded coordinates are zero on both sides and contribute nothing).
+template <int DIM, int SP>
+__device__ __forceinline__ float box_lb_n(const float* __restrict__ box, const float* q) {
+    float r = 0.0f;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+        float lo = box[j], hi = box[SP + j];
+        float dlo = lo > q[j] ? __fsub_rn(lo, q[j]) : 0.0f;
+        float dhi = q[j] > hi ? __fsub_rn(q[j], hi) : 0.0f;
+        float dd = __fadd_rn(dlo, dhi);
+        r = __fadd_rn(r, __fmul_rn(dd, dd));
+    }
+    return r;
+}
+
 template <int P>
 __device__ __forceinline__ void load_pt(const float* __restrict__ pts, int64_t i, float* out) {
     if (P == 4) {

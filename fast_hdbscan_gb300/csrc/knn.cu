@@ -1,13 +1,16 @@
 // Exact k-nearest-neighbour search (core distances), warp-cooperative.
 //
 // One warp owns one bucket of 32 Morton-consecutive query points (lane =
-// query).  The warp walks the bucket tree depth-first with a shared stack in
-// shared memory; a node is entered when ANY lane's lower bound is within
-// that lane's current k-th distance.  At a leaf, lane t loads candidate t of
-// the bucket (one coalesced 16/32-byte load per lane) and the 32 candidates
-// are broadcast with warp shuffles, so every query sees every candidate of
-// the leaf without divergent global loads.  Each lane keeps a sorted top-K
-// list in registers (fully unrolled compare-exchange insertion).
+// query).  It first scans its own bucket -- which contains the queries
+// themselves -- to get a tight k-th distance, then walks up the bucket tree to
+// the root: at every ancestor it searches the sibling subtree depth-first
+// (shared-memory stack; a node is entered when ANY lane's lower bound is
+// within that lane's current k-th distance).  At a
+// leaf the warp stages the bucket's points in shared memory with one
+// coalesced load per lane, and every lane then reads candidate t with a
+// broadcast shared-memory load.  Each lane keeps its sorted top-K list
+// (squared distance, Morton position) in registers; caller indices are only
+// looked up to break exact distance ties and for the final output.
 //
 // Ordering: (squared distance, caller index), ascending -- the reference's
 // parallel_tree_query order with equal distances ordered by index.
@@ -21,77 +24,90 @@ namespace {
 constexpr int kKnnWarps = 4;
 constexpr int kStack = 64;
 
-template <int P, int K>
+__device__ __forceinline__ int32_t orig_of(const int32_t* __restrict__ orig, int32_t s) {
+    return s < 0 ? INT32_MAX : __ldg(orig + s);
+}
+
+template <int DIM, int SP, int K>
 __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k,
                                                               float* __restrict__ d_s,
                                                               int32_t* __restrict__ i_s,
                                                               float* __restrict__ d_o,
                                                               int32_t* __restrict__ i_o) {
     __shared__ int32_t s_stack[kKnnWarps][kStack];
+    __shared__ float4 s_cand[kKnnWarps][32 * (SP / 4)];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t leaf = (int64_t)blockIdx.x * kKnnWarps + warp;
     if (leaf >= ix.nleaves) return;
     const int64_t qi = leaf * kLeaf + lane;
     const bool valid = qi < ix.n;
-    float q[P];
-    if (valid) load_pt<P>(ix.pts, qi, q);
-    else
-#pragma unroll
-        for (int j = 0; j < P; ++j) q[j] = 0.0f;
-
-    // Centre of this bucket's box: orders children (nearer first).
-    float ctr[P];
+    float q[DIM];
     {
-        float b[2 * P];
-        load_box<P>(ix.box, ix.slots - 1 + leaf, b);
+        float t[SP];
+        if (valid) load_pt<SP>(ix.pts, qi, t);
+        else
 #pragma unroll
-        for (int j = 0; j < P; ++j) ctr[j] = 0.5f * (b[j] + b[P + j]);
+            for (int j = 0; j < SP; ++j) t[j] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) q[j] = t[j];
+    }
+    // Centre of this bucket's box: orders children (nearer first).
+    float ctr[DIM];
+    {
+        float b[2 * SP];
+        load_box<SP>(ix.box, ix.slots - 1 + leaf, b);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) ctr[j] = 0.5f * (b[j] + b[SP + j]);
     }
 
     // Slots [0, K-k) hold a -1 sentinel so that the live list has length k.
     float bd[K];
-    int32_t bo[K], bs[K];
+    int32_t bs[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         bd[j] = (j < K - k) ? -1.0f : INFINITY;
-        bo[j] = INT32_MAX;
         bs[j] = -1;
     }
+    float4* cand = s_cand[warp];
+    const int32_t* __restrict__ orig = ix.orig;
 
-    // Candidates of one bucket: lane t holds candidate t, broadcast by shuffle.
     auto scan_leaf = [&](int64_t lf, bool need) {
         const int64_t base = lf * kLeaf;
         const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
-        float c[P];
-        int32_t co = INT32_MAX;
         if (lane < cnt) {
-            load_pt<P>(ix.pts, base + lane, c);
-            co = __ldg(ix.orig + base + lane);
-        } else {
+            const float4* src = reinterpret_cast<const float4*>(ix.pts) + (base + lane) * (SP / 4);
 #pragma unroll
-            for (int j = 0; j < P; ++j) c[j] = 0.0f;
+            for (int h = 0; h < SP / 4; ++h) cand[lane * (SP / 4) + h] = __ldg(src + h);
         }
+        __syncwarp();
+#pragma unroll 2
         for (int t = 0; t < cnt; ++t) {
-            float cc[P];
+            float c[SP];
 #pragma unroll
-            for (int j = 0; j < P; ++j) cc[j] = __shfl_sync(kFull, c[j], t);
-            const int32_t o = __shfl_sync(kFull, co, t);
-            const float dd = rdist_rn<P>(q, cc);
-            if (need && (dd < bd[K - 1] || (dd == bd[K - 1] && o < bo[K - 1]))) {
-                bd[K - 1] = dd;
-                bo[K - 1] = o;
-                bs[K - 1] = (int32_t)(base + t);
+            for (int h = 0; h < SP / 4; ++h) {
+                float4 v = cand[t * (SP / 4) + h];
+                c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
+            }
+            const float dd = rdist_rn<DIM>(q, c);
+            if (need && dd <= bd[K - 1]) {
+                const int32_t sidx = (int32_t)(base + t);
+                if (dd < bd[K - 1] || orig_of(orig, sidx) < orig_of(orig, bs[K - 1])) {
+                    bd[K - 1] = dd;
+                    bs[K - 1] = sidx;
 #pragma unroll
-                for (int j = K - 1; j > 0; --j) {
-                    const bool sw = bd[j] < bd[j - 1] || (bd[j] == bd[j - 1] && bo[j] < bo[j - 1]);
-                    if (sw) {
-                        float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
-                        int32_t ti = bo[j]; bo[j] = bo[j - 1]; bo[j - 1] = ti;
-                        ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
+                    for (int j = K - 1; j > 0; --j) {
+                        const bool sw = bd[j] < bd[j - 1] ||
+                                        (bd[j] == bd[j - 1] &&
+                                         orig_of(orig, bs[j]) < orig_of(orig, bs[j - 1]));
+                        if (sw) {
+                            float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
+                            int32_t ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
+                        }
                     }
                 }
             }
         }
+        __syncwarp();
     };
 
     // Seed with the warp's own bucket (it holds the queries themselves), so
@@ -99,74 +115,82 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
     // skips this bucket.
     scan_leaf(leaf, valid);
 
+    // Walk up from the home bucket to the root: at each ancestor search the
+    // sibling subtree depth first, pruned by lower bounds.  Subtrees' boxes
+    // overlap, so no ancestor box bounds the search; but near subtrees come
+    // first, and a far sibling whose box is out of every lane's reach costs a
+    // single box test.
     int32_t* st = s_stack[warp];
-    int sp = 1;
-    if (lane == 0) st[0] = 0;
-    __syncwarp();
     const int64_t first_leaf_node = ix.slots - 1;
-    const int64_t home_node = first_leaf_node + leaf;
-    while (sp > 0) {
-        --sp;
-        const int32_t node = st[sp];
+    int64_t x = first_leaf_node + leaf;
+    while (x > 0) {
+        const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+        int sp = 1;
+        if (lane == 0) st[0] = sib;
         __syncwarp();
-        if (node == home_node) continue;
-        float b[2 * P];
-        load_box<P>(ix.box, node, b);
-        const float lb = box_lb<P>(b, q);
-        const bool need = valid && lb <= bd[K - 1];
-        if (!__any_sync(kFull, need)) continue;
-        if (node >= first_leaf_node) {
-            scan_leaf(node - first_leaf_node, need);
-        } else {
-            const int32_t l = 2 * node + 1, r = l + 1;
-            float bl[2 * P], br[2 * P];
-            load_box<P>(ix.box, l, bl);
-            load_box<P>(ix.box, r, br);
-            const float ll = box_lb<P>(bl, ctr), lr = box_lb<P>(br, ctr);
-            const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
-            if (lane == 0) {
-                st[sp] = far;
-                st[sp + 1] = near;
-            }
-            sp += 2;
+        while (sp > 0) {
+            --sp;
+            const int32_t node = st[sp];
             __syncwarp();
+            float b[2 * SP];
+            load_box<SP>(ix.box, node, b);
+            const float lb = box_lb_n<DIM, SP>(b, q);
+            const bool need = valid && lb <= bd[K - 1];
+            if (!__any_sync(kFull, need)) continue;
+            if (node >= first_leaf_node) {
+                scan_leaf(node - first_leaf_node, need);
+            } else {
+                const int32_t l = 2 * node + 1, r = l + 1;
+                float bl[2 * SP], br[2 * SP];
+                load_box<SP>(ix.box, l, bl);
+                load_box<SP>(ix.box, r, br);
+                const float ll = box_lb_n<DIM, SP>(bl, ctr), lr = box_lb_n<DIM, SP>(br, ctr);
+                const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
+                if (lane == 0) {
+                    st[sp] = far;
+                    st[sp + 1] = near;
+                }
+                sp += 2;
+                __syncwarp();
+            }
         }
+        x = (x - 1) >> 1;
     }
     if (!valid) return;
-    const int64_t o_row = ix.orig[qi];
+    const int64_t o_row = orig[qi];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         if (j < K - k) continue;
         const int jj = j - (K - k);
-        const bool have = bs[j] >= 0;
         if (d_s) {
             d_s[qi * k + jj] = bd[j];
             i_s[qi * k + jj] = bs[j];
         }
         if (d_o) {
             d_o[o_row * k + jj] = bd[j];
-            i_o[o_row * k + jj] = have ? bo[j] : -1;
+            i_o[o_row * k + jj] = bs[j] >= 0 ? orig[bs[j]] : -1;
         }
     }
 }
 
-template <int P, int K>
+template <int DIM, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
                cudaStream_t s) {
+    constexpr int SP = DIM <= 4 ? 4 : 8;
     unsigned g = grid_for(ix.nleaves, kKnnWarps);
     ::fhg::note_launch();
-    knn_kernel<P, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o);
+    knn_kernel<DIM, SP, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
-template <int P>
+template <int DIM>
 int dispatch_k(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
                cudaStream_t s) {
-    if (k <= 8) return launch_knn<P, 8>(ix, k, d_s, i_s, d_o, i_o, s);
-    if (k <= 16) return launch_knn<P, 16>(ix, k, d_s, i_s, d_o, i_o, s);
-    if (k <= 32) return launch_knn<P, 32>(ix, k, d_s, i_s, d_o, i_o, s);
-    return launch_knn<P, 64>(ix, k, d_s, i_s, d_o, i_o, s);
+    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, s);
+    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, s);
+    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, s);
+    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, s);
 }
 
 }  // namespace
@@ -182,8 +206,16 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
         return FHG_ERR_INVALID;
     }
     Stage stage(s, "knn");
-    return ix.pad == 4 ? dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, s)
-                       : dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, s);
+    switch (ix.d) {
+        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, s);
+        default: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, s);
+    }
 }
 
 }  // namespace fhg

@@ -67,31 +67,33 @@ __global__ void node_init_kernel(int64_t nodes, int64_t n, int32_t* stamp, int32
     sz[i] = i < n ? 1 : 0;
 }
 
-__device__ __forceinline__ bool in_low(int64_t i, int64_t s, int64_t half) {
-    return (i & (s - 1)) < half;
+// Thread t of a level works on the t-th rank of the lower (or upper) halves
+// of the rank intervals [a, a + s), a = 0, s, 2s, ...
+__device__ __forceinline__ int64_t low_rank(int64_t t, int64_t s, int64_t half) {
+    return (t / half) * s + (t % half);
 }
 
 __global__ void lvl_init_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
                                 const int32_t* __restrict__ B, int32_t* P, int32_t* stamp,
                                 int32_t* M, int32_t* SUM, int lev) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m || !in_low(i, s, half)) return;
+    const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
+    if (i >= m) return;
     int32_t a = A[i], b = B[i];
     P[a] = a; stamp[a] = lev; M[a] = -1; SUM[a] = 0;
     P[b] = b; stamp[b] = lev; M[b] = -1; SUM[b] = 0;
 }
 __global__ void lvl_union_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
                                  const int32_t* __restrict__ B, int32_t* P) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m || !in_low(i, s, half)) return;
+    const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
+    if (i >= m) return;
     uf_union(P, A[i], B[i]);
 }
 __global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
                                   const int32_t* __restrict__ B, int32_t* P, int32_t* M,
                                   int32_t* SUM, const int32_t* __restrict__ SZ, int32_t* claim,
                                   int lev) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m || !in_low(i, s, half)) return;
+    const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
+    if (i >= m) return;
     int32_t a = A[i], b = B[i];
     int32_t r = uf_find(P, a);
     atomicMax(&M[r], (int32_t)i);
@@ -102,20 +104,76 @@ __global__ void lvl_size_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
                                 const int32_t* __restrict__ A, int32_t* P,
                                 const int32_t* __restrict__ M, const int32_t* __restrict__ SUM,
                                 int32_t* SZ) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m || !in_low(i, s, half)) return;
+    const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
+    if (i >= m) return;
     int32_t r = uf_find(P, A[i]);
     if (M[r] == (int32_t)i) SZ[n + i] = SUM[r];
 }
 __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n, int32_t* A,
                                    int32_t* B, int32_t* P, const int32_t* __restrict__ M,
                                    const int32_t* __restrict__ stamp, int lev) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m || in_low(i, s, half)) return;
+    const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half) + half;
+    if (i >= m) return;
     int32_t a = A[i], b = B[i];
     if (stamp[a] == lev) A[i] = (int32_t)(n + M[uf_find(P, a)]);
     if (stamp[b] == lev) B[i] = (int32_t)(n + M[uf_find(P, b)]);
 }
+// Final levels: one block per interval of kLeafRanks consecutive ranks.  Every
+// endpoint label is already the root node at the interval's start, so the
+// block replays the reference's sequential union-find (cluster_trees.py:72-93)
+// over at most 2 * kLeafRanks distinct labels held in shared memory.
+constexpr int kLeafRanks = 512;
+constexpr int kLeafSlots = 4 * kLeafRanks;  // open-addressing table, load <= 1/2
+
+__device__ __forceinline__ int32_t leaf_slot(int32_t* keys, int32_t label) {
+    uint32_t h = ((uint32_t)label * 2654435761u) >> 21;  // 11 bits: 2048 slots
+    for (;;) {
+        int32_t prev = atomicCAS(&keys[h], -1, label);
+        if (prev == -1 || prev == label) return (int32_t)h;
+        h = (h + 1) & (kLeafSlots - 1);
+    }
+}
+
+__global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n, int32_t* A,
+                                                            int32_t* B, int32_t* SZ) {
+    __shared__ int32_t keys[kLeafSlots], par[kLeafSlots], node[kLeafSlots];
+    __shared__ int32_t size[kLeafSlots];
+    __shared__ int16_t sa[kLeafRanks], sb[kLeafRanks];
+    const int64_t a = (int64_t)blockIdx.x * kLeafRanks;
+    const int cnt = (int)(m - a < kLeafRanks ? m - a : kLeafRanks);
+    for (int t = threadIdx.x; t < kLeafSlots; t += blockDim.x) keys[t] = -1;
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        int32_t la = A[a + t], lb = B[a + t];
+        int32_t ha = leaf_slot(keys, la), hb = leaf_slot(keys, lb);
+        sa[t] = (int16_t)ha;
+        sb[t] = (int16_t)hb;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kLeafSlots; t += blockDim.x) {
+        int32_t k = keys[t];
+        par[t] = t;
+        node[t] = k;
+        size[t] = k >= 0 ? SZ[k] : 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int t = 0; t < cnt; ++t) {
+            int32_t x = sa[t], y = sb[t];
+            while (par[x] != x) { par[x] = par[par[x]]; x = par[x]; }
+            while (par[y] != y) { par[y] = par[par[y]]; y = par[y]; }
+            const int64_t i = a + t;
+            A[i] = node[x];
+            B[i] = node[y];
+            const int32_t sz = size[x] + size[y];
+            SZ[n + i] = sz;
+            par[y] = x;
+            node[x] = (int32_t)(n + i);
+            size[x] = sz;
+        }
+    }
+}
+
 __global__ void linkage_rows_kernel(int64_t m, int64_t n, const int32_t* __restrict__ A,
                                     const int32_t* __restrict__ B, int32_t* SZ,
                                     int32_t* __restrict__ left, int32_t* __restrict__ right) {
@@ -210,13 +268,22 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     int64_t S = 1;
     while (S < m) S *= 2;
     int lev = 0;
-    for (int64_t sz = S; sz >= 2; sz /= 2, ++lev) {
+    for (int64_t sz = S; sz >= 2 * kLeafRanks; sz /= 2, ++lev) {
         const int64_t half = sz / 2;
-        LAUNCH(lvl_init_kernel, m, m, sz, half, A, B, P, stamp, M, SUM, lev);
-        LAUNCH(lvl_union_kernel, m, m, sz, half, A, B, P);
-        LAUNCH(lvl_reduce_kernel, m, m, sz, half, A, B, P, M, SUM, out->size, claim, lev);
-        LAUNCH(lvl_size_kernel, m, m, sz, half, n, A, P, M, SUM, out->size);
-        LAUNCH(lvl_relabel_kernel, m, m, sz, half, n, A, B, P, M, stamp, lev);
+        const int64_t intervals = (m + sz - 1) / sz;
+        const int64_t lo_threads = intervals * half;
+        const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
+        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, P, stamp, M, SUM, lev);
+        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, P);
+        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, P, M, SUM, out->size, claim, lev);
+        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, P, M, SUM, out->size);
+        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, P, M, stamp, lev);
+    }
+    {
+        const int64_t blocks = (m + kLeafRanks - 1) / kLeafRanks;
+        ::fhg::note_launch();
+        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, out->size);
+        FHG_CUDA(cudaGetLastError());
     }
     FHG_TRY(ws.alloc(&out->left, (size_t)m));
     FHG_TRY(ws.alloc(&out->right, (size_t)m));

@@ -39,9 +39,20 @@ __global__ void row_of_child_kernel(int64_t rows, int64_t n, const int32_t* __re
     if (c >= n) row_of_cluster[c - n] = (int32_t)r;
     else if (row_of_point) row_of_point[c] = (int32_t)r;
 }
-// One thread per cluster: float32 sum of lambda * size over its rows in order.
+// lambda * size of every row, in parent-grouped row order (contiguous per
+// cluster), so that each cluster's sequential sum below streams its addends.
+__global__ void products_kernel(int64_t rows, const int32_t* __restrict__ order,
+                                const float* __restrict__ lam, const float* __restrict__ csize,
+                                float* __restrict__ prod) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= rows) return;
+    int32_t r = order[j];
+    prod[j] = __fmul_rn(lam[r], csize[r]);
+}
+// One thread per cluster: the float32 sum of its rows' products, strictly in
+// row order (a float32 sum is not associative, so the order is the result).
 __global__ void score_kernel(int64_t C, const int64_t* __restrict__ start,
-                             const int32_t* __restrict__ cnt, const int32_t* __restrict__ order,
+                             const int32_t* __restrict__ cnt, const float* __restrict__ prod,
                              const int32_t* __restrict__ row_of_cluster,
                              const float* __restrict__ lam, const float* __restrict__ csize,
                              float* __restrict__ score) {
@@ -53,10 +64,15 @@ __global__ void score_kernel(int64_t C, const int64_t* __restrict__ start,
         if (r >= 0 && csize[r] > 1.0f) s = __fmul_rn(-lam[r], csize[r]);
     }
     const int64_t b = start[c], e = b + cnt[c];
-    for (int64_t j = b; j < e; ++j) {
-        int32_t r = order[j];
-        s = __fadd_rn(s, __fmul_rn(lam[r], csize[r]));
+    int64_t j = b;
+    for (; j + 8 <= e; j += 8) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldg(prod + j + u);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s = __fadd_rn(s, v[u]);
     }
+    for (; j < e; ++j) s = __fadd_rn(s, __ldg(prod + j));
     score[c] = s;
 }
 
@@ -409,8 +425,14 @@ int prepare(Workspace& ws, const Condensed& ct, Prepared* P) {
         LAUNCH(widen_kernel, C, C, P->cnt, cnt64);
         FHG_TRY(scan_exclusive_i64(tmp, cnt64, P->start, C, nullptr));
     }
-    LAUNCH(score_kernel, C, C, P->start, P->cnt, P->order, P->row_of_cluster, ct.lambda, ct.csize,
-           P->score);
+    {
+        Workspace tmp(s);
+        float* prod;
+        FHG_TRY(tmp.alloc(&prod, (size_t)rows));
+        LAUNCH(products_kernel, rows, rows, P->order, ct.lambda, ct.csize, prod);
+        LAUNCH(score_kernel, C, C, P->start, P->cnt, prod, P->row_of_cluster, ct.lambda,
+               ct.csize, P->score);
+    }
     FHG_TRY(ws.alloc(&P->corder, (size_t)rows));
     FHG_TRY(ws.alloc(&P->cstart, (size_t)C));
     FHG_TRY(ws.alloc(&P->ccnt, (size_t)C));
