@@ -350,3 +350,142 @@ int sorted_mst_to_f64(const Linkage& lk, double* out, cudaStream_t s) {
 }
 
 }  // namespace fhg
+
+// ---------------------------------------------------------------------------
+// Linkage tree without any device allocation.
+//
+// Some callers cannot allocate device memory while they run: a process whose
+// HBM is entirely reserved up front by its own pool allocator, or a
+// latency-critical loop that must never enter the CUDA allocator.  For them,
+// fhg_mst_to_linkage_tree_noalloc builds the same linkage tree as
+// fhg_mst_to_linkage_tree (presorted input) using only the scratch array
+// below, a file-scope device array of fixed size that every GPU loading this
+// library holds until the process exits.  Inputs and outputs stay the
+// caller's buffers.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace fhg {
+namespace {
+
+constexpr int64_t kNoAllocMaxEdges = FHG_NOALLOC_MAX_EDGES;
+constexpr int64_t kNoAllocAlign = 256;
+
+constexpr int64_t noalloc_round(int64_t b) { return (b + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+
+// src, dst, A, B, left, right: int32[m]; w: double[m]; size, P, stamp,
+// claim, M, SUM: int32[2m + 1]
+constexpr int64_t noalloc_bytes(int64_t m) {
+    return 6 * noalloc_round(4 * m) + noalloc_round(8 * m) + 6 * noalloc_round(4 * (2 * m + 1));
+}
+
+constexpr int64_t kNoAllocScratchBytes = noalloc_bytes(kNoAllocMaxEdges);
+
+// The scratch array.  Its contents persist from call to call; every buffer
+// carved from it is initialised by the kernels of each call before use.
+static __device__ __align__(256) unsigned char g_linkage_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Device address of g_linkage_scratch on the current device.  In host code the
+// array's name only stands for the device symbol, so the address is asked of
+// the runtime once per device (with that device current) and cached.
+int noalloc_scratch_base(unsigned char** out) {
+    int dev = -1;
+    FHG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("fhg_mst_to_linkage_tree_noalloc: device %d out of range", dev);
+        return FHG_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_linkage_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error("cudaGetSymbolAddress(g_linkage_scratch) failed on device %d: %s", dev,
+                      cudaGetErrorString(e));
+            return FHG_ERR_CUDA;
+        }
+        g_noalloc_base[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    return FHG_OK;
+}
+
+template <class T>
+T* carve(unsigned char*& cur, int64_t count) {
+    T* p = reinterpret_cast<T*>(cur);
+    cur += noalloc_round((int64_t)sizeof(T) * count);
+    return p;
+}
+
+int link_presorted_noalloc(const double* smst, int64_t m, double* out, cudaStream_t s) {
+    unsigned char* base = nullptr;
+    FHG_TRY(noalloc_scratch_base(&base));
+    const int64_t n = m + 1, nodes = n + m;
+    unsigned char* cur = base;
+    int32_t* src = carve<int32_t>(cur, m);
+    int32_t* dst = carve<int32_t>(cur, m);
+    int32_t* A = carve<int32_t>(cur, m);
+    int32_t* B = carve<int32_t>(cur, m);
+    int32_t* left = carve<int32_t>(cur, m);
+    int32_t* right = carve<int32_t>(cur, m);
+    double* w = carve<double>(cur, m);
+    int32_t* size = carve<int32_t>(cur, nodes);
+    int32_t* P = carve<int32_t>(cur, nodes);
+    int32_t* stamp = carve<int32_t>(cur, nodes);
+    int32_t* claim = carve<int32_t>(cur, nodes);
+    int32_t* M = carve<int32_t>(cur, nodes);
+    int32_t* SUM = carve<int32_t>(cur, nodes);
+
+    LAUNCH(split_mst_kernel, m, m, smst, src, dst, w);
+    LAUNCH(node_init_kernel, nodes, nodes, n, stamp, claim, size);
+    FHG_CUDA(cudaMemcpyAsync(A, src, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
+    FHG_CUDA(cudaMemcpyAsync(B, dst, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
+    int64_t S = 1;
+    while (S < m) S *= 2;
+    int lev = 0;
+    for (int64_t sz = S; sz >= 2 * kLeafRanks; sz /= 2, ++lev) {
+        const int64_t half = sz / 2;
+        const int64_t intervals = (m + sz - 1) / sz;
+        const int64_t lo_threads = intervals * half;
+        const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
+        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, P, stamp, M, SUM, lev);
+        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, P);
+        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, P, M, SUM, size, claim, lev);
+        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, P, M, SUM, size);
+        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, P, M, stamp, lev);
+    }
+    {
+        const int64_t blocks = (m + kLeafRanks - 1) / kLeafRanks;
+        ::fhg::note_launch();
+        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, size);
+        FHG_CUDA(cudaGetLastError());
+    }
+    LAUNCH(linkage_rows_kernel, m, m, n, A, B, size, left, right);
+    LAUNCH(linkage_f64_kernel, m, m, left, right, w, size, n, out);
+    return FHG_OK;
+}
+
+}  // namespace
+}  // namespace fhg
+
+extern "C" __attribute__((visibility("default"))) int fhg_mst_to_linkage_tree_noalloc(
+    const double* sorted_mst_dev, int64_t m, double* linkage_dev, void* stream) {
+    if (m <= 0) return FHG_OK;
+    if (m > fhg::kNoAllocMaxEdges) {
+        fhg::set_error("fhg_mst_to_linkage_tree_noalloc: %lld edges exceed the fixed scratch "
+                       "limit of %lld edges (FHG_NOALLOC_MAX_EDGES); use "
+                       "fhg_mst_to_linkage_tree",
+                       (long long)m, (long long)fhg::kNoAllocMaxEdges);
+        return FHG_ERR_INVALID;
+    }
+    if (!sorted_mst_dev || !linkage_dev) {
+        fhg::set_error("fhg_mst_to_linkage_tree_noalloc: null pointer argument");
+        return FHG_ERR_INVALID;
+    }
+    return fhg::link_presorted_noalloc(sorted_mst_dev, m, linkage_dev,
+                                       reinterpret_cast<cudaStream_t>(stream));
+}

@@ -93,6 +93,25 @@ int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* str
 int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, double* linkage_dev,
                             void* stream);
 
+/* Same result as fhg_mst_to_linkage_tree, with no device allocation at all.
+ * No counterpart in the reference: this entry point exists for callers that
+ * cannot allocate device memory while they run -- a process whose HBM is
+ * reserved up front by its own pool allocator, or a latency-critical loop
+ * that must never enter the CUDA allocator.  All scratch comes from a fixed
+ * device array compiled into libfhg.so (about 5.3 MB for the limit below),
+ * which every GPU that loads the library holds until the process exits.
+ *   - m must not exceed FHG_NOALLOC_MAX_EDGES; larger inputs are rejected
+ *     with FHG_ERR_INVALID (use fhg_mst_to_linkage_tree instead).
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress, with that device current); make that first call
+ *     before any stream capture.
+ *   - Every call shares the one array: calls that overlap on the GPU (for
+ *     instance on two streams) race and corrupt each other's results.  Each
+ *     call initialises what it reads, so back-to-back calls are safe. */
+#define FHG_NOALLOC_MAX_EDGES 65536
+int fhg_mst_to_linkage_tree_noalloc(const double* sorted_mst_dev, int64_t m,
+                                    double* linkage_dev, void* stream);
+
 /* Replaces cluster_trees.py:205 condense_tree(hierarchy, min_cluster_size,
  * max_cluster_size) for unit sample weights.  Output buffers hold 2*m rows;
  * *n_rows_host receives the row count.  Rows come in the reference's order. */
