@@ -63,6 +63,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, device):
+    """The largest value over all ranks (the slowest rank's step time)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def make_data(n, seed):
     from fast_hdbscan_gb300 import synthetic
 
@@ -203,10 +214,7 @@ def run_gb300(args):
     lib.fhg_profile_report(buf, len(buf))
     stages = json.loads(buf.value.decode() or "{}")
     ms_step = ev0.elapsed_time(ev1) / args.steps
-    t = torch.tensor([ms_step], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_step_max = float(t.item())
+    ms_step_max = max_over_ranks(ms_step, torch.device("cuda", local))
     value = n * world / (ms_step_max / 1e3)
     clock_info = clocks.summary()
 
@@ -250,11 +258,8 @@ def run_gb300(args):
         for _ in range(args.steps):
             est.fit(Xp)
         barrier()
-        e2e_s = (time.perf_counter() - t0) / args.steps
-        tt = torch.tensor([e2e_s], device="cuda")
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps,
+                               torch.device("cuda", local))
         rows_out = est._condensed_tree.shape[0]
         d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 24 + n * ms * 4 + n * 4)
         e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",

@@ -76,6 +76,9 @@ def check_array(X, ensure_all_finite=True, dtype="numeric"):
         raise ValueError(f"Expected 2D array, got {arr.ndim}D array instead")
     if arr.dtype.kind in "biu":
         arr = arr.astype(np.float64)
+    if arr.shape[0] < 1:
+        raise ValueError(f"Found array with 0 sample(s) (shape={arr.shape}) while a minimum "
+                         "of 1 is required.")
     if ensure_all_finite and not np.all(np.isfinite(arr)):
         raise ValueError("Input contains NaN or infinity.")
     return arr

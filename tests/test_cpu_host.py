@@ -1,0 +1,147 @@
+"""CPU checks of the host side: the C ABI library's exports, argument
+validation and degenerate paths that must not touch the GPU, and the
+multi-process timing reduction of bench.py (world size 2, gloo)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names += re.findall(r"\b(fhg_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    from fast_hdbscan_gb300 import build, _native
+
+    lib_path = build.build()
+    lib = ctypes.CDLL(lib_path)
+    declared = _declared_functions()
+    assert len(declared) >= 15
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+    # every declared function is also bound by the Python layer or documented
+    # as a direct C entry point
+    bound = set(_native.SIGNATURES)
+    direct = {"fhg_launch_count", "fhg_profile_enable", "fhg_profile_report",
+              "fhg_mst_to_linkage_tree_noalloc"}
+    assert set(declared) <= bound | direct
+    assert lib.fhg_abi_version() == 1
+
+
+def test_library_error_reporting_without_gpu():
+    """Argument errors are reported before any CUDA call."""
+    from fast_hdbscan_gb300 import build
+
+    lib = ctypes.CDLL(build.build())
+    lib.fhg_last_error.restype = ctypes.c_char_p
+    lib.fhg_index_build.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                    ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]
+    out = ctypes.c_void_p()
+    rc = lib.fhg_index_build(None, 10, 3, None, ctypes.byref(out))
+    assert rc == 1 and b"null" in lib.fhg_last_error()
+    lib.fhg_mst_to_linkage_tree_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int64,
+                                                    ctypes.c_void_p, ctypes.c_void_p]
+    rc = lib.fhg_mst_to_linkage_tree_noalloc(None, 65537, None, None)
+    assert rc == 1 and b"FHG_NOALLOC_MAX_EDGES" in lib.fhg_last_error()
+
+
+def test_badargs_raise_before_the_engine():
+    """fast_hdbscan/tests/test_hdbscan.py:138-166."""
+    from fast_hdbscan_gb300 import fast_hdbscan
+
+    X = np.random.default_rng(0).random((50, 2))
+    with pytest.raises(ValueError):
+        fast_hdbscan("fail")
+    with pytest.raises(ValueError):
+        fast_hdbscan(None)
+    for kw in (dict(min_cluster_size="fail"), dict(min_samples="fail"), dict(min_samples=-1),
+               dict(cluster_selection_epsilon="fail"), dict(cluster_selection_epsilon=-1),
+               dict(cluster_selection_epsilon=-0.1), dict(cluster_selection_persistence="fail"),
+               dict(cluster_selection_persistence=1),
+               dict(cluster_selection_persistence=-0.1),
+               dict(cluster_selection_method="fail"),
+               dict(semi_supervised=True, ss_algorithm="fail"),
+               dict(semi_supervised=True, data_labels=None)):
+        with pytest.raises(ValueError):
+            fast_hdbscan(X, **kw)
+
+
+def test_degenerate_inputs_need_no_engine():
+    """hdbscan.py:278-304: fewer than two points."""
+    from fast_hdbscan_gb300 import fast_hdbscan
+
+    labels, probs, slt, ct, mst, nbrs, core = fast_hdbscan(np.zeros((1, 2)), return_trees=True)
+    assert labels.shape == (1,) and np.all(labels == -1)
+    assert probs.shape == (1,) and slt.shape == (0, 4) and mst.shape == (0, 3)
+    assert np.all(np.isinf(core))
+    with pytest.raises(ValueError):  # check_array: at least one sample
+        fast_hdbscan(np.zeros((0, 2)))
+
+
+def test_out_of_scope_routes_raise_not_implemented():
+    from fast_hdbscan_gb300 import fast_hdbscan
+    from fast_hdbscan_gb300.hdbscan import compute_minimum_spanning_tree
+
+    X = np.random.default_rng(1).random((20, 2))
+    with pytest.raises(NotImplementedError):
+        fast_hdbscan(X, metric="cosine")
+    with pytest.raises(NotImplementedError):
+        fast_hdbscan(X, algorithm="kruskal")
+    with pytest.raises(ValueError):
+        compute_minimum_spanning_tree(X, algorithm="prim")
+    with pytest.raises(NotImplementedError):
+        fast_hdbscan(np.random.default_rng(2).random((20, 9)))
+
+
+def test_estimator_params_roundtrip():
+    from fast_hdbscan_gb300 import HDBSCAN
+
+    est = HDBSCAN(min_cluster_size=7, min_samples=3, cluster_selection_method="leaf")
+    p = est.get_params()
+    assert p["min_cluster_size"] == 7 and p["min_samples"] == 3
+    assert p["cluster_selection_method"] == "leaf"
+    est.set_params(min_cluster_size=11)
+    assert est.min_cluster_size == 11
+
+
+def _gloo_worker(rank, world, port, queue):
+    import torch
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from bench import max_over_ranks
+
+    queue.put((rank, max_over_ranks(10.0 * (rank + 1), torch.device("cpu"))))
+    dist.destroy_process_group()
+
+
+def test_bench_max_over_ranks_gloo():
+    """bench.py reports the slowest rank's step time (world size 2, gloo)."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+    got = dict(q.get(timeout=10) for _ in range(2))
+    assert got == {0: 20.0, 1: 20.0}

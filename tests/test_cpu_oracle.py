@@ -1,0 +1,117 @@
+"""CPU checks of the oracle (no GPU): pinned against the reference fixtures.
+
+The fixtures in tests/golden were produced by the unmodified reference
+(make_golden.py).  In reference tie mode the oracle must reproduce every
+array of every fixture bit for bit; in canonical mode (the GPU engine's tie
+rules) core distances and the MST weight multiset are identical and labels
+agree up to the reference's tie choices.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle as O
+
+FIXTURES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+# The reference indexes knn[-1] when min_samples >= n (k exceeds the point
+# count); its MST for that fixture has edges to "point -1".  Only its labels
+# and probabilities (all noise) are meaningful there.
+QUIRK = {"edge_mcs_gt_n"}
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def _kw(g):
+    return dict(cluster_selection_method=str(g["cluster_selection_method"]),
+                max_cluster_size=float(g["max_cluster_size"]),
+                allow_single_cluster=bool(g["allow_single_cluster"]),
+                cluster_selection_epsilon=float(g["cluster_selection_epsilon"]),
+                cluster_selection_persistence=float(g["cluster_selection_persistence"]))
+
+
+@pytest.mark.parametrize("name", FIXTURES)
+def test_oracle_reference_mode_bitexact(name):
+    g = _load(name)
+    X = g["X"]
+    if X.shape[0] < 2:
+        pytest.skip("degenerate input handled in Python")
+    tree = O.build_kdtree(X)
+    if "kd_idx_array" in g.files:
+        a = tree.arrays()
+        for key in ("idx_array", "idx_start", "idx_end", "is_leaf", "node_bounds"):
+            np.testing.assert_array_equal(a[key], g["kd_" + key])
+    k = g["knn_rdist"].shape[1]
+    rd, ix = O.tree_query(tree, k, mode=0)
+    np.testing.assert_array_equal(rd, g["knn_rdist"])
+    np.testing.assert_array_equal(ix, g["knn_idx"])
+    if name in QUIRK:  # the canonical mode spans the points with +inf edges instead
+        fit = O.fit(X, int(g["min_samples"]), int(g["min_cluster_size"]), mode=1, **_kw(g))
+        np.testing.assert_array_equal(fit.labels, g["labels"])
+        np.testing.assert_array_equal(fit.probabilities, g["probabilities"])
+        return
+    fit = O.fit(X, int(g["min_samples"]), int(g["min_cluster_size"]), mode=0, **_kw(g))
+    np.testing.assert_array_equal(fit.labels, g["labels"])
+    np.testing.assert_array_equal(fit.probabilities, g["probabilities"])
+    np.testing.assert_array_equal(fit.mst, g["mst_raw"])
+    np.testing.assert_array_equal(fit.core, g["core"])
+    np.testing.assert_array_equal(fit.neighbors, g["neighbors"])
+    np.testing.assert_array_equal(fit.sorted_mst, g["sorted_mst"])
+    np.testing.assert_array_equal(fit.linkage, g["linkage"])
+    for a, b in zip(fit.condensed, (g["ct_parent"], g["ct_child"], g["ct_lambda"], g["ct_size"])):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", sorted(set(FIXTURES) - QUIRK))
+def test_oracle_canonical_mode_invariants(name):
+    g = _load(name)
+    X = g["X"]
+    if X.shape[0] < 2:
+        pytest.skip("degenerate input handled in Python")
+    fit = O.fit(X, int(g["min_samples"]), int(g["min_cluster_size"]), mode=1, **_kw(g))
+    np.testing.assert_array_equal(fit.core, g["core"])
+    np.testing.assert_array_equal(np.sort(fit.mst[:, 2]), np.sort(g["mst_raw"][:, 2]))
+    assert len(set(fit.labels.tolist()) - {-1}) == len(set(g["labels"].tolist()) - {-1})
+
+
+def test_oracle_known_answer():
+    """fast_hdbscan/tests/test_hdbscan.py:169-186 through the oracle."""
+    np.random.seed(0)
+    X = np.random.rand(150, 2)
+    f = O.fit(X, None, 5, mode=0)
+    u, c = np.unique(f.labels, return_counts=True)
+    assert len(u) == 8 and c[u == -1] == 69
+    f = O.fit(X, None, 5, mode=0, cluster_selection_epsilon=0.2)
+    u, c = np.unique(f.labels, return_counts=True)
+    assert len(u) == 2 and c[u == -1] == 2
+
+
+def test_oracle_min_cluster_size_invariant():
+    """fast_hdbscan/tests/test_hdbscan.py:120-130: every cluster holds at
+    least min_cluster_size points, for both tie modes."""
+    X = _load("blobs200")["X"]
+    for mcs in (2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 200):
+        for mode in (0, 1):
+            labels = O.fit(X, None, mcs, mode=mode).labels
+            kept = labels[labels != -1]
+            if kept.size:
+                assert np.bincount(kept).min() >= mcs
+
+
+def test_oracle_parallel_threads_same_weights():
+    """The reference's parallel loops race on the pruning bound, so its MST
+    edge choice between equal weights can change with the thread count; the
+    weight multiset cannot."""
+    g = _load("vd3d_5k")
+    a = O.fit(g["X"], 15, 25, mode=0, nthreads=1)
+    b = O.fit(g["X"], 15, 25, mode=0, nthreads=4)
+    np.testing.assert_array_equal(np.sort(a.mst[:, 2]), np.sort(b.mst[:, 2]))
+    # the canonical mode is deterministic in any thread count
+    c1 = O.fit(g["X"], 15, 25, mode=1, nthreads=1)
+    c4 = O.fit(g["X"], 15, 25, mode=1, nthreads=4)
+    np.testing.assert_array_equal(c1.mst, c4.mst)
+    np.testing.assert_array_equal(c1.labels, c4.labels)
