@@ -7,10 +7,11 @@
 // (shared-memory stack; a node is entered when ANY lane's lower bound is
 // within that lane's current k-th distance).  At a
 // leaf the warp stages the bucket's points in shared memory with one
-// coalesced load per lane, and every lane then reads candidate t with a
-// broadcast shared-memory load.  Each lane keeps its sorted top-K list
-// (squared distance, Morton position) in registers; caller indices are only
-// looked up to break exact distance ties and for the final output.
+// coalesced load per lane, and every lane reads candidate t with a broadcast
+// shared-memory load and marks it if it is within the lane's k-th distance;
+// then each lane inserts its own marked candidates.  Each lane keeps its
+// sorted top-K list (squared distance, Morton position) in registers; caller
+// indices are only looked up to break exact distance ties and for the output.
 //
 // Ordering: (squared distance, caller index), ascending -- the reference's
 // parallel_tree_query order with equal distances ordered by index.
@@ -71,6 +72,27 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
     float4* cand = s_cand[warp];
     const int32_t* __restrict__ orig = ix.orig;
 
+    // Inserts (dd, sidx) into this lane's sorted list if it beats the k-th.
+    auto insert = [&](float dd, int32_t sidx) {
+        if (dd > bd[K - 1]) return;
+        if (dd == bd[K - 1] && !(orig_of(orig, sidx) < orig_of(orig, bs[K - 1]))) return;
+        bd[K - 1] = dd;
+        bs[K - 1] = sidx;
+#pragma unroll
+        for (int j = K - 1; j > 0; --j) {
+            const bool sw = bd[j] < bd[j - 1] ||
+                            (bd[j] == bd[j - 1] && orig_of(orig, bs[j]) < orig_of(orig, bs[j - 1]));
+            if (sw) {
+                float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
+                int32_t ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
+            }
+        }
+    };
+
+    // One bucket: first every lane marks the candidates within its current
+    // k-th distance (one bit each), then each lane inserts only its own
+    // marked candidates -- the warp pays for the busiest lane, not for every
+    // candidate some lane wants.
     auto scan_leaf = [&](int64_t lf, bool need) {
         const int64_t base = lf * kLeaf;
         const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
@@ -80,7 +102,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
             for (int h = 0; h < SP / 4; ++h) cand[lane * (SP / 4) + h] = __ldg(src + h);
         }
         __syncwarp();
-#pragma unroll 2
+        const float thr = need ? bd[K - 1] : -INFINITY;
+        uint32_t acc = 0u;
+#pragma unroll 4
         for (int t = 0; t < cnt; ++t) {
             float c[SP];
 #pragma unroll
@@ -88,24 +112,18 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
                 float4 v = cand[t * (SP / 4) + h];
                 c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
             }
-            const float dd = rdist_rn<DIM>(q, c);
-            if (need && dd <= bd[K - 1]) {
-                const int32_t sidx = (int32_t)(base + t);
-                if (dd < bd[K - 1] || orig_of(orig, sidx) < orig_of(orig, bs[K - 1])) {
-                    bd[K - 1] = dd;
-                    bs[K - 1] = sidx;
+            acc |= (rdist_rn<DIM>(q, c) <= thr ? 1u : 0u) << t;
+        }
+        while (acc) {
+            const int t = __ffs(acc) - 1;
+            acc &= acc - 1u;
+            float c[SP];
 #pragma unroll
-                    for (int j = K - 1; j > 0; --j) {
-                        const bool sw = bd[j] < bd[j - 1] ||
-                                        (bd[j] == bd[j - 1] &&
-                                         orig_of(orig, bs[j]) < orig_of(orig, bs[j - 1]));
-                        if (sw) {
-                            float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
-                            int32_t ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
-                        }
-                    }
-                }
+            for (int h = 0; h < SP / 4; ++h) {
+                float4 v = cand[t * (SP / 4) + h];
+                c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
             }
+            insert(rdist_rn<DIM>(q, c), (int32_t)(base + t));
         }
         __syncwarp();
     };

@@ -18,7 +18,6 @@
 // O(n log n), depth O(log^2 n), whatever the height of the dendrogram.
 #include "primitives.cuh"
 #include "trees.cuh"
-#include "uf.cuh"
 
 namespace fhg {
 namespace {
@@ -58,13 +57,62 @@ __global__ void apply_perm_kernel(const int32_t* __restrict__ perm, const int32_
     sdst[i] = B[i] = dst[e];
     sw[i] = w ? w[e] : __dsqrt_rn((double)w2[e]);
 }
-__global__ void node_init_kernel(int64_t nodes, int64_t n, int32_t* stamp, int32_t* claim,
-                                 int32_t* sz) {
+// Per-node state of the contraction, one 32-byte record per node id so that
+// every access to a (randomly placed) node touches a single sector:
+//   P      union-find parent (valid when stamp == the current level)
+//   stamp  level at which the node was last an endpoint of a lower half
+//   M      largest rank of its contracted component (at the root)
+//   SUM    size of its contracted component (at the root)
+//   claim  level at which its size was last added to a SUM
+//   SZ     number of points under the node
+struct __align__(32) NodeRec {
+    int32_t P, stamp, M, SUM, claim, SZ, pad0, pad1;
+};
+
+__device__ __forceinline__ int32_t rec_find(NodeRec* R, int32_t x) {
+    int32_t cur = R[x].P;
+    if (cur != x) {
+        int32_t prev = x, next;
+        while (cur > (next = R[cur].P)) {
+            R[prev].P = next;
+            prev = cur;
+            cur = next;
+        }
+    }
+    return cur;
+}
+
+__device__ __forceinline__ void rec_union(NodeRec* R, int32_t a, int32_t b) {
+    int32_t ra = rec_find(R, a), rb = rec_find(R, b);
+    while (ra != rb) {
+        if (ra < rb) {
+            int32_t t = ra; ra = rb; rb = t;
+        }
+        int32_t old = atomicCAS(&R[ra].P, ra, rb);
+        if (old == ra) return;
+        ra = rec_find(R, old);
+        rb = rec_find(R, rb);
+    }
+}
+
+__global__ void node_init_kernel(int64_t nodes, int64_t n, NodeRec* R) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nodes) return;
-    stamp[i] = -1;
-    claim[i] = -1;
-    sz[i] = i < n ? 1 : 0;
+    NodeRec r;
+    r.P = (int32_t)i;
+    r.stamp = -1;
+    r.M = -1;
+    r.SUM = 0;
+    r.claim = -1;
+    r.SZ = i < n ? 1 : 0;
+    r.pad0 = r.pad1 = 0;
+    R[i] = r;
+}
+
+__global__ void node_sizes_kernel(int64_t nodes, const NodeRec* __restrict__ R,
+                                  int32_t* __restrict__ size) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nodes) size[i] = R[i].SZ;
 }
 
 // Thread t of a level works on the t-th rank of the lower (or upper) halves
@@ -74,49 +122,43 @@ __device__ __forceinline__ int64_t low_rank(int64_t t, int64_t s, int64_t half) 
 }
 
 __global__ void lvl_init_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
-                                const int32_t* __restrict__ B, int32_t* P, int32_t* stamp,
-                                int32_t* M, int32_t* SUM, int lev) {
+                                const int32_t* __restrict__ B, NodeRec* R, int lev) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
-    int32_t a = A[i], b = B[i];
-    P[a] = a; stamp[a] = lev; M[a] = -1; SUM[a] = 0;
-    P[b] = b; stamp[b] = lev; M[b] = -1; SUM[b] = 0;
+    const int32_t a = A[i], b = B[i];
+    *reinterpret_cast<int4*>(&R[a]) = make_int4(a, lev, -1, 0);
+    *reinterpret_cast<int4*>(&R[b]) = make_int4(b, lev, -1, 0);
 }
 __global__ void lvl_union_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
-                                 const int32_t* __restrict__ B, int32_t* P) {
+                                 const int32_t* __restrict__ B, NodeRec* R) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
-    uf_union(P, A[i], B[i]);
+    rec_union(R, A[i], B[i]);
 }
 __global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
-                                  const int32_t* __restrict__ B, int32_t* P, int32_t* M,
-                                  int32_t* SUM, const int32_t* __restrict__ SZ, int32_t* claim,
-                                  int lev) {
+                                  const int32_t* __restrict__ B, NodeRec* R, int lev) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
-    int32_t a = A[i], b = B[i];
-    int32_t r = uf_find(P, a);
-    atomicMax(&M[r], (int32_t)i);
-    if (atomicExch(&claim[a], lev) != lev) atomicAdd(&SUM[r], SZ[a]);
-    if (atomicExch(&claim[b], lev) != lev) atomicAdd(&SUM[r], SZ[b]);
+    const int32_t a = A[i], b = B[i];
+    const int32_t r = rec_find(R, a);
+    atomicMax(&R[r].M, (int32_t)i);
+    if (atomicExch(&R[a].claim, lev) != lev) atomicAdd(&R[r].SUM, R[a].SZ);
+    if (atomicExch(&R[b].claim, lev) != lev) atomicAdd(&R[r].SUM, R[b].SZ);
 }
 __global__ void lvl_size_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
-                                const int32_t* __restrict__ A, int32_t* P,
-                                const int32_t* __restrict__ M, const int32_t* __restrict__ SUM,
-                                int32_t* SZ) {
+                                const int32_t* __restrict__ A, NodeRec* R) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
-    int32_t r = uf_find(P, A[i]);
-    if (M[r] == (int32_t)i) SZ[n + i] = SUM[r];
+    const int32_t r = rec_find(R, A[i]);
+    if (R[r].M == (int32_t)i) R[n + i].SZ = R[r].SUM;
 }
 __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n, int32_t* A,
-                                   int32_t* B, int32_t* P, const int32_t* __restrict__ M,
-                                   const int32_t* __restrict__ stamp, int lev) {
+                                   int32_t* B, NodeRec* R, int lev) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half) + half;
     if (i >= m) return;
-    int32_t a = A[i], b = B[i];
-    if (stamp[a] == lev) A[i] = (int32_t)(n + M[uf_find(P, a)]);
-    if (stamp[b] == lev) B[i] = (int32_t)(n + M[uf_find(P, b)]);
+    const int32_t a = A[i], b = B[i];
+    if (R[a].stamp == lev) A[i] = (int32_t)(n + R[rec_find(R, a)].M);
+    if (R[b].stamp == lev) B[i] = (int32_t)(n + R[rec_find(R, b)].M);
 }
 // Final levels: one block per interval of kLeafRanks consecutive ranks.  Every
 // endpoint label is already the root node at the interval's start, so the
@@ -135,7 +177,7 @@ __device__ __forceinline__ int32_t leaf_slot(int32_t* keys, int32_t label) {
 }
 
 __global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n, int32_t* A,
-                                                            int32_t* B, int32_t* SZ) {
+                                                            int32_t* B, NodeRec* R) {
     __shared__ int32_t keys[kLeafSlots], par[kLeafSlots], node[kLeafSlots];
     __shared__ int32_t size[kLeafSlots];
     __shared__ int16_t sa[kLeafRanks], sb[kLeafRanks];
@@ -154,7 +196,7 @@ __global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n
         int32_t k = keys[t];
         par[t] = t;
         node[t] = k;
-        size[t] = k >= 0 ? SZ[k] : 0;
+        size[t] = k >= 0 ? R[k].SZ : 0;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -166,7 +208,7 @@ __global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n
             A[i] = node[x];
             B[i] = node[y];
             const int32_t sz = size[x] + size[y];
-            SZ[n + i] = sz;
+            R[n + i].SZ = sz;
             par[y] = x;
             node[x] = (int32_t)(n + i);
             size[x] = sz;
@@ -175,14 +217,13 @@ __global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n
 }
 
 __global__ void linkage_rows_kernel(int64_t m, int64_t n, const int32_t* __restrict__ A,
-                                    const int32_t* __restrict__ B, int32_t* SZ,
-                                    int32_t* __restrict__ left, int32_t* __restrict__ right) {
+                                    const int32_t* __restrict__ B, int32_t* __restrict__ left,
+                                    int32_t* __restrict__ right) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     int32_t a = A[i], b = B[i];
     left[i] = max(a, b);
     right[i] = min(a, b);
-    SZ[n + i] = SZ[a] + SZ[b];
 }
 
 __global__ void linkage_f64_kernel(int64_t m, const int32_t* __restrict__ left,
@@ -226,14 +267,13 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     out->m = m > 0 ? m : 0;
     const int64_t nodes = n + (m > 0 ? m : 0);
     FHG_TRY(ws.alloc(&out->size, (size_t)nodes));
-    int32_t *P, *stamp, *claim, *M, *SUM;
-    FHG_TRY(ws.alloc(&P, (size_t)nodes));
-    FHG_TRY(ws.alloc(&stamp, (size_t)nodes));
-    FHG_TRY(ws.alloc(&claim, (size_t)nodes));
-    FHG_TRY(ws.alloc(&M, (size_t)nodes));
-    FHG_TRY(ws.alloc(&SUM, (size_t)nodes));
-    LAUNCH(node_init_kernel, nodes, nodes, n, stamp, claim, out->size);
-    if (m <= 0) return FHG_OK;
+    NodeRec* R;
+    FHG_TRY(ws.alloc(&R, (size_t)nodes));
+    LAUNCH(node_init_kernel, nodes, nodes, n, R);
+    if (m <= 0) {
+        LAUNCH(node_sizes_kernel, nodes, nodes, R, out->size);
+        return FHG_OK;
+    }
 
     // ---- sort by (weight, src, dst): stable LSD over dst, src, weight
     int32_t* perm;
@@ -273,21 +313,22 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
         const int64_t intervals = (m + sz - 1) / sz;
         const int64_t lo_threads = intervals * half;
         const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
-        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, P, stamp, M, SUM, lev);
-        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, P);
-        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, P, M, SUM, out->size, claim, lev);
-        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, P, M, SUM, out->size);
-        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, P, M, stamp, lev);
+        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, R, lev);
+        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, R);
+        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, R, lev);
+        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, R);
+        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, R, lev);
     }
     {
         const int64_t blocks = (m + kLeafRanks - 1) / kLeafRanks;
         ::fhg::note_launch();
-        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, out->size);
+        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, R);
         FHG_CUDA(cudaGetLastError());
     }
     FHG_TRY(ws.alloc(&out->left, (size_t)m));
     FHG_TRY(ws.alloc(&out->right, (size_t)m));
-    LAUNCH(linkage_rows_kernel, m, m, n, A, B, out->size, out->left, out->right);
+    LAUNCH(linkage_rows_kernel, m, m, n, A, B, out->left, out->right);
+    LAUNCH(node_sizes_kernel, nodes, nodes, R, out->size);
     return FHG_OK;
 }
 
@@ -299,6 +340,10 @@ __global__ void split_mst_kernel(int64_t m, const double* __restrict__ mst, int3
     src[i] = (int32_t)mst[3 * i + 0];
     dst[i] = (int32_t)mst[3 * i + 1];
     w[i] = mst[3 * i + 2];
+}
+__global__ void leaf_sizes_kernel(int64_t n, int32_t* __restrict__ size) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) size[i] = 1;
 }
 __global__ void split_linkage_kernel(int64_t m, int64_t n, const double* __restrict__ lk,
                                      int32_t* __restrict__ left, int32_t* __restrict__ right,
@@ -332,10 +377,7 @@ int linkage_from_f64(Workspace& ws, const double* lk, int64_t m, Linkage* out) {
     FHG_TRY(ws.alloc(&out->left, (size_t)(m > 0 ? m : 1)));
     FHG_TRY(ws.alloc(&out->right, (size_t)(m > 0 ? m : 1)));
     FHG_TRY(ws.alloc(&out->w, (size_t)(m > 0 ? m : 1)));
-    int32_t *stamp, *claim;
-    FHG_TRY(ws.alloc(&stamp, (size_t)(n + m)));
-    FHG_TRY(ws.alloc(&claim, (size_t)(n + m)));
-    LAUNCH(node_init_kernel, n + m, n + m, n, stamp, claim, out->size);
+    LAUNCH(leaf_sizes_kernel, n, n, out->size);
     LAUNCH(split_linkage_kernel, m, m, n, lk, out->left, out->right, out->w, out->size);
     return FHG_OK;
 }
@@ -373,10 +415,11 @@ constexpr int64_t kNoAllocAlign = 256;
 
 constexpr int64_t noalloc_round(int64_t b) { return (b + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
 
-// src, dst, A, B, left, right: int32[m]; w: double[m]; size, P, stamp,
-// claim, M, SUM: int32[2m + 1]
+// src, dst, A, B, left, right: int32[m]; w: double[m]; node records:
+// NodeRec[2m + 1]; node sizes: int32[2m + 1]
 constexpr int64_t noalloc_bytes(int64_t m) {
-    return 6 * noalloc_round(4 * m) + noalloc_round(8 * m) + 6 * noalloc_round(4 * (2 * m + 1));
+    return 6 * noalloc_round(4 * m) + noalloc_round(8 * m) +
+           noalloc_round((int64_t)sizeof(NodeRec) * (2 * m + 1)) + noalloc_round(4 * (2 * m + 1));
 }
 
 constexpr int64_t kNoAllocScratchBytes = noalloc_bytes(kNoAllocMaxEdges);
@@ -433,15 +476,11 @@ int link_presorted_noalloc(const double* smst, int64_t m, double* out, cudaStrea
     int32_t* left = carve<int32_t>(cur, m);
     int32_t* right = carve<int32_t>(cur, m);
     double* w = carve<double>(cur, m);
+    NodeRec* R = carve<NodeRec>(cur, nodes);
     int32_t* size = carve<int32_t>(cur, nodes);
-    int32_t* P = carve<int32_t>(cur, nodes);
-    int32_t* stamp = carve<int32_t>(cur, nodes);
-    int32_t* claim = carve<int32_t>(cur, nodes);
-    int32_t* M = carve<int32_t>(cur, nodes);
-    int32_t* SUM = carve<int32_t>(cur, nodes);
 
     LAUNCH(split_mst_kernel, m, m, smst, src, dst, w);
-    LAUNCH(node_init_kernel, nodes, nodes, n, stamp, claim, size);
+    LAUNCH(node_init_kernel, nodes, nodes, n, R);
     FHG_CUDA(cudaMemcpyAsync(A, src, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
     FHG_CUDA(cudaMemcpyAsync(B, dst, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
     int64_t S = 1;
@@ -452,19 +491,20 @@ int link_presorted_noalloc(const double* smst, int64_t m, double* out, cudaStrea
         const int64_t intervals = (m + sz - 1) / sz;
         const int64_t lo_threads = intervals * half;
         const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
-        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, P, stamp, M, SUM, lev);
-        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, P);
-        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, P, M, SUM, size, claim, lev);
-        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, P, M, SUM, size);
-        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, P, M, stamp, lev);
+        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, R, lev);
+        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, R);
+        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, R, lev);
+        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, R);
+        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, R, lev);
     }
     {
         const int64_t blocks = (m + kLeafRanks - 1) / kLeafRanks;
         ::fhg::note_launch();
-        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, size);
+        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, R);
         FHG_CUDA(cudaGetLastError());
     }
-    LAUNCH(linkage_rows_kernel, m, m, n, A, B, size, left, right);
+    LAUNCH(linkage_rows_kernel, m, m, n, A, B, left, right);
+    LAUNCH(node_sizes_kernel, nodes, nodes, R, size);
     LAUNCH(linkage_f64_kernel, m, m, left, right, w, size, n, out);
     return FHG_OK;
 }

@@ -98,7 +98,7 @@ int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, double* lin
  * cannot allocate device memory while they run -- a process whose HBM is
  * reserved up front by its own pool allocator, or a latency-critical loop
  * that must never enter the CUDA allocator.  All scratch comes from a fixed
- * device array compiled into libfhg.so (about 5.3 MB for the limit below),
+ * device array compiled into libfhg.so (about 6.8 MB for the limit below),
  * which every GPU that loads the library holds until the process exits.
  *   - m must not exceed FHG_NOALLOC_MAX_EDGES; larger inputs are rejected
  *     with FHG_ERR_INVALID (use fhg_mst_to_linkage_tree instead).
