@@ -29,6 +29,7 @@ _D = ctypes.c_double
 SIGNATURES = {
     "fhg_last_error": (ctypes.c_char_p, []),
     "fhg_abi_version": (_INT, []),
+    "fhg_release_cached_memory": (_INT, []),
     "fhg_index_build": (_INT, [_P, _I64, _I32, _P, ctypes.POINTER(_P)]),
     "fhg_index_free": (_INT, [_P, _P]),
     "fhg_index_shape": (_INT, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I32)]),
@@ -85,6 +86,11 @@ def check(rc):
     if rc == FHG_ERR_OOM:
         raise MemoryError(msg)
     raise EngineError(f"fhg error {rc}: {msg}")
+
+
+def release_cached_memory():
+    """Returns the device memory the engine's pool keeps cached between calls."""
+    check(load().fhg_release_cached_memory())
 
 
 def _torch():

@@ -37,6 +37,7 @@ namespace {
 constexpr int kSW = 4;        // warps per block, search kernel
 constexpr int kStack = 64;
 constexpr int kMaxRounds = 64;
+constexpr int kLocalLevels = 4;  // first search pass: subtrees of up to 16 buckets
 constexpr int32_t kEmpty = -2;  // node_comp of a node with no points
 constexpr int32_t kMixed = -1;  // node_comp of a node spanning components
 
@@ -184,24 +185,35 @@ __global__ void compact_kernel(int64_t n, const uint32_t* __restrict__ flag,
 }
 
 // ---------------------------------------------------------- per round: nodes
-__global__ void node_comp_leaf_kernel(const int32_t* __restrict__ comp, int64_t n,
-                                      int64_t nleaves, int64_t slots, int32_t* __restrict__ nc) {
+// Per node: x = its single component (node_comp, boruvka.py:98-124), kMixed
+// or kEmpty; y = bits of the least core distance of its points.  Every edge
+// into the node weighs at least that core distance, so a node whose least
+// core distance exceeds a query's threshold is skipped like a distant one.
+__global__ void node_comp_leaf_kernel(const int32_t* __restrict__ comp,
+                                      const float* __restrict__ core2, int64_t n,
+                                      int64_t nleaves, int64_t slots, int2* __restrict__ nc) {
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (leaf >= slots) return;
     int64_t i = leaf * kLeaf + lane;
     bool valid = leaf < nleaves && i < n;
     int32_t c = valid ? comp[i] : 0;
+    // non-negative floats order like their bit patterns
+    int32_t kb = valid ? __float_as_int(core2[i]) : INT32_MAX;
     int32_t c0 = __shfl_sync(kFull, c, 0);
     bool same = __all_sync(kFull, !valid || c == c0);
-    if (lane == 0) nc[slots - 1 + leaf] = leaf >= nleaves ? kEmpty : (same ? c0 : kMixed);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) kb = min(kb, __shfl_xor_sync(kFull, kb, o));
+    if (lane == 0)
+        nc[slots - 1 + leaf] = make_int2(leaf >= nleaves ? kEmpty : (same ? c0 : kMixed), kb);
 }
-__global__ void node_comp_level_kernel(int32_t* __restrict__ nc, int64_t first, int64_t count) {
+__global__ void node_comp_level_kernel(int2* __restrict__ nc, int64_t first, int64_t count) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     int64_t node = first + t;
-    int32_t l = nc[2 * node + 1], r = nc[2 * node + 2];
-    nc[node] = l == kEmpty ? r : (r == kEmpty ? l : (l == r ? l : kMixed));
+    const int2 l = nc[2 * node + 1], r = nc[2 * node + 2];
+    nc[node] = make_int2(l.x == kEmpty ? r.x : (r.x == kEmpty ? l.x : (l.x == r.x ? l.x : kMixed)),
+                         min(l.y, r.y));
 }
 
 __global__ void reset_keys_kernel(const int32_t* __restrict__ reps, int64_t nrep,
@@ -216,6 +228,41 @@ __global__ void reset_keys_kernel(const int32_t* __restrict__ reps, int64_t nrep
     par[c] = c;
 }
 
+// ------------------------------------------------------- per round: seeds
+// Every point's best edge among its own kNN list (boruvka.py:474 uses the same
+// lists), published to its component's key before any point searches, so the
+// search starts from every component's seed bound.
+__global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
+                            const float* __restrict__ knn_d, const float* __restrict__ core2,
+                            const int32_t* __restrict__ comp, const int32_t* __restrict__ orig,
+                            unsigned long long* keyA, float* __restrict__ cand_w,
+                            int32_t* __restrict__ cand_q) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t c = comp[p];
+    const float cp = core2[p];
+    float bw = INFINITY;
+    int32_t bq = -1, bo = INT32_MAX;
+    for (int j = 1; j < k; ++j) {
+        int32_t qs = knn_s[p * k + j];
+        if (qs < 0) break;
+        if (comp[qs] == c) continue;
+        float w = fmaxf(fmaxf(knn_d[p * k + j], cp), core2[qs]);
+        int32_t oq = orig[qs];
+        if (w < bw || (w == bw && oq < bo)) {
+            bw = w;
+            bq = qs;
+            bo = oq;
+        }
+    }
+    cand_w[p] = bw;
+    cand_q[p] = bq;
+    if (bq >= 0) {
+        unsigned long long key = pack_key(bw, min(orig[p], bo));
+        if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
+    }
+}
+
 // ------------------------------------------------------- per round: search
 // One warp per bucket of 32 query points, as in the kNN kernel.  A node is
 // entered when some lane's point lies outside the node's single component
@@ -223,12 +270,18 @@ __global__ void reset_keys_kernel(const int32_t* __restrict__ reps, int64_t nrep
 // weight and its component's running best (boruvka.py:182-191).  Candidates
 // of a leaf are staged in shared memory; a candidate in the query's own
 // component, or with a core distance above the threshold, costs one compare.
+//
+// A point whose seed already weighs its own core distance (the least weight
+// any of its edges can have) is settled without a search when every point
+// at that distance is in its kNN list: the core distance is below the k-th
+// distance, or no point outside the list lies exactly at the k-th distance
+// (knn_tie).  Any other edge then weighs more than the seed.
 template <int DIM, int SP>
 __global__ void __launch_bounds__(kSW * 32) search_kernel(
-    IndexView ix, int k, const int32_t* __restrict__ knn_s, const float* __restrict__ knn_d,
+    IndexView ix, int k, const float* __restrict__ knn_d, const int8_t* __restrict__ knn_tie,
     const float* __restrict__ core2, const int32_t* __restrict__ comp,
-    const int32_t* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
-    int32_t* __restrict__ cand_q) {
+    const int2* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
+    int32_t* __restrict__ cand_q, int lvl_lo, int lvl_hi) {
     __shared__ int32_t s_stack[kSW][kStack];
     __shared__ float4 s_xyz[kSW][32 * (SP / 4)];
     __shared__ int2 s_cc[kSW][32];      // (component, core bits)
@@ -238,16 +291,30 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     if (leaf >= ix.nleaves) return;
     const int64_t p = leaf * kLeaf + lane;
     const bool valid = p < ix.n;
+    int32_t c = -3;
+    float cp = 0.0f, bw = INFINITY;
+    int32_t bq = -1, bo = INT32_MAX;
+    bool active = false;
+    if (valid) {
+        c = comp[p];
+        cp = core2[p];
+        bw = cand_w[p];
+        bq = cand_q[p];
+        if (bq >= 0) bo = ix.orig[bq];
+        const bool settled =
+            bq >= 0 && bw == cp && (cp < knn_d[p * k + k - 1] || !knn_tie[p]);
+        const float thr0 = fminf(bw, key_weight(*(volatile unsigned long long*)&keyA[c]));
+        active = !settled && !(cp > thr0);
+    }
+    if (!__any_sync(kFull, active)) return;
+    const int32_t seed_q = bq;
+    float thr = bw;
+    if (valid) thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
     float q[DIM];
-    int32_t c = -3, op = 0;
-    float cp = 0.0f;
     {
         float t[SP];
         if (valid) {
             load_pt<SP>(ix.pts, p, t);
-            c = comp[p];
-            op = ix.orig[p];
-            cp = core2[p];
         } else {
 #pragma unroll
             for (int j = 0; j < SP; ++j) t[j] = 0.0f;
@@ -255,30 +322,6 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
 #pragma unroll
         for (int j = 0; j < DIM; ++j) q[j] = t[j];
     }
-    float bw = INFINITY;
-    int32_t bq = -1, bo = INT32_MAX;
-    // Seed from the point's own kNN list (boruvka.py:474 uses the same lists).
-    if (valid) {
-        for (int j = 1; j < k; ++j) {
-            int32_t qs = knn_s[p * k + j];
-            if (qs < 0) break;
-            if (comp[qs] == c) continue;
-            float w = fmaxf(fmaxf(knn_d[p * k + j], cp), core2[qs]);
-            int32_t oq = ix.orig[qs];
-            if (w < bw || (w == bw && oq < bo)) {
-                bw = w;
-                bq = qs;
-                bo = oq;
-            }
-        }
-        if (bq >= 0) {
-            unsigned long long key = pack_key(bw, min(op, bo));
-            if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
-        }
-    }
-    float thr = bw;
-    if (valid) thr = fminf(thr, key_weight(*(volatile unsigned long long*)&keyA[c]));
-    bool active = valid && !(cp > thr);
 
     float ctr[DIM];
     {
@@ -334,15 +377,16 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     const int64_t first_leaf_node = ix.slots - 1;
     const int64_t home_node = first_leaf_node + leaf;
     // A home bucket spanning several components holds the nearest candidates.
-    const int32_t home_nc = nc[home_node];
-    const bool home_first = home_nc == kMixed;
+    const int32_t home_nc = nc[home_node].x;
+    const bool home_first = lvl_lo == 0 && home_nc == kMixed;
     if (home_first && __any_sync(kFull, active)) scan_leaf(leaf, active);
 
     // Walk up from the home bucket to the root, searching the sibling subtree
     // at every ancestor (nearest subtrees first).
     int32_t* st = s_stack[warp];
     int64_t x = home_node;
-    while (x > 0) {
+    for (int l = 0; l < lvl_lo && x > 0; ++l) x = (x - 1) >> 1;
+    for (int l = lvl_lo; l < lvl_hi && x > 0; ++l) {
         const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
         int sp = 1;
         if (lane == 0) st[0] = sib;
@@ -351,8 +395,8 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
             --sp;
             const int32_t node = st[sp];
             __syncwarp();
-            const int32_t ncn = nc[node];
-            bool need = active && ncn != c && ncn != kEmpty;
+            const int2 ncn = nc[node];
+            bool need = active && ncn.x != c && ncn.x != kEmpty && !(__int_as_float(ncn.y) > thr);
             if (need) {
                 float b[2 * SP];
                 load_box<SP>(ix.box, node, b);
@@ -378,13 +422,11 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
         }
         x = (x - 1) >> 1;
     }
-    if (!valid) return;
+    if (!valid || bq == seed_q) return;
     cand_w[p] = bw;
     cand_q[p] = bq;
-    if (bq >= 0) {
-        unsigned long long key = pack_key(bw, min(op, bo));
-        if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
-    }
+    unsigned long long key = pack_key(bw, min(ix.orig[p], bo));
+    if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
 }
 
 __global__ void stage_b_kernel(int64_t n, const int32_t* __restrict__ comp,
@@ -498,29 +540,44 @@ __global__ void finalize_edges_kernel(int64_t m, const int32_t* __restrict__ src
 }
 
 template <int DIM>
-int launch_search(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
-                  const float* core2, const int32_t* comp, const int32_t* nc,
+int launch_search(const fhg_index& ix, int k, const float* knn_d, const int8_t* knn_tie,
+                  const float* core2, const int32_t* comp, const int2* nc,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : 8;
-    ::fhg::note_launch();
-    search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
-        view_of(ix), k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q);
-    FHG_CUDA(cudaGetLastError());
+    // Local pass (home bucket and the kLocalLevels nearest sibling subtrees),
+    // then the rest of the walk: every component's bound from its nearby
+    // candidates is published before any point searches far away.
+    const int spans[2][2] = {{0, kLocalLevels}, {kLocalLevels, 64}};
+    for (const auto& sp : spans) {
+        ::fhg::note_launch();
+        search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
+            view_of(ix), k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, sp[0],
+            sp[1]);
+        FHG_CUDA(cudaGetLastError());
+    }
     return FHG_OK;
 }
 
 int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
-                 const float* core2, const int32_t* comp, const int32_t* nc,
-                 unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
+                 const int8_t* knn_tie, const float* core2, const int32_t* comp,
+                 const int2* nc, unsigned long long* keyA, float* cand_w, int32_t* cand_q,
+                 cudaStream_t s) {
+    const int64_t n = ix.n;
+    if (n > 0) {
+        ::fhg::note_launch();
+        seed_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, k, knn_s, knn_d, core2, comp, ix.orig,
+                                                       keyA, cand_w, cand_q);
+        FHG_CUDA(cudaGetLastError());
+    }
     switch (ix.d) {
-        case 1: return launch_search<1>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 2: return launch_search<2>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 3: return launch_search<3>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 4: return launch_search<4>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 5: return launch_search<5>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 6: return launch_search<6>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 7: return launch_search<7>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
-        default: return launch_search<8>(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 1: return launch_search<1>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 2: return launch_search<2>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 3: return launch_search<3>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 4: return launch_search<4>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 5: return launch_search<5>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 6: return launch_search<6>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 7: return launch_search<7>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        default: return launch_search<8>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
     }
 }
 
@@ -558,7 +615,8 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
 
     float *knn_d, *core2, *knn_d_o = nullptr, *w0, *cand_w;
     int32_t *knn_s, *knn_i_o = nullptr, *target, *par, *comp, *cmin, *reps, *reps2, *winner, *tgt,
-        *nc, *cand_q;
+        *cand_q;
+    int2* nc;
     uint32_t *flag, *pos, *keyB, *cnt;
     unsigned long long* keyA;
     int* iflag;
@@ -568,7 +626,9 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         FHG_TRY(ws.alloc(&knn_d_o, (size_t)(n * k)));
         FHG_TRY(ws.alloc(&knn_i_o, (size_t)(n * k)));
     }
-    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s));
+    int8_t* knn_tie;
+    FHG_TRY(ws.alloc(&knn_tie, (size_t)n));
+    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s, knn_tie));
     FHG_TRY(ws.alloc(&core2, (size_t)n));
     LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2);
     if (core_o || nbr_o)
@@ -652,14 +712,15 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         }
         {  // node_comp (boruvka.py:98-124), bottom-up
             Stage stage(s, "boruvka_nodes");
-            LAUNCH(node_comp_leaf_kernel, ix.slots * 32, comp, n, ix.nleaves, ix.slots, nc);
+            LAUNCH(node_comp_leaf_kernel, ix.slots * 32, comp, core2, n, ix.nleaves, ix.slots, nc);
             for (int64_t width = ix.slots / 2; width >= 1; width /= 2)
                 LAUNCH(node_comp_level_kernel, width, nc, width - 1, width);
             LAUNCH(reset_keys_kernel, ncomp, reps, ncomp, keyA, keyB, winner, par);
         }
         {
             Stage stage(s, "boruvka_search");
-            FHG_TRY(search_round(ix, k, knn_s, knn_d, core2, comp, nc, keyA, cand_w, cand_q, s));
+            FHG_TRY(search_round(ix, k, knn_s, knn_d, knn_tie, core2, comp, nc, keyA, cand_w,
+                                 cand_q, s));
         }
         Stage merge_stage(s, "boruvka_merge");
         LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);

@@ -61,6 +61,35 @@ Stage::~Stage() {
     g_prof.push_back(StageRec{name_, a_, b});
 }
 
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+
+int device_pool(cudaMemPool_t* out) {
+    int dev = -1;
+    FHG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("device %d out of range", dev);
+        return FHG_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        FHG_CUDA(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = UINT64_MAX;
+        FHG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        g_pools[dev] = pool;
+    }
+    *out = g_pools[dev];
+    return FHG_OK;
+}
+
 }  // namespace fhg
 
 using namespace fhg;
@@ -73,6 +102,13 @@ FHG_API const char* fhg_last_error(void) { return last_error(); }
 FHG_API int fhg_abi_version(void) { return 1; }
 
 FHG_API uint64_t fhg_launch_count(void) { return g_launches.load(); }
+
+FHG_API int fhg_release_cached_memory(void) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (int d = 0; d < kMaxDevices; ++d)
+        if (g_pools[d]) FHG_CUDA(cudaMemPoolTrimTo(g_pools[d], 0));
+    return FHG_OK;
+}
 
 FHG_API int fhg_profile_enable(int on) {
     g_prof_on.store(on != 0);

@@ -57,6 +57,13 @@ struct Status {
         if (_s != FHG_OK) return _s;       \
     } while (0)
 
+// The library's stream-ordered memory pool on the current device.  Freed
+// blocks stay cached in the pool (release threshold: unlimited), so that the
+// synchronisations inside a fit never hand memory back to the driver and the
+// next allocation never has to map it again; fhg_release_cached_memory()
+// returns the cached blocks.
+int device_pool(cudaMemPool_t* out);
+
 // Stream-ordered scratch allocation.  Every buffer of a call is released on
 // the same stream when the Workspace goes out of scope.
 class Workspace {
@@ -71,9 +78,14 @@ class Workspace {
         void* p = nullptr;
         size_t bytes = count * sizeof(T);
         if (bytes == 0) bytes = 16;
-        cudaError_t e = cudaMallocAsync(&p, bytes, stream_);
+        if (!pool_) {
+            int rc = device_pool(&pool_);
+            if (rc != FHG_OK) return rc;
+        }
+        cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool_, stream_);
         if (e != cudaSuccess) {
-            set_error("cudaMallocAsync(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+            set_error("cudaMallocFromPoolAsync(%zu bytes) failed: %s", bytes,
+                      cudaGetErrorString(e));
             return e == cudaErrorMemoryAllocation ? FHG_ERR_OOM : FHG_ERR_CUDA;
         }
         bufs_.push_back(p);
@@ -88,6 +100,7 @@ class Workspace {
 
   private:
     cudaStream_t stream_;
+    cudaMemPool_t pool_ = nullptr;
     std::vector<void*> bufs_;
 };
 

@@ -23,6 +23,10 @@ namespace fhg {
 namespace {
 
 constexpr int kKnnWarps = 4;
+// Resident blocks asked of the register allocator: small lists fit in 80
+// registers, which keeps 24 warps per SM; larger lists take what they need.
+template <int K>
+constexpr int knn_min_blocks() { return K <= 16 ? 6 : 1; }
 constexpr int kStack = 64;
 
 __device__ __forceinline__ int32_t orig_of(const int32_t* __restrict__ orig, int32_t s) {
@@ -30,11 +34,12 @@ __device__ __forceinline__ int32_t orig_of(const int32_t* __restrict__ orig, int
 }
 
 template <int DIM, int SP, int K>
-__global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k,
+__global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kernel(IndexView ix, int k,
                                                               float* __restrict__ d_s,
                                                               int32_t* __restrict__ i_s,
                                                               float* __restrict__ d_o,
-                                                              int32_t* __restrict__ i_o) {
+                                                              int32_t* __restrict__ i_o,
+                                                              int8_t* __restrict__ tie_s) {
     __shared__ int32_t s_stack[kKnnWarps][kStack];
     __shared__ float4 s_cand[kKnnWarps][32 * (SP / 4)];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -72,10 +77,17 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
     float4* cand = s_cand[warp];
     const int32_t* __restrict__ orig = ix.orig;
 
+    // Smallest distance of a point examined but left out of the list: equal to
+    // the final k-th distance exactly when another point ties with the k-th.
+    float rejmin = INFINITY;
     // Inserts (dd, sidx) into this lane's sorted list if it beats the k-th.
     auto insert = [&](float dd, int32_t sidx) {
-        if (dd > bd[K - 1]) return;
-        if (dd == bd[K - 1] && !(orig_of(orig, sidx) < orig_of(orig, bs[K - 1]))) return;
+        if (dd > bd[K - 1] ||
+            (dd == bd[K - 1] && !(orig_of(orig, sidx) < orig_of(orig, bs[K - 1])))) {
+            rejmin = fminf(rejmin, dd);
+            return;
+        }
+        rejmin = fminf(rejmin, bd[K - 1]);
         bd[K - 1] = dd;
         bs[K - 1] = sidx;
 #pragma unroll
@@ -175,6 +187,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
         x = (x - 1) >> 1;
     }
     if (!valid) return;
+    if (tie_s) tie_s[qi] = rejmin == bd[K - 1] ? 1 : 0;
     const int64_t o_row = orig[qi];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
@@ -193,28 +206,29 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(IndexView ix, int k
 
 template <int DIM, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-               cudaStream_t s) {
+               int8_t* tie_s, cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : 8;
     unsigned g = grid_for(ix.nleaves, kKnnWarps);
     ::fhg::note_launch();
-    knn_kernel<DIM, SP, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o);
+    knn_kernel<DIM, SP, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o,
+                                                         tie_s);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
 template <int DIM>
 int dispatch_k(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-               cudaStream_t s) {
-    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, s);
-    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, s);
-    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, s);
-    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, s);
+               int8_t* tie_s, cudaStream_t s) {
+    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
 }
 
 }  // namespace
 
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-              cudaStream_t s) {
+              cudaStream_t s, int8_t* tie_s) {
     if (k < 1 || k > 64) {
         set_error("knn: k must be in [1, 64] (got %d)", k);
         return FHG_ERR_INVALID;
@@ -225,14 +239,14 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
     }
     Stage stage(s, "knn");
     switch (ix.d) {
-        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, s);
-        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, s);
-        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, s);
-        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, s);
-        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, s);
-        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, s);
-        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, s);
-        default: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, s);
+        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        default: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
     }
 }
 

@@ -216,14 +216,68 @@ __global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n
     }
 }
 
+// inv (nullable) maps renumbered point labels back to the caller's indices.
 __global__ void linkage_rows_kernel(int64_t m, int64_t n, const int32_t* __restrict__ A,
-                                    const int32_t* __restrict__ B, int32_t* __restrict__ left,
+                                    const int32_t* __restrict__ B,
+                                    const int32_t* __restrict__ inv, int32_t* __restrict__ left,
                                     int32_t* __restrict__ right) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     int32_t a = A[i], b = B[i];
+    if (inv) {
+        if (a < n) a = inv[a];
+        if (b < n) b = inv[b];
+    }
     left[i] = max(a, b);
     right[i] = min(a, b);
+}
+
+// Point renumbering.  A point's new label orders it by the rank of its first
+// (lightest) edge, the lower endpoint of that edge first; in every interval
+// of the contraction the point labels then lie in a window about as wide as
+// the interval, so the node records the level touches stay cache resident.
+__global__ void fill_i32_kernel(int32_t* a, int64_t n, int32_t v) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+__global__ void first_rank_kernel(int64_t m, const int32_t* __restrict__ A,
+                                  const int32_t* __restrict__ B, int32_t* first) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    atomicMin(&first[A[i]], (int32_t)i);
+    atomicMin(&first[B[i]], (int32_t)i);
+}
+__device__ __forceinline__ int64_t first_slot(const int32_t* __restrict__ B, int32_t f,
+                                              int32_t p) {
+    return 2 * (int64_t)f + (B[f] == p ? 1 : 0);
+}
+__global__ void slot_flags_kernel(int64_t n, const int32_t* __restrict__ first,
+                                  const int32_t* __restrict__ B, uint32_t* __restrict__ flag) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t f = first[p];
+    if (f != INT32_MAX) flag[first_slot(B, f, (int32_t)p)] = 1u;
+}
+__global__ void new_labels_kernel(int64_t n, const int32_t* __restrict__ first,
+                                  const int32_t* __restrict__ B, const uint32_t* __restrict__ pos,
+                                  int32_t* __restrict__ newid, int32_t* __restrict__ inv) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t f = first[p];
+    if (f == INT32_MAX) {  // no edge: never a label
+        newid[p] = -1;
+        return;
+    }
+    const int32_t id = (int32_t)pos[first_slot(B, f, (int32_t)p)];
+    newid[p] = id;
+    inv[id] = (int32_t)p;
+}
+__global__ void relabel_edges_kernel(int64_t m, const int32_t* __restrict__ newid, int32_t* A,
+                                     int32_t* B) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    A[i] = newid[A[i]];
+    B[i] = newid[B[i]];
 }
 
 __global__ void linkage_f64_kernel(int64_t m, const int32_t* __restrict__ left,
@@ -303,8 +357,28 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     FHG_TRY(ws.alloc(&B, (size_t)m));
     LAUNCH(apply_perm_kernel, m, perm, src, dst, w, w2, out->ssrc, out->sdst, out->w, A, B, m);
 
-    // ---- rank-halving contraction
     Stage stage(s, "linkage");
+    // ---- point renumbering by first edge rank
+    int32_t *first, *newid, *inv;
+    uint32_t *slot_flag, *slot_pos, *slot_cnt;
+    FHG_TRY(ws.alloc(&first, (size_t)n));
+    FHG_TRY(ws.alloc(&newid, (size_t)n));
+    FHG_TRY(ws.alloc(&inv, (size_t)n));
+    {
+        Workspace tmp(s);
+        FHG_TRY(tmp.alloc(&slot_flag, (size_t)(2 * m)));
+        FHG_TRY(tmp.alloc(&slot_pos, (size_t)(2 * m)));
+        FHG_TRY(tmp.alloc(&slot_cnt, 1));
+        LAUNCH(fill_i32_kernel, n, first, n, INT32_MAX);
+        LAUNCH(first_rank_kernel, m, m, A, B, first);
+        FHG_CUDA(cudaMemsetAsync(slot_flag, 0, sizeof(uint32_t) * 2 * m, s));
+        LAUNCH(slot_flags_kernel, n, n, first, B, slot_flag);
+        FHG_TRY(scan_exclusive_u32(tmp, slot_flag, slot_pos, 2 * m, slot_cnt));
+        LAUNCH(new_labels_kernel, n, n, first, B, slot_pos, newid, inv);
+        LAUNCH(relabel_edges_kernel, m, m, newid, A, B);
+    }
+
+    // ---- rank-halving contraction
     int64_t S = 1;
     while (S < m) S *= 2;
     int lev = 0;
@@ -327,7 +401,7 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     }
     FHG_TRY(ws.alloc(&out->left, (size_t)m));
     FHG_TRY(ws.alloc(&out->right, (size_t)m));
-    LAUNCH(linkage_rows_kernel, m, m, n, A, B, out->left, out->right);
+    LAUNCH(linkage_rows_kernel, m, m, n, A, B, inv, out->left, out->right);
     LAUNCH(node_sizes_kernel, nodes, nodes, R, out->size);
     return FHG_OK;
 }
@@ -503,7 +577,7 @@ int link_presorted_noalloc(const double* smst, int64_t m, double* out, cudaStrea
         leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, R);
         FHG_CUDA(cudaGetLastError());
     }
-    LAUNCH(linkage_rows_kernel, m, m, n, A, B, left, right);
+    LAUNCH(linkage_rows_kernel, m, m, n, A, B, (const int32_t*)nullptr, left, right);
     LAUNCH(node_sizes_kernel, nodes, nodes, R, size);
     LAUNCH(linkage_f64_kernel, m, m, left, right, w, size, n, out);
     return FHG_OK;

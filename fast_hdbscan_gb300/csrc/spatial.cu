@@ -155,10 +155,13 @@ int build_boxes(fhg_index* ix, cudaStream_t s) {
 }
 
 int index_alloc(fhg_index* ix, cudaStream_t s) {
-    FHG_CUDA(cudaMallocAsync(&ix->pts, sizeof(float) * ix->n * ix->pad + 16, s));
-    FHG_CUDA(cudaMallocAsync(&ix->orig, sizeof(int32_t) * ix->n + 16, s));
-    FHG_CUDA(cudaMallocAsync(&ix->rank, sizeof(int32_t) * ix->n + 16, s));
-    FHG_CUDA(cudaMallocAsync(&ix->box, sizeof(float) * ix->nnodes * 2 * ix->pad + 16, s));
+    cudaMemPool_t pool;
+    FHG_TRY(device_pool(&pool));
+    FHG_CUDA(cudaMallocFromPoolAsync(&ix->pts, sizeof(float) * ix->n * ix->pad + 16, pool, s));
+    FHG_CUDA(cudaMallocFromPoolAsync(&ix->orig, sizeof(int32_t) * ix->n + 16, pool, s));
+    FHG_CUDA(cudaMallocFromPoolAsync(&ix->rank, sizeof(int32_t) * ix->n + 16, pool, s));
+    FHG_CUDA(cudaMallocFromPoolAsync(&ix->box, sizeof(float) * ix->nnodes * 2 * ix->pad + 16,
+                                     pool, s));
     return FHG_OK;
 }
 

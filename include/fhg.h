@@ -50,6 +50,13 @@ uint64_t fhg_launch_count(void);
 int fhg_profile_enable(int on);
 int fhg_profile_report(char* buf, int64_t cap);
 
+/* Device scratch comes from one stream-ordered memory pool per device, owned
+ * by this library, that keeps freed blocks cached for the next call (no
+ * counterpart in the reference, which allocates host memory through numpy).
+ * fhg_release_cached_memory returns every cached block that no call is using
+ * to the driver. */
+int fhg_release_cached_memory(void);
+
 /* Opaque spatial index: points sorted along a Morton curve into buckets of
  * 32 with a complete binary tree of bounding boxes over the buckets. */
 typedef struct fhg_index fhg_index;

@@ -145,3 +145,17 @@ def test_missing_data_remap(engine):
     clean = list(range(1, 5)) + list(range(6, 200))
     clean_model = HDBSCAN().fit(Xm[clean])
     assert np.allclose(clean_model.labels_, model.labels_[clean])
+
+
+def test_cached_pool_release_between_fits(engine):
+    """Scratch comes from the engine's caching pool: a fit after the pool has
+    handed its cached blocks back gives the same result."""
+    from fast_hdbscan_gb300 import _native
+    from fast_hdbscan_gb300.hdbscan import fast_hdbscan
+
+    X = synthetic.varying_density(30_000, seed=5)
+    a = fast_hdbscan(X, min_samples=10, min_cluster_size=40)
+    _native.release_cached_memory()
+    b = fast_hdbscan(X, min_samples=10, min_cluster_size=40)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
