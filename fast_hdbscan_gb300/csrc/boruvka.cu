@@ -622,10 +622,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     int* iflag;
     FHG_TRY(ws.alloc(&knn_d, (size_t)(n * k)));
     FHG_TRY(ws.alloc(&knn_s, (size_t)(n * k)));
-    if (nbr_o) {
-        FHG_TRY(ws.alloc(&knn_d_o, (size_t)(n * k)));
-        FHG_TRY(ws.alloc(&knn_i_o, (size_t)(n * k)));
-    }
+    if (nbr_o) FHG_TRY(ws.alloc(&knn_i_o, (size_t)(n * k)));  // neighbour ids only
     int8_t* knn_tie;
     FHG_TRY(ws.alloc(&knn_tie, (size_t)n));
     FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s, knn_tie));

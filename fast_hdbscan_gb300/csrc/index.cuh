@@ -110,7 +110,8 @@ int index_free(fhg_index* ix, cudaStream_t s);
 
 // kNN over the index.  Outputs (all nullable):
 //   d_s/i_s : rows in Morton order, neighbour ids as Morton positions
-//   d_o/i_o : rows in caller order, neighbour ids as caller indices
+//   d_o/i_o : rows in caller order, neighbour ids as caller indices (i_o may
+//             be given alone)
 //   tie_s   : per point (Morton order), 1 when some point outside its list
 //             lies at exactly its k-th distance
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,

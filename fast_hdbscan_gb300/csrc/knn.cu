@@ -197,10 +197,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
             d_s[qi * k + jj] = bd[j];
             i_s[qi * k + jj] = bs[j];
         }
-        if (d_o) {
-            d_o[o_row * k + jj] = bd[j];
-            i_o[o_row * k + jj] = bs[j] >= 0 ? orig[bs[j]] : -1;
-        }
+        if (d_o) d_o[o_row * k + jj] = bd[j];
+        if (i_o) i_o[o_row * k + jj] = bs[j] >= 0 ? orig[bs[j]] : -1;
     }
 }
 
@@ -233,8 +231,8 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
         set_error("knn: k must be in [1, 64] (got %d)", k);
         return FHG_ERR_INVALID;
     }
-    if ((d_s == nullptr) != (i_s == nullptr) || (d_o == nullptr) != (i_o == nullptr)) {
-        set_error("knn: distance and index outputs must be given together");
+    if ((d_s == nullptr) != (i_s == nullptr) || (d_o != nullptr && i_o == nullptr)) {
+        set_error("knn: Morton-order outputs come in pairs; caller-order distances need ids");
         return FHG_ERR_INVALID;
     }
     Stage stage(s, "knn");

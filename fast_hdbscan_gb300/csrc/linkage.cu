@@ -141,9 +141,19 @@ __global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, const int3
     if (i >= m) return;
     const int32_t a = A[i], b = B[i];
     const int32_t r = rec_find(R, a);
-    atomicMax(&R[r].M, (int32_t)i);
-    if (atomicExch(&R[a].claim, lev) != lev) atomicAdd(&R[r].SUM, R[a].SZ);
-    if (atomicExch(&R[b].claim, lev) != lev) atomicAdd(&R[r].SUM, R[b].SZ);
+    int32_t add = 0;
+    if (atomicExch(&R[a].claim, lev) != lev) add += R[a].SZ;
+    if (atomicExch(&R[b].claim, lev) != lev) add += R[b].SZ;
+    // Consecutive ranks mostly share a root (a large component absorbs long
+    // runs of edges): combine the lanes of each root first, then one atomic
+    // per root per warp instead of one per rank.
+    const unsigned peers = __match_any_sync(__activemask(), r);
+    const int32_t mx = __reduce_max_sync(peers, (int32_t)i);
+    const int32_t sum = (int32_t)__reduce_add_sync(peers, (unsigned)add);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+        atomicMax(&R[r].M, mx);
+        if (sum) atomicAdd(&R[r].SUM, sum);
+    }
 }
 __global__ void lvl_size_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
                                 const int32_t* __restrict__ A, NodeRec* R) {
