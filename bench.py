@@ -135,18 +135,43 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- gb300 arm
-def algorithmic_bytes(stage, n, k, d_pad, rounds, comps):
-    """Minimum HBM bytes per launch of each timed kernel (fixed formulas)."""
-    if stage == "knn":
-        # read every point once (padded float4 + caller index), write the
-        # kNN rows (squared distance + index) in Morton order
-        return n * (4 * d_pad + 4) + n * k * 8
-    if stage == "boruvka_search":
-        # per round: kNN seed rows (index + distance + neighbour component),
-        # each point's coordinates, core, component and index, its candidate
-        # (weight + index), and one 8-byte component key per component
-        per_round = n * k * 12 + n * (4 * d_pad + 4 + 4 + 4 + 8) + 8 * comps / max(rounds, 1)
-        return per_round
+def tree_nodes(n):
+    """Nodes of the bucket tree: a complete binary tree over the 32-point
+    buckets, its leaf level padded to a power of two."""
+    leaves = (n + 31) // 32
+    slots = 1
+    while slots < leaves:
+        slots *= 2
+    return 2 * slots - 1
+
+
+def algorithmic_bytes(kernel, n, k, d_pad):
+    """Least HBM bytes one launch of each timed kernel must move (fixed
+    formulas; every other access of the walk is a cache-resident re-read)."""
+    if kernel == "knn_kernel":
+        # read every point once (padded coordinates + caller index); write the
+        # Morton-order rows (squared distance + position), the caller-order
+        # neighbour ids and the one-byte boundary-tie flag
+        return n * (4 * d_pad + 4) + n * k * 8 + n * k * 4 + n
+    if kernel == "search_kernel":
+        # per pass: each point's component, core distance, candidate (weight
+        # + position), k-th distance and tie flag; each tree node's
+        # (component, least core) word
+        return n * (4 + 4 + 8 + 4 + 1) + tree_nodes(n) * 8
+    return None
+
+
+def traffic_per_point(kernel):
+    """DRAM bytes per point and launch measured by ncu, from the committed
+    summary (profiles/ncu_traffic_per_point.txt: '<kernel> <bytes>' lines)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic_per_point.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == kernel:
+                return float(parts[1])
+    except OSError:
+        pass
     return None
 
 
@@ -219,8 +244,10 @@ def run_gb300(args):
     clock_info = clocks.summary()
 
     # per-stage share and the dominant kernel's roofline
-    total_stage = sum(v[0] for v in stages.values()) or 1.0
-    kernel_stages = {k: v for k, v in stages.items() if k in ("knn", "boruvka_search")}
+    # kernel records nest inside the stage records: shares are over stages
+    nested = ("knn_kernel", "search_kernel")
+    total_stage = sum(v[0] for k, v in stages.items() if k not in nested) or 1.0
+    kernel_stages = {k: v for k, v in stages.items() if k in ("knn_kernel", "search_kernel")}
     dom = max(kernel_stages, key=lambda k: kernel_stages[k][0]) if kernel_stages else None
     peaks = {}
     try:
@@ -233,19 +260,16 @@ def run_gb300(args):
     if dom:
         tot_ms, cnt = kernel_stages[dom]
         per_launch_ms = tot_ms / cnt
-        alg = algorithmic_bytes(dom, n, ms + 1, 4 if d <= 4 else 8, rounds, n)
+        alg = algorithmic_bytes(dom, n, ms + 1, 4 if d <= 4 else 8)
         achieved = alg / (per_launch_ms / 1e3) / 1e9
-        traffic = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
-            tj = json.load(open(tpath))
-            ent = tj.get(dom)
-            if ent:
-                traffic = ent["dram_bytes_per_point"] * n
+        tpp = traffic_per_point(dom)
+        traffic = round(tpp * n) if tpp is not None else None
         roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak,
                     "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 5),
                     "traffic": traffic, "algorithmic_bytes_per_launch": alg,
-                    "ms_per_launch": round(per_launch_ms, 4)}
+                    "launches_per_step": cnt // max(args.steps, 1),
+                    "ms_per_launch": round(per_launch_ms, 4),
+                    "kernel_share_of_stage_time": round(tot_ms / total_stage, 4)}
 
     # e2e through the public estimator, pinned host input, outputs to host
     e2e = None
@@ -282,7 +306,8 @@ def run_gb300(args):
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": int(launches),
             "clocks": clock_info,
             "stages_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in stages.items()},
-            "stage_share": {k: round(v[0] / total_stage, 4) for k, v in stages.items()},
+            "stage_share": {k: round(v[0] / total_stage, 4) for k, v in stages.items()
+                            if k not in nested},
             "boruvka_rounds": rounds,
         }
         print(json.dumps(line), flush=True)

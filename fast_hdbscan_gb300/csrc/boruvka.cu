@@ -549,6 +549,7 @@ int launch_search(const fhg_index& ix, int k, const float* knn_d, const int8_t* 
     // candidates is published before any point searches far away.
     const int spans[2][2] = {{0, kLocalLevels}, {kLocalLevels, 64}};
     for (const auto& sp : spans) {
+        Stage stage(s, "search_kernel");
         ::fhg::note_launch();
         search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
             view_of(ix), k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, sp[0],

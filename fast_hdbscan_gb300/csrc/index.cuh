@@ -29,11 +29,12 @@ struct IndexView {
     int64_t n, nleaves, slots;
     const float* __restrict__ pts;
     const int32_t* __restrict__ orig;
+    const int32_t* __restrict__ rank;
     const float* __restrict__ box;
 };
 
 inline IndexView view_of(const fhg_index& ix) {
-    return IndexView{ix.n, ix.nleaves, ix.slots, ix.pts, ix.orig, ix.box};
+    return IndexView{ix.n, ix.nleaves, ix.slots, ix.pts, ix.orig, ix.rank, ix.box};
 }
 
 // Squared float32 distance with every multiply and add rounded separately,

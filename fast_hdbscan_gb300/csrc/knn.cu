@@ -10,8 +10,9 @@
 // coalesced load per lane, and every lane reads candidate t with a broadcast
 // shared-memory load and marks it if it is within the lane's k-th distance;
 // then each lane inserts its own marked candidates.  Each lane keeps its
-// sorted top-K list (squared distance, Morton position) in registers; caller
-// indices are only looked up to break exact distance ties and for the output.
+// sorted top-K list (squared distance, caller index) in registers: exact
+// distance ties are broken without a memory access, and the Morton positions
+// of the result are looked up once at the end.
 //
 // Ordering: (squared distance, caller index), ascending -- the reference's
 // parallel_tree_query order with equal distances ordered by index.
@@ -29,10 +30,6 @@ template <int K>
 constexpr int knn_min_blocks() { return K <= 16 ? 6 : 1; }
 constexpr int kStack = 64;
 
-__device__ __forceinline__ int32_t orig_of(const int32_t* __restrict__ orig, int32_t s) {
-    return s < 0 ? INT32_MAX : __ldg(orig + s);
-}
-
 template <int DIM, int SP, int K>
 __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kernel(IndexView ix, int k,
                                                               float* __restrict__ d_s,
@@ -42,6 +39,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
                                                               int8_t* __restrict__ tie_s) {
     __shared__ int32_t s_stack[kKnnWarps][kStack];
     __shared__ float4 s_cand[kKnnWarps][32 * (SP / 4)];
+    __shared__ int32_t s_corig[kKnnWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t leaf = (int64_t)blockIdx.x * kKnnWarps + warp;
     if (leaf >= ix.nleaves) return;
@@ -66,38 +64,45 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
         for (int j = 0; j < DIM; ++j) ctr[j] = 0.5f * (b[j] + b[SP + j]);
     }
 
-    // Slots [0, K-k) hold a -1 sentinel so that the live list has length k.
+    // Slots [0, K-k) hold a -1 sentinel so that the live list has length k;
+    // empty live slots hold (+inf, INT32_MAX).
     float bd[K];
-    int32_t bs[K];
+    int32_t bo[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         bd[j] = (j < K - k) ? -1.0f : INFINITY;
-        bs[j] = -1;
+        bo[j] = (j < K - k) ? -1 : INT32_MAX;
     }
     float4* cand = s_cand[warp];
+    int32_t* corig = s_corig[warp];
     const int32_t* __restrict__ orig = ix.orig;
 
     // Smallest distance of a point examined but left out of the list: equal to
     // the final k-th distance exactly when another point ties with the k-th.
     float rejmin = INFINITY;
-    // Inserts (dd, sidx) into this lane's sorted list if it beats the k-th.
-    auto insert = [&](float dd, int32_t sidx) {
-        if (dd > bd[K - 1] ||
-            (dd == bd[K - 1] && !(orig_of(orig, sidx) < orig_of(orig, bs[K - 1])))) {
+    // Inserts (dd, o) into this lane's sorted list if it precedes the k-th.
+    // Every slot's new value depends only on the old list (no chain of
+    // compare-and-swap steps): slot j takes slot j-1's entry if that entry
+    // follows (dd, o), else (dd, o) if slot j's own entry follows it.
+    auto insert = [&](float dd, int32_t o) {
+        if (!(dd < bd[K - 1] || (dd == bd[K - 1] && o < bo[K - 1]))) {
             rejmin = fminf(rejmin, dd);
             return;
         }
         rejmin = fminf(rejmin, bd[K - 1]);
-        bd[K - 1] = dd;
-        bs[K - 1] = sidx;
+        bool gt_hi = true;
 #pragma unroll
         for (int j = K - 1; j > 0; --j) {
-            const bool sw = bd[j] < bd[j - 1] ||
-                            (bd[j] == bd[j - 1] && orig_of(orig, bs[j]) < orig_of(orig, bs[j - 1]));
-            if (sw) {
-                float tf = bd[j]; bd[j] = bd[j - 1]; bd[j - 1] = tf;
-                int32_t ti = bs[j]; bs[j] = bs[j - 1]; bs[j - 1] = ti;
-            }
+            const bool gt_lo = bd[j - 1] > dd || (bd[j - 1] == dd && bo[j - 1] > o);
+            const float nd = gt_lo ? bd[j - 1] : (gt_hi ? dd : bd[j]);
+            const int32_t no = gt_lo ? bo[j - 1] : (gt_hi ? o : bo[j]);
+            bd[j] = nd;
+            bo[j] = no;
+            gt_hi = gt_lo;
+        }
+        if (gt_hi) {
+            bd[0] = dd;
+            bo[0] = o;
         }
     };
 
@@ -112,6 +117,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
             const float4* src = reinterpret_cast<const float4*>(ix.pts) + (base + lane) * (SP / 4);
 #pragma unroll
             for (int h = 0; h < SP / 4; ++h) cand[lane * (SP / 4) + h] = __ldg(src + h);
+            corig[lane] = __ldg(orig + base + lane);
         }
         __syncwarp();
         const float thr = need ? bd[K - 1] : -INFINITY;
@@ -135,7 +141,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
                 float4 v = cand[t * (SP / 4) + h];
                 c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
             }
-            insert(rdist_rn<DIM>(q, c), (int32_t)(base + t));
+            insert(rdist_rn<DIM>(q, c), corig[t]);
         }
         __syncwarp();
     };
@@ -193,12 +199,13 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
     for (int j = 0; j < K; ++j) {
         if (j < K - k) continue;
         const int jj = j - (K - k);
+        const int32_t o = bo[j] == INT32_MAX ? -1 : bo[j];  // k > n leaves slots empty
         if (d_s) {
             d_s[qi * k + jj] = bd[j];
-            i_s[qi * k + jj] = bs[j];
+            i_s[qi * k + jj] = o >= 0 ? __ldg(ix.rank + o) : -1;
         }
         if (d_o) d_o[o_row * k + jj] = bd[j];
-        if (i_o) i_o[o_row * k + jj] = bs[j] >= 0 ? orig[bs[j]] : -1;
+        if (i_o) i_o[o_row * k + jj] = o;
     }
 }
 
@@ -207,6 +214,7 @@ int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o,
                int8_t* tie_s, cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : 8;
     unsigned g = grid_for(ix.nleaves, kKnnWarps);
+    Stage stage(s, "knn_kernel");
     ::fhg::note_launch();
     knn_kernel<DIM, SP, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o,
                                                          tie_s);
