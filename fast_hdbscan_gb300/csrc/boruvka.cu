@@ -382,12 +382,33 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     if (home_first && __any_sync(kFull, active)) scan_leaf(leaf, active);
 
     // Walk up from the home bucket to the root, searching the sibling subtree
-    // at every ancestor (nearest subtrees first).
+    // at every ancestor (nearest subtrees first).  As in the kNN walk,
+    // children are tested when their parent is expanded and only needed ones
+    // are pushed; a bucket's test is repeated from registers right before it
+    // is scanned.  A lane's key for a node is max(box bound, least core) when
+    // the node holds points of another component, else +inf; the node is
+    // needed when the key is within the lane's threshold.
     int32_t* st = s_stack[warp];
+    auto other = [&](int2 ncn) { return ncn.x != c && ncn.x != kEmpty; };
     int64_t x = home_node;
-    for (int l = 0; l < lvl_lo && x > 0; ++l) x = (x - 1) >> 1;
-    for (int l = lvl_lo; l < lvl_hi && x > 0; ++l) {
+    for (int lv = 0; lv < lvl_lo && x > 0; ++lv) x = (x - 1) >> 1;
+    for (int lv = lvl_lo; lv < lvl_hi && x > 0; ++lv) {
         const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+        x = (x - 1) >> 1;
+        {
+            const int2 ncn = nc[sib];
+            bool need = active && other(ncn) && !(__int_as_float(ncn.y) > thr);
+            if (need) {
+                float b[2 * SP];
+                load_box<SP>(ix.box, sib, b);
+                need = box_lb_n<DIM, SP>(b, q) <= thr;
+            }
+            if (!__any_sync(kFull, need)) continue;
+            if (sib >= first_leaf_node) {
+                scan_leaf(sib - first_leaf_node, need);
+                continue;
+            }
+        }
         int sp = 1;
         if (lane == 0) st[0] = sib;
         __syncwarp();
@@ -395,32 +416,48 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
             --sp;
             const int32_t node = st[sp];
             __syncwarp();
-            const int2 ncn = nc[node];
-            bool need = active && ncn.x != c && ncn.x != kEmpty && !(__int_as_float(ncn.y) > thr);
-            if (need) {
-                float b[2 * SP];
-                load_box<SP>(ix.box, node, b);
-                need = box_lb_n<DIM, SP>(b, q) <= thr;
-            }
-            if (!__any_sync(kFull, need)) continue;
-            if (node >= first_leaf_node) {
-                scan_leaf(node - first_leaf_node, need);
-            } else {
-                const int32_t l = 2 * node + 1, r = l + 1;
-                float bl[2 * SP], br[2 * SP];
+            const int32_t l = 2 * node + 1, r = l + 1;
+            const int2 ncl = nc[l], ncr = nc[r];
+            bool nl = active && other(ncl) && !(__int_as_float(ncl.y) > thr);
+            bool nr = active && other(ncr) && !(__int_as_float(ncr.y) > thr);
+            const bool pl = __any_sync(kFull, nl), pr = __any_sync(kFull, nr);
+            if (!pl && !pr) continue;
+            float bl[2 * SP], br[2 * SP];
+            float kl = INFINITY, kr = INFINITY;
+            if (pl) {
                 load_box<SP>(ix.box, l, bl);
+                if (other(ncl)) kl = fmaxf(box_lb_n<DIM, SP>(bl, q), __int_as_float(ncl.y));
+                nl = nl && kl <= thr;
+            }
+            if (pr) {
                 load_box<SP>(ix.box, r, br);
-                const float ll = box_lb_n<DIM, SP>(bl, ctr), lr = box_lb_n<DIM, SP>(br, ctr);
-                const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
-                if (lane == 0) {
-                    st[sp] = far;
-                    st[sp + 1] = near;
+                if (other(ncr)) kr = fmaxf(box_lb_n<DIM, SP>(br, q), __int_as_float(ncr.y));
+                nr = nr && kr <= thr;
+            }
+            const bool al = __any_sync(kFull, nl), ar = __any_sync(kFull, nr);
+            if (!al && !ar) continue;
+            const bool left_first =
+                !(al && ar) ? al : box_lb_n<DIM, SP>(bl, ctr) <= box_lb_n<DIM, SP>(br, ctr);
+            if (l >= first_leaf_node) {
+                // thresholds may shrink while the first bucket is scanned
+                const int32_t n1 = left_first ? l : r, n2 = left_first ? r : l;
+                if (left_first ? al : ar) scan_leaf(n1 - first_leaf_node, left_first ? nl : nr);
+                if (left_first ? ar : al) {
+                    const bool need2 = active && (left_first ? kr : kl) <= thr;
+                    if (__any_sync(kFull, need2)) scan_leaf(n2 - first_leaf_node, need2);
                 }
-                sp += 2;
+            } else {
+                const int32_t nearc = left_first ? l : r, farc = left_first ? r : l;
+                const bool an = left_first ? al : ar, af = left_first ? ar : al;
+                if (lane == 0) {
+                    int t = sp;
+                    if (af) st[t++] = farc;
+                    if (an) st[t] = nearc;
+                }
+                sp += (an ? 1 : 0) + (af ? 1 : 0);
                 __syncwarp();
             }
         }
-        x = (x - 1) >> 1;
     }
     if (!valid || bq == seed_q) return;
     cand_w[p] = bw;
