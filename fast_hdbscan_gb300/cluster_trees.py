@@ -163,15 +163,52 @@ def get_point_membership_strength_vector(tree, clusters, labels):
 
 
 def simplify_hierarchy(condensed_tree, persistence_threshold):
-    """cluster_trees.py:774."""
-    raise NotImplementedError("cluster_selection_persistence is not on the GPU engine yet")
+    """cluster_trees.py:774.  Like the reference, relabels the rows it keeps in
+    the argument's arrays in place and returns the simplified tree."""
+    ct = condensed_tree
+    rows = len(ct.parent)
+    if rows == 0:
+        return ct
+    d = _ct_dev(ct)
+    E = _native.empty
+    op, oc, ol, os_ = E(rows, np.int64), E(rows, np.int64), E(rows, np.float32), E(rows, np.float32)
+    k = ctypes.c_int64(0)
+    V = _native.vptr
+    _native.check(_native.load().fhg_simplify_hierarchy(
+        *[V(x) for x in d], rows, float(persistence_threshold), V(op), V(oc), V(ol), V(os_),
+        ctypes.byref(k), _native.stream_ptr()))
+    for host, dev in zip((ct.parent, ct.child, ct.lambda_val), d[:3]):
+        if isinstance(host, np.ndarray) and host.flags.writeable:
+            np.copyto(host, dev.cpu().numpy().astype(host.dtype, copy=False))
+    r = k.value
+    return CondensedTree(op[:r].cpu().numpy(), oc[:r].cpu().numpy(), ol[:r].cpu().numpy(),
+                         os_[:r].cpu().numpy())
 
 
 def cluster_epsilon_search(clusters, cluster_tree, min_epsilon=0.0):
     """cluster_trees.py:834."""
-    raise NotImplementedError("cluster_selection_epsilon is not on the GPU engine yet")
+    clusters = np.asarray(clusters, dtype=np.int64)
+    if len(clusters) == 0:
+        return np.zeros(0, dtype=np.int64)
+    rows = len(cluster_tree.parent)
+    d = _ct_dev(cluster_tree)
+    d_sel = _dev(clusters, np.int64)
+    out = _native.empty(len(clusters), np.int64)
+    k = ctypes.c_int64(0)
+    V = _native.vptr
+    _native.check(_native.load().fhg_cluster_epsilon_search(
+        *[V(x) for x in d], rows, V(d_sel), len(clusters), float(min_epsilon), V(out),
+        ctypes.byref(k), _native.stream_ptr()))
+    return out[:k.value].cpu().numpy()
 
 
 def get_cluster_labelling_at_cut(linkage_tree, cut, min_cluster_size):
-    """cluster_trees.py:906."""
-    raise NotImplementedError("DBSCAN cuts are not on the GPU engine yet")
+    """cluster_trees.py:906 (HDBSCAN.dbscan_clustering)."""
+    lk = np.ascontiguousarray(linkage_tree, dtype=np.float64)
+    m = lk.shape[0]
+    labels = _native.empty(m + 1, np.int64)
+    d_lk = _dev(lk, np.float64) if m > 0 else None
+    _native.check(_native.load().fhg_labelling_at_cut(
+        _native.vptr(d_lk), m, float(cut), int(min_cluster_size), _native.vptr(labels),
+        _native.stream_ptr()))
+    return labels.cpu().numpy().astype(np.intp, copy=False)

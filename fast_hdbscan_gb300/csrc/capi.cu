@@ -408,6 +408,82 @@ FHG_API int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* c
     return membership_strengths(ws, ct, sel, n_sel, labels_dev, probs_dev);
 }
 
+// --------------------------------------------------------- selection options
+FHG_API int fhg_simplify_hierarchy(int64_t* parent_dev, int64_t* child_dev, float* lambda_dev,
+                                   const float* child_size_dev, int64_t rows, double threshold,
+                                   int64_t* out_parent_dev, int64_t* out_child_dev,
+                                   float* out_lambda_dev, float* out_child_size_dev,
+                                   int64_t* out_rows_host, void* stream) {
+    FHG_TRY(check_ptrs("fhg_simplify_hierarchy", {out_rows_host}));
+    *out_rows_host = 0;
+    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_simplify_hierarchy",
+                       {parent_dev, child_dev, lambda_dev, child_size_dev, out_parent_dev,
+                        out_child_dev, out_lambda_dev, out_child_size_dev}));
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    Condensed ct, out;
+    FHG_TRY(condensed_from_arrays(ws, parent_dev, child_dev, lambda_dev, child_size_dev, rows, &ct));
+    FHG_TRY(simplify_hierarchy(ws, ct, threshold, &out));
+    // the input arrays, relabelled in place where rows are kept
+    FHG_TRY(condensed_to_arrays(ct, parent_dev, child_dev, lambda_dev,
+                                const_cast<float*>(child_size_dev), s));
+    FHG_TRY(condensed_to_arrays(out, out_parent_dev, out_child_dev, out_lambda_dev,
+                                out_child_size_dev, s));
+    *out_rows_host = out.rows;
+    return FHG_OK;
+}
+
+FHG_API int fhg_cluster_epsilon_search(const int64_t* parent_dev, const int64_t* child_dev,
+                                       const float* lambda_dev, const float* child_size_dev,
+                                       int64_t rows, const int64_t* clusters_dev,
+                                       int64_t n_clusters, double min_epsilon, int64_t* out_dev,
+                                       int64_t* n_out_host, void* stream) {
+    FHG_TRY(check_ptrs("fhg_cluster_epsilon_search", {n_out_host}));
+    *n_out_host = 0;
+    if (n_clusters <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_cluster_epsilon_search",
+                       {parent_dev, child_dev, lambda_dev, child_size_dev, clusters_dev, out_dev}));
+    if (rows <= 0) {
+        set_error("fhg_cluster_epsilon_search: empty cluster tree");
+        return FHG_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    Condensed ct;
+    FHG_TRY(condensed_from_arrays(ws, parent_dev, child_dev, lambda_dev, child_size_dev, rows, &ct));
+    int32_t *sel, *out;
+    FHG_TRY(ws.alloc(&sel, (size_t)n_clusters));
+    FHG_TRY(ws.alloc(&out, (size_t)n_clusters));
+    ::fhg::note_launch();
+    narrow_sel_kernel<<<grid_for(n_clusters, 256), 256, 0, s>>>(n_clusters, clusters_dev, sel);
+    FHG_CUDA(cudaGetLastError());
+    int64_t k = 0;
+    FHG_TRY(epsilon_search(ws, ct, sel, n_clusters, min_epsilon, out, &k));
+    if (k > 0) {
+        ::fhg::note_launch();
+        widen_sel_kernel<<<grid_for(k, 256), 256, 0, s>>>(k, out, out_dev);
+        FHG_CUDA(cudaGetLastError());
+    }
+    *n_out_host = k;
+    return FHG_OK;
+}
+
+FHG_API int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cut,
+                                 int64_t min_cluster_size, int64_t* labels_dev, void* stream) {
+    if (m < 0) {
+        set_error("fhg_labelling_at_cut: negative row count");
+        return FHG_ERR_INVALID;
+    }
+    FHG_TRY(check_ptrs("fhg_labelling_at_cut", {labels_dev}));
+    if (m > 0) FHG_TRY(check_ptrs("fhg_labelling_at_cut", {linkage_dev}));
+    cudaStream_t s = as_stream(stream);
+    Workspace ws(s);
+    Linkage lk;
+    FHG_TRY(linkage_from_f64(ws, linkage_dev, m, &lk));
+    return labelling_at_cut(ws, lk, cut, min_cluster_size, labels_dev);
+}
+
 // ---------------------------------------------------------------- fused fit
 FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
                             int64_t min_cluster_size, int32_t selection_method,
@@ -425,10 +501,6 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     if (selection_method != 0 && selection_method != 1) {
         set_error("Invalid cluster_selection_method %d", selection_method);
         return FHG_ERR_INVALID;
-    }
-    if (epsilon > 0.0 || persistence > 0.0) {
-        set_error("cluster_selection_epsilon/persistence are not implemented on the GPU yet");
-        return FHG_ERR_UNSUPPORTED;
     }
     if (n < 2) {
         set_error("fhg_hdbscan_fit needs at least two points");
@@ -461,6 +533,11 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     // hdbscan.py:521: the fit path condenses without max_cluster_size; only
     // the EOM selection reads it.
     FHG_TRY(condense_tree(ws, lk, min_cluster_size, INFINITY, &ct));
+    if (persistence > 0.0 && ct.rows > 0) {  // hdbscan.py:528
+        Condensed simple;
+        FHG_TRY(simplify_hierarchy(ws, ct, persistence, &simple));
+        ct = simple;
+    }
     if (ct_rows_host) *ct_rows_host = ct.rows;
     if (ct_parent_dev && ct_child_dev && ct_lambda_dev && ct_size_dev)
         FHG_TRY(condensed_to_arrays(ct, ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, s));
@@ -469,6 +546,14 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     int64_t k = 0;
     if (selection_method == 0) FHG_TRY(select_eom(ws, ct, max_cluster_size, allow_single_cluster != 0, sel, &k));
     else FHG_TRY(select_leaf(ws, ct, sel, &k));
+    if (k > 1 && epsilon > 0.0) {  // hdbscan.py:555
+        int32_t* searched;
+        FHG_TRY(ws.alloc(&searched, (size_t)k));
+        int64_t k2 = 0;
+        FHG_TRY(epsilon_search(ws, ct, sel, k, epsilon, searched, &k2));
+        sel = searched;
+        k = k2;
+    }
     if (n_selected_host) *n_selected_host = k;
     if (selected_dev && k > 0) {
         ::fhg::note_launch();

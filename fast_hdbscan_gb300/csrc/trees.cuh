@@ -60,6 +60,17 @@ int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t
 int membership_strengths(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t n_sel,
                          const int64_t* labels, float* probs);
 
+// Selection options (cluster_trees.py:774, :834, :906).
+// simplify_hierarchy relabels the kept rows of `ct` in place, as the
+// reference mutates its argument, and returns the compacted tree in `out`.
+int simplify_hierarchy(Workspace& ws, const Condensed& ct, double threshold, Condensed* out);
+// The reference's order of the searched selection; out holds up to n_sel.
+int epsilon_search(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t n_sel,
+                   double min_epsilon, int32_t* out, int64_t* n_out);
+// DBSCAN labels of every point at a cut of the linkage tree.
+int labelling_at_cut(Workspace& ws, const Linkage& lk, double cut, int64_t min_cluster_size,
+                     int64_t* labels);
+
 // Device-side copies to the reference's dtypes.
 int linkage_to_f64(const Linkage& lk, double* out, cudaStream_t s);
 int condensed_to_arrays(const Condensed& ct, int64_t* parent, int64_t* child, float* lambda,

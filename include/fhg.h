@@ -156,9 +156,37 @@ int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* child_dev
                              const int64_t* sel_dev, int64_t n_sel, const int64_t* labels_dev,
                              int64_t n_samples, float* probs_dev, void* stream);
 
+/* Replaces cluster_trees.py:774 simplify_hierarchy(condensed_tree,
+ * persistence_threshold).  Like the reference, relabels the rows it keeps in
+ * the input arrays in place; the simplified tree (kept rows, in order) goes
+ * to out_* (room for `rows` rows), *out_rows_host receives its row count. */
+int fhg_simplify_hierarchy(int64_t* parent_dev, int64_t* child_dev, float* lambda_dev,
+                           const float* child_size_dev, int64_t rows, double threshold,
+                           int64_t* out_parent_dev, int64_t* out_child_dev,
+                           float* out_lambda_dev, float* out_child_size_dev,
+                           int64_t* out_rows_host, void* stream);
+
+/* Replaces cluster_trees.py:834 cluster_epsilon_search(clusters,
+ * cluster_tree, min_epsilon) over the child_size > 1 rows of the given tree.
+ * out_dev holds up to n_clusters ids; *n_out_host receives the count. */
+int fhg_cluster_epsilon_search(const int64_t* parent_dev, const int64_t* child_dev,
+                               const float* lambda_dev, const float* child_size_dev,
+                               int64_t rows, const int64_t* clusters_dev, int64_t n_clusters,
+                               double min_epsilon, int64_t* out_dev, int64_t* n_out_host,
+                               void* stream);
+
+/* Replaces cluster_trees.py:906 get_cluster_labelling_at_cut(linkage_tree,
+ * cut, min_cluster_size) (hdbscan.py:824 HDBSCAN.dbscan_clustering):
+ * labels_dev receives int64[m + 1] labels, -1 for noise. */
+int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cut,
+                         int64_t min_cluster_size, int64_t* labels_dev, void* stream);
+
 /* The whole fit of hdbscan.py:686 HDBSCAN.fit / :199 fast_hdbscan on device
  * data (Euclidean, no sample weights): spatial index, kNN core distances,
- * Boruvka MST and the tree passes, with every intermediate kept in HBM.
+ * Boruvka MST and the tree passes (with cluster_selection_persistence and
+ * cluster_selection_epsilon as in hdbscan.py:528-559), with every
+ * intermediate kept in HBM.  The condensed tree returned is the simplified
+ * one when persistence > 0; selected_dev receives the final selection.
  *   selection_method: 0 = "eom", 1 = "leaf".
  *   Required outputs: labels_dev (int64[n]), probs_dev (float32[n]).
  *   Optional outputs (NULL to skip): mst_dev ((n-1) x 3 float64, sorted as

@@ -1005,8 +1005,34 @@ static int64_t traverse_upwards(const ctree* c, double min_eps, int64_t root, in
     }
 }
 
-/* cluster_trees.py:834 cluster_epsilon_search (segments_in_branch :881 marks
- * every cluster below the chosen ancestor as processed) */
+/* cluster_trees.py:881 segments_in_branch: the closure of {seg} under
+ * x -> {children[i], children[i+1]}, i = np.searchsorted(parents, x), over the
+ * cluster tree sorted by parent.  The lookup does not check parents[i] == x:
+ * for a leaf x it takes the first two children of the next larger parent, as
+ * the reference does.  Marks the closure in `processed`. */
+static void segments_in_branch(const int64_t* sp, const int64_t* sc, int64_t len, int64_t seg,
+                               uint8_t* processed, int64_t mx) {
+    int64_t* stack = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * (mx + 2)));
+    int64_t top = 0;
+    stack[top++] = seg;
+    while (top) {
+        int64_t x = stack[--top];
+        if (x < 0 || x > mx || processed[x]) continue;
+        processed[x] = 1;
+        int64_t lo = 0, hi = len;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) / 2;
+            if (sp[mid] < x) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo >= len) continue;
+        stack[top++] = sc[lo];
+        if (lo + 1 < len) stack[top++] = sc[lo + 1];
+    }
+    free(stack);
+}
+
+/* cluster_trees.py:834 cluster_epsilon_search */
 int64_t orc_cluster_epsilon_search(const int64_t* parent, const int64_t* child, const float* lam,
                                    const float* size, int64_t rows, const int64_t* clusters,
                                    int64_t n_clusters, double min_eps, int64_t* out) {
@@ -1017,6 +1043,24 @@ int64_t orc_cluster_epsilon_search(const int64_t* parent, const int64_t* child, 
         if (c.child[i] > mx) mx = c.child[i];
     }
     uint8_t* processed = (uint8_t*)calloc((size_t)(mx + 2), 1);
+    /* np.argsort(cluster_tree.parent): a stable order (siblings share a parent,
+     * so the pair of children taken for a parent is the same either way) */
+    int64_t* sp = (int64_t*)malloc(sizeof(int64_t) * (size_t)(c.n + 1));
+    int64_t* sc = (int64_t*)malloc(sizeof(int64_t) * (size_t)(c.n + 1));
+    for (int64_t i = 0; i < c.n; ++i) {
+        sp[i] = c.parent[i];
+        sc[i] = c.child[i];
+    }
+    for (int64_t i = 1; i < c.n; ++i) { /* insertion sort, stable */
+        int64_t kp = sp[i], kc = sc[i], j = i - 1;
+        while (j >= 0 && sp[j] > kp) {
+            sp[j + 1] = sp[j];
+            sc[j + 1] = sc[j];
+            --j;
+        }
+        sp[j + 1] = kp;
+        sc[j + 1] = kc;
+    }
     int64_t ns = 0;
     for (int64_t q = 0; q < n_clusters; ++q) {
         int64_t cl = clusters[q];
@@ -1029,23 +1073,15 @@ int64_t orc_cluster_epsilon_search(const int64_t* parent, const int64_t* child, 
             if (!processed[cl]) {
                 int64_t par = traverse_upwards(&c, min_eps, root, cl);
                 out[ns++] = par;
-                /* segments_in_branch: par and all its cluster-tree descendants */
-                int64_t* stack = (int64_t*)malloc(sizeof(int64_t) * (size_t)(mx + 2));
-                int64_t sp = 0;
-                stack[sp++] = par;
-                while (sp) {
-                    int64_t s = stack[--sp];
-                    if (s <= mx) processed[s] = 1;
-                    for (int64_t i = 0; i < c.n; ++i)
-                        if (c.parent[i] == s) stack[sp++] = c.child[i];
-                }
-                free(stack);
+                segments_in_branch(sp, sc, c.n, par, processed, mx);
             }
         } else {
             out[ns++] = cl;
         }
     }
     free(processed);
+    free(sp);
+    free(sc);
     free_ctree(&c);
     return ns;
 }

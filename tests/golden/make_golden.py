@@ -144,17 +144,75 @@ def run_case(name, factory, kwargs, ref):
           f"noise={(out['labels'] == -1).sum()} ({time.time() - t0:.1f}s)")
 
 
+def add_cuts(name):
+    """DBSCAN cuts of the fixture's linkage tree (hdbscan.py:824 ->
+    get_cluster_labelling_at_cut) at quantiles of its merge distances, with
+    the estimator's min_cluster_size for the cut (min_samples when given)."""
+    from fast_hdbscan.cluster_trees import get_cluster_labelling_at_cut
+
+    path = os.path.join(HERE, name + ".npz")
+    g = dict(np.load(path))
+    lk = g["linkage"]
+    if lk.shape[0] == 0:
+        return
+    finite = lk[:, 2][np.isfinite(lk[:, 2])]
+    cuts = np.unique(np.quantile(finite, [0.1, 0.5, 0.9, 0.99])) if finite.size else np.zeros(0)
+    cuts = np.concatenate([cuts, [np.inf]])
+    mcs = int(g["min_samples"])
+    g["dbscan_cuts"] = cuts.astype(np.float64)
+    g["dbscan_min_cluster_size"] = np.int64(mcs)
+    g["dbscan_labels"] = np.stack(
+        [np.asarray(get_cluster_labelling_at_cut(lk, c, mcs), dtype=np.int64) for c in cuts])
+    np.savez_compressed(path, **g)
+
+
+def _crafted_cluster_tree():
+    """A cluster tree (child_size > 1 rows) where segments_in_branch's
+    unchecked searchsorted matters: root 10 -> (11, 12), 11 -> (13, 14),
+    12 -> (15, 16), 15 -> (17, 18).  From leaf 13 the lookup lands on parent
+    15, so 17 and 18 are marked as processed with 11's branch."""
+    parent = np.array([10, 10, 11, 11, 12, 12, 15, 15], dtype=np.int64)
+    child = np.array([11, 12, 13, 14, 15, 16, 17, 18], dtype=np.int64)
+    lam = np.array([0.5, 0.5, 2.0, 2.0, 1.0, 1.0, 4.0, 4.0], dtype=np.float32)
+    size = np.array([6, 8, 3, 3, 5, 3, 2, 3], dtype=np.float32)
+    return parent, child, lam, size
+
+
+def function_fixtures():
+    """Function-level fixtures: cluster_epsilon_search on a crafted tree."""
+    from fast_hdbscan.cluster_trees import CondensedTree, cluster_epsilon_search
+
+    parent, child, lam, size = _crafted_cluster_tree()
+    tree = CondensedTree(parent, child, lam, size)
+    cases = [([13, 17], 1.5), ([13, 14, 16, 17, 18], 1.5), ([17, 13], 1.5),
+             ([13, 17], 0.75), ([16, 17, 18], 3.0)]
+    out = {"parent": parent, "child": child, "lambda_val": lam, "child_size": size}
+    for i, (sel, eps) in enumerate(cases):
+        res = cluster_epsilon_search(np.array(sel, dtype=np.int64), tree, min_epsilon=eps)
+        out[f"sel_{i}"] = np.array(sel, dtype=np.int64)
+        out[f"eps_{i}"] = np.float64(eps)
+        out[f"out_{i}"] = np.asarray(res, dtype=np.int64)
+        print(f"eps search {sel} eps={eps} -> {list(out[f'out_{i}'])}")
+    np.savez_compressed(os.path.join(HERE, "fn_eps_search.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--only", nargs="*")
+    ap.add_argument("--cuts-only", action="store_true",
+                    help="only add the DBSCAN-cut fields to existing fixtures")
     args = ap.parse_args()
     sys.path.insert(1, args.reference)
     import fast_hdbscan  # noqa: F401
     for name, (factory, kwargs) in CASES.items():
         if args.only and name not in args.only:
             continue
-        run_case(name, factory, kwargs, args.reference)
+        if not args.cuts_only:
+            run_case(name, factory, kwargs, args.reference)
+        add_cuts(name)
+    if not args.only:
+        function_fixtures()
 
 
 if __name__ == "__main__":

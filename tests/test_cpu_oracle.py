@@ -15,7 +15,9 @@ import pytest
 from conftest import GOLDEN
 from oracle import oracle as O
 
-FIXTURES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+# fit fixtures; fn_*.npz hold function-level cases
+FIXTURES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith("fn_"))
 # The reference indexes knn[-1] when min_samples >= n (k exceeds the point
 # count); its MST for that fixture has edges to "point -1".  Only its labels
 # and probabilities (all noise) are meaningful there.
@@ -115,3 +117,29 @@ def test_oracle_parallel_threads_same_weights():
     c4 = O.fit(g["X"], 15, 25, mode=1, nthreads=4)
     np.testing.assert_array_equal(c1.mst, c4.mst)
     np.testing.assert_array_equal(c1.labels, c4.labels)
+
+
+@pytest.mark.parametrize("name", sorted(set(FIXTURES) - QUIRK))
+def test_oracle_dbscan_cut_bitexact(name):
+    """get_cluster_labelling_at_cut (cluster_trees.py:906) at several cuts of
+    every fixture's reference linkage tree."""
+    g = _load(name)
+    if "dbscan_cuts" not in g.files:
+        pytest.skip("no linkage tree")
+    for cut, want in zip(g["dbscan_cuts"], g["dbscan_labels"]):
+        got = O.get_cluster_labelling_at_cut(g["linkage"], float(cut),
+                                             int(g["dbscan_min_cluster_size"]))
+        np.testing.assert_array_equal(got, want)
+
+
+def test_oracle_epsilon_search_crafted_tree():
+    """cluster_epsilon_search (cluster_trees.py:834) on a tree where the
+    reference's segments_in_branch lookup marks clusters outside the branch."""
+    g = np.load(os.path.join(GOLDEN, "fn_eps_search.npz"))
+    ct = O.CondensedTree(g["parent"], g["child"], g["lambda_val"], g["child_size"])
+    i = 0
+    while f"sel_{i}" in g.files:
+        got = O.cluster_epsilon_search(ct, g[f"sel_{i}"], float(g[f"eps_{i}"]))
+        np.testing.assert_array_equal(got, g[f"out_{i}"])
+        i += 1
+    assert i >= 5

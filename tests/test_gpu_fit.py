@@ -23,9 +23,10 @@ from fast_hdbscan_gb300 import synthetic
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN_FIT = ["ka150", "blobs200", "blobs200_ms1", "blobs200_leaf", "blobs200_maxcs",
-              "blobs200_single", "blobs2d_2k", "blobs2d_20k", "umap5d_5k", "vd3d_5k",
-              "vd3d_20k", "edge_two", "edge_1d", "edge_highms", "edge_dups", "edge_mcs_gt_n"]
+GOLDEN_FIT = ["ka150", "ka150_eps", "blobs200", "blobs200_ms1", "blobs200_leaf",
+              "blobs200_maxcs", "blobs200_single", "blobs200_persist", "blobs2d_2k",
+              "blobs2d_20k", "umap5d_5k", "vd3d_5k", "vd3d_20k", "edge_two", "edge_1d",
+              "edge_highms", "edge_dups", "edge_mcs_gt_n"]
 
 
 def _golden(name):
@@ -35,7 +36,9 @@ def _golden(name):
 def _kw(g):
     return dict(cluster_selection_method=str(g["cluster_selection_method"]),
                 max_cluster_size=float(g["max_cluster_size"]),
-                allow_single_cluster=bool(g["allow_single_cluster"]))
+                allow_single_cluster=bool(g["allow_single_cluster"]),
+                cluster_selection_epsilon=float(g["cluster_selection_epsilon"]),
+                cluster_selection_persistence=float(g["cluster_selection_persistence"]))
 
 
 def _align_labels(ref, other):
