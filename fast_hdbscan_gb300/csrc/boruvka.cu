@@ -51,11 +51,19 @@ __device__ __forceinline__ float key_weight(unsigned long long k) {
 // ------------------------------------------------------------- kNN to core
 // core2 = squared distance to the k-th neighbour (itself included); +inf when
 // there are fewer than k points, 0 for min_samples <= 1 (boruvka.py:581-601).
+// open[p] arrives as the kNN kernel's boundary-tie flag and leaves as "a seed
+// of weight core2[p] is not provably final": some point outside p's list may
+// lie within its core distance (the core distance reaches the k-th distance
+// and another point ties with the k-th).
 __global__ void core_from_knn_kernel(int64_t n, int kk, int k, int ms,
-                                     const float* __restrict__ knn_d_s, float* __restrict__ core2) {
+                                     const float* __restrict__ knn_d_s, float* __restrict__ core2,
+                                     int8_t* __restrict__ open) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    core2[p] = ms <= 1 ? 0.0f : (k > kk ? INFINITY : knn_d_s[p * kk + kk - 1]);
+    const float kth = knn_d_s[p * kk + kk - 1];
+    const float c = ms <= 1 ? 0.0f : (k > kk ? INFINITY : kth);
+    core2[p] = c;
+    open[p] = (open[p] && !(c < kth)) ? 1 : 0;
 }
 
 __global__ void outputs_kernel(int64_t n, int kk, int k, const int32_t* __restrict__ orig,
@@ -232,13 +240,20 @@ __global__ void reset_keys_kernel(const int32_t* __restrict__ reps, int64_t nrep
 // Every point's best edge among its own kNN list (boruvka.py:474 uses the same
 // lists), published to its component's key before any point searches, so the
 // search starts from every component's seed bound.
+// exhausted[p]: every kNN neighbour of p was already in p's component in an
+// earlier round -- it stays so, as components only merge.
 __global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
                             const float* __restrict__ knn_d, const float* __restrict__ core2,
                             const int32_t* __restrict__ comp, const int32_t* __restrict__ orig,
                             unsigned long long* keyA, float* __restrict__ cand_w,
-                            int32_t* __restrict__ cand_q) {
+                            int32_t* __restrict__ cand_q, int8_t* __restrict__ exhausted) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
+    if (exhausted[p]) {
+        cand_w[p] = INFINITY;
+        cand_q[p] = -1;
+        return;
+    }
     const int32_t c = comp[p];
     const float cp = core2[p];
     float bw = INFINITY;
@@ -260,6 +275,8 @@ __global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
     if (bq >= 0) {
         unsigned long long key = pack_key(bw, min(orig[p], bo));
         if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
+    } else {
+        exhausted[p] = 1;
     }
 }
 
@@ -275,10 +292,10 @@ __global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
 // any of its edges can have) is settled without a search when every point
 // at that distance is in its kNN list: the core distance is below the k-th
 // distance, or no point outside the list lies exactly at the k-th distance
-// (knn_tie).  Any other edge then weighs more than the seed.
+// (knn_open clear).  Any other edge then weighs more than the seed.
 template <int DIM, int SP>
 __global__ void __launch_bounds__(kSW * 32) search_kernel(
-    IndexView ix, int k, const float* __restrict__ knn_d, const int8_t* __restrict__ knn_tie,
+    IndexView ix, const int8_t* __restrict__ knn_open,
     const float* __restrict__ core2, const int32_t* __restrict__ comp,
     const int2* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
     int32_t* __restrict__ cand_q, int lvl_lo, int lvl_hi) {
@@ -301,8 +318,7 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
         bw = cand_w[p];
         bq = cand_q[p];
         if (bq >= 0) bo = ix.orig[bq];
-        const bool settled =
-            bq >= 0 && bw == cp && (cp < knn_d[p * k + k - 1] || !knn_tie[p]);
+        const bool settled = bq >= 0 && bw == cp && !knn_open[p];
         const float thr0 = fminf(bw, key_weight(*(volatile unsigned long long*)&keyA[c]));
         active = !settled && !(cp > thr0);
     }
@@ -577,7 +593,7 @@ __global__ void finalize_edges_kernel(int64_t m, const int32_t* __restrict__ src
 }
 
 template <int DIM>
-int launch_search(const fhg_index& ix, int k, const float* knn_d, const int8_t* knn_tie,
+int launch_search(const fhg_index& ix, const int8_t* knn_open,
                   const float* core2, const int32_t* comp, const int2* nc,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : 8;
@@ -589,7 +605,7 @@ int launch_search(const fhg_index& ix, int k, const float* knn_d, const int8_t* 
         Stage stage(s, "search_kernel");
         ::fhg::note_launch();
         search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
-            view_of(ix), k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, sp[0],
+            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, sp[0],
             sp[1]);
         FHG_CUDA(cudaGetLastError());
     }
@@ -597,25 +613,26 @@ int launch_search(const fhg_index& ix, int k, const float* knn_d, const int8_t* 
 }
 
 int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
-                 const int8_t* knn_tie, const float* core2, const int32_t* comp,
+                 const int8_t* knn_open, int8_t* exhausted, const float* core2,
+                 const int32_t* comp,
                  const int2* nc, unsigned long long* keyA, float* cand_w, int32_t* cand_q,
                  cudaStream_t s) {
     const int64_t n = ix.n;
     if (n > 0) {
         ::fhg::note_launch();
         seed_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, k, knn_s, knn_d, core2, comp, ix.orig,
-                                                       keyA, cand_w, cand_q);
+                                                       keyA, cand_w, cand_q, exhausted);
         FHG_CUDA(cudaGetLastError());
     }
     switch (ix.d) {
-        case 1: return launch_search<1>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 2: return launch_search<2>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 3: return launch_search<3>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 4: return launch_search<4>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 5: return launch_search<5>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 6: return launch_search<6>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 7: return launch_search<7>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
-        default: return launch_search<8>(ix, k, knn_d, knn_tie, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 1: return launch_search<1>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 2: return launch_search<2>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 3: return launch_search<3>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 4: return launch_search<4>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 5: return launch_search<5>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 6: return launch_search<6>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 7: return launch_search<7>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        default: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
     }
 }
 
@@ -661,11 +678,11 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&knn_d, (size_t)(n * k)));
     FHG_TRY(ws.alloc(&knn_s, (size_t)(n * k)));
     if (nbr_o) FHG_TRY(ws.alloc(&knn_i_o, (size_t)(n * k)));  // neighbour ids only
-    int8_t* knn_tie;
-    FHG_TRY(ws.alloc(&knn_tie, (size_t)n));
-    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s, knn_tie));
+    int8_t* knn_open;  // the kNN kernel's tie flags, then "seed not provably final"
+    FHG_TRY(ws.alloc(&knn_open, (size_t)n));
+    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s, knn_open));
     FHG_TRY(ws.alloc(&core2, (size_t)n));
-    LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2);
+    LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2, knn_open);
     if (core_o || nbr_o)
         LAUNCH(outputs_kernel, n, n, k, kq, ix.orig, core2, knn_i_o, core_o, nbr_o);
     if (n < 2) return FHG_OK;
@@ -734,6 +751,9 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&nc, (size_t)ix.nnodes));
     FHG_TRY(ws.alloc(&cand_w, (size_t)n));
     FHG_TRY(ws.alloc(&cand_q, (size_t)n));
+    int8_t* exhausted;
+    FHG_TRY(ws.alloc(&exhausted, (size_t)n));
+    FHG_CUDA(cudaMemsetAsync(exhausted, 0, (size_t)n, s));
     uint32_t* kpos;
     FHG_TRY(ws.alloc(&kpos, (size_t)n));
     FHG_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t) * n, s));
@@ -754,8 +774,8 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         }
         {
             Stage stage(s, "boruvka_search");
-            FHG_TRY(search_round(ix, k, knn_s, knn_d, knn_tie, core2, comp, nc, keyA, cand_w,
-                                 cand_q, s));
+            FHG_TRY(search_round(ix, k, knn_s, knn_d, knn_open, exhausted, core2, comp, nc, keyA,
+                                 cand_w, cand_q, s));
         }
         Stage merge_stage(s, "boruvka_merge");
         LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);
