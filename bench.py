@@ -209,7 +209,7 @@ def run_gb300(args):
 
     def step():
         _native.check(lib.fhg_hdbscan_fit(
-            V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, V(labels), V(probs), V(mst),
+            V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, None, 0, V(labels), V(probs), V(mst),
             V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core),
             V(sel), ctypes.byref(nsel), _native.stream_ptr()))
 

@@ -34,10 +34,11 @@ SIGNATURES = {
     "fhg_index_free": (_INT, [_P, _P]),
     "fhg_index_shape": (_INT, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I32)]),
     "fhg_index_knn": (_INT, [_P, _I32, _P, _P, _P]),
-    "fhg_index_boruvka": (_INT, [_P, _I32, _P, _P, _P, ctypes.POINTER(_I32), _P]),
+    "fhg_index_boruvka": (_INT, [_P, _I32, _P, _I32, _P, _P, _P, ctypes.POINTER(_I32), _P]),
     "fhg_sort_mst": (_INT, [_P, _I64, _P, _P]),
-    "fhg_mst_to_linkage_tree": (_INT, [_P, _I64, _P, _P]),
-    "fhg_condense_tree": (_INT, [_P, _I64, _I64, _D, _P, _P, _P, _P, ctypes.POINTER(_I64), _P]),
+    "fhg_mst_to_linkage_tree": (_INT, [_P, _I64, _P, _P, _P]),
+    "fhg_condense_tree": (_INT, [_P, _I64, _I64, _D, _P, _P, _P, _P, _P, ctypes.POINTER(_I64),
+                                 _P]),
     "fhg_extract_eom_clusters": (_INT, [_P, _P, _P, _P, _I64, _D, _INT, _P,
                                         ctypes.POINTER(_I64), _P]),
     "fhg_label_points": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _I64, _P, _P, _P]),
@@ -48,7 +49,7 @@ SIGNATURES = {
     "fhg_cluster_epsilon_search": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _P,
                                           ctypes.POINTER(_I64), _P]),
     "fhg_labelling_at_cut": (_INT, [_P, _I64, _D, _I64, _P, _P]),
-    "fhg_hdbscan_fit": (_INT, [_P, _I64, _I32, _I32, _I64, _I32, _D, _INT, _D, _D,
+    "fhg_hdbscan_fit": (_INT, [_P, _I64, _I32, _I32, _I64, _I32, _D, _INT, _D, _D, _P, _I32,
                                _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_I64),
                                _P, _P, _P, ctypes.POINTER(_I64), _P]),
 }

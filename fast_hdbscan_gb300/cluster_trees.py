@@ -43,24 +43,33 @@ def sort_mst(mst):
     return d_out.cpu().numpy()
 
 
-def mst_to_linkage_tree(sorted_mst):
-    """cluster_trees.py:65."""
+def _linkage(sorted_mst, sample_weights):
     sorted_mst = np.ascontiguousarray(sorted_mst, dtype=np.float64)
     m = sorted_mst.shape[0]
     if m == 0:
         return np.empty((0, 4), dtype=np.float64)
     d_in = _dev(sorted_mst, np.float64)
+    d_w = None if sample_weights is None else _dev(sample_weights, np.float32)
     d_out = _native.empty((m, 4), np.float64)
     _native.check(_native.load().fhg_mst_to_linkage_tree(
-        _native.vptr(d_in), m, _native.vptr(d_out), _native.stream_ptr()))
+        _native.vptr(d_in), m, _native.vptr(d_w), _native.vptr(d_out), _native.stream_ptr()))
     return d_out.cpu().numpy()
+
+
+def mst_to_linkage_tree(sorted_mst):
+    """cluster_trees.py:65."""
+    return _linkage(sorted_mst, None)
+
+
+def mst_to_linkage_tree_w_sample_weights(sorted_mst, sample_weights):
+    """cluster_trees.py:98: sizes are float32 sums of the sample weights."""
+    return _linkage(sorted_mst, np.asarray(sample_weights, dtype=np.float32))
 
 
 def condense_tree(hierarchy, min_cluster_size=10, max_cluster_size=np.inf, sample_weights=None,
                   lambda_method="hdbscan"):
-    """cluster_trees.py:205 (unit sample weights, hdbscan lambda)."""
-    if sample_weights is not None:
-        raise NotImplementedError("sample_weights are not supported by the GPU engine yet")
+    """cluster_trees.py:205 (hdbscan lambda).  With sample weights the
+    hierarchy's size column holds weight sums (mst_to_linkage_tree_w_sample_weights)."""
     if lambda_method != "hdbscan":
         raise NotImplementedError("only lambda_method='hdbscan' is on the fit path")
     h = np.ascontiguousarray(hierarchy, dtype=np.float64)
@@ -68,12 +77,14 @@ def condense_tree(hierarchy, min_cluster_size=10, max_cluster_size=np.inf, sampl
     if m == 0:
         return empty_condensed_tree()
     d_h = _dev(h, np.float64)
+    d_w = None if sample_weights is None else _dev(sample_weights, np.float32)
     cap = 2 * m
     p, c = _native.empty(cap, np.int64), _native.empty(cap, np.int64)
     lam, sz = _native.empty(cap, np.float32), _native.empty(cap, np.float32)
     rows = ctypes.c_int64(0)
     _native.check(_native.load().fhg_condense_tree(
-        _native.vptr(d_h), m, int(min_cluster_size), float(max_cluster_size), _native.vptr(p),
+        _native.vptr(d_h), m, int(min_cluster_size), float(max_cluster_size), _native.vptr(d_w),
+        _native.vptr(p),
         _native.vptr(c), _native.vptr(lam), _native.vptr(sz), ctypes.byref(rows),
         _native.stream_ptr()))
     r = rows.value

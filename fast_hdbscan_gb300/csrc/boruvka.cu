@@ -53,8 +53,11 @@ __device__ __forceinline__ float key_weight(unsigned long long k) {
 // there are fewer than k points, 0 for min_samples <= 1 (boruvka.py:581-601).
 // open[p] arrives as the kNN kernel's boundary-tie flag and leaves as "a seed
 // of weight core2[p] is not provably final": some point outside p's list may
-// lie within its core distance (the core distance reaches the k-th distance
-// and another point ties with the k-th).
+// lie within core2[p] in squared distance (the core value passes the list's
+// k-th squared distance, or reaches it while another point ties with it).
+__device__ __forceinline__ int8_t seed_open(float c, float kth, int8_t tie) {
+    return (!(c < kth) && (c > kth || tie)) ? 1 : 0;
+}
 __global__ void core_from_knn_kernel(int64_t n, int kk, int k, int ms,
                                      const float* __restrict__ knn_d_s, float* __restrict__ core2,
                                      int8_t* __restrict__ open) {
@@ -63,7 +66,37 @@ __global__ void core_from_knn_kernel(int64_t n, int kk, int k, int ms,
     const float kth = knn_d_s[p * kk + kk - 1];
     const float c = ms <= 1 ? 0.0f : (k > kk ? INFINITY : kth);
     core2[p] = c;
-    open[p] = (open[p] && !(c < kth)) ? 1 : 0;
+    open[p] = seed_open(c, kth, open[p]);
+}
+
+// Weighted core distance (boruvka.py:527 sample_weight_core_distance): the
+// plain distance (sqrt of the squared one, boruvka.py:563 queries without
+// output_rdist) to the first neighbour at which the running weight, the
+// point's own included, reaches min_samples.  Slots past the list are the
+// reference's padding (+inf, index -1 -> the weight of the last point).
+__global__ void weighted_core_kernel(int64_t n, int kk, int kq, int ms,
+                                     const float* __restrict__ knn_d_s,
+                                     const int32_t* __restrict__ knn_s,
+                                     const float* __restrict__ w_s, float w_last,
+                                     float* __restrict__ core2, int8_t* __restrict__ open) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double total = 0.0;
+    int j = 0;
+    while (total < (double)ms && j < kq) {
+        const int32_t q = j < kk ? knn_s[p * kk + j] : -1;
+        total += (double)(q >= 0 ? w_s[q] : w_last);
+        ++j;
+    }
+    const int jj = j > 0 ? j - 1 : kq - 1;
+    const float c = jj < kk ? __fsqrt_rn(knn_d_s[p * kk + jj]) : INFINITY;
+    core2[p] = c;
+    open[p] = seed_open(c, knn_d_s[p * kk + kk - 1], open[p]);
+}
+__global__ void gather_weights_kernel(int64_t n, const int32_t* __restrict__ orig,
+                                      const float* __restrict__ w, float* __restrict__ w_s) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) w_s[p] = w[orig[p]];
 }
 
 __global__ void outputs_kernel(int64_t n, int kk, int k, const int32_t* __restrict__ orig,
@@ -80,9 +113,10 @@ __global__ void outputs_kernel(int64_t n, int kk, int k, const int32_t* __restri
 }
 
 // ----------------------------------------------------------------- round 0
+// plain_d: the weighted path's round 0 works on plain (not squared) distances.
 __global__ void round0_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
                               const float* __restrict__ knn_d, const float* __restrict__ core2,
-                              int32_t* __restrict__ target, float* __restrict__ w0,
+                              int plain_d, int32_t* __restrict__ target, float* __restrict__ w0,
                               int* __restrict__ eq_flag) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
@@ -96,7 +130,8 @@ __global__ void round0_kernel(int64_t n, int k, const int32_t* __restrict__ knn_
         if (cp >= cq) {
             if (q != p) {
                 t = q;
-                w = fmaxf(cp, knn_d[p * k + j]);
+                const float d = knn_d[p * k + j];
+                w = fmaxf(cp, plain_d ? __fsqrt_rn(d) : d);
                 if (cq == cp) atomicOr(eq_flag, 1);
             }
             break;
@@ -653,14 +688,23 @@ int finalize_edges(const MstResult& r, double* edges, cudaStream_t s) {
 }
 
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
-                float* core_o, int32_t* nbr_o) {
+                float* core_o, int32_t* nbr_o, const float* weights, int weighted_k) {
     cudaStream_t s = ws.stream();
     const int64_t n = ix.n;
-    const int kq = min_samples > 1 ? min_samples + 1 : 2;  // the reference's k
-    const int k = (int)(kq < n ? kq : n);                  // neighbours that exist
+    const bool weighted = weights != nullptr && n > 1;
+    // the reference's k (boruvka.py:561-585)
+    const int kq = weighted ? weighted_k : (min_samples > 1 ? min_samples + 1 : 2);
+    const int k = (int)(kq < n ? kq : n);  // neighbours that exist
     *out = MstResult();
+    if (kq < 1) {
+        set_error("weighted kNN: k = %d (2 * min_samples / mean weight) is below 1", kq);
+        return FHG_ERR_INVALID;
+    }
     if (k > 64) {
-        set_error("min_samples must be at most 63 (got %d)", min_samples);
+        if (weighted)
+            set_error("weighted kNN: k = %d (2 * min_samples / mean weight) exceeds 64", kq);
+        else
+            set_error("min_samples must be at most 63 (got %d)", min_samples);
         return FHG_ERR_UNSUPPORTED;
     }
     const int64_t m_cap = n > 1 ? n - 1 : 1;
@@ -682,7 +726,19 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&knn_open, (size_t)n));
     FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s, knn_open));
     FHG_TRY(ws.alloc(&core2, (size_t)n));
-    LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2, knn_open);
+    if (weighted) {
+        float* w_s;
+        float w_last = 0.0f;
+        FHG_TRY(ws.alloc(&w_s, (size_t)n));
+        LAUNCH(gather_weights_kernel, n, n, ix.orig, weights, w_s);
+        FHG_CUDA(cudaMemcpyAsync(&w_last, weights + (n - 1), sizeof(float), cudaMemcpyDeviceToHost,
+                                 s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        LAUNCH(weighted_core_kernel, n, n, k, kq, min_samples, knn_d, knn_s, w_s, w_last, core2,
+               knn_open);
+    } else {
+        LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2, knn_open);
+    }
     if (core_o || nbr_o)
         LAUNCH(outputs_kernel, n, n, k, kq, ix.orig, core2, knn_i_o, core_o, nbr_o);
     if (n < 2) return FHG_OK;
@@ -700,7 +756,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
 
     // ---- round 0: kNN-seeded links (boruvka.py:474)
     std::unique_ptr<Stage> r0_stage(new Stage(s, "boruvka_round0"));
-    LAUNCH(round0_kernel, n, n, k, knn_s, knn_d, core2, target, w0, iflag);
+    LAUNCH(round0_kernel, n, n, k, knn_s, knn_d, core2, weighted ? 1 : 0, target, w0, iflag);
     int h_flag[2] = {0, 0};
     FHG_CUDA(cudaMemcpyAsync(h_flag, iflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     FHG_CUDA(cudaStreamSynchronize(s));

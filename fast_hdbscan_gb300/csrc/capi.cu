@@ -99,7 +99,7 @@ using namespace fhg;
 static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 FHG_API const char* fhg_last_error(void) { return last_error(); }
-FHG_API int fhg_abi_version(void) { return 1; }
+FHG_API int fhg_abi_version(void) { return 2; }
 
 FHG_API uint64_t fhg_launch_count(void) { return g_launches.load(); }
 
@@ -186,9 +186,10 @@ FHG_API int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t
     return index_knn(*index, k, nullptr, nullptr, rdist_dev, idx_dev, as_stream(stream));
 }
 
-FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples, double* edges_dev,
-                              int32_t* neighbors_dev, float* core_dev, int32_t* n_rounds_host,
-                              void* stream) {
+FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples,
+                              const float* sample_weights_dev, int32_t weighted_k,
+                              double* edges_dev, int32_t* neighbors_dev, float* core_dev,
+                              int32_t* n_rounds_host, void* stream) {
     if (!index || !edges_dev || !neighbors_dev || !core_dev) {
         set_error("fhg_index_boruvka: null pointer");
         return FHG_ERR_INVALID;
@@ -200,7 +201,8 @@ FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples, double* edg
     cudaStream_t s = as_stream(stream);
     Workspace ws(s);
     MstResult r;
-    FHG_TRY(boruvka_mst(ws, *index, min_samples, &r, core_dev, neighbors_dev));
+    FHG_TRY(boruvka_mst(ws, *index, min_samples, &r, core_dev, neighbors_dev, sample_weights_dev,
+                        weighted_k));
     FHG_TRY(finalize_edges(r, edges_dev, s));
     if (n_rounds_host) *n_rounds_host = r.rounds;
     if (r.m != index->n - 1 && index->n > 1) {
@@ -257,7 +259,8 @@ FHG_API int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, v
     return sorted_mst_to_f64(lk, sorted_dev, s);
 }
 
-FHG_API int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, double* linkage_dev,
+FHG_API int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m,
+                                    const float* sample_weights_dev, double* linkage_dev,
                                     void* stream) {
     if (m <= 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_mst_to_linkage_tree", {sorted_mst_dev, linkage_dev}));
@@ -268,13 +271,14 @@ FHG_API int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, dou
     FHG_TRY(split_mst_f64(ws, sorted_mst_dev, m, &src, &dst, &w));
     Linkage lk;
     FHG_TRY(sort_and_link(ws, m + 1, src, dst, w, nullptr, &lk, /*presorted=*/true));
+    if (sample_weights_dev) FHG_TRY(weighted_sizes(ws, lk, sample_weights_dev));
     return linkage_to_f64(lk, linkage_dev, s);
 }
 
 FHG_API int fhg_condense_tree(const double* linkage_dev, int64_t m, int64_t min_cluster_size,
-                              double max_cluster_size, int64_t* parent_dev, int64_t* child_dev,
-                              float* lambda_dev, float* child_size_dev, int64_t* n_rows_host,
-                              void* stream) {
+                              double max_cluster_size, const float* sample_weights_dev,
+                              int64_t* parent_dev, int64_t* child_dev, float* lambda_dev,
+                              float* child_size_dev, int64_t* n_rows_host, void* stream) {
     FHG_TRY(check_ptrs("fhg_condense_tree", {n_rows_host}));
     *n_rows_host = 0;
     if (m <= 0) return FHG_OK;
@@ -288,6 +292,11 @@ FHG_API int fhg_condense_tree(const double* linkage_dev, int64_t m, int64_t min_
     Workspace ws(s);
     Linkage lk;
     FHG_TRY(linkage_from_f64(ws, linkage_dev, m, &lk));
+    if (sample_weights_dev) {
+        // the size column holds weight sums: leaf counts come from the rows
+        FHG_TRY(linkage_leaf_counts(ws, lk));
+        FHG_TRY(weighted_sizes(ws, lk, sample_weights_dev));
+    }
     Condensed ct;
     FHG_TRY(condense_tree(ws, lk, min_cluster_size, max_cluster_size, &ct));
     FHG_TRY(condensed_to_arrays(ct, parent_dev, child_dev, lambda_dev, child_size_dev, s));
@@ -488,7 +497,8 @@ FHG_API int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cu
 FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
                             int64_t min_cluster_size, int32_t selection_method,
                             double max_cluster_size, int allow_single_cluster, double epsilon,
-                            double persistence, int64_t* labels_dev, float* probs_dev,
+                            double persistence, const float* sample_weights_dev,
+                            int32_t weighted_k, int64_t* labels_dev, float* probs_dev,
                             double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
                             int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
                             int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
@@ -516,7 +526,8 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
         ~IndexGuard() { index_free(p, s); }
     } guard{ix, s};
     MstResult mst;
-    FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev));
+    FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev, sample_weights_dev,
+                        weighted_k));
     if (mst.m != n - 1) {
         set_error("boruvka: spanning forest has %lld edges for %lld points", (long long)mst.m,
                   (long long)n);
@@ -524,6 +535,7 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     }
     Linkage lk;
     FHG_TRY(sort_and_link(ws, n, mst.src, mst.dst, nullptr, mst.w2, &lk));
+    if (sample_weights_dev) FHG_TRY(weighted_sizes(ws, lk, sample_weights_dev));
     {
         Stage stage(s, "outputs");
         if (mst_dev) FHG_TRY(sorted_mst_to_f64(lk, mst_dev, s));

@@ -34,14 +34,17 @@ __device__ __forceinline__ float lambda_of(double d) {
 // node-indexed arrays of its two children.
 __global__ void cases_kernel(int64_t m, int64_t n, const int32_t* __restrict__ left,
                              const int32_t* __restrict__ right, const double* __restrict__ w,
-                             const int32_t* __restrict__ size, double mcs, double max_cs,
-                             int8_t* __restrict__ kase, float* __restrict__ lam,
+                             const int32_t* __restrict__ size, const float* __restrict__ wsize,
+                             double mcs, double max_cs, int8_t* __restrict__ kase,
+                             float* __restrict__ lam,
                              int32_t* __restrict__ par, int8_t* __restrict__ cont,
                              int8_t* __restrict__ birth, int8_t* __restrict__ side) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int32_t L = left[i], R = right[i];
-    const double lc = (double)(float)size[L], rc = (double)(float)size[R];
+    // counts: leaves, or the points' sample weights (cluster_trees.py:253-262)
+    const double lc = wsize ? (double)wsize[L] : (double)(float)size[L];
+    const double rc = wsize ? (double)wsize[R] : (double)(float)size[R];
     int8_t c;
     if (L < n && rc >= mcs) c = C1;
     else if (lc < mcs && rc >= mcs) c = C2;
@@ -240,7 +243,8 @@ __global__ void rows_kernel(int64_t rows, int64_t n, const int32_t* __restrict__
                             const int32_t* __restrict__ emit_u, const int32_t* __restrict__ label,
                             const float* __restrict__ lam, const int32_t* __restrict__ left,
                             const int32_t* __restrict__ right, const int32_t* __restrict__ size,
-                            const int64_t* __restrict__ k6, int32_t* __restrict__ oparent,
+                            const float* __restrict__ wsize, const int64_t* __restrict__ k6,
+                            int32_t* __restrict__ oparent,
                             int32_t* __restrict__ ochild, float* __restrict__ olam,
                             float* __restrict__ osize) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -260,7 +264,8 @@ __global__ void rows_kernel(int64_t rows, int64_t n, const int32_t* __restrict__
         oparent[r] = label[u];
         ochild[r] = (int32_t)(n + 1 + 2 * k6[j] + s);
         olam[r] = lam[u];
-        osize[r] = (float)size[s == 0 ? left[u] : right[u]];
+        const int32_t v = s == 0 ? left[u] : right[u];
+        osize[r] = wsize ? wsize[v] : (float)size[v];
     }
 }
 
@@ -314,7 +319,8 @@ int condense_tree(Workspace& ws, const Linkage& lk, int64_t mcs, double max_cs, 
     FHG_TRY(ws.alloc(&cont, (size_t)nodes));
     FHG_TRY(ws.alloc(&birth, (size_t)nodes));
     FHG_TRY(ws.alloc(&side, (size_t)nodes));
-    LAUNCH(cases_kernel, m, m, n, lk.left, lk.right, lk.w, lk.size, (double)mcs, max_cs, kase, lam,
+    LAUNCH(cases_kernel, m, m, n, lk.left, lk.right, lk.w, lk.size, lk.wsize, (double)mcs, max_cs,
+           kase, lam,
            par, cont, birth, side);
 
     FHG_TRY(ws.alloc(&anc, (size_t)m));
@@ -441,7 +447,7 @@ int condense_tree(Workspace& ws, const Linkage& lk, int64_t mcs, double max_cs, 
         LAUNCH(gather_u32_kernel, rows, rows, kseg, order, key);
         FHG_TRY(radix_sort_u32(tmp, key, order, rows, 0, bits_for(rows)));
         LAUNCH(rows_kernel, rows, rows, n, order, items, reached, emit_u, label, lam, lk.left,
-               lk.right, lk.size, k6, out->parent, out->child, out->lambda, out->csize);
+               lk.right, lk.size, lk.wsize, k6, out->parent, out->child, out->lambda, out->csize);
     }
     return FHG_OK;
 }

@@ -292,14 +292,14 @@ __global__ void relabel_edges_kernel(int64_t m, const int32_t* __restrict__ newi
 
 __global__ void linkage_f64_kernel(int64_t m, const int32_t* __restrict__ left,
                                    const int32_t* __restrict__ right, const double* __restrict__ w,
-                                   const int32_t* __restrict__ sz, int64_t n,
-                                   double* __restrict__ out) {
+                                   const int32_t* __restrict__ sz, const float* __restrict__ wsz,
+                                   int64_t n, double* __restrict__ out) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     out[4 * i + 0] = (double)left[i];
     out[4 * i + 1] = (double)right[i];
     out[4 * i + 2] = w[i];
-    out[4 * i + 3] = (double)sz[n + i];
+    out[4 * i + 3] = wsz ? (double)wsz[n + i] : (double)sz[n + i];
 }
 __global__ void sorted_mst_f64_kernel(int64_t m, const int32_t* __restrict__ ssrc,
                                       const int32_t* __restrict__ sdst,
@@ -467,7 +467,7 @@ int linkage_from_f64(Workspace& ws, const double* lk, int64_t m, Linkage* out) {
 }
 
 int linkage_to_f64(const Linkage& lk, double* out, cudaStream_t s) {
-    LAUNCH(linkage_f64_kernel, lk.m, lk.m, lk.left, lk.right, lk.w, lk.size, lk.n, out);
+    LAUNCH(linkage_f64_kernel, lk.m, lk.m, lk.left, lk.right, lk.w, lk.size, lk.wsize, lk.n, out);
     return FHG_OK;
 }
 int sorted_mst_to_f64(const Linkage& lk, double* out, cudaStream_t s) {
@@ -589,7 +589,7 @@ int link_presorted_noalloc(const double* smst, int64_t m, double* out, cudaStrea
     }
     LAUNCH(linkage_rows_kernel, m, m, n, A, B, (const int32_t*)nullptr, left, right);
     LAUNCH(node_sizes_kernel, nodes, nodes, R, size);
-    LAUNCH(linkage_f64_kernel, m, m, left, right, w, size, n, out);
+    LAUNCH(linkage_f64_kernel, m, m, left, right, w, size, (const float*)nullptr, n, out);
     return FHG_OK;
 }
 

@@ -14,11 +14,14 @@ struct MstResult {
 };
 
 // Runs kNN (k = min_samples + 1, or 2 when min_samples <= 1) and Boruvka.
+// With sample weights (caller order, nullable) the reference's weighted path:
+// k = weighted_k = int(2 * min_samples / mean weight), weighted core
+// distances, round 0 on plain distances (boruvka.py:561-573).
 // `ws` owns every returned buffer.  Optional outputs (nullable):
 //   core_o  [n]       sqrt core distance, caller order
 //   nbr_o   [n*(k-1)] neighbours without the point itself, caller order
-//   knn_d_o/knn_i_o [n*k] full kNN rows, caller order
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
-                float* core_o, int32_t* nbr_o);
+                float* core_o, int32_t* nbr_o, const float* weights = nullptr,
+                int weighted_k = 0);
 
 }  // namespace fhg

@@ -509,7 +509,131 @@ __global__ void rows_compact_kernel(int64_t rows, const uint32_t* __restrict__ k
     os[j] = csize[i];
 }
 
+// ---------------------------------------------------------- sample weights
+__global__ void point_pre_kernel(int64_t n, int64_t m, const int32_t* __restrict__ par,
+                                 const int8_t* __restrict__ side,
+                                 const int32_t* __restrict__ left,
+                                 const int32_t* __restrict__ size,
+                                 const int64_t* __restrict__ pre, const float* __restrict__ w,
+                                 double* __restrict__ vals) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t q = par[p];
+    if (q < 0) return;
+    const int64_t qi = q - n;
+    vals[pre[qi] + (side[p] == 0 ? 1 : 2 * (int64_t)size[left[qi]])] = (double)w[p];
+}
+__global__ void subtree_sums_kernel(int64_t m, int64_t n, int64_t positions,
+                                    const int64_t* __restrict__ pre,
+                                    const int32_t* __restrict__ size,
+                                    const double* __restrict__ excl,
+                                    const double* __restrict__ total, float* __restrict__ wsize) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int64_t b = pre[i], e = b + 2 * (int64_t)size[n + i] - 1;
+    const double hi = e < positions ? excl[e] : *total;
+    wsize[n + i] = (float)(hi - excl[b]);
+}
+// Representative point of every internal node: its leftmost leaf.
+__global__ void rep_init_kernel(int64_t m, const int32_t* __restrict__ left,
+                                int32_t* __restrict__ jmp) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) jmp[i] = left[i];
+}
+__global__ void rep_edges_kernel(int64_t m, int64_t n, const int32_t* __restrict__ left,
+                                 const int32_t* __restrict__ right,
+                                 const int32_t* __restrict__ rep, int32_t* __restrict__ src,
+                                 int32_t* __restrict__ dst) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int32_t l = left[i], r = right[i];
+    src[i] = l < n ? l : rep[l - n];
+    dst[i] = r < n ? r : rep[r - n];
+}
+
 }  // namespace
+
+// Parent and side (0 left, 1 right) of every node, and the preorder position
+// of every internal node (subtree of node n+i: [pre[i], pre[i] + 2*size - 1)).
+static int linkage_preorder(Workspace& ws, const Linkage& lk, int32_t* par, int8_t* side,
+                            int64_t* pre) {
+    cudaStream_t s = ws.stream();
+    const int64_t n = lk.n, m = lk.m, nodes = n + m;
+    if (m == 0) {
+        FHG_CUDA(cudaMemsetAsync(par, 0xff, sizeof(int32_t) * nodes, s));
+        return FHG_OK;
+    }
+    LAUNCH(cut_parents_kernel, m, m, n, lk.left, lk.right, par, side);
+    const int R = bits_for(m) + 1;
+    Workspace tmp(s);
+    int32_t *anc, *anc2;
+    int64_t* pre2;
+    FHG_TRY(tmp.alloc(&anc, (size_t)m));
+    FHG_TRY(tmp.alloc(&anc2, (size_t)m));
+    FHG_TRY(tmp.alloc(&pre2, (size_t)m));
+    LAUNCH(cut_pre_init_kernel, m, m, n, par, side, lk.left, lk.size, anc, pre);
+    int64_t* cur = pre;
+    for (int r = 0; r < R; ++r) {
+        int64_t* nxt = cur == pre ? pre2 : pre;
+        LAUNCH(cut_pre_step_kernel, m, m, anc, cur, anc2, nxt);
+        std::swap(anc, anc2);
+        cur = nxt;
+    }
+    if (cur != pre)
+        FHG_CUDA(cudaMemcpyAsync(pre, cur, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
+    return FHG_OK;
+}
+
+int weighted_sizes(Workspace& ws, Linkage& lk, const float* weights) {
+    cudaStream_t s = ws.stream();
+    const int64_t n = lk.n, m = lk.m, nodes = n + m;
+    FHG_TRY(ws.alloc(&lk.wsize, (size_t)nodes));
+    FHG_CUDA(cudaMemcpyAsync(lk.wsize, weights, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    if (m == 0) return FHG_OK;
+    Workspace tmp(s);
+    int32_t* par;
+    int8_t* side;
+    int64_t* pre;
+    double *vals, *excl, *total;
+    const int64_t positions = 2 * n - 1;
+    FHG_TRY(tmp.alloc(&par, (size_t)nodes));
+    FHG_TRY(tmp.alloc(&side, (size_t)nodes));
+    FHG_TRY(tmp.alloc(&pre, (size_t)m));
+    FHG_TRY(linkage_preorder(tmp, lk, par, side, pre));
+    FHG_TRY(tmp.alloc(&vals, (size_t)positions));
+    FHG_TRY(tmp.alloc(&excl, (size_t)positions));
+    FHG_TRY(tmp.alloc(&total, 1));
+    FHG_CUDA(cudaMemsetAsync(vals, 0, sizeof(double) * positions, s));
+    LAUNCH(point_pre_kernel, n, n, m, par, side, lk.left, lk.size, pre, weights, vals);
+    FHG_TRY(scan_exclusive_f64(tmp, vals, excl, positions, total));
+    LAUNCH(subtree_sums_kernel, m, m, n, positions, pre, lk.size, excl, total, lk.wsize);
+    return FHG_OK;
+}
+
+int linkage_leaf_counts(Workspace& ws, Linkage& lk) {
+    cudaStream_t s = ws.stream();
+    const int64_t n = lk.n, m = lk.m;
+    if (m == 0) return FHG_OK;
+    int32_t *jmp, *jmp2, *src, *dst;
+    FHG_TRY(ws.alloc(&src, (size_t)m));
+    FHG_TRY(ws.alloc(&dst, (size_t)m));
+    {
+        Workspace tmp(s);
+        FHG_TRY(tmp.alloc(&jmp, (size_t)m));
+        FHG_TRY(tmp.alloc(&jmp2, (size_t)m));
+        LAUNCH(rep_init_kernel, m, m, lk.left, jmp);
+        const int R = bits_for(m) + 1;
+        for (int r = 0; r < R; ++r) {
+            LAUNCH(cut_jump_kernel, m, m, n, jmp, jmp2);
+            std::swap(jmp, jmp2);
+        }
+        LAUNCH(rep_edges_kernel, m, m, n, lk.left, lk.right, jmp, src, dst);
+    }
+    Linkage rebuilt;
+    FHG_TRY(sort_and_link(ws, n, src, dst, lk.w, nullptr, &rebuilt, /*presorted=*/true));
+    lk.size = rebuilt.size;
+    return FHG_OK;
+}
 
 // The cluster tree (child_size > 1 rows, in row order) with the lookups the
 // option passes need.
@@ -685,9 +809,9 @@ int labelling_at_cut(Workspace& ws, const Linkage& lk, double cut, int64_t mcs,
     cudaStream_t s = ws.stream();
     const int64_t n = lk.n, m = lk.m, nodes = n + m;
     Stage stage(s, "dbscan_cut");
-    int32_t *par, *anc, *anc2, *jmp, *jmp2, *up, *up2, *prep, *count;
+    int32_t *par, *jmp, *jmp2, *up, *up2, *prep, *count;
     int8_t *side, *rk;
-    int64_t *pre, *pre2;
+    int64_t* pre;
     uint32_t *flag, *pos, *total;
     FHG_TRY(ws.alloc(&par, (size_t)nodes));
     FHG_TRY(ws.alloc(&side, (size_t)nodes));
@@ -695,35 +819,14 @@ int labelling_at_cut(Workspace& ws, const Linkage& lk, double cut, int64_t mcs,
     FHG_TRY(ws.alloc(&count, (size_t)n));
     FHG_TRY(ws.alloc(&total, 1));
     FHG_CUDA(cudaMemsetAsync(count, 0, sizeof(int32_t) * n, s));
-    if (m == 0) {
-        FHG_CUDA(cudaMemsetAsync(par, 0xff, sizeof(int32_t) * nodes, s));
-    } else {
-        LAUNCH(cut_parents_kernel, m, m, n, lk.left, lk.right, par, side);
-    }
+    if (m == 0) FHG_CUDA(cudaMemsetAsync(par, 0xff, sizeof(int32_t) * nodes, s));
     FHG_TRY(ws.alloc(&jmp, (size_t)(m > 0 ? m : 1)));
     FHG_TRY(ws.alloc(&up, (size_t)(m > 0 ? m : 1)));
     if (m > 0) {
         const int R = bits_for(m) + 1;
-        FHG_TRY(ws.alloc(&anc, (size_t)m));
         FHG_TRY(ws.alloc(&pre, (size_t)m));
         FHG_TRY(ws.alloc(&rk, (size_t)m));
-        {
-            Workspace tmp(s);
-            FHG_TRY(tmp.alloc(&anc2, (size_t)m));
-            FHG_TRY(tmp.alloc(&pre2, (size_t)m));
-            LAUNCH(cut_pre_init_kernel, m, m, n, par, side, lk.left, lk.size, anc, pre);
-            for (int r = 0; r < R; ++r) {
-                LAUNCH(cut_pre_step_kernel, m, m, anc, pre, anc2, pre2);
-                std::swap(anc, anc2);
-                std::swap(pre, pre2);
-            }
-            if (R & 1) {
-                FHG_CUDA(cudaMemcpyAsync(anc2, anc, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
-                FHG_CUDA(cudaMemcpyAsync(pre2, pre, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
-                std::swap(anc, anc2);
-                std::swap(pre, pre2);
-            }
-        }
+        FHG_TRY(linkage_preorder(ws, lk, par, side, pre));
         // ranks, one level at a time
         FHG_CUDA(cudaMemsetAsync(rk, 1, (size_t)m, s));
         const int64_t positions = 2 * n - 1;

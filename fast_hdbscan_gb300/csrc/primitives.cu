@@ -226,6 +226,9 @@ int scan_exclusive_i64(Workspace& ws, const int64_t* in, int64_t* out, int64_t n
                        int64_t* total) {
     return scan_exclusive<int64_t>(ws, in, out, n, total);
 }
+int scan_exclusive_f64(Workspace& ws, const double* in, double* out, int64_t n, double* total) {
+    return scan_exclusive<double>(ws, in, out, n, total);
+}
 int radix_sort_u64(Workspace& ws, uint64_t* keys, int32_t* vals, int64_t n, int begin_bit,
                    int end_bit) {
     return radix_sort<uint64_t>(ws, keys, vals, n, begin_bit, end_bit);

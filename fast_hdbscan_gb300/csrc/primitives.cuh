@@ -10,6 +10,8 @@ namespace fhg {
 int scan_exclusive_u32(Workspace& ws, const uint32_t* in, uint32_t* out, int64_t n,
                        uint32_t* total);
 int scan_exclusive_i64(Workspace& ws, const int64_t* in, int64_t* out, int64_t n, int64_t* total);
+// Fixed tile order, so the rounding is the same on every run.
+int scan_exclusive_f64(Workspace& ws, const double* in, double* out, int64_t n, double* total);
 
 // Stable sort of (keys, vals) by key bits [begin_bit, end_bit), 8 bits per pass.
 int radix_sort_u64(Workspace& ws, uint64_t* keys, int32_t* vals, int64_t n, int begin_bit,

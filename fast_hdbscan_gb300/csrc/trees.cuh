@@ -13,6 +13,7 @@ struct Linkage {
     int32_t* right = nullptr;  // [m] min(root_l, root_r)  (hierarchy[:, 1])
     double* w = nullptr;       // [m] merge distance       (hierarchy[:, 2])
     int32_t* size = nullptr;   // [2n-1] leaves under every node (points: 1)
+    float* wsize = nullptr;    // [2n-1] sample-weight sums, or null (unit weights)
     int32_t* ssrc = nullptr;   // [m] sorted MST src (caller index)
     int32_t* sdst = nullptr;   // [m] sorted MST dst
 };
@@ -59,6 +60,15 @@ int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t
 // Membership strengths for given labels (cluster_trees.py:1011).
 int membership_strengths(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t n_sel,
                          const int64_t* labels, float* probs);
+
+// Sample weights (cluster_trees.py:98 mst_to_linkage_tree_w_sample_weights):
+// lk.wsize[v] = the weights of the points under v, summed in float64 over a
+// preorder numbering and rounded to float32 (the reference sums float32 along
+// the merges; the two agree whenever its float32 sums are exact).
+int weighted_sizes(Workspace& ws, Linkage& lk, const float* weights);
+// Leaf counts (lk.size) of a linkage tree given by its rows only, rebuilt by
+// the rank-halving linkage over one representative point per child.
+int linkage_leaf_counts(Workspace& ws, Linkage& lk);
 
 // Selection options (cluster_trees.py:774, :834, :906).
 // simplify_hierarchy relabels the kept rows of `ct` in place, as the

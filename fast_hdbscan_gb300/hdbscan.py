@@ -15,7 +15,7 @@ from collections import namedtuple
 import numpy as np
 
 from . import _native
-from .boruvka import parallel_boruvka
+from .boruvka import parallel_boruvka, weighted_knn_k
 from .cluster_trees import (
     CondensedTree,
     cluster_tree_from_condensed_tree,
@@ -188,8 +188,6 @@ def _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data
     if cannot_link is not None or cannot_link_groups is not None:
         raise ValueError("cannot_link constraints are only supported with algorithm='kruskal'. "
                          "Got algorithm='boruvka'.")
-    if sample_weights is not None:
-        raise NotImplementedError("sample_weights are not supported by the GPU engine yet")
     if semi_supervised:
         raise NotImplementedError("semi-supervised selection is outside the GPU engine's path")
     if data is not None and data.shape[1] > 8:
@@ -218,7 +216,7 @@ FitResult = namedtuple("FitResult", ["labels", "probabilities", "linkage", "cond
 
 def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
             max_cluster_size=np.inf, allow_single_cluster=False, cluster_selection_epsilon=0.0,
-            cluster_selection_persistence=0.0, return_trees=True):
+            cluster_selection_persistence=0.0, return_trees=True, sample_weights=None):
     """One call of fhg_hdbscan_fit: every stage on the GPU, outputs copied back.
 
     X may be a NumPy array, a CPU torch tensor (pinned for asynchronous
@@ -230,7 +228,12 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
         Xd = _native.to_device(np.ascontiguousarray(X, dtype=np.float32), np.float32)
     n, d = Xd.shape
     ms = min_cluster_size if min_samples is None else min_samples
-    kcols = ms if ms > 1 else 1
+    d_w, wk = None, 0
+    if sample_weights is not None and len(sample_weights) > 1:
+        w = np.ascontiguousarray(sample_weights, dtype=np.float32)
+        wk = weighted_knn_k(w, ms)
+        d_w = _native.to_device(w, np.float32)
+    kcols = max(wk - 1, 1) if d_w is not None else (ms if ms > 1 else 1)
     method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
     if method is None:
         raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
@@ -249,7 +252,8 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
     rc = _native.load().fhg_hdbscan_fit(
         V(Xd), n, d, int(ms), int(min_cluster_size), method, float(max_cluster_size),
         int(bool(allow_single_cluster)), float(cluster_selection_epsilon),
-        float(cluster_selection_persistence), V(labels), V(probs), V(mst), V(linkage), V(ctp),
+        float(cluster_selection_persistence), V(d_w), wk, V(labels), V(probs), V(mst),
+        V(linkage), V(ctp),
         V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
         _native.stream_ptr())
     if rc == _native.FHG_ERR_INVALID and "KeyError" in _native.load().fhg_last_error().decode():
@@ -301,7 +305,8 @@ def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc
                         cannot_link_groups)
     fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
                  max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
-                 cluster_selection_persistence, return_trees=return_trees)
+                 cluster_selection_persistence, return_trees=return_trees,
+                 sample_weights=sample_weights)
     result = (fr.labels, fr.probabilities, fr.linkage, fr.condensed, fr.sorted_mst,
               fr.neighbors, fr.core_distances)
     return result[: (None if return_trees else 2)]
@@ -321,7 +326,10 @@ def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, rep
     _unsupported_routes(metric, algorithm, sample_weights, False, data, cannot_link,
                         cannot_link_groups)
     tree = build_kdtree(data)
-    return parallel_boruvka(tree, 1, min_samples=min_samples)
+    if sample_weights is None:
+        return parallel_boruvka(tree, 1, min_samples=min_samples)
+    return parallel_boruvka(tree, 1, min_samples=min_samples,
+                            sample_weights=np.asarray(sample_weights, dtype=np.float32))
 
 
 def clusters_from_spanning_tree(minimum_spanning_tree, data_labels=None, semi_supervised=False,
@@ -330,12 +338,18 @@ def clusters_from_spanning_tree(minimum_spanning_tree, data_labels=None, semi_su
                                 allow_single_cluster=False, cluster_selection_epsilon=0.0,
                                 cluster_selection_persistence=0.0, sample_weights=None):
     """hdbscan.py:497: labels, probabilities, linkage, condensed tree, sorted MST."""
-    if semi_supervised or sample_weights is not None:
-        raise NotImplementedError("semi-supervised and weighted selection are not on the GPU path")
+    if semi_supervised:
+        raise NotImplementedError("semi-supervised selection is not on the GPU path")
     n_points = minimum_spanning_tree.shape[0] + 1
     sorted_mst = sort_mst(minimum_spanning_tree)
-    linkage_tree = mst_to_linkage_tree(sorted_mst)
-    condensed_tree = condense_tree(linkage_tree, min_cluster_size=min_cluster_size)
+    if sample_weights is None:
+        linkage_tree = mst_to_linkage_tree(sorted_mst)
+    else:
+        from .cluster_trees import mst_to_linkage_tree_w_sample_weights
+
+        linkage_tree = mst_to_linkage_tree_w_sample_weights(sorted_mst, sample_weights)
+    condensed_tree = condense_tree(linkage_tree, min_cluster_size=min_cluster_size,
+                                   sample_weights=sample_weights)
     if cluster_selection_persistence > 0.0 and len(condensed_tree.parent) > 0:
         from .cluster_trees import simplify_hierarchy
 

@@ -78,27 +78,36 @@ int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t* idx_de
                   void* stream);
 
 /* Replaces boruvka.py:542 parallel_boruvka(tree, n_threads, min_samples,
- * sample_weights=None, reproducible=False): the minimum spanning tree of the
- * mutual-reachability graph.
+ * sample_weights, reproducible): the minimum spanning tree of the
+ * mutual-reachability graph.  The result does not depend on `reproducible`
+ * or on any thread count: ties are broken by a total order on indices.
+ *   sample_weights_dev NULL, or n float32 weights (caller order): the
+ *                 reference's weighted path (boruvka.py:561-573), which queries
+ *                 k = weighted_k = int(2 * min_samples / mean weight)
+ *                 neighbours and takes sample_weight_core_distance (:527).
  *   edges_dev     (n-1) x 3 float64: src, dst, sqrt(weight), in Boruvka order
  *                 (round by round; within a round by each component's lowest
  *                 point index), src inside the component that chose the edge.
- *   neighbors_dev n x max(min_samples,1) int32: kNN without the point itself
- *                 (neighbors[:, 1:] of the k = min_samples + 1 query).
- *   core_dev      n float32: sqrt of the squared core distance.
+ *   neighbors_dev n x (k-1) int32: kNN without the point itself
+ *                 (neighbors[:, 1:]; k = min_samples + 1, at least 2, or
+ *                 weighted_k).
+ *   core_dev      n float32: sqrt of the core value (boruvka.py:647).
  *   n_rounds_host optional: Boruvka rounds after the kNN-seeded round. */
-int fhg_index_boruvka(fhg_index* index, int32_t min_samples, double* edges_dev,
-                      int32_t* neighbors_dev, float* core_dev, int32_t* n_rounds_host,
-                      void* stream);
+int fhg_index_boruvka(fhg_index* index, int32_t min_samples, const float* sample_weights_dev,
+                      int32_t weighted_k, double* edges_dev, int32_t* neighbors_dev,
+                      float* core_dev, int32_t* n_rounds_host, void* stream);
 
 /* Replaces the np.lexsort((mst[:,1], mst[:,0], mst[:,2])) of hdbscan.py:511:
  * rows of an m x 3 float64 edge list ordered by (weight, src, dst). */
 int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream);
 
-/* Replaces cluster_trees.py:65 mst_to_linkage_tree(sorted_mst): m x 4 float64
- * rows [max(root_l, root_r), min(root_l, root_r), weight, size]. */
-int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m, double* linkage_dev,
-                            void* stream);
+/* Replaces cluster_trees.py:65 mst_to_linkage_tree(sorted_mst) and, with
+ * sample_weights_dev (m + 1 float32, else NULL), :98
+ * mst_to_linkage_tree_w_sample_weights: m x 4 float64 rows
+ * [max(root_l, root_r), min(root_l, root_r), weight, size], size = points
+ * (or the float32 sum of their weights) under the merge. */
+int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m,
+                            const float* sample_weights_dev, double* linkage_dev, void* stream);
 
 /* Same result as fhg_mst_to_linkage_tree, with no device allocation at all.
  * No counterpart in the reference: this entry point exists for callers that
@@ -120,12 +129,15 @@ int fhg_mst_to_linkage_tree_noalloc(const double* sorted_mst_dev, int64_t m,
                                     double* linkage_dev, void* stream);
 
 /* Replaces cluster_trees.py:205 condense_tree(hierarchy, min_cluster_size,
- * max_cluster_size) for unit sample weights.  Output buffers hold 2*m rows;
- * *n_rows_host receives the row count.  Rows come in the reference's order. */
+ * max_cluster_size, sample_weights) (sample_weights_dev: m + 1 float32, or
+ * NULL for unit weights; with weights the hierarchy's size column holds weight
+ * sums, as mst_to_linkage_tree_w_sample_weights writes it).  Output buffers
+ * hold 2*m rows; *n_rows_host receives the row count.  Rows come in the
+ * reference's order. */
 int fhg_condense_tree(const double* linkage_dev, int64_t m, int64_t min_cluster_size,
-                      double max_cluster_size, int64_t* parent_dev, int64_t* child_dev,
-                      float* lambda_dev, float* child_size_dev, int64_t* n_rows_host,
-                      void* stream);
+                      double max_cluster_size, const float* sample_weights_dev,
+                      int64_t* parent_dev, int64_t* child_dev, float* lambda_dev,
+                      float* child_size_dev, int64_t* n_rows_host, void* stream);
 
 /* Replaces cluster_trees.py:724 extract_eom_clusters(condensed_tree,
  * cluster_tree, max_cluster_size, allow_single_cluster).  sel_dev holds up
@@ -182,20 +194,24 @@ int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cut,
                          int64_t min_cluster_size, int64_t* labels_dev, void* stream);
 
 /* The whole fit of hdbscan.py:686 HDBSCAN.fit / :199 fast_hdbscan on device
- * data (Euclidean, no sample weights): spatial index, kNN core distances,
- * Boruvka MST and the tree passes (with cluster_selection_persistence and
- * cluster_selection_epsilon as in hdbscan.py:528-559), with every
- * intermediate kept in HBM.  The condensed tree returned is the simplified
- * one when persistence > 0; selected_dev receives the final selection.
+ * data (Euclidean): spatial index, kNN core distances, Boruvka MST and the
+ * tree passes (with cluster_selection_persistence and
+ * cluster_selection_epsilon as in hdbscan.py:528-559, and sample weights as
+ * in fhg_index_boruvka / fhg_mst_to_linkage_tree / fhg_condense_tree), with
+ * every intermediate kept in HBM.  The condensed tree returned is the
+ * simplified one when persistence > 0; selected_dev receives the final
+ * selection.
  *   selection_method: 0 = "eom", 1 = "leaf".
  *   Required outputs: labels_dev (int64[n]), probs_dev (float32[n]).
  *   Optional outputs (NULL to skip): mst_dev ((n-1) x 3 float64, sorted as
  *   in hdbscan.py:511), linkage_dev ((n-1) x 4), ct_* (condensed tree, room
- *   for 2n rows; *ct_rows_host = rows), neighbors_dev (n x max(ms, 1)),
- *   core_dev (n), selected_dev (room for n ids; *n_selected_host = count). */
+ *   for 2n rows; *ct_rows_host = rows), neighbors_dev (n x (k-1), k as in
+ *   fhg_index_boruvka), core_dev (n), selected_dev (room for n ids;
+ *   *n_selected_host = count). */
 int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
                     int64_t min_cluster_size, int32_t selection_method, double max_cluster_size,
                     int allow_single_cluster, double epsilon, double persistence,
+                    const float* sample_weights_dev, int32_t weighted_k,
                     int64_t* labels_dev, float* probs_dev, double* mst_dev, double* linkage_dev,
                     int64_t* ct_parent_dev, int64_t* ct_child_dev, float* ct_lambda_dev,
                     float* ct_size_dev, int64_t* ct_rows_host, int32_t* neighbors_dev,

@@ -587,17 +587,36 @@ static int64_t init_from_knn(const int32_t* knn_idx, const float* knn_d, int64_t
     return m;
 }
 
-/* boruvka.py:542 parallel_boruvka (no sample weights) */
+/* boruvka.py:542 parallel_boruvka.  weights == NULL: the unweighted path;
+ * otherwise (boruvka.py:561-573) the kNN query of k = wk neighbours returns
+ * plain distances (output_rdist=False: sqrt of the float32 rdist),
+ * sample_weight_core_distance (:527) picks the core distance, round 0 works
+ * on those plain distances and the Boruvka rounds compare them with squared
+ * distances, exactly as the reference does. */
 int64_t orc_parallel_boruvka(const orc_kdtree* t, int64_t min_samples, int mode, int nthreads,
-                             double* edges, int32_t* neighbors, float* core_out,
-                             int64_t* n_rounds) {
+                             const float* weights, int64_t wk, double* edges, int32_t* neighbors,
+                             float* core_out, int64_t* n_rounds) {
     int64_t n = t->n;
-    int64_t k = min_samples > 1 ? min_samples + 1 : 2;
+    int64_t k = weights ? wk : (min_samples > 1 ? min_samples + 1 : 2);
     float* kd = (float*)malloc(sizeof(float) * (size_t)(n * k));
     int32_t* ki = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n * k));
     orc_tree_query(t, k, mode, nthreads, kd, ki);
     float* core = (float*)malloc(sizeof(float) * (size_t)n);
-    for (int64_t i = 0; i < n; ++i) core[i] = min_samples > 1 ? kd[i * k + k - 1] : 0.0f;
+    if (weights) {
+        for (int64_t i = 0; i < n * k; ++i) kd[i] = sqrtf(kd[i]);
+        for (int64_t i = 0; i < n; ++i) {
+            double total = 0.0;
+            int64_t j = 0;
+            while (total < (double)min_samples && j < k) {
+                int32_t q = ki[i * k + j];
+                total += (double)weights[q >= 0 ? q : n + q];  /* numba wraps index -1 */
+                ++j;
+            }
+            core[i] = kd[i * k + (j > 0 ? j - 1 : k - 1)];
+        }
+    } else {
+        for (int64_t i = 0; i < n; ++i) core[i] = min_samples > 1 ? kd[i * k + k - 1] : 0.0f;
+    }
 
     int32_t* parent = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
     int32_t* rank = (int32_t*)calloc((size_t)n, sizeof(int32_t));
@@ -698,6 +717,34 @@ static int64_t lm_find(int64_t* parent, int64_t node) {
     return node;
 }
 
+/* cluster_trees.py:98 mst_to_linkage_tree_w_sample_weights: sizes are float32
+ * sums of the weights (create_linkage_merge_data_w_sample_weights, :29). */
+void orc_mst_to_linkage_tree_w(const double* smst, int64_t m, const float* w, double* out) {
+    int64_t n = m + 1;
+    int64_t* parent = (int64_t*)malloc(sizeof(int64_t) * (size_t)(2 * n - 1));
+    float* size = (float*)malloc(sizeof(float) * (size_t)(2 * n - 1));
+    for (int64_t i = 0; i < 2 * n - 1; ++i) {
+        parent[i] = -1;
+        size[i] = i < n ? w[i] : 0.0f;
+    }
+    int64_t next = n;
+    for (int64_t e = 0; e < m; ++e) {
+        int64_t l = (int64_t)smst[3 * e], r = (int64_t)smst[3 * e + 1];
+        int64_t lc = lm_find(parent, l), rc = lm_find(parent, r);
+        out[4 * e + 0] = (double)(lc > rc ? lc : rc);
+        out[4 * e + 1] = (double)(lc > rc ? rc : lc);
+        out[4 * e + 2] = smst[3 * e + 2];
+        float sz = size[lc] + size[rc];
+        out[4 * e + 3] = (double)sz;
+        size[next] = sz;
+        parent[lc] = next;
+        parent[rc] = next;
+        ++next;
+    }
+    free(parent);
+    free(size);
+}
+
 /* cluster_trees.py:65 mst_to_linkage_tree */
 void orc_mst_to_linkage_tree(const double* smst, int64_t m, double* out) {
     int64_t n = m + 1;
@@ -748,8 +795,8 @@ static int64_t bfs_hier(const double* h, int64_t root, int64_t num_points, int64
 /* cluster_trees.py:192 hdbscan_lambda_value, rounded to the float32 store */
 static inline float lambda_of(double dist) { return (float)(dist > 0.0 ? 1.0 / dist : INFINITY); }
 
-/* cluster_trees.py:205 condense_tree (unit sample weights) */
-int64_t orc_condense_tree(const double* h, int64_t m, int64_t mcs, double max_cs,
+/* cluster_trees.py:205 condense_tree; w == NULL: unit sample weights */
+int64_t orc_condense_tree(const double* h, int64_t m, int64_t mcs, double max_cs, const float* w,
                           int64_t* parents, int64_t* children, float* lambdas, float* sizes) {
     int64_t root = 2 * m, num_points = m + 1, next_label = num_points + 1;
     int64_t* node_list = (int64_t*)malloc(sizeof(int64_t) * (size_t)(root + 1));
@@ -766,8 +813,10 @@ int64_t orc_condense_tree(const double* h, int64_t m, int64_t mcs, double max_cs
         const double* row = h + 4 * (node - num_points);
         int64_t left = (int64_t)row[0], right = (int64_t)row[1];
         float lam = lambda_of(row[2]);
-        float lc = left >= num_points ? (float)h[4 * (left - num_points) + 3] : 1.0f;
-        float rc = right >= num_points ? (float)h[4 * (right - num_points) + 3] : 1.0f;
+        float lc = left >= num_points ? (float)h[4 * (left - num_points) + 3]
+                                      : (w ? w[left] : 1.0f);
+        float rc = right >= num_points ? (float)h[4 * (right - num_points) + 3]
+                                       : (w ? w[right] : 1.0f);
         int elim_l = 0, elim_r = 0;
         if (left < num_points && rc >= (float)mcs) {
             relabel[right] = parent_node;

@@ -43,18 +43,23 @@ void orc_tree_query(const orc_kdtree* t, int64_t k, int mode, int nthreads,
 
 /* boruvka.py:542 parallel_boruvka: returns number of edges written to
  * edges[(n-1)*3] (src, dst, sqrt weight), neighbors[n*ms], core[n]. */
+/* weights: NULL, or sample weights (caller order) with wk = the reference's
+ * weighted kNN k (boruvka.py:561-563) */
 int64_t orc_parallel_boruvka(const orc_kdtree* t, int64_t min_samples, int mode,
-                             int nthreads, double* edges, int32_t* neighbors,
-                             float* core, int64_t* n_rounds);
+                             int nthreads, const float* weights, int64_t wk, double* edges,
+                             int32_t* neighbors, float* core, int64_t* n_rounds);
 
 /* hdbscan.py:511 lexsort by (weight, src, dst) */
 void orc_sort_mst(const double* mst, int64_t m, double* out);
 /* cluster_trees.py:65 mst_to_linkage_tree */
 void orc_mst_to_linkage_tree(const double* sorted_mst, int64_t m, double* out);
+/* cluster_trees.py:98 mst_to_linkage_tree_w_sample_weights */
+void orc_mst_to_linkage_tree_w(const double* sorted_mst, int64_t m, const float* w, double* out);
 /* cluster_trees.py:205 condense_tree; returns number of rows.  Buffers must
  * hold 2*m rows. */
 int64_t orc_condense_tree(const double* linkage, int64_t m, int64_t min_cluster_size,
-                          double max_cluster_size, int64_t* parent, int64_t* child,
+                          double max_cluster_size, const float* weights, int64_t* parent,
+                          int64_t* child,
                           float* lambda_val, float* child_size);
 /* cluster_trees.py:774 simplify_hierarchy (in place); returns kept rows */
 int64_t orc_simplify_hierarchy(int64_t* parent, int64_t* child, float* lambda_val,

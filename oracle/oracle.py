@@ -37,11 +37,12 @@ def lib():
         L.orc_kdtree_arrays.argtypes = [_P] * 6
         L.orc_tree_query.argtypes = [_P, _I64, _INT, _INT, _P, _P]
         L.orc_parallel_boruvka.restype = _I64
-        L.orc_parallel_boruvka.argtypes = [_P, _I64, _INT, _INT, _P, _P, _P, _P]
+        L.orc_parallel_boruvka.argtypes = [_P, _I64, _INT, _INT, _P, _I64, _P, _P, _P, _P]
         L.orc_sort_mst.argtypes = [_P, _I64, _P]
         L.orc_mst_to_linkage_tree.argtypes = [_P, _I64, _P]
+        L.orc_mst_to_linkage_tree_w.argtypes = [_P, _I64, _P, _P]
         L.orc_condense_tree.restype = _I64
-        L.orc_condense_tree.argtypes = [_P, _I64, _I64, _D, _P, _P, _P, _P]
+        L.orc_condense_tree.argtypes = [_P, _I64, _I64, _D, _P, _P, _P, _P, _P]
         L.orc_simplify_hierarchy.restype = _I64
         L.orc_simplify_hierarchy.argtypes = [_P, _P, _P, _P, _I64, _D]
         L.orc_extract_eom_clusters.restype = _I64
@@ -60,7 +61,7 @@ def lib():
 
 
 def _p(a):
-    return a.ctypes.data_as(ctypes.c_void_p)
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
 class KDTree:
@@ -104,15 +105,29 @@ def tree_query(tree, k, mode=0, nthreads=1):
     return rd, ix
 
 
-def parallel_boruvka(tree, min_samples=10, mode=0, nthreads=1):
+def weighted_knn_k(sample_weights, min_samples):
+    """boruvka.py:561-563: k = int(2 * min_samples / mean(sample_weights)).  The
+    mean is taken in float64 (the reference accumulates float32; the two agree
+    unless 2 * min_samples / mean falls within rounding of an integer)."""
+    w = np.asarray(sample_weights, np.float32)
+    mean = float(np.sum(w, dtype=np.float64)) / w.shape[0]
+    return int(2 * (min_samples / mean))
+
+
+def parallel_boruvka(tree, min_samples=10, mode=0, nthreads=1, sample_weights=None):
     """boruvka.py:542 parallel_boruvka -> (edges, neighbors, core, rounds)."""
     n = tree.data.shape[0]
-    k = min_samples + 1 if min_samples > 1 else 2
+    w = None
+    if sample_weights is not None and len(sample_weights) > 1:
+        w = np.ascontiguousarray(sample_weights, np.float32)
+        k = weighted_knn_k(w, min_samples)
+    else:
+        k = min_samples + 1 if min_samples > 1 else 2
     edges = np.zeros((max(n - 1, 0), 3), np.float64)
-    nbrs = np.empty((n, k - 1), np.int32)
+    nbrs = np.empty((n, max(k - 1, 0)), np.int32)
     core = np.empty(n, np.float32)
     rounds = np.zeros(1, np.int64)
-    m = lib().orc_parallel_boruvka(tree._h, min_samples, mode, nthreads, _p(edges),
+    m = lib().orc_parallel_boruvka(tree._h, min_samples, mode, nthreads, _p(w), k, _p(edges),
                                    _p(nbrs), _p(core), _p(rounds))
     return edges[:m], nbrs, core, int(rounds[0])
 
@@ -125,14 +140,19 @@ def sort_mst(mst):
     return out
 
 
-def mst_to_linkage_tree(sorted_mst):
+def mst_to_linkage_tree(sorted_mst, sample_weights=None):
+    """cluster_trees.py:65 (and :98 mst_to_linkage_tree_w_sample_weights)."""
     sorted_mst = np.ascontiguousarray(sorted_mst, np.float64)
     out = np.empty((sorted_mst.shape[0], 4), np.float64)
-    lib().orc_mst_to_linkage_tree(_p(sorted_mst), sorted_mst.shape[0], _p(out))
+    if sample_weights is None:
+        lib().orc_mst_to_linkage_tree(_p(sorted_mst), sorted_mst.shape[0], _p(out))
+    else:
+        w = np.ascontiguousarray(sample_weights, np.float32)
+        lib().orc_mst_to_linkage_tree_w(_p(sorted_mst), sorted_mst.shape[0], _p(w), _p(out))
     return out
 
 
-def condense_tree(hierarchy, min_cluster_size=10, max_cluster_size=np.inf):
+def condense_tree(hierarchy, min_cluster_size=10, max_cluster_size=np.inf, sample_weights=None):
     h = np.ascontiguousarray(hierarchy, np.float64)
     m = h.shape[0]
     cap = max(2 * m, 1)
@@ -140,8 +160,9 @@ def condense_tree(hierarchy, min_cluster_size=10, max_cluster_size=np.inf):
     c = np.empty(cap, np.int64)
     lam = np.empty(cap, np.float32)
     sz = np.empty(cap, np.float32)
+    w = None if sample_weights is None else np.ascontiguousarray(sample_weights, np.float32)
     rows = lib().orc_condense_tree(_p(h), m, int(min_cluster_size), float(max_cluster_size),
-                                   _p(p), _p(c), _p(lam), _p(sz))
+                                   _p(w), _p(p), _p(c), _p(lam), _p(sz))
     return CondensedTree(p[:rows].copy(), c[:rows].copy(), lam[:rows].copy(), sz[:rows].copy())
 
 
@@ -217,12 +238,12 @@ def get_cluster_labelling_at_cut(linkage, cut, min_cluster_size):
 def clusters_from_spanning_tree(mst, min_cluster_size=10, cluster_selection_method="eom",
                                 max_cluster_size=np.inf, allow_single_cluster=False,
                                 cluster_selection_epsilon=0.0,
-                                cluster_selection_persistence=0.0):
-    """hdbscan.py:497 clusters_from_spanning_tree (unsupervised, unweighted)."""
+                                cluster_selection_persistence=0.0, sample_weights=None):
+    """hdbscan.py:497 clusters_from_spanning_tree (unsupervised)."""
     n_points = mst.shape[0] + 1
     smst = sort_mst(mst)
-    linkage = mst_to_linkage_tree(smst)
-    ct = condense_tree(linkage, min_cluster_size)
+    linkage = mst_to_linkage_tree(smst, sample_weights)
+    ct = condense_tree(linkage, min_cluster_size, sample_weights=sample_weights)
     if cluster_selection_persistence > 0.0 and len(ct.parent) > 0:
         ct = simplify_hierarchy(ct, cluster_selection_persistence)
     n_ct = int((ct.child_size > 1).sum())
@@ -243,14 +264,14 @@ Fit = namedtuple("Fit", ["labels", "probabilities", "linkage", "condensed", "sor
                          "mst", "neighbors", "core", "selected", "rounds"])
 
 
-def fit(X, min_samples=None, min_cluster_size=5, mode=0, nthreads=1, **kw):
+def fit(X, min_samples=None, min_cluster_size=5, mode=0, nthreads=1, sample_weights=None, **kw):
     """hdbscan.py:199 fast_hdbscan restated for the Euclidean Boruvka path."""
     X = np.ascontiguousarray(X, np.float32)
     if X.ndim == 1:
         X = X.reshape(-1, 1)
     ms = min_cluster_size if min_samples is None else min_samples
     tree = build_kdtree(X)
-    mst, nbrs, core, rounds = parallel_boruvka(tree, ms, mode, nthreads)
+    mst, nbrs, core, rounds = parallel_boruvka(tree, ms, mode, nthreads, sample_weights)
     labels, probs, linkage, ct, smst, sel = clusters_from_spanning_tree(
-        mst, min_cluster_size=min_cluster_size, **kw)
+        mst, min_cluster_size=min_cluster_size, sample_weights=sample_weights, **kw)
     return Fit(labels, probs, linkage, ct, smst, mst, nbrs, core, sel, rounds)

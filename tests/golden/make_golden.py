@@ -45,6 +45,22 @@ def _blobs200():
     return StandardScaler().fit_transform(X)
 
 
+def _blobs200_labels():
+    from sklearn.datasets import make_blobs
+    from sklearn.utils import shuffle
+
+    X, y = make_blobs(n_samples=200, random_state=10)
+    X, y = shuffle(X, y, random_state=7)
+    return y.astype(np.float32)
+
+
+def _weights_sixty_fourths(n, seed):
+    """Multiples of 1/64 in [0.5, 2]: float32 sums of them are exact, so the
+    weighted k and the weighted tree sizes do not depend on summation order."""
+    rng = np.random.default_rng(seed)
+    return (rng.integers(32, 129, n) / 64.0).astype(np.float32)
+
+
 def _rand(seed, n, d):
     np.random.seed(seed)
     return np.random.rand(n, d)
@@ -78,6 +94,16 @@ CASES = {
                 dict(min_samples=15, min_cluster_size=25)),
     "vd3d_20k": (lambda: synthetic.varying_density(20000, seed=13),
                  dict(min_samples=15, min_cluster_size=50)),
+    # sample weights (hdbscan.py:199 sample_weights; boruvka.py:527-573;
+    # cluster_trees.py:98, :205)
+    "blobs200_w_labels": (_blobs200, dict(min_cluster_size=5, sample_weights=_blobs200_labels)),
+    "blobs2d_2k_w": (lambda: synthetic.blobs_2d(2000, seed=10),
+                     dict(min_samples=10, min_cluster_size=50,
+                          sample_weights=lambda: _weights_sixty_fourths(2000, 4))),
+    "vd3d_5k_w": (lambda: synthetic.varying_density(5000, seed=12),
+                  dict(min_samples=15, min_cluster_size=25,
+                       sample_weights=lambda: np.random.default_rng(5).integers(
+                           1, 4, 5000).astype(np.float32))),
     "edge_two": (lambda: np.array([[0.0, 0.0], [0.1, 0.0]]), dict(min_cluster_size=2)),
     "edge_dups": (lambda: np.full((50, 3), 1.0), dict(min_cluster_size=5)),
     "edge_1d": (_one_d, dict(min_cluster_size=10)),
@@ -95,6 +121,9 @@ def run_case(name, factory, kwargs, ref):
     X = np.ascontiguousarray(factory(), dtype=np.float32)
     kwargs = dict(kwargs)
     kwargs.setdefault("min_samples", None)  # the HDBSCAN estimator's default
+    w = kwargs.pop("sample_weights", None)
+    if w is not None:
+        w = np.ascontiguousarray(w(), dtype=np.float32)
     mcs = kwargs.get("min_cluster_size", 5)
     ms = kwargs.get("min_samples") or mcs
     t0 = time.time()
@@ -104,8 +133,15 @@ def run_case(name, factory, kwargs, ref):
         out[key] = np.float64(kwargs.get(key, np.inf if key == "max_cluster_size" else 0.0))
     out["allow_single_cluster"] = np.bool_(kwargs.get("allow_single_cluster", False))
     out["cluster_selection_method"] = np.array(kwargs.get("cluster_selection_method", "eom"))
+    if w is not None:
+        out["sample_weights"] = w
 
-    if X.shape[0] >= 2:
+    if X.shape[0] >= 2 and w is not None:
+        mst_raw, nbrs, core = compute_minimum_spanning_tree(X, min_samples=ms, sample_weights=w)
+        out["mst_raw"] = mst_raw
+        out["core"] = core
+        out["neighbors"] = nbrs
+    elif X.shape[0] >= 2:
         tree = build_kdtree(X)
         k = ms + 1 if ms > 1 else 2
         k = min(k, X.shape[0])
@@ -122,7 +158,7 @@ def run_case(name, factory, kwargs, ref):
         out["core"] = core
         out["neighbors"] = nbrs
 
-    res = fast_hdbscan(X, return_trees=True, **kwargs)
+    res = fast_hdbscan(X, return_trees=True, sample_weights=w, **kwargs)
     labels, probs, linkage, ct, smst, nbrs2, core2 = res
     out["labels"] = np.asarray(labels)
     out["probabilities"] = np.asarray(probs)

@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol():
     direct = {"fhg_launch_count", "fhg_profile_enable", "fhg_profile_report",
               "fhg_mst_to_linkage_tree_noalloc"}
     assert set(declared) <= bound | direct
-    assert lib.fhg_abi_version() == 1
+    assert lib.fhg_abi_version() == 2
 
 
 def test_library_error_reporting_without_gpu():

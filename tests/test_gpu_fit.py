@@ -26,7 +26,8 @@ pytestmark = pytest.mark.gpu
 GOLDEN_FIT = ["ka150", "ka150_eps", "blobs200", "blobs200_ms1", "blobs200_leaf",
               "blobs200_maxcs", "blobs200_single", "blobs200_persist", "blobs2d_2k",
               "blobs2d_20k", "umap5d_5k", "vd3d_5k", "vd3d_20k", "edge_two", "edge_1d",
-              "edge_highms", "edge_dups", "edge_mcs_gt_n"]
+              "edge_highms", "edge_dups", "edge_mcs_gt_n", "blobs200_w_labels", "blobs2d_2k_w",
+              "vd3d_5k_w"]
 
 
 def _golden(name):
@@ -90,8 +91,10 @@ def test_fit_vs_oracle_and_reference(engine, name):
     g = _golden(name)
     X = g["X"]
     ms, mcs = int(g["min_samples"]), int(g["min_cluster_size"])
-    res = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs, return_trees=True, **_kw(g))
-    orc = O.fit(X, ms, mcs, mode=1, **_kw(g))
+    w = g["sample_weights"] if "sample_weights" in g.files else None
+    res = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs, return_trees=True,
+                       sample_weights=w, **_kw(g))
+    orc = O.fit(X, ms, mcs, mode=1, sample_weights=w, **_kw(g))
     _assert_fit_equal(res, orc)
     # reference fixtures
     if name != "edge_mcs_gt_n":  # the reference indexes [-1] when k exceeds n
@@ -162,3 +165,30 @@ def test_cached_pool_release_between_fits(engine):
     b = fast_hdbscan(X, min_samples=10, min_cluster_size=40)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_sample_weight_known_answer(engine):
+    """fast_hdbscan/tests/test_hdbscan.py:112-117: weights = the blob labels
+    (one blob weighs 0) leave n_clusters - 1 clusters."""
+    from fast_hdbscan_gb300 import HDBSCAN
+    from fast_hdbscan_gb300.hdbscan import fast_hdbscan
+
+    g = _golden("blobs200_w_labels")
+    labels, _ = fast_hdbscan(g["X"], sample_weights=g["sample_weights"], min_cluster_size=5,
+                             min_samples=None)
+    assert len(set(labels.tolist()) - {-1}) == 2
+    model = HDBSCAN(min_cluster_size=5).fit(g["X"], sample_weight=g["sample_weights"])
+    np.testing.assert_array_equal(model.labels_, labels)
+
+
+@pytest.mark.parametrize("n,seed", [(100_000, 8), (40_000, 9)])
+def test_weighted_fit_vs_oracle_synthetic(engine, n, seed):
+    from fast_hdbscan_gb300.hdbscan import fast_hdbscan
+    from oracle import oracle as O
+
+    X = synthetic.varying_density(n, seed=seed)
+    w = np.random.default_rng(seed).integers(1, 5, n).astype(np.float32)
+    res = fast_hdbscan(X, min_samples=10, min_cluster_size=50, return_trees=True,
+                       sample_weights=w)
+    orc = O.fit(X, 10, 50, mode=1, nthreads=8, sample_weights=w)
+    _assert_fit_equal(res, orc)

@@ -77,3 +77,25 @@ def test_selection_labels_bitexact(engine, name):
     np.testing.assert_array_equal(labels, g["labels"])
     probs = get_point_membership_strength_vector(ct, sel, labels)
     np.testing.assert_array_equal(probs, g["probabilities"])
+
+
+WEIGHTED = ["blobs200_w_labels", "blobs2d_2k_w", "vd3d_5k_w"]
+
+
+@pytest.mark.parametrize("name", WEIGHTED)
+def test_weighted_linkage_and_condense_bitexact(engine, name):
+    """cluster_trees.py:98 mst_to_linkage_tree_w_sample_weights and :205
+    condense_tree(sample_weights=...) on the reference's own sorted MST and
+    linkage tree.  The fixtures' weights (integers, multiples of 1/64) have
+    exact float32 sums, so the weighted sizes are bit-identical."""
+    from fast_hdbscan_gb300.cluster_trees import (
+        condense_tree, mst_to_linkage_tree_w_sample_weights, sort_mst)
+
+    g = _golden(name)
+    w = g["sample_weights"]
+    np.testing.assert_array_equal(sort_mst(g["mst_raw"]), g["sorted_mst"])
+    np.testing.assert_array_equal(mst_to_linkage_tree_w_sample_weights(g["sorted_mst"], w),
+                                  g["linkage"])
+    ct = condense_tree(g["linkage"], int(g["min_cluster_size"]), sample_weights=w)
+    for a, b in zip(ct, _ct(g)):
+        np.testing.assert_array_equal(a, b)

@@ -44,9 +44,15 @@ def _call(lib, name, sorted_mst):
     d_out = torch.full((m, 4), -7.0, dtype=torch.float64, device="cuda")
     fn = getattr(lib, name)
     fn.restype = ctypes.c_int
-    fn.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
-    rc = fn(ctypes.c_void_p(d_in.data_ptr()), m, ctypes.c_void_p(d_out.data_ptr()),
-            _native.stream_ptr())
+    if name == "fhg_mst_to_linkage_tree":  # (sorted_mst, m, sample_weights, linkage, stream)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                       ctypes.c_void_p]
+        rc = fn(ctypes.c_void_p(d_in.data_ptr()), m, None, ctypes.c_void_p(d_out.data_ptr()),
+                _native.stream_ptr())
+    else:
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+        rc = fn(ctypes.c_void_p(d_in.data_ptr()), m, ctypes.c_void_p(d_out.data_ptr()),
+                _native.stream_ptr())
     torch.cuda.synchronize()
     return rc, d_out.cpu().numpy()
 
