@@ -99,17 +99,18 @@ __global__ void gather_weights_kernel(int64_t n, const int32_t* __restrict__ ori
     if (p < n) w_s[p] = w[orig[p]];
 }
 
+// Core distances in caller order; neighbour columns past the kNN list (the
+// reference's padding when k exceeds the point count) are -1.  The kNN kernel
+// writes the other neighbour columns itself.
 __global__ void outputs_kernel(int64_t n, int kk, int k, const int32_t* __restrict__ orig,
-                               const float* __restrict__ core2,
-                               const int32_t* __restrict__ knn_i_o, float* __restrict__ core_o,
+                               const float* __restrict__ core2, float* __restrict__ core_o,
                                int32_t* __restrict__ nbr_o) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     int64_t o = orig[p];
     if (core_o) core_o[o] = __fsqrt_rn(core2[p]);
     if (nbr_o)
-        for (int j = 1; j < k; ++j)
-            nbr_o[o * (k - 1) + j - 1] = j < kk ? knn_i_o[o * kk + j] : -1;
+        for (int j = kk > 1 ? kk : 1; j < k; ++j) nbr_o[o * (k - 1) + j - 1] = -1;
 }
 
 // ----------------------------------------------------------------- round 0
@@ -713,7 +714,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&out->w2, (size_t)m_cap));
 
     float *knn_d, *core2, *knn_d_o = nullptr, *w0, *cand_w;
-    int32_t *knn_s, *knn_i_o = nullptr, *target, *par, *comp, *cmin, *reps, *reps2, *winner, *tgt,
+    int32_t *knn_s, *target, *par, *comp, *cmin, *reps, *reps2, *winner, *tgt,
         *cand_q;
     int2* nc;
     uint32_t *flag, *pos, *keyB, *cnt;
@@ -721,10 +722,10 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     int* iflag;
     FHG_TRY(ws.alloc(&knn_d, (size_t)(n * k)));
     FHG_TRY(ws.alloc(&knn_s, (size_t)(n * k)));
-    if (nbr_o) FHG_TRY(ws.alloc(&knn_i_o, (size_t)(n * k)));  // neighbour ids only
     int8_t* knn_open;  // the kNN kernel's tie flags, then "seed not provably final"
     FHG_TRY(ws.alloc(&knn_open, (size_t)n));
-    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, knn_i_o, s, knn_open));
+    // the neighbours[:, 1:] matrix (kq - 1 columns) straight from the kNN kernel
+    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
     FHG_TRY(ws.alloc(&core2, (size_t)n));
     if (weighted) {
         float* w_s;
@@ -740,7 +741,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         LAUNCH(core_from_knn_kernel, n, n, k, kq, min_samples, knn_d, core2, knn_open);
     }
     if (core_o || nbr_o)
-        LAUNCH(outputs_kernel, n, n, k, kq, ix.orig, core2, knn_i_o, core_o, nbr_o);
+        LAUNCH(outputs_kernel, n, n, k, kq, ix.orig, core2, core_o, nbr_o);
     if (n < 2) return FHG_OK;
 
     FHG_TRY(ws.alloc(&target, (size_t)n));

@@ -112,10 +112,12 @@ int index_free(fhg_index* ix, cudaStream_t s);
 // kNN over the index.  Outputs (all nullable):
 //   d_s/i_s : rows in Morton order, neighbour ids as Morton positions
 //   d_o/i_o : rows in caller order, neighbour ids as caller indices (i_o may
-//             be given alone)
+//             be given alone; then its rows may have their own stride and
+//             drop their first io_skip columns -- the neighbours[:, 1:]
+//             matrix of the fit)
 //   tie_s   : per point (Morton order), 1 when some point outside its list
 //             lies at exactly its k-th distance
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-              cudaStream_t s, int8_t* tie_s = nullptr);
+              cudaStream_t s, int8_t* tie_s = nullptr, int io_stride = 0, int io_skip = 0);
 
 }  // namespace fhg

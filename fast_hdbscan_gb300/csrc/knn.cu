@@ -36,7 +36,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
                                                               int32_t* __restrict__ i_s,
                                                               float* __restrict__ d_o,
                                                               int32_t* __restrict__ i_o,
-                                                              int8_t* __restrict__ tie_s) {
+                                                              int8_t* __restrict__ tie_s,
+                                                              int io_stride, int io_skip) {
     __shared__ int32_t s_stack[kKnnWarps][kStack];
     __shared__ float4 s_cand[kKnnWarps][32 * (SP / 4)];
     __shared__ int32_t s_corig[kKnnWarps][32];
@@ -205,54 +206,56 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
             i_s[qi * k + jj] = o >= 0 ? __ldg(ix.rank + o) : -1;
         }
         if (d_o) d_o[o_row * k + jj] = bd[j];
-        if (i_o) i_o[o_row * k + jj] = o;
+        if (i_o && jj >= io_skip) i_o[o_row * io_stride + jj - io_skip] = o;
     }
 }
 
 template <int DIM, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-               int8_t* tie_s, cudaStream_t s) {
+               int8_t* tie_s, int io_stride, int io_skip, cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : 8;
     unsigned g = grid_for(ix.nleaves, kKnnWarps);
     Stage stage(s, "knn_kernel");
     ::fhg::note_launch();
     knn_kernel<DIM, SP, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o,
-                                                         tie_s);
+                                                         tie_s, io_stride, io_skip);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
 template <int DIM>
 int dispatch_k(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-               int8_t* tie_s, cudaStream_t s) {
-    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+               int8_t* tie_s, int ios, int iok, cudaStream_t s) {
+    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
+    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
+    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
+    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
 }
 
 }  // namespace
 
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-              cudaStream_t s, int8_t* tie_s) {
+              cudaStream_t s, int8_t* tie_s, int io_stride, int io_skip) {
+    if (io_stride <= 0) io_stride = k;
     if (k < 1 || k > 64) {
         set_error("knn: k must be in [1, 64] (got %d)", k);
         return FHG_ERR_INVALID;
     }
-    if ((d_s == nullptr) != (i_s == nullptr) || (d_o != nullptr && i_o == nullptr)) {
+    if ((d_s == nullptr) != (i_s == nullptr) || (d_o != nullptr && i_o == nullptr) ||
+        (d_o != nullptr && (io_stride != k || io_skip != 0))) {
         set_error("knn: Morton-order outputs come in pairs; caller-order distances need ids");
         return FHG_ERR_INVALID;
     }
     Stage stage(s, "knn");
     switch (ix.d) {
-        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
-        default: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, s);
+        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        default: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
     }
 }
 
