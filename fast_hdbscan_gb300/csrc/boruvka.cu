@@ -375,13 +375,6 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
         for (int j = 0; j < DIM; ++j) q[j] = t[j];
     }
 
-    float ctr[DIM];
-    {
-        float b[2 * SP];
-        load_box<SP>(ix.box, ix.slots - 1 + leaf, b);
-#pragma unroll
-        for (int j = 0; j < DIM; ++j) ctr[j] = 0.5f * (b[j] + b[SP + j]);
-    }
     float4* xyz = s_xyz[warp];
     int2* cc = s_cc[warp];
     int32_t* co = s_orig[warp];
@@ -446,6 +439,8 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     for (int lv = 0; lv < lvl_lo && x > 0; ++lv) x = (x - 1) >> 1;
     for (int lv = lvl_lo; lv < lvl_hi && x > 0; ++lv) {
         const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+        // children nearer the home bucket in Morton order first
+        const bool right_side = (x & 1) != 0;
         x = (x - 1) >> 1;
         {
             const int2 ncn = nc[sib];
@@ -488,8 +483,7 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
             }
             const bool al = __any_sync(kFull, nl), ar = __any_sync(kFull, nr);
             if (!al && !ar) continue;
-            const bool left_first =
-                !(al && ar) ? al : box_lb_n<DIM, SP>(bl, ctr) <= box_lb_n<DIM, SP>(br, ctr);
+            const bool left_first = !(al && ar) ? al : right_side;
             if (l >= first_leaf_node) {
                 // thresholds may shrink while the first bucket is scanned
                 const int32_t n1 = left_first ? l : r, n2 = left_first ? r : l;

@@ -30,6 +30,14 @@ template <int K>
 constexpr int knn_min_blocks() { return K <= 16 ? 6 : 1; }
 constexpr int kStack = 64;
 
+__device__ __forceinline__ unsigned long long pack_entry(float d, int32_t o) {
+    return ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)o;
+}
+__device__ __forceinline__ float entry_dist(unsigned long long e) {
+    return __uint_as_float((uint32_t)(e >> 32));
+}
+__device__ __forceinline__ int32_t entry_orig(unsigned long long e) { return (int32_t)(uint32_t)e; }
+
 template <int DIM, int SP, int K>
 __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kernel(IndexView ix, int k,
                                                               float* __restrict__ d_s,
@@ -56,24 +64,15 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
 #pragma unroll
         for (int j = 0; j < DIM; ++j) q[j] = t[j];
     }
-    // Centre of this bucket's box: orders children (nearer first).
-    float ctr[DIM];
-    {
-        float b[2 * SP];
-        load_box<SP>(ix.box, ix.slots - 1 + leaf, b);
-#pragma unroll
-        for (int j = 0; j < DIM; ++j) ctr[j] = 0.5f * (b[j] + b[SP + j]);
-    }
-
-    // Slots [0, K-k) hold a -1 sentinel so that the live list has length k;
+    // Each list entry is one 64-bit key: squared distance bits above the
+    // caller index.  Non-negative floats order like their bit patterns, so
+    // one unsigned compare orders entries by (distance, caller index).
+    // Slots [0, K-k) hold a 0 sentinel so that the live list has length k;
     // empty live slots hold (+inf, INT32_MAX).
-    float bd[K];
-    int32_t bo[K];
+    unsigned long long key[K];
+    const unsigned long long kEmptyKey = pack_entry(INFINITY, INT32_MAX);
 #pragma unroll
-    for (int j = 0; j < K; ++j) {
-        bd[j] = (j < K - k) ? -1.0f : INFINITY;
-        bo[j] = (j < K - k) ? -1 : INT32_MAX;
-    }
+    for (int j = 0; j < K; ++j) key[j] = (j < K - k) ? 0ull : kEmptyKey;
     float4* cand = s_cand[warp];
     int32_t* corig = s_corig[warp];
     const int32_t* __restrict__ orig = ix.orig;
@@ -86,25 +85,20 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
     // compare-and-swap steps): slot j takes slot j-1's entry if that entry
     // follows (dd, o), else (dd, o) if slot j's own entry follows it.
     auto insert = [&](float dd, int32_t o) {
-        if (!(dd < bd[K - 1] || (dd == bd[K - 1] && o < bo[K - 1]))) {
+        const unsigned long long nk = pack_entry(dd, o);
+        if (!(nk < key[K - 1])) {
             rejmin = fminf(rejmin, dd);
             return;
         }
-        rejmin = fminf(rejmin, bd[K - 1]);
+        rejmin = fminf(rejmin, entry_dist(key[K - 1]));
         bool gt_hi = true;
 #pragma unroll
         for (int j = K - 1; j > 0; --j) {
-            const bool gt_lo = bd[j - 1] > dd || (bd[j - 1] == dd && bo[j - 1] > o);
-            const float nd = gt_lo ? bd[j - 1] : (gt_hi ? dd : bd[j]);
-            const int32_t no = gt_lo ? bo[j - 1] : (gt_hi ? o : bo[j]);
-            bd[j] = nd;
-            bo[j] = no;
+            const bool gt_lo = key[j - 1] > nk;
+            key[j] = gt_lo ? key[j - 1] : (gt_hi ? nk : key[j]);
             gt_hi = gt_lo;
         }
-        if (gt_hi) {
-            bd[0] = dd;
-            bo[0] = o;
-        }
+        if (gt_hi) key[0] = nk;
     };
 
     // One bucket: first every lane marks the candidates within its current
@@ -121,7 +115,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
             corig[lane] = __ldg(orig + base + lane);
         }
         __syncwarp();
-        const float thr = need ? bd[K - 1] : -INFINITY;
+        const float thr = need ? entry_dist(key[K - 1]) : -INFINITY;
         uint32_t acc = 0u;
 #pragma unroll 4
         for (int t = 0; t < cnt; ++t) {
@@ -156,12 +150,15 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
     // sibling subtree depth first, pruned by lower bounds.  Subtrees' boxes
     // overlap, so no ancestor box bounds the search; but near subtrees come
     // first, and a far sibling whose box is out of every lane's reach costs a
-    // single box test.
+    // single box test.  Inside a sibling subtree the child nearer the home
+    // bucket in Morton order goes first: the left child of a subtree to the
+    // right of the home path, the right child of one to its left.
     int32_t* st = s_stack[warp];
     const int64_t first_leaf_node = ix.slots - 1;
     int64_t x = first_leaf_node + leaf;
     while (x > 0) {
         const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+        const bool right_side = (x & 1) != 0;
         int sp = 1;
         if (lane == 0) st[0] = sib;
         __syncwarp();
@@ -172,17 +169,13 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
             float b[2 * SP];
             load_box<SP>(ix.box, node, b);
             const float lb = box_lb_n<DIM, SP>(b, q);
-            const bool need = valid && lb <= bd[K - 1];
+            const bool need = valid && lb <= entry_dist(key[K - 1]);
             if (!__any_sync(kFull, need)) continue;
             if (node >= first_leaf_node) {
                 scan_leaf(node - first_leaf_node, need);
             } else {
                 const int32_t l = 2 * node + 1, r = l + 1;
-                float bl[2 * SP], br[2 * SP];
-                load_box<SP>(ix.box, l, bl);
-                load_box<SP>(ix.box, r, br);
-                const float ll = box_lb_n<DIM, SP>(bl, ctr), lr = box_lb_n<DIM, SP>(br, ctr);
-                const int32_t near = ll <= lr ? l : r, far = ll <= lr ? r : l;
+                const int32_t near = right_side ? l : r, far = right_side ? r : l;
                 if (lane == 0) {
                     st[sp] = far;
                     st[sp + 1] = near;
@@ -194,18 +187,20 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
         x = (x - 1) >> 1;
     }
     if (!valid) return;
-    if (tie_s) tie_s[qi] = rejmin == bd[K - 1] ? 1 : 0;
+    if (tie_s) tie_s[qi] = rejmin == entry_dist(key[K - 1]) ? 1 : 0;
     const int64_t o_row = orig[qi];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         if (j < K - k) continue;
         const int jj = j - (K - k);
-        const int32_t o = bo[j] == INT32_MAX ? -1 : bo[j];  // k > n leaves slots empty
+        const float dj = entry_dist(key[j]);
+        const int32_t oj = entry_orig(key[j]);
+        const int32_t o = oj == INT32_MAX ? -1 : oj;  // k > n leaves slots empty
         if (d_s) {
-            d_s[qi * k + jj] = bd[j];
+            d_s[qi * k + jj] = dj;
             i_s[qi * k + jj] = o >= 0 ? __ldg(ix.rank + o) : -1;
         }
-        if (d_o) d_o[o_row * k + jj] = bd[j];
+        if (d_o) d_o[o_row * k + jj] = dj;
         if (i_o && jj >= io_skip) i_o[o_row * io_stride + jj - io_skip] = o;
     }
 }
