@@ -276,7 +276,11 @@ def run_gb300(args):
     if not args.no_e2e:
         Xp = torch.from_numpy(Xh).pin_memory()
         est = HDBSCAN(min_cluster_size=mcs, min_samples=ms)
-        est.fit(Xp)
+        # warm-up fits: the estimator holds one fit's outputs while the next
+        # runs, so the pinned host buffers reach their steady state (two sets
+        # in PyTorch's caching host allocator) before the timed fits
+        for _ in range(max(args.warmup, 2)):
+            est.fit(Xp)
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -285,7 +289,9 @@ def run_gb300(args):
         e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps,
                                torch.device("cuda", local))
         rows_out = est._condensed_tree.shape[0]
-        d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 24 + n * ms * 4 + n * 4)
+        # labels i64, probabilities f32, sorted MST (n-1) x 3 f64, linkage (n-1) x 4 f64,
+        # condensed records 28 B/row, neighbours n x ms i32, core distances f32, selection
+        d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 28 + n * ms * 4 + n * 4)
         e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",
                "h2d_bytes_per_step": int(n * d * 4), "d2h_bytes_per_step": int(d2h),
                "s_per_step": round(e2e_s, 4)}

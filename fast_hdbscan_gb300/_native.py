@@ -44,6 +44,7 @@ SIGNATURES = {
     "fhg_label_points": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _I64, _P, _P, _P]),
     "fhg_cluster_tree_leaves": (_INT, [_P, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), _P]),
     "fhg_membership_strengths": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _P, _I64, _P, _P]),
+    "fhg_condensed_record_array": (_INT, [_P, _P, _P, _P, _I64, _P, _P]),
     "fhg_simplify_hierarchy": (_INT, [_P, _P, _P, _P, _I64, _D, _P, _P, _P, _P,
                                       ctypes.POINTER(_I64), _P]),
     "fhg_cluster_epsilon_search": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _P,

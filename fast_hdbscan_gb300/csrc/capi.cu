@@ -417,6 +417,52 @@ FHG_API int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* c
     return membership_strengths(ws, ct, sel, n_sel, labels_dev, probs_dev);
 }
 
+// ------------------------------------------------------ record array layout
+namespace fhg {
+namespace capi {
+// One 28-byte record per row: int64 parent, int64 child, float64 lambda,
+// float32 size -- numpy's packed layout of the dtype to_numpy_rec_array
+// builds.  Rows start at 4-byte boundaries, so each is written as 7 words.
+__global__ void condensed_records_kernel(int64_t rows, const int64_t* __restrict__ parent,
+                                         const int64_t* __restrict__ child,
+                                         const float* __restrict__ lambda,
+                                         const float* __restrict__ size,
+                                         uint32_t* __restrict__ out) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const uint64_t p = (uint64_t)parent[r], c = (uint64_t)child[r];
+    const uint64_t l = (uint64_t)__double_as_longlong((double)lambda[r]);
+    uint32_t* o = out + 7 * r;
+    o[0] = (uint32_t)p;
+    o[1] = (uint32_t)(p >> 32);
+    o[2] = (uint32_t)c;
+    o[3] = (uint32_t)(c >> 32);
+    o[4] = (uint32_t)l;
+    o[5] = (uint32_t)(l >> 32);
+    o[6] = __float_as_uint(size[r]);
+}
+}  // namespace capi
+}  // namespace fhg
+
+FHG_API int fhg_condensed_record_array(const int64_t* parent_dev, const int64_t* child_dev,
+                                       const float* lambda_dev, const float* child_size_dev,
+                                       int64_t rows, void* records_dev, void* stream) {
+    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_ptrs("fhg_condensed_record_array",
+                       {parent_dev, child_dev, lambda_dev, child_size_dev, records_dev}));
+    if (reinterpret_cast<uintptr_t>(records_dev) % 4 != 0) {
+        set_error("fhg_condensed_record_array: records_dev must be 4-byte aligned");
+        return FHG_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    ::fhg::note_launch();
+    fhg::capi::condensed_records_kernel<<<grid_for(rows, 256), 256, 0, s>>>(
+        rows, parent_dev, child_dev, lambda_dev, child_size_dev,
+        static_cast<uint32_t*>(records_dev));
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
 // --------------------------------------------------------- selection options
 FHG_API int fhg_simplify_hierarchy(int64_t* parent_dev, int64_t* child_dev, float* lambda_dev,
                                    const float* child_size_dev, int64_t rows, double threshold,

@@ -115,13 +115,16 @@ def _check_sample_weight(sample_weight, X, dtype):
     return sw
 
 
+_REC_DTYPE = np.dtype([("parent", np.intp), ("child", np.intp), ("lambda_val", float),
+                       ("child_size", np.float32)])
+
+
 def to_numpy_rec_array(named_tuple_tree):
     """hdbscan.py:93."""
     if isinstance(named_tuple_tree, np.ndarray) and named_tuple_tree.dtype.names is not None:
         return named_tuple_tree
     size = named_tuple_tree.parent.shape[0]
-    result = np.empty(size, dtype=[("parent", np.intp), ("child", np.intp),
-                                   ("lambda_val", float), ("child_size", np.float32)])
+    result = np.empty(size, dtype=_REC_DTYPE)
     result["parent"] = named_tuple_tree.parent
     result["child"] = named_tuple_tree.child
     result["lambda_val"] = named_tuple_tree.lambda_val
@@ -216,11 +219,15 @@ FitResult = namedtuple("FitResult", ["labels", "probabilities", "linkage", "cond
 
 def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
             max_cluster_size=np.inf, allow_single_cluster=False, cluster_selection_epsilon=0.0,
-            cluster_selection_persistence=0.0, return_trees=True, sample_weights=None):
+            cluster_selection_persistence=0.0, return_trees=True, sample_weights=None,
+            condensed_records=False):
     """One call of fhg_hdbscan_fit: every stage on the GPU, outputs copied back.
 
     X may be a NumPy array, a CPU torch tensor (pinned for asynchronous
-    copies) or a CUDA tensor; it is used as float32."""
+    copies) or a CUDA tensor; it is used as float32.  Outputs come back
+    through pinned host buffers (one batch of asynchronous copies).  With
+    condensed_records the condensed tree comes back as the record array
+    HDBSCAN.fit stores (hdbscan.py:93), laid out on the GPU."""
     torch = _native._torch()
     if isinstance(X, torch.Tensor):
         Xd = X.to(device="cuda", dtype=torch.float32, non_blocking=True).contiguous()
@@ -262,15 +269,29 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
     r, k = rows.value, nsel.value
     outs = [labels, probs, sel[:k]]
     if trees:
-        outs += [mst, linkage, ctp[:r], ctc[:r], ctl[:r], cts[:r], nbrs, core]
-    host = [t.to("cpu", non_blocking=True) for t in outs]
+        outs += [mst, linkage, nbrs, core]
+        if condensed_records:
+            rec = torch.empty(max(r, 1) * 28, dtype=torch.uint8, device="cuda")
+            _native.check(_native.load().fhg_condensed_record_array(
+                V(ctp), V(ctc), V(ctl), V(cts), r, V(rec), _native.stream_ptr()))
+            outs += [rec[: r * 28]]
+        else:
+            outs += [ctp[:r], ctc[:r], ctl[:r], cts[:r]]
+    host = []
+    for t in outs:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        host.append(h)
     torch.cuda.current_stream().synchronize()
     host = [h.numpy() for h in host]
     labels_h = host[0].astype(np.intp, copy=False)
     if not trees:
         return FitResult(labels_h, host[1], None, None, None, None, None, host[2])
-    ct = CondensedTree(host[5], host[6], host[7], host[8])
-    return FitResult(labels_h, host[1], host[4], ct, host[3], host[9], host[10], host[2])
+    if condensed_records:
+        ct = host[7].view(_REC_DTYPE)
+    else:
+        ct = CondensedTree(host[7], host[8], host[9], host[10])
+    return FitResult(labels_h, host[1], host[4], ct, host[3], host[5], host[6], host[2])
 
 
 def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc",
@@ -282,6 +303,24 @@ def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc
                  validate_cannot_link=True, cannot_link_groups=None, metric_kwds=None):
     """hdbscan.py:199 fast_hdbscan on the GPU engine.  Besides NumPy input,
     `data` may be a torch tensor (CUDA, or pinned host memory) of finite values."""
+    return _fast_hdbscan(
+        data, data_labels, semi_supervised, ss_algorithm, min_samples, min_cluster_size,
+        cluster_selection_method, max_cluster_size, allow_single_cluster,
+        cluster_selection_epsilon, cluster_selection_persistence, sample_weights, reproducible,
+        return_trees, metric, algorithm, knn_k, cannot_link, validate_cannot_link,
+        cannot_link_groups, metric_kwds)
+
+
+def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc",
+                  min_samples=10, min_cluster_size=10, cluster_selection_method="eom",
+                  max_cluster_size=np.inf, allow_single_cluster=False,
+                  cluster_selection_epsilon=0.0, cluster_selection_persistence=0.0,
+                  sample_weights=None, reproducible=False, return_trees=False,
+                  metric="euclidean", algorithm="boruvka", knn_k=None, cannot_link=None,
+                  validate_cannot_link=True, cannot_link_groups=None, metric_kwds=None,
+                  condensed_records=False):
+    """fast_hdbscan with one more option for HDBSCAN.fit: the condensed tree
+    as the record array the estimator stores, laid out on the GPU."""
     if _is_tensor(data):
         pass
     elif metric == "euclidean":
@@ -306,7 +345,7 @@ def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc
     fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
                  max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
                  cluster_selection_persistence, return_trees=return_trees,
-                 sample_weights=sample_weights)
+                 sample_weights=sample_weights, condensed_records=condensed_records)
     result = (fr.labels, fr.probabilities, fr.linkage, fr.condensed, fr.sorted_mst,
               fr.neighbors, fr.core_distances)
     return result[: (None if return_trees else 2)]
@@ -421,7 +460,8 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
                 kwargs = self.get_params()
                 (self.labels_, self.probabilities_, self._single_linkage_tree,
                  self._condensed_tree, self._min_spanning_tree, self._neighbors,
-                 self._core_distances) = fast_hdbscan(Xd, None, return_trees=True, **kwargs)
+                 self._core_distances) = _fast_hdbscan(Xd, None, return_trees=True,
+                                                       condensed_records=True, **kwargs)
                 self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
                 return self
             X = Xd.cpu().numpy()
@@ -440,8 +480,9 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
             clean_data = X
         kwargs = self.get_params()
         (self.labels_, self.probabilities_, self._single_linkage_tree, self._condensed_tree,
-         self._min_spanning_tree, self._neighbors, self._core_distances) = fast_hdbscan(
-            clean_data, None, return_trees=True, sample_weights=sample_weight, **kwargs)
+         self._min_spanning_tree, self._neighbors, self._core_distances) = _fast_hdbscan(
+            clean_data, None, return_trees=True, sample_weights=sample_weight,
+            condensed_records=True, **kwargs)
         self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
         if not self._all_finite:
             self._condensed_tree = remap_condensed_tree(self._condensed_tree, internal_to_raw,

@@ -168,6 +168,14 @@ int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* child_dev
                              const int64_t* sel_dev, int64_t n_sel, const int64_t* labels_dev,
                              int64_t n_samples, float* probs_dev, void* stream);
 
+/* Replaces hdbscan.py:93 to_numpy_rec_array(condensed_tree) (called by
+ * HDBSCAN.fit, hdbscan.py:805): rows x 28 bytes at records_dev (4-byte
+ * aligned), numpy's packed layout of the dtype [("parent", intp),
+ * ("child", intp), ("lambda_val", float64), ("child_size", float32)]. */
+int fhg_condensed_record_array(const int64_t* parent_dev, const int64_t* child_dev,
+                               const float* lambda_dev, const float* child_size_dev,
+                               int64_t rows, void* records_dev, void* stream);
+
 /* Replaces cluster_trees.py:774 simplify_hierarchy(condensed_tree,
  * persistence_threshold).  Like the reference, relabels the rows it keeps in
  * the input arrays in place; the simplified tree (kept rows, in order) goes

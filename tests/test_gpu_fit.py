@@ -192,3 +192,19 @@ def test_weighted_fit_vs_oracle_synthetic(engine, n, seed):
                        sample_weights=w)
     orc = O.fit(X, 10, 50, mode=1, nthreads=8, sample_weights=w)
     _assert_fit_equal(res, orc)
+
+
+def test_estimator_condensed_record_array_on_gpu(engine):
+    """HDBSCAN.fit stores hdbscan.py:93 to_numpy_rec_array(condensed tree); the
+    engine lays the records out on the GPU -- same bytes as the host conversion."""
+    from fast_hdbscan_gb300 import HDBSCAN
+    from fast_hdbscan_gb300.hdbscan import fast_hdbscan, to_numpy_rec_array
+
+    g = _golden("blobs2d_2k")
+    model = HDBSCAN(min_cluster_size=50, min_samples=10).fit(g["X"])
+    ct = fast_hdbscan(g["X"], min_samples=10, min_cluster_size=50, return_trees=True)[3]
+    want = to_numpy_rec_array(ct)
+    assert model._condensed_tree.dtype == want.dtype
+    assert model._condensed_tree.tobytes() == want.tobytes()
+    np.testing.assert_array_equal(model.labels_, fast_hdbscan(g["X"], min_samples=10,
+                                                              min_cluster_size=50)[0])
