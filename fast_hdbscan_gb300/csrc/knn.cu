@@ -24,6 +24,8 @@ namespace fhg {
 namespace {
 
 constexpr int kKnnWarps = 4;
+// Buckets needed by at most this many lanes are scanned query by query.
+constexpr int kTransposeMax = 20;
 // Resident blocks asked of the register allocator: small lists fit in 80
 // registers, which keeps 24 warps per SM; larger lists take what they need.
 template <int K>
@@ -108,24 +110,49 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
     auto scan_leaf = [&](int64_t lf, bool need) {
         const int64_t base = lf * kLeaf;
         const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
+        float own[SP];  // this lane's candidate (lane t holds candidate t)
+#pragma unroll
+        for (int j = 0; j < SP; ++j) own[j] = 0.0f;
         if (lane < cnt) {
             const float4* src = reinterpret_cast<const float4*>(ix.pts) + (base + lane) * (SP / 4);
 #pragma unroll
-            for (int h = 0; h < SP / 4; ++h) cand[lane * (SP / 4) + h] = __ldg(src + h);
+            for (int h = 0; h < SP / 4; ++h) {
+                const float4 v = __ldg(src + h);
+                cand[lane * (SP / 4) + h] = v;
+                own[4 * h] = v.x; own[4 * h + 1] = v.y; own[4 * h + 2] = v.z; own[4 * h + 3] = v.w;
+            }
             corig[lane] = __ldg(orig + base + lane);
         }
         __syncwarp();
         const float thr = need ? entry_dist(key[K - 1]) : -INFINITY;
         uint32_t acc = 0u;
-#pragma unroll 4
-        for (int t = 0; t < cnt; ++t) {
-            float c[SP];
+        const unsigned needy = __ballot_sync(kFull, need);
+        if (__popc(needy) <= kTransposeMax) {
+            // Few lanes need the bucket: each lane takes its own candidate and
+            // the warp visits only the needing queries; the ballot over the
+            // candidates is that query's mask.  Same distances bit for bit.
+            unsigned mq = needy;
+            while (mq) {
+                const int i = __ffs(mq) - 1;
+                mq &= mq - 1u;
+                float qi[DIM];
 #pragma unroll
-            for (int h = 0; h < SP / 4; ++h) {
-                float4 v = cand[t * (SP / 4) + h];
-                c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
+                for (int j = 0; j < DIM; ++j) qi[j] = __shfl_sync(kFull, q[j], i);
+                const float ti = __shfl_sync(kFull, thr, i);
+                const unsigned bits = __ballot_sync(kFull, lane < cnt && rdist_rn<DIM>(qi, own) <= ti);
+                if (lane == i) acc = bits;
             }
-            acc |= (rdist_rn<DIM>(q, c) <= thr ? 1u : 0u) << t;
+        } else {
+#pragma unroll 4
+            for (int t = 0; t < cnt; ++t) {
+                float c[SP];
+#pragma unroll
+                for (int h = 0; h < SP / 4; ++h) {
+                    float4 v = cand[t * (SP / 4) + h];
+                    c[4 * h] = v.x; c[4 * h + 1] = v.y; c[4 * h + 2] = v.z; c[4 * h + 3] = v.w;
+                }
+                acc |= (rdist_rn<DIM>(q, c) <= thr ? 1u : 0u) << t;
+            }
         }
         while (acc) {
             const int t = __ffs(acc) - 1;
