@@ -50,6 +50,8 @@ SIGNATURES = {
     "fhg_cluster_epsilon_search": (_INT, [_P, _P, _P, _P, _I64, _P, _I64, _D, _P,
                                           ctypes.POINTER(_I64), _P]),
     "fhg_labelling_at_cut": (_INT, [_P, _I64, _D, _I64, _P, _P]),
+    "fhg_hdbscan_fit_batch": (_INT, [_I64, _P, _P, _P, _P, _P, _I32, _D, _INT, _P, _P, _I32,
+                                     _P, _P]),
     "fhg_hdbscan_fit": (_INT, [_P, _I64, _I32, _I32, _I64, _I32, _D, _INT, _D, _D, _P, _I32,
                                _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_I64),
                                _P, _P, _P, ctypes.POINTER(_I64), _P]),

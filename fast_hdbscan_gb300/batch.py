@@ -1,0 +1,83 @@
+"""Many independent HDBSCAN fits in one call (fhg_hdbscan_fit_batch).
+
+    from fast_hdbscan_gb300.batch import fit_many
+    results = fit_many([X0, X1, ...], min_samples=[5, 10, ...], min_cluster_size=[...])
+
+Every instance gets exactly the labels and probabilities of a single fit
+(fast_hdbscan(X, min_samples, min_cluster_size)); the fits run concurrently on
+a pool of worker streams inside the engine.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+
+def _per_instance(v, count, name):
+    if np.ndim(v) == 0:
+        return [v] * count
+    v = list(v)
+    if len(v) != count:
+        raise ValueError(f"{name} needs one value per instance ({count}), got {len(v)}")
+    return v
+
+
+def fit_many(instances, min_samples=10, min_cluster_size=10, cluster_selection_method="eom",
+             max_cluster_size=np.inf, allow_single_cluster=False, workers=16):
+    """Returns [(labels intp[n_i], probabilities float32[n_i]), ...].
+
+    ``min_samples`` / ``min_cluster_size``: one value, or one per instance
+    (min_samples None means min_cluster_size, as in fast_hdbscan)."""
+    torch = _native._torch()
+    count = len(instances)
+    ms = _per_instance(min_samples, count, "min_samples")
+    mcs = _per_instance(min_cluster_size, count, "min_cluster_size")
+    method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
+    if method is None:
+        raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+    Xs = [np.ascontiguousarray(X, dtype=np.float32) for X in instances]
+    for X in Xs:
+        if X.ndim != 2 or X.shape[1] > 8 or not np.all(np.isfinite(X)):
+            raise ValueError("every instance must be a finite n x d array with d <= 8")
+    results = [None] * count
+    run = [i for i in range(count) if Xs[i].shape[0] >= 2]
+    for i in range(count):
+        if Xs[i].shape[0] < 2:  # hdbscan.py:278-304
+            results[i] = (np.full(Xs[i].shape[0], -1, dtype=np.intp),
+                          np.zeros(Xs[i].shape[0], dtype=np.float32))
+    if not run:
+        return results
+    sizes = np.array([Xs[i].size for i in run], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    npts = np.array([Xs[i].shape[0] for i in run], dtype=np.int64)
+    poffs = np.concatenate([[0], np.cumsum(npts)])
+    flat = torch.from_numpy(np.concatenate([Xs[i].ravel() for i in run])).pin_memory()
+    d_x = flat.to("cuda", non_blocking=True)
+    d_lab = torch.empty(int(poffs[-1]), dtype=torch.int64, device="cuda")
+    d_prob = torch.empty(int(poffs[-1]), dtype=torch.float32, device="cuda")
+    m = len(run)
+    P = ctypes.c_void_p
+    xp = (P * m)(*[d_x.data_ptr() + 4 * int(offs[j]) for j in range(m)])
+    lp = (P * m)(*[d_lab.data_ptr() + 8 * int(poffs[j]) for j in range(m)])
+    pp = (P * m)(*[d_prob.data_ptr() + 4 * int(poffs[j]) for j in range(m)])
+    nn = (ctypes.c_int64 * m)(*[int(v) for v in npts])
+    dd = (ctypes.c_int32 * m)(*[Xs[i].shape[1] for i in run])
+    msa = (ctypes.c_int32 * m)(*[int(mcs[i] if ms[i] is None else ms[i]) for i in run])
+    mcsa = (ctypes.c_int64 * m)(*[int(mcs[i]) for i in run])
+    status = (ctypes.c_int32 * m)()
+    _native.check(_native.load().fhg_hdbscan_fit_batch(
+        m, ctypes.cast(xp, P), ctypes.cast(nn, P), ctypes.cast(dd, P), ctypes.cast(msa, P),
+        ctypes.cast(mcsa, P), method, float(max_cluster_size), int(bool(allow_single_cluster)),
+        ctypes.cast(lp, P), ctypes.cast(pp, P), int(workers), ctypes.cast(status, P),
+        _native.stream_ptr()))
+    lab = torch.empty(d_lab.shape, dtype=torch.int64, pin_memory=True)
+    prob = torch.empty(d_prob.shape, dtype=torch.float32, pin_memory=True)
+    lab.copy_(d_lab, non_blocking=True)
+    prob.copy_(d_prob, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    lab, prob = lab.numpy(), prob.numpy()
+    for j, i in enumerate(run):
+        a, b = int(poffs[j]), int(poffs[j + 1])
+        results[i] = (lab[a:b].astype(np.intp, copy=True), prob[a:b].copy())
+    return results

@@ -68,7 +68,7 @@ def build(force=False, verbose=False, ptxas_info=False):
     objs = [os.path.join(OBJ_DIR, os.path.basename(s)[:-3] + ".o") for s in sources]
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-Xcompiler", "-pthread"]
         subprocess.check_call(cmd)
         os.replace(tmp, LIB)
     return LIB

@@ -1,0 +1,114 @@
+// Many independent HDBSCAN fits at once (min_samples sweeps, per-cluster
+// re-clustering, collections of small datasets).
+//
+// A fit of a few thousand points is launch- and synchronisation-bound: a few
+// hundred short kernels and a handful of host reads of counts.  The batch
+// executor therefore overlaps fits rather than enlarging them: a pool of host
+// worker threads, each owning a non-blocking CUDA stream, takes instances
+// from a shared counter and runs the fused fit (fhg_hdbscan_fit) on its own
+// stream; the device interleaves the kernels of all streams.  Every
+// instance's result is exactly the single-fit result.  The work is ordered
+// after everything already queued on the caller's stream, and the caller's
+// stream waits for all of it.
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fhg_common.cuh"
+
+extern "C" int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                               int64_t min_cluster_size, int32_t selection_method,
+                               double max_cluster_size, int allow_single_cluster, double epsilon,
+                               double persistence, const float* sample_weights_dev,
+                               int32_t weighted_k, int64_t* labels_dev, float* probs_dev,
+                               double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+                               int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+                               int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
+                               int64_t* selected_dev, int64_t* n_selected_host, void* stream);
+
+using namespace fhg;
+
+extern "C" __attribute__((visibility("default"))) int fhg_hdbscan_fit_batch(
+    int64_t count, const float* const* X_dev, const int64_t* n, const int32_t* d,
+    const int32_t* min_samples, const int64_t* min_cluster_size, int32_t selection_method,
+    double max_cluster_size, int allow_single_cluster, int64_t* const* labels_dev,
+    float* const* probs_dev, int32_t n_workers, int32_t* status_host, void* stream) {
+    if (count <= 0) return FHG_OK;
+    if (!X_dev || !n || !d || !min_samples || !min_cluster_size || !labels_dev || !probs_dev ||
+        !status_host) {
+        set_error("fhg_hdbscan_fit_batch: null pointer argument");
+        return FHG_ERR_INVALID;
+    }
+    if (n_workers < 1) n_workers = 1;
+    if (n_workers > count) n_workers = (int32_t)count;
+    int dev = 0;
+    FHG_CUDA(cudaGetDevice(&dev));
+    cudaStream_t caller = reinterpret_cast<cudaStream_t>(stream);
+    cudaEvent_t start;
+    FHG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    FHG_CUDA(cudaEventRecord(start, caller));
+
+    std::atomic<int64_t> next{0};
+    std::mutex err_mu;
+    int first_rc = FHG_OK;
+    std::string first_msg;
+    std::vector<cudaEvent_t> done(n_workers, nullptr);
+    std::vector<int> setup_rc(n_workers, FHG_OK);
+
+    auto worker = [&](int w) {
+        cudaSetDevice(dev);
+        cudaStream_t s = nullptr;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&done[w], cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamWaitEvent(s, start, 0) != cudaSuccess) {
+            setup_rc[w] = FHG_ERR_CUDA;
+            if (s) cudaStreamDestroy(s);
+            return;
+        }
+        for (;;) {
+            const int64_t i = next.fetch_add(1);
+            if (i >= count) break;
+            const int rc = fhg_hdbscan_fit(X_dev[i], n[i], d[i], min_samples[i],
+                                           min_cluster_size[i], selection_method,
+                                           max_cluster_size, allow_single_cluster, 0.0, 0.0,
+                                           nullptr, 0, labels_dev[i], probs_dev[i], nullptr,
+                                           nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                           nullptr, nullptr, nullptr, nullptr, s);
+            status_host[i] = rc;
+            if (rc != FHG_OK) {
+                std::lock_guard<std::mutex> lk(err_mu);
+                if (first_rc == FHG_OK) {
+                    first_rc = rc;
+                    first_msg = "instance " + std::to_string((long long)i) + ": " + last_error();
+                }
+            }
+        }
+        cudaEventRecord(done[w], s);
+        cudaStreamDestroy(s);  // released once its work has completed
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(n_workers);
+    for (int w = 0; w < n_workers; ++w) pool.emplace_back(worker, w);
+    for (auto& t : pool) t.join();
+
+    int rc = FHG_OK;
+    for (int w = 0; w < n_workers; ++w) {
+        if (setup_rc[w] != FHG_OK) rc = setup_rc[w];
+        if (done[w]) {
+            if (setup_rc[w] == FHG_OK) cudaStreamWaitEvent(caller, done[w], 0);
+            cudaEventDestroy(done[w]);
+        }
+    }
+    cudaEventDestroy(start);
+    if (rc != FHG_OK) {
+        set_error("fhg_hdbscan_fit_batch: a worker could not create its stream");
+        return rc;
+    }
+    if (first_rc != FHG_OK) {
+        set_error("%s", first_msg.c_str());
+        return first_rc;
+    }
+    return FHG_OK;
+}

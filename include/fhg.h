@@ -201,6 +201,22 @@ int fhg_cluster_epsilon_search(const int64_t* parent_dev, const int64_t* child_d
 int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cut,
                          int64_t min_cluster_size, int64_t* labels_dev, void* stream);
 
+/* Many independent fits (no reference counterpart: the reference runs one
+ * fit per call, e.g. sub_clusters.py:75-95 loops over clusters in Python).
+ * Instance i is X_dev[i] (n[i] >= 2 points, d[i] <= 8) with min_samples[i],
+ * min_cluster_size[i] and the shared selection options; its labels and
+ * probabilities go to labels_dev[i] / probs_dev[i] (device pointers; the
+ * pointer arrays themselves are host memory), status_host[i] receives its
+ * FHG_* status.  n_workers host threads, each with its own stream, run the
+ * fused fit on instances taken in order; results equal fhg_hdbscan_fit's.
+ * The work follows what is queued on `stream`, which waits for all of it. */
+int fhg_hdbscan_fit_batch(int64_t count, const float* const* X_dev, const int64_t* n,
+                          const int32_t* d, const int32_t* min_samples,
+                          const int64_t* min_cluster_size, int32_t selection_method,
+                          double max_cluster_size, int allow_single_cluster,
+                          int64_t* const* labels_dev, float* const* probs_dev, int32_t n_workers,
+                          int32_t* status_host, void* stream);
+
 /* The whole fit of hdbscan.py:686 HDBSCAN.fit / :199 fast_hdbscan on device
  * data (Euclidean): spatial index, kNN core distances, Boruvka MST and the
  * tree passes (with cluster_selection_persistence and
