@@ -38,8 +38,8 @@ def fit_many(instances, min_samples=10, min_cluster_size=10, cluster_selection_m
         raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
     Xs = [np.ascontiguousarray(X, dtype=np.float32) for X in instances]
     for X in Xs:
-        if X.ndim != 2 or X.shape[1] > 8 or not np.all(np.isfinite(X)):
-            raise ValueError("every instance must be a finite n x d array with d <= 8")
+        if X.ndim != 2 or X.shape[1] > 30 or not np.all(np.isfinite(X)):
+            raise ValueError("every instance must be a finite n x d array with d <= 30")
     results = [None] * count
     run = [i for i in range(count) if Xs[i].shape[0] >= 2]
     for i in range(count):

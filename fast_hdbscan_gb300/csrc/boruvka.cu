@@ -626,7 +626,7 @@ template <int DIM>
 int launch_search(const fhg_index& ix, const int8_t* knn_open,
                   const float* core2, const int32_t* comp, const int2* nc,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
-    constexpr int SP = DIM <= 4 ? 4 : 8;
+    constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);  // as in the kNN kernel
     // Local pass (home bucket and the kLocalLevels nearest sibling subtrees),
     // then the rest of the walk: every component's bound from its nearby
     // candidates is published before any point searches far away.
@@ -662,7 +662,11 @@ int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* 
         case 5: return launch_search<5>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
         case 6: return launch_search<6>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
         case 7: return launch_search<7>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        default: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 8: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        default:
+            if (ix.d <= 16)
+                return launch_search<16>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+            return launch_search<32>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
     }
 }
 

@@ -85,14 +85,11 @@ __device__ __forceinline__ float box_lb_n(const float* __restrict__ box, const f
 
 template <int P>
 __device__ __forceinline__ void load_pt(const float* __restrict__ pts, int64_t i, float* out) {
-    if (P == 4) {
-        float4 v = __ldg(reinterpret_cast<const float4*>(pts) + i);
-        out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
-    } else {
-        const float4* p4 = reinterpret_cast<const float4*>(pts) + 2 * i;
-        float4 a = __ldg(p4), b = __ldg(p4 + 1);
-        out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
-        out[4] = b.x; out[5] = b.y; out[6] = b.z; out[7] = b.w;
+    const float4* p4 = reinterpret_cast<const float4*>(pts) + (P / 4) * i;
+#pragma unroll
+    for (int h = 0; h < P / 4; ++h) {
+        const float4 v = __ldg(p4 + h);
+        out[4 * h] = v.x; out[4 * h + 1] = v.y; out[4 * h + 2] = v.z; out[4 * h + 3] = v.w;
     }
 }
 

@@ -28,8 +28,8 @@ constexpr int kKnnWarps = 4;
 constexpr int kTransposeMax = 20;
 // Resident blocks asked of the register allocator: small lists fit in 80
 // registers, which keeps 24 warps per SM; larger lists take what they need.
-template <int K>
-constexpr int knn_min_blocks() { return K <= 16 ? 6 : 1; }
+template <int DIM, int K>
+constexpr int knn_min_blocks() { return (K <= 16 && DIM <= 8) ? 6 : 1; }
 constexpr int kStack = 64;
 
 __device__ __forceinline__ unsigned long long pack_entry(float d, int32_t o) {
@@ -41,7 +41,7 @@ __device__ __forceinline__ float entry_dist(unsigned long long e) {
 __device__ __forceinline__ int32_t entry_orig(unsigned long long e) { return (int32_t)(uint32_t)e; }
 
 template <int DIM, int SP, int K>
-__global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kernel(IndexView ix, int k,
+__global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_kernel(IndexView ix, int k,
                                                               float* __restrict__ d_s,
                                                               int32_t* __restrict__ i_s,
                                                               float* __restrict__ d_o,
@@ -235,7 +235,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<K>()) knn_kerne
 template <int DIM, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
                int8_t* tie_s, int io_stride, int io_skip, cudaStream_t s) {
-    constexpr int SP = DIM <= 4 ? 4 : 8;
+    // padded width; for d > 8 the kernels run over all SP = DIM padded
+    // coordinates (the padding is zero and adds exact zeros to distances)
+    constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);
     unsigned g = grid_for(ix.nleaves, kKnnWarps);
     Stage stage(s, "knn_kernel");
     ::fhg::note_launch();
@@ -277,7 +279,11 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
         case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
         case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
         case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        default: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 8: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        default:
+            if (ix.d <= 16)
+                return dispatch_k<16>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+            return dispatch_k<32>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
     }
 }
 

@@ -9,28 +9,34 @@ namespace fhg {
 namespace {
 
 constexpr int kBBThreads = 256;
+constexpr int kMaxDim = 32;  // bounding box layout: lo[0..32), hi[32..64)
 
-// Per-block min/max of every dimension: partial[block][2][8].
+// Per-block min/max of every dimension: partial[block][2][kMaxDim].  MAXD is
+// 8 or kMaxDim; the loops are unrolled and predicated on d (no local memory).
+template <int MAXD>
 __global__ void bbox_partial_kernel(const float* __restrict__ X, int64_t n, int d,
                                     float* __restrict__ partial) {
-    float lo[8], hi[8];
+    float lo[MAXD], hi[MAXD];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < MAXD; ++j) {
         lo[j] = INFINITY;
         hi[j] = -INFINITY;
     }
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        for (int j = 0; j < d; ++j) {
-            float v = X[i * d + j];
-            lo[j] = fminf(lo[j], v);
-            hi[j] = fmaxf(hi[j], v);
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j) {
+            if (j < d) {
+                float v = X[i * d + j];
+                lo[j] = fminf(lo[j], v);
+                hi[j] = fmaxf(hi[j], v);
+            }
         }
     }
-    __shared__ float s_lo[kBBThreads / 32][8], s_hi[kBBThreads / 32][8];
+    __shared__ float s_lo[kBBThreads / 32][MAXD], s_hi[kBBThreads / 32][MAXD];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < MAXD; ++j) {
         float a = lo[j], b = hi[j];
         for (int o = 16; o; o >>= 1) {
             a = fminf(a, __shfl_xor_sync(kFull, a, o));
@@ -42,48 +48,60 @@ __global__ void bbox_partial_kernel(const float* __restrict__ X, int64_t n, int 
         }
     }
     __syncthreads();
-    if (threadIdx.x < 8) {
+    if (threadIdx.x < MAXD) {
         float a = INFINITY, b = -INFINITY;
         for (int ww = 0; ww < kBBThreads / 32; ++ww) {
             a = fminf(a, s_lo[ww][threadIdx.x]);
             b = fmaxf(b, s_hi[ww][threadIdx.x]);
         }
-        partial[blockIdx.x * 16 + threadIdx.x] = a;
-        partial[blockIdx.x * 16 + 8 + threadIdx.x] = b;
+        partial[blockIdx.x * 2 * kMaxDim + threadIdx.x] = a;
+        partial[blockIdx.x * 2 * kMaxDim + kMaxDim + threadIdx.x] = b;
     }
 }
 
-__global__ void bbox_final_kernel(const float* __restrict__ partial, int nb, float* bb) {
-    int j = threadIdx.x;  // 16 threads: 8 lo + 8 hi
-    if (j >= 16) return;
-    bool is_lo = j < 8;
+__global__ void bbox_final_kernel(const float* __restrict__ partial, int nb, int d, float* bb) {
+    int j = threadIdx.x;  // 2 * kMaxDim threads: lo then hi
+    if (j >= 2 * kMaxDim) return;
+    bool is_lo = j < kMaxDim;
     float acc = is_lo ? INFINITY : -INFINITY;
-    for (int b = 0; b < nb; ++b) {
-        float v = partial[b * 16 + j];
-        acc = is_lo ? fminf(acc, v) : fmaxf(acc, v);
-    }
+    if ((j % kMaxDim) < d)
+        for (int b = 0; b < nb; ++b) {
+            float v = partial[b * 2 * kMaxDim + j];
+            acc = is_lo ? fminf(acc, v) : fmaxf(acc, v);
+        }
     bb[j] = acc;
 }
 
-// 63-bit (or less) Morton key from a common-scale quantisation of all axes.
+// 63-bit (or less) Morton key from a common-scale quantisation of all axes
+// (bits per axis = min(63 / d, 31); at least one).
+template <int MAXD>
 __global__ void morton_kernel(const float* __restrict__ X, int64_t n, int d,
                               const float* __restrict__ bb, int bits,
                               uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float ext = 0.0f;
-    for (int j = 0; j < d; ++j) ext = fmaxf(ext, bb[8 + j] - bb[j]);
+#pragma unroll
+    for (int j = 0; j < MAXD; ++j)
+        if (j < d) ext = fmaxf(ext, bb[kMaxDim + j] - bb[j]);
     const float qmax = (float)((1ull << bits) - 1ull);
     const float scale = ext > 0.0f ? qmax / ext : 0.0f;
-    uint64_t key = 0;
-    uint32_t q[8];
-    for (int j = 0; j < d; ++j) {
-        float t = (X[i * d + j] - bb[j]) * scale;
-        t = fminf(fmaxf(t, 0.0f), qmax);
-        q[j] = (uint32_t)t;
+    uint32_t q[MAXD];
+#pragma unroll
+    for (int j = 0; j < MAXD; ++j) {
+        q[j] = 0;
+        if (j < d) {
+            float t = (X[i * d + j] - bb[j]) * scale;
+            t = fminf(fmaxf(t, 0.0f), qmax);
+            q[j] = (uint32_t)t;
+        }
     }
-    for (int b = 0; b < bits; ++b)
-        for (int j = 0; j < d; ++j) key |= (uint64_t)((q[j] >> b) & 1u) << (b * d + j);
+    uint64_t key = 0;
+    for (int b = 0; b < bits; ++b) {
+#pragma unroll
+        for (int j = 0; j < MAXD; ++j)
+            if (j < d) key |= (uint64_t)((q[j] >> b) & 1u) << (b * d + j);
+    }
     keys[i] = key;
     vals[i] = (int32_t)i;
 }
@@ -179,8 +197,8 @@ int index_free(fhg_index* ix, cudaStream_t s) {
 
 int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index** out) {
     *out = nullptr;
-    if (n < 1 || d < 1 || d > 8) {
-        set_error("index_build: need n >= 1 and 1 <= d <= 8 (got n=%lld, d=%d)", (long long)n, d);
+    if (n < 1 || d < 1 || d > kMaxDim) {
+        set_error("index_build: need n >= 1 and 1 <= d <= 32 (got n=%lld, d=%d)", (long long)n, d);
         return FHG_ERR_INVALID;
     }
     if (n >= ((int64_t)1 << 31) - 64) {
@@ -191,7 +209,7 @@ int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index*
     fhg_index* ix = new fhg_index();
     ix->n = n;
     ix->d = d;
-    ix->pad = d <= 4 ? 4 : 8;
+    ix->pad = d <= 4 ? 4 : (d <= 8 ? 8 : (d <= 16 ? 16 : 32));
     ix->nleaves = (n + kLeaf - 1) / kLeaf;
     ix->slots = 1;
     while (ix->slots < ix->nleaves) ix->slots *= 2;
@@ -206,17 +224,23 @@ int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index*
         float *partial, *bb;
         uint64_t* keys;
         int nb = (int)std::min<int64_t>(1024, (n + kBBThreads - 1) / kBBThreads);
-        rc = ws.alloc(&partial, (size_t)nb * 16);
-        if (rc == FHG_OK) rc = ws.alloc(&bb, 16);
+        rc = ws.alloc(&partial, (size_t)nb * 2 * kMaxDim);
+        if (rc == FHG_OK) rc = ws.alloc(&bb, 2 * kMaxDim);
         if (rc == FHG_OK) rc = ws.alloc(&keys, (size_t)n);
         if (rc == FHG_OK) {
             ::fhg::note_launch();
-            bbox_partial_kernel<<<nb, kBBThreads, 0, s>>>(X, n, d, partial);
+            if (d <= 8) bbox_partial_kernel<8><<<nb, kBBThreads, 0, s>>>(X, n, d, partial);
+            else bbox_partial_kernel<kMaxDim><<<nb, kBBThreads, 0, s>>>(X, n, d, partial);
             ::fhg::note_launch();
-            bbox_final_kernel<<<1, 32, 0, s>>>(partial, nb, bb);
-            int bits = std::min(63 / d, 31);
+            bbox_final_kernel<<<1, 2 * kMaxDim, 0, s>>>(partial, nb, d, bb);
+            int bits = std::max(1, std::min(63 / d, 31));
             ::fhg::note_launch();
-            morton_kernel<<<grid_for(n, 256), 256, 0, s>>>(X, n, d, bb, bits, keys, ix->orig);
+            if (d <= 8)
+                morton_kernel<8><<<grid_for(n, 256), 256, 0, s>>>(X, n, d, bb, bits, keys,
+                                                                   ix->orig);
+            else
+                morton_kernel<kMaxDim><<<grid_for(n, 256), 256, 0, s>>>(X, n, d, bb, bits, keys,
+                                                                        ix->orig);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 set_error("morton kernels: %s", cudaGetErrorString(e));
@@ -235,7 +259,14 @@ int index_build(const float* X, int64_t n, int32_t d, cudaStream_t s, fhg_index*
                 rc = FHG_ERR_CUDA;
             }
         }
-        if (rc == FHG_OK) rc = ix->pad == 4 ? build_boxes<4>(ix, s) : build_boxes<8>(ix, s);
+        if (rc == FHG_OK) {
+            switch (ix->pad) {
+                case 4: rc = build_boxes<4>(ix, s); break;
+                case 8: rc = build_boxes<8>(ix, s); break;
+                case 16: rc = build_boxes<16>(ix, s); break;
+                default: rc = build_boxes<32>(ix, s); break;
+            }
+        }
     }
     if (rc != FHG_OK) {
         index_free(ix, s);

@@ -193,9 +193,13 @@ def _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data
                          "Got algorithm='boruvka'.")
     if semi_supervised:
         raise NotImplementedError("semi-supervised selection is outside the GPU engine's path")
-    if data is not None and data.shape[1] > 8:
+    if data is not None and data.shape[1] > 32:
         raise NotImplementedError(
-            f"{data.shape[1]}-dimensional data: the GPU spatial path supports up to 8 dimensions")
+            f"{data.shape[1]}-dimensional data: the GPU spatial path supports up to 32 dimensions")
+    if data is not None and data.shape[1] > 30 and sample_weights is None:
+        raise NotImplementedError(
+            "the reference routes data with more than 30 dimensions (and no sample weights) to "
+            "its approximate NNDescent back-end (hdbscan.py:447), which is not on the GPU path")
 
 
 def _degenerate(n, return_trees):

@@ -104,6 +104,11 @@ CASES = {
                   dict(min_samples=15, min_cluster_size=25,
                        sample_weights=lambda: np.random.default_rng(5).integers(
                            1, 4, 5000).astype(np.float32))),
+    # more than 8 dimensions (the reference's KD-tree Boruvka path serves d <= 30)
+    "hd12_2k": (lambda: synthetic.umap_like(2000, seed=31, dim=12, n_blobs=8),
+                dict(min_samples=10, min_cluster_size=25)),
+    "hd24_1k": (lambda: synthetic.umap_like(1000, seed=32, dim=24, n_blobs=6),
+                dict(min_samples=8, min_cluster_size=20)),
     "edge_two": (lambda: np.array([[0.0, 0.0], [0.1, 0.0]]), dict(min_cluster_size=2)),
     "edge_dups": (lambda: np.full((50, 3), 1.0), dict(min_cluster_size=5)),
     "edge_1d": (_one_d, dict(min_cluster_size=10)),

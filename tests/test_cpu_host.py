@@ -100,8 +100,11 @@ def test_out_of_scope_routes_raise_not_implemented():
         fast_hdbscan(X, algorithm="kruskal")
     with pytest.raises(ValueError):
         compute_minimum_spanning_tree(X, algorithm="prim")
+    with pytest.raises(NotImplementedError):  # hdbscan.py:447: NNDescent above 30 dims
+        fast_hdbscan(np.random.default_rng(2).random((20, 31)))
     with pytest.raises(NotImplementedError):
-        fast_hdbscan(np.random.default_rng(2).random((20, 9)))
+        fast_hdbscan(np.random.default_rng(2).random((20, 40)),
+                     sample_weights=np.ones(20, np.float32))
 
 
 def test_estimator_params_roundtrip():

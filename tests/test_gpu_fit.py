@@ -27,7 +27,7 @@ GOLDEN_FIT = ["ka150", "ka150_eps", "blobs200", "blobs200_ms1", "blobs200_leaf",
               "blobs200_maxcs", "blobs200_single", "blobs200_persist", "blobs2d_2k",
               "blobs2d_20k", "umap5d_5k", "vd3d_5k", "vd3d_20k", "edge_two", "edge_1d",
               "edge_highms", "edge_dups", "edge_mcs_gt_n", "blobs200_w_labels", "blobs2d_2k_w",
-              "vd3d_5k_w"]
+              "vd3d_5k_w", "hd12_2k", "hd24_1k"]
 
 
 def _golden(name):
@@ -208,3 +208,17 @@ def test_estimator_condensed_record_array_on_gpu(engine):
     assert model._condensed_tree.tobytes() == want.tobytes()
     np.testing.assert_array_equal(model.labels_, fast_hdbscan(g["X"], min_samples=10,
                                                               min_cluster_size=50)[0])
+
+
+@pytest.mark.parametrize("n,dim,ms,mcs", [(100_000, 16, 10, 100), (30_000, 30, 10, 50),
+                                          (50_000, 11, 5, 30)])
+def test_high_dimensional_fit_vs_oracle(engine, n, dim, ms, mcs):
+    """9-32 dimensions: the kernels run over the padded width (16 or 32); the
+    padding adds exact zeros, so every output matches the oracle bit for bit."""
+    from fast_hdbscan_gb300.hdbscan import fast_hdbscan
+    from oracle import oracle as O
+
+    X = synthetic.umap_like(n, seed=40 + dim, dim=dim, n_blobs=12)
+    res = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs, return_trees=True)
+    orc = O.fit(X, ms, mcs, mode=1, nthreads=16)
+    _assert_fit_equal(res, orc)
