@@ -40,6 +40,15 @@ METRIC = "HDBSCAN fit points/s at 10M x 3-D (varying density, min_samples=15)"
 WORKLOAD = dict(workload="varying_density_10M_3d", n=10_000_000, d=3, min_samples=15,
                 min_cluster_size=500, seed=3,
                 generator="200 Gaussians, std lognormal(0,1), centres U[-100,100]^3")
+# Other configurations of the benchmark family, for reports (--workload):
+# the 2M x 5-D UMAP-like input (40 blobs, std log-uniform [0.2, 2], Dirichlet
+# weights, centres U[-20, 20]^5, 10 % noise).
+OTHER_WORKLOADS = {
+    "umap2m": dict(workload="umap_like_2M_5d", n=2_000_000, d=5, min_samples=10,
+                   min_cluster_size=500, seed=1,
+                   generator="40 blobs, std logU[0.2,2], Dirichlet weights, centres "
+                             "U[-20,20]^5, 10% noise"),
+}
 CPU_SAMPLE_N = 1_000_000
 
 
@@ -53,8 +62,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N)
-    ap.add_argument("--workload", default="fit", choices=["fit", "batched"],
-                    help="fit: the metric's 10M x 3-D fit; batched: many independent fits")
+    ap.add_argument("--workload", default="fit", choices=["fit", "batched", *OTHER_WORKLOADS],
+                    help="fit: the metric's 10M x 3-D fit; batched: many independent fits; "
+                         "umap2m: the 2M x 5-D fit")
     ap.add_argument("--instances", type=int, default=4096, help="batched workload size")
     return ap.parse_args()
 
@@ -80,6 +90,8 @@ def max_over_ranks(value, device):
 def make_data(n, seed):
     from fast_hdbscan_gb300 import synthetic
 
+    if WORKLOAD["workload"].startswith("umap_like"):
+        return synthetic.umap_like(n, seed=seed, dim=WORKLOAD["d"])
     return synthetic.varying_density(n, seed=seed)
 
 
@@ -442,6 +454,14 @@ def run_batched(args):
 
 def main():
     args = parse_args()
+    if args.workload in OTHER_WORKLOADS:
+        WORKLOAD.clear()
+        WORKLOAD.update(OTHER_WORKLOADS[args.workload])
+        if args.n == 10_000_000:
+            args.n = WORKLOAD["n"]
+        global METRIC
+        METRIC = f"HDBSCAN fit points/s at {WORKLOAD['n'] // 1_000_000}M x {WORKLOAD['d']}-D"
+        args.workload = "fit"
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
