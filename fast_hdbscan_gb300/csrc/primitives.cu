@@ -102,8 +102,8 @@ int scan_exclusive(Workspace& ws, const T* in, T* out, int64_t n, T* total) {
 // ---------------------------------------------------------------- radix sort
 constexpr int kRsThreads = 256;
 constexpr int kRsWarps = kRsThreads / 32;
-constexpr int kRsChunks = 16;                       // 32-item chunks per warp
-constexpr int kRsTile = kRsWarps * kRsChunks * 32;  // 4096 items per block
+constexpr int kRsChunks = 8;                        // 32-item chunks per warp
+constexpr int kRsTile = kRsWarps * kRsChunks * 32;  // 2048 items per block
 
 template <class K>
 __global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const K* __restrict__ keys,
@@ -122,17 +122,26 @@ __global__ void __launch_bounds__(kRsThreads) rs_hist_kernel(const K* __restrict
     hist[(int64_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// Stable scatter of one 8-bit digit.  Each warp ranks its 16 chunks of 32
+// items per digit (lanes by __match_any_sync); the tile's items are then laid
+// out in digit order in shared memory and written out so that consecutive
+// threads store consecutive positions of one digit's run (coalesced), in the
+// same stable order as a direct scatter.
 template <class K>
 __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
     const K* __restrict__ kin, const int32_t* __restrict__ vin, K* __restrict__ kout,
     int32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ offs,
     int64_t tiles) {
     __shared__ uint32_t wcnt[kRsWarps][256];
+    __shared__ uint32_t tstart[256];
+    __shared__ K skey[kRsTile];
+    __shared__ int32_t sval[kRsTile];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < kRsWarps * 256; i += kRsThreads) (&wcnt[0][0])[i] = 0;
     __syncthreads();
     const unsigned lt_mask = (1u << lane) - 1u;
-    const int64_t base = (int64_t)blockIdx.x * kRsTile + (int64_t)w * (kRsChunks * 32);
+    const int64_t tile0 = (int64_t)blockIdx.x * kRsTile;
+    const int64_t base = tile0 + (int64_t)w * (kRsChunks * 32);
     K key[kRsChunks];
     int32_t val[kRsChunks];
     uint32_t pos[kRsChunks];
@@ -156,22 +165,32 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
         dig[c] = d;
     }
     __syncthreads();
-    {
-        uint32_t s = 0;
+    {   // per digit: warps' offsets inside the digit, then the digit's start in the tile
+        uint32_t sum = 0;
         for (int ww = 0; ww < kRsWarps; ++ww) {
             uint32_t c = wcnt[ww][threadIdx.x];
-            wcnt[ww][threadIdx.x] = s;
-            s += c;
+            wcnt[ww][threadIdx.x] = sum;
+            sum += c;
         }
+        tstart[threadIdx.x] = block_exclusive_scan<uint32_t>(sum, nullptr);
     }
     __syncthreads();
 #pragma unroll
     for (int c = 0; c < kRsChunks; ++c) {
         if (dig[c] < 256) {
-            uint32_t dst = offs[(int64_t)dig[c] * tiles + blockIdx.x] + wcnt[w][dig[c]] + pos[c];
-            kout[dst] = key[c];
-            vout[dst] = val[c];
+            const uint32_t lp = tstart[dig[c]] + wcnt[w][dig[c]] + pos[c];
+            skey[lp] = key[c];
+            sval[lp] = val[c];
         }
+    }
+    __syncthreads();
+    const int cnt = (int)(n - tile0 < kRsTile ? n - tile0 : kRsTile);
+    for (int i = threadIdx.x; i < cnt; i += kRsThreads) {
+        const K k = skey[i];
+        const int d = (int)((unsigned)(k >> shift) & 255u);
+        const uint32_t dst = offs[(int64_t)d * tiles + blockIdx.x] + (uint32_t)i - tstart[d];
+        kout[dst] = k;
+        vout[dst] = sval[i];
     }
 }
 
