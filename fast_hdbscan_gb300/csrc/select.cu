@@ -28,7 +28,9 @@ __global__ void parent_keys_kernel(int64_t rows, int64_t n, const int32_t* __res
     if (r >= rows) return;
     int32_t c = parent[r] - (int32_t)n;
     key[r] = (uint32_t)c;
-    atomicAdd(&cnt[c], 1);
+    // rows of one parent come in runs: one atomic per parent per warp
+    const unsigned peers = __match_any_sync(__activemask(), c);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cnt[c], __popc(peers));
 }
 __global__ void row_of_child_kernel(int64_t rows, int64_t n, const int32_t* __restrict__ child,
                                     int32_t* __restrict__ row_of_cluster,
@@ -315,8 +317,22 @@ __global__ void root_stats_kernel(int64_t rows, int64_t n, const int32_t* __rest
     if (r >= rows) return;
     int32_t c = parent[r] - (int32_t)n;
     unsigned int b = __float_as_uint(lam[r]);
-    if (c == 0) atomicMax(root_max, b);
-    if (csize[r] == 1.0f) atomicMax(&death[c], b);
+    const int lane = threadIdx.x & 31;
+    const unsigned act = __activemask();
+    // non-negative floats order like their bits; lanes combine first, then one
+    // atomic per target per warp
+    const unsigned roots = __ballot_sync(act, c == 0);
+    if (c == 0) {
+        const unsigned m = __reduce_max_sync(roots, b);
+        if (lane == __ffs(roots) - 1) atomicMax(root_max, m);
+    }
+    const bool pt = csize[r] == 1.0f;
+    const unsigned pts = __ballot_sync(act, pt);
+    if (pt) {
+        const unsigned peers = __match_any_sync(pts, c);
+        const unsigned m = __reduce_max_sync(peers, b);
+        if (lane == __ffs(peers) - 1) atomicMax(&death[c], m);
+    }
 }
 __global__ void point_labels_kernel(int64_t n, int64_t n_distinct, double eps,
                                     const int32_t* __restrict__ row_of_point,
@@ -463,7 +479,10 @@ __global__ void narrow_rows_kernel(int64_t rows, const int64_t* __restrict__ p,
     if (r >= rows) return;
     op[r] = (int32_t)p[r];
     oc[r] = (int32_t)c[r];
-    atomicMax(mx, (unsigned long long)max(p[r], c[r]));
+    // labels fit 32 bits: combine the warp first, then one atomic per warp
+    const unsigned act = __activemask();
+    const unsigned m = __reduce_max_sync(act, (unsigned)max(p[r], c[r]));
+    if ((int)(threadIdx.x & 31) == __ffs(act) - 1) atomicMax(mx, (unsigned long long)m);
 }
 }  // namespace
 
