@@ -166,8 +166,8 @@ def algorithmic_bytes(kernel, n, k, d_pad):
     if kernel == "knn_kernel":
         # read every point once (padded coordinates + caller index); write the
         # Morton-order rows (squared distance + position), the caller-order
-        # neighbour ids and the one-byte boundary-tie flag
-        return n * (4 * d_pad + 4) + n * k * 8 + n * k * 4 + n
+        # neighbour matrix (k - 1 columns) and the one-byte boundary-tie flag
+        return n * (4 * d_pad + 4) + n * k * 8 + n * (k - 1) * 4 + n
     if kernel == "search_kernel":
         # per pass: each point's component, core distance, candidate (weight
         # + position), k-th distance and tie flag; each tree node's
