@@ -55,6 +55,10 @@ SIGNATURES = {
     "fhg_hdbscan_fit": (_INT, [_P, _I64, _I32, _I32, _I64, _I32, _D, _INT, _D, _D, _P, _I32,
                                _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_I64),
                                _P, _P, _P, ctypes.POINTER(_I64), _P]),
+    "fhg_hdbscan_fit_export": (_INT, [_P, _I64, _I32, _I32, _I64, _I32, _D, _INT, _D, _D, _P,
+                                      _I32, _P, _P, _P, _P, _P, _P, _P, _P,
+                                      ctypes.POINTER(_I64), _P, _P, _P, ctypes.POINTER(_I64),
+                                      _P, _P, _P, _P, _P, _P, _P]),
 }
 
 _lib = None
@@ -145,6 +149,15 @@ def vptr(t):
     if t is None:
         return _P()
     assert t.is_cuda and t.is_contiguous()
+    return _P(t.data_ptr())
+
+
+def hptr(t):
+    """Host pointer of a contiguous CPU tensor (pinned or pageable), or NULL
+    for None."""
+    if t is None:
+        return _P()
+    assert not t.is_cuda and t.is_contiguous()
     return _P(t.data_ptr())
 
 

@@ -540,15 +540,68 @@ FHG_API int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cu
 }
 
 // ---------------------------------------------------------------- fused fit
-FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
-                            int64_t min_cluster_size, int32_t selection_method,
-                            double max_cluster_size, int allow_single_cluster, double epsilon,
-                            double persistence, const float* sample_weights_dev,
-                            int32_t weighted_k, int64_t* labels_dev, float* probs_dev,
-                            double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
-                            int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
-                            int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
-                            int64_t* selected_dev, int64_t* n_selected_host, void* stream) {
+namespace {
+
+// Host destinations of the large fit outputs, each copied on a side stream as
+// soon as the fit has finished writing it, so that the transfers overlap the
+// later stages.  NULL members are not copied.
+struct FitExport {
+    int32_t* neighbors_host = nullptr;
+    float* core_host = nullptr;
+    double* mst_host = nullptr;
+    double* linkage_host = nullptr;
+    void* records_dev = nullptr;
+    void* records_host = nullptr;
+    int64_t* records_rows_host = nullptr;
+};
+
+// Device-to-host copies ordered after the work queued so far on the fit's
+// stream, issued on a side stream; the fit's stream waits for all of them
+// when the export ends (also on an error return).
+class SideCopies {
+public:
+    explicit SideCopies(cudaStream_t main) : main_(main) {}
+    SideCopies(const SideCopies&) = delete;
+    SideCopies& operator=(const SideCopies&) = delete;
+    ~SideCopies() {
+        if (!side_) return;
+        cudaEventRecord(ev_, side_);
+        cudaStreamWaitEvent(main_, ev_, 0);
+        cudaEventDestroy(ev_);
+        cudaStreamDestroy(side_);  // released once its copies have completed
+    }
+    int copy(void* dst, const void* src, size_t bytes) {
+        if (!dst || bytes == 0) return FHG_OK;
+        if (!side_) {
+            FHG_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+            if (cudaEventCreateWithFlags(&ev_, cudaEventDisableTiming) != cudaSuccess) {
+                cudaStreamDestroy(side_);
+                side_ = nullptr;
+                set_error("fit export: cudaEventCreateWithFlags failed");
+                return FHG_ERR_CUDA;
+            }
+        }
+        FHG_CUDA(cudaEventRecord(ev_, main_));
+        FHG_CUDA(cudaStreamWaitEvent(side_, ev_, 0));
+        FHG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, side_));
+        return FHG_OK;
+    }
+
+private:
+    cudaStream_t main_;
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t ev_ = nullptr;
+};
+
+int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+             int64_t min_cluster_size, int32_t selection_method, double max_cluster_size,
+             int allow_single_cluster, double epsilon, double persistence,
+             const float* sample_weights_dev, int32_t weighted_k, int64_t* labels_dev,
+             float* probs_dev, double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+             int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+             int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
+             int64_t* selected_dev, int64_t* n_selected_host, void* stream,
+             const FitExport& ex) {
     FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev, labels_dev, probs_dev}));
     if (min_samples < 1 || min_cluster_size < 1) {
         set_error("Min samples and min cluster size must be positive integers!");
@@ -563,6 +616,7 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
         return FHG_ERR_INVALID;
     }
     cudaStream_t s = as_stream(stream);
+    SideCopies side(s);  // declared before the workspace: joins after its frees are queued
     Workspace ws(s);
     fhg_index* ix = nullptr;
     FHG_TRY(index_build(X_dev, n, d, s, &ix));
@@ -574,6 +628,13 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
     MstResult mst;
     FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev, sample_weights_dev,
                         weighted_k));
+    if (neighbors_dev) {
+        // the row width boruvka_mst writes: k - 1 for its k-neighbour query
+        const int64_t kq = sample_weights_dev ? weighted_k : (min_samples > 1 ? min_samples + 1 : 2);
+        const int64_t kcols = kq > 1 ? kq - 1 : 0;
+        FHG_TRY(side.copy(ex.neighbors_host, neighbors_dev, sizeof(int32_t) * n * kcols));
+    }
+    if (core_dev) FHG_TRY(side.copy(ex.core_host, core_dev, sizeof(float) * n));
     if (mst.m != n - 1) {
         set_error("boruvka: spanning forest has %lld edges for %lld points", (long long)mst.m,
                   (long long)n);
@@ -587,6 +648,8 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
         if (mst_dev) FHG_TRY(sorted_mst_to_f64(lk, mst_dev, s));
         if (linkage_dev) FHG_TRY(linkage_to_f64(lk, linkage_dev, s));
     }
+    if (mst_dev) FHG_TRY(side.copy(ex.mst_host, mst_dev, sizeof(double) * 3 * (n - 1)));
+    if (linkage_dev) FHG_TRY(side.copy(ex.linkage_host, linkage_dev, sizeof(double) * 4 * (n - 1)));
     Condensed ct;
     // hdbscan.py:521: the fit path condenses without max_cluster_size; only
     // the EOM selection reads it.
@@ -597,8 +660,20 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
         ct = simple;
     }
     if (ct_rows_host) *ct_rows_host = ct.rows;
-    if (ct_parent_dev && ct_child_dev && ct_lambda_dev && ct_size_dev)
+    if (ct_parent_dev && ct_child_dev && ct_lambda_dev && ct_size_dev) {
         FHG_TRY(condensed_to_arrays(ct, ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, s));
+        if (ex.records_dev) {
+            if (ex.records_rows_host) *ex.records_rows_host = ct.rows;
+            if (ct.rows > 0) {
+                ::fhg::note_launch();
+                fhg::capi::condensed_records_kernel<<<grid_for(ct.rows, 256), 256, 0, s>>>(
+                    ct.rows, ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev,
+                    static_cast<uint32_t*>(ex.records_dev));
+                FHG_CUDA(cudaGetLastError());
+                FHG_TRY(side.copy(ex.records_host, ex.records_dev, (size_t)ct.rows * 28));
+            }
+        }
+    }
     int32_t* sel;
     FHG_TRY(ws.alloc(&sel, (size_t)(ct.n_clusters > 0 ? ct.n_clusters : 1)));
     int64_t k = 0;
@@ -625,4 +700,57 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
         return FHG_OK;
     }
     return label_points(ws, ct, sel, k, epsilon, labels_dev, probs_dev);
+}
+
+}  // namespace
+
+FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                            int64_t min_cluster_size, int32_t selection_method,
+                            double max_cluster_size, int allow_single_cluster, double epsilon,
+                            double persistence, const float* sample_weights_dev,
+                            int32_t weighted_k, int64_t* labels_dev, float* probs_dev,
+                            double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+                            int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+                            int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
+                            int64_t* selected_dev, int64_t* n_selected_host, void* stream) {
+    return fit_impl(X_dev, n, d, min_samples, min_cluster_size, selection_method,
+                    max_cluster_size, allow_single_cluster, epsilon, persistence,
+                    sample_weights_dev, weighted_k, labels_dev, probs_dev, mst_dev, linkage_dev,
+                    ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, ct_rows_host,
+                    neighbors_dev, core_dev, selected_dev, n_selected_host, stream, FitExport());
+}
+
+FHG_API int fhg_hdbscan_fit_export(
+    const float* X_dev, int64_t n, int32_t d, int32_t min_samples, int64_t min_cluster_size,
+    int32_t selection_method, double max_cluster_size, int allow_single_cluster, double epsilon,
+    double persistence, const float* sample_weights_dev, int32_t weighted_k, int64_t* labels_dev,
+    float* probs_dev, double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+    int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev, int64_t* ct_rows_host,
+    int32_t* neighbors_dev, float* core_dev, int64_t* selected_dev, int64_t* n_selected_host,
+    int32_t* neighbors_host, float* core_host, double* mst_host, double* linkage_host,
+    void* ct_records_dev, void* ct_records_host, void* stream) {
+    if (ct_records_dev && reinterpret_cast<uintptr_t>(ct_records_dev) % 4 != 0) {
+        set_error("fhg_hdbscan_fit_export: ct_records_dev must be 4-byte aligned");
+        return FHG_ERR_INVALID;
+    }
+    if ((neighbors_host && !neighbors_dev) || (core_host && !core_dev) ||
+        (mst_host && !mst_dev) || (linkage_host && !linkage_dev) ||
+        (ct_records_host && !ct_records_dev) ||
+        (ct_records_dev && !(ct_parent_dev && ct_child_dev && ct_lambda_dev && ct_size_dev))) {
+        set_error("fhg_hdbscan_fit_export: every exported output needs its device buffer");
+        return FHG_ERR_INVALID;
+    }
+    FitExport ex;
+    ex.neighbors_host = neighbors_host;
+    ex.core_host = core_host;
+    ex.mst_host = mst_host;
+    ex.linkage_host = linkage_host;
+    ex.records_dev = ct_records_dev;
+    ex.records_host = ct_records_host;
+    ex.records_rows_host = ct_rows_host;
+    return fit_impl(X_dev, n, d, min_samples, min_cluster_size, selection_method,
+                    max_cluster_size, allow_single_cluster, epsilon, persistence,
+                    sample_weights_dev, weighted_k, labels_dev, probs_dev, mst_dev, linkage_dev,
+                    ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, ct_rows_host,
+                    neighbors_dev, core_dev, selected_dev, n_selected_host, stream, ex);
 }

@@ -259,28 +259,40 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
     core = E(n, np.float32) if trees else None
     sel = E(n, np.int64)
     rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
-    V = _native.vptr
-    rc = _native.load().fhg_hdbscan_fit(
-        V(Xd), n, d, int(ms), int(min_cluster_size), method, float(max_cluster_size),
-        int(bool(allow_single_cluster)), float(cluster_selection_epsilon),
-        float(cluster_selection_persistence), V(d_w), wk, V(labels), V(probs), V(mst),
-        V(linkage), V(ctp),
-        V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
-        _native.stream_ptr())
-    if rc == _native.FHG_ERR_INVALID and "KeyError" in _native.load().fhg_last_error().decode():
-        raise KeyError(_native.load().fhg_last_error().decode())
+    V, H = _native.vptr, _native.hptr
+    lib = _native.load()
+
+    def pinned(t):
+        return torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+
+    if trees:
+        # the large outputs travel to host while the later stages run
+        h_nbrs, h_core, h_mst, h_link = pinned(nbrs), pinned(core), pinned(mst), pinned(linkage)
+        rec = h_rec = None
+        if condensed_records:
+            rec = torch.empty(2 * n * 28, dtype=torch.uint8, device="cuda")
+            h_rec = pinned(rec)
+        rc = lib.fhg_hdbscan_fit_export(
+            V(Xd), n, d, int(ms), int(min_cluster_size), method, float(max_cluster_size),
+            int(bool(allow_single_cluster)), float(cluster_selection_epsilon),
+            float(cluster_selection_persistence), V(d_w), wk, V(labels), V(probs), V(mst),
+            V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core),
+            V(sel), ctypes.byref(nsel), H(h_nbrs), H(h_core), H(h_mst), H(h_link), V(rec),
+            H(h_rec), _native.stream_ptr())
+    else:
+        rc = lib.fhg_hdbscan_fit(
+            V(Xd), n, d, int(ms), int(min_cluster_size), method, float(max_cluster_size),
+            int(bool(allow_single_cluster)), float(cluster_selection_epsilon),
+            float(cluster_selection_persistence), V(d_w), wk, V(labels), V(probs), None, None,
+            None, None, None, None, ctypes.byref(rows), None, None, V(sel), ctypes.byref(nsel),
+            _native.stream_ptr())
+    if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
+        raise KeyError(lib.fhg_last_error().decode())
     _native.check(rc)
     r, k = rows.value, nsel.value
     outs = [labels, probs, sel[:k]]
-    if trees:
-        outs += [mst, linkage, nbrs, core]
-        if condensed_records:
-            rec = torch.empty(max(r, 1) * 28, dtype=torch.uint8, device="cuda")
-            _native.check(_native.load().fhg_condensed_record_array(
-                V(ctp), V(ctc), V(ctl), V(cts), r, V(rec), _native.stream_ptr()))
-            outs += [rec[: r * 28]]
-        else:
-            outs += [ctp[:r], ctc[:r], ctl[:r], cts[:r]]
+    if trees and not condensed_records:
+        outs += [ctp[:r], ctc[:r], ctl[:r], cts[:r]]
     host = []
     for t in outs:
         h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
@@ -288,6 +300,10 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
         host.append(h)
     torch.cuda.current_stream().synchronize()
     host = [h.numpy() for h in host]
+    if trees:
+        host[3:3] = [h_mst.numpy(), h_link.numpy(), h_nbrs.numpy(), h_core.numpy()]
+        if condensed_records:
+            host.append(h_rec.numpy()[: r * 28])
     labels_h = host[0].astype(np.intp, copy=False)
     if not trees:
         return FitResult(labels_h, host[1], None, None, None, None, None, host[2])

@@ -242,6 +242,33 @@ int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_sample
                     float* core_dev, int64_t* selected_dev, int64_t* n_selected_host,
                     void* stream);
 
+/* fhg_hdbscan_fit, with the large outputs also copied to host memory while
+ * the fit runs: each non-NULL *_host destination receives its output from a
+ * side stream as soon as the fit has finished writing it (neighbours and
+ * core distances after the MST, the sorted MST and the linkage tree before
+ * the condensed tree is built, the condensed tree's record array before
+ * cluster selection), so that the transfers overlap the later stages.  Host
+ * destinations should be pinned for the copies to run asynchronously.  On
+ * return every copy is ordered before work queued later on `stream`;
+ * synchronise the stream before reading the host buffers.
+ *   ct_records_dev (room for 2n records of 28 bytes, 4-byte aligned) receives
+ *   the condensed tree as the record array HDBSCAN.fit stores (hdbscan.py:93,
+ *   fields parent i8, child i8, lambda_val f4, child_size f4, packed), as
+ *   fhg_condensed_record_array writes it; it needs the ct_* buffers.
+ * Each exported output needs its device buffer (FHG_ERR_INVALID otherwise). */
+int fhg_hdbscan_fit_export(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                           int64_t min_cluster_size, int32_t selection_method,
+                           double max_cluster_size, int allow_single_cluster, double epsilon,
+                           double persistence, const float* sample_weights_dev,
+                           int32_t weighted_k, int64_t* labels_dev, float* probs_dev,
+                           double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+                           int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+                           int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
+                           int64_t* selected_dev, int64_t* n_selected_host,
+                           int32_t* neighbors_host, float* core_host, double* mst_host,
+                           double* linkage_host, void* ct_records_dev, void* ct_records_host,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -222,3 +222,63 @@ def test_high_dimensional_fit_vs_oracle(engine, n, dim, ms, mcs):
     res = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs, return_trees=True)
     orc = O.fit(X, ms, mcs, mode=1, nthreads=16)
     _assert_fit_equal(res, orc)
+
+
+def test_fit_export_copies_match_device_outputs(engine):
+    """fhg_hdbscan_fit_export: the host copies it overlaps with the later stages
+    equal the device outputs of the same fit, byte for byte, whether the host
+    destinations are pinned or pageable; an exported output without its device
+    buffer is refused."""
+    import ctypes
+
+    import torch
+
+    from fast_hdbscan_gb300 import _native
+
+    X = synthetic.varying_density(50_000, seed=21)
+    n, d, ms, mcs = X.shape[0], X.shape[1], 7, 40
+    lib = _native.load()
+    V = _native.vptr
+    Xd = torch.from_numpy(X).cuda()
+
+    def dev(shape, dt):
+        return torch.empty(shape, dtype=dt, device="cuda")
+
+    for pinned in (True, False):
+        labels, probs = dev(n, torch.int64), dev(n, torch.float32)
+        mst, link = dev((n - 1, 3), torch.float64), dev((n - 1, 4), torch.float64)
+        ctp, ctc = dev(2 * n, torch.int64), dev(2 * n, torch.int64)
+        ctl, cts = dev(2 * n, torch.float32), dev(2 * n, torch.float32)
+        nbrs, core, sel = dev((n, ms), torch.int32), dev(n, torch.float32), dev(n, torch.int64)
+        rec = dev(2 * n * 28, torch.uint8)
+        hosts = [torch.empty(t.shape, dtype=t.dtype, pin_memory=pinned)
+                 for t in (nbrs, core, mst, link, rec)]
+        rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
+        _native.check(lib.fhg_hdbscan_fit_export(
+            V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, None, 0, V(labels), V(probs),
+            V(mst), V(link), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs),
+            V(core), V(sel), ctypes.byref(nsel), *[_native.hptr(h) for h in hosts[:4]], V(rec),
+            _native.hptr(hosts[4]), _native.stream_ptr()))
+        torch.cuda.current_stream().synchronize()
+        r = rows.value
+        for h, t in zip(hosts[:4], (nbrs, core, mst, link)):
+            assert torch.equal(h, t.cpu())
+        assert torch.equal(hosts[4][: r * 28], rec[: r * 28].cpu())
+        want = torch.empty(max(r, 1) * 28, dtype=torch.uint8, device="cuda")
+        _native.check(lib.fhg_condensed_record_array(V(ctp), V(ctc), V(ctl), V(cts), r,
+                                                      V(want), _native.stream_ptr()))
+        assert torch.equal(hosts[4][: r * 28], want[: r * 28].cpu())
+    # the same fit through fhg_hdbscan_fit
+    labels2, probs2 = dev(n, torch.int64), dev(n, torch.float32)
+    _native.check(lib.fhg_hdbscan_fit(
+        V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, None, 0, V(labels2), V(probs2),
+        None, None, None, None, None, None, ctypes.byref(rows), None, None, None,
+        ctypes.byref(nsel), _native.stream_ptr()))
+    assert torch.equal(labels, labels2) and torch.equal(probs, probs2)
+    h = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    rc = lib.fhg_hdbscan_fit_export(
+        V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, None, 0, V(labels), V(probs),
+        None, None, None, None, None, None, ctypes.byref(rows), None, None, None,
+        ctypes.byref(nsel), None, _native.hptr(h), None, None, None, None, _native.stream_ptr())
+    assert rc == _native.FHG_ERR_INVALID
+    assert "device buffer" in lib.fhg_last_error().decode()
