@@ -169,14 +169,19 @@ __global__ void cyc_init_kernel(int64_t n, const int32_t* __restrict__ target,
     nxt[p] = target[p] >= 0 ? target[p] : (int32_t)p;
     mx[p] = orig[p];
 }
+// `changed` (nullable) is set when some node's window maximum grew.  A step
+// that grows none has converged: every node's maximum is then at least the
+// next window's, and by induction the maximum over all it reaches.
 __global__ void cyc_step_kernel(int64_t n, const int32_t* __restrict__ nxt,
                                 const int32_t* __restrict__ mx, int32_t* __restrict__ nxt2,
-                                int32_t* __restrict__ mx2) {
+                                int32_t* __restrict__ mx2, int* __restrict__ changed) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     int32_t q = nxt[p];
     nxt2[p] = nxt[q];
-    mx2[p] = max(mx[p], mx[q]);
+    const int32_t a = mx[p], b = mx[q];
+    mx2[p] = max(a, b);
+    if (changed && b > a) *changed = 1;
 }
 __global__ void cyc_drop_kernel(int64_t n, const int32_t* __restrict__ nxt,
                                 const int32_t* __restrict__ mx, const int32_t* __restrict__ orig,
@@ -766,11 +771,21 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         FHG_TRY(ws.alloc(&nxt2, (size_t)n));
         FHG_TRY(ws.alloc(&mx2, (size_t)n));
         LAUNCH(cyc_init_kernel, n, n, target, ix.orig, nxt, mx);
+        // link chains are short: every fourth step reports whether it changed
+        // anything, and the doubling stops at the first that did not
         int R = bits_for(n) + 1;
         for (int r = 0; r < R; ++r) {
-            LAUNCH(cyc_step_kernel, n, n, nxt, mx, nxt2, mx2);
+            const bool check = (r & 3) == 3 && r + 1 < R;
+            if (check) FHG_CUDA(cudaMemsetAsync(iflag, 0, sizeof(int), s));
+            LAUNCH(cyc_step_kernel, n, n, nxt, mx, nxt2, mx2, check ? iflag : nullptr);
             int32_t* t1 = nxt; nxt = nxt2; nxt2 = t1;
             t1 = mx; mx = mx2; mx2 = t1;
+            if (check) {
+                int h_changed = 1;
+                FHG_CUDA(cudaMemcpyAsync(&h_changed, iflag, sizeof(int), cudaMemcpyDeviceToHost, s));
+                FHG_CUDA(cudaStreamSynchronize(s));
+                if (!h_changed) break;
+            }
         }
         LAUNCH(cyc_drop_kernel, n, n, nxt, mx, ix.orig, target);
     }

@@ -63,52 +63,90 @@ __global__ void cases_kernel(int64_t m, int64_t n, const int32_t* __restrict__ l
     birth[L] = birth[R] = (c == C6) ? 1 : 0;
 }
 
-// Pointer-doubling state of internal node i (node id n + i).
+// Pointer-doubling state of internal node i (node id n + i), one 32-byte
+// record so that the gather of an ancestor's state touches a single sector:
+//   anc  current ancestor (internal index; the root is its own ancestor)
+//   dep  edges from the node up to anc;  pre  preorder offset up to anc
+//   top  topmost non-continuing node on the path (-1: none yet)
+//   bth  nearest cluster birth on the path (-1: none yet)
+struct __align__(32) PjRec {
+    int32_t anc, dep, top, bth;
+    long long pre, pad;
+};
+__device__ __forceinline__ PjRec pj_load(const PjRec* __restrict__ R, int64_t i) {
+    const int4 a = __ldg(reinterpret_cast<const int4*>(R + i));
+    const longlong2 b = __ldg(reinterpret_cast<const longlong2*>(R + i) + 1);
+    PjRec r;
+    r.anc = a.x; r.dep = a.y; r.top = a.z; r.bth = a.w;
+    r.pre = b.x; r.pad = 0;
+    return r;
+}
+__device__ __forceinline__ void pj_store(PjRec* R, int64_t i, const PjRec& r) {
+    reinterpret_cast<int4*>(R + i)[0] = make_int4(r.anc, r.dep, r.top, r.bth);
+    reinterpret_cast<longlong2*>(R + i)[1] = make_longlong2(r.pre, 0);
+}
+
 __global__ void pj_init_kernel(int64_t m, int64_t n, const int32_t* __restrict__ par,
                                const int8_t* __restrict__ cont, const int8_t* __restrict__ birth,
                                const int8_t* __restrict__ side, const int32_t* __restrict__ left,
-                               const int32_t* __restrict__ size, int32_t* __restrict__ anc,
-                               int32_t* __restrict__ dep, int64_t* __restrict__ pre,
-                               int32_t* __restrict__ top, int32_t* __restrict__ bth) {
+                               const int32_t* __restrict__ size, PjRec* __restrict__ R) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int64_t v = n + i;
+    PjRec r;
     if (i == m - 1) {  // root
-        anc[i] = (int32_t)i;
-        dep[i] = 0;
-        pre[i] = 0;
-        top[i] = -1;
-        bth[i] = (int32_t)v;
-        return;
+        r.anc = (int32_t)i;
+        r.dep = 0;
+        r.pre = 0;
+        r.top = -1;
+        r.bth = (int32_t)v;
+    } else {
+        const int32_t p = par[v];
+        r.anc = p;
+        r.dep = 1;
+        r.pre = side[v] == 0 ? 1 : 2 * (long long)size[left[p]];
+        r.top = cont[v] ? -1 : (int32_t)v;
+        r.bth = birth[v] ? (int32_t)v : -1;
     }
-    const int32_t p = par[v];
-    anc[i] = p;
-    dep[i] = 1;
-    pre[i] = side[v] == 0 ? 1 : 2 * (int64_t)size[left[p]];
-    top[i] = cont[v] ? -1 : (int32_t)v;
-    bth[i] = birth[v] ? (int32_t)v : -1;
+    pj_store(R, i, r);
 }
 
-__global__ void pj_step_kernel(int64_t m, const int32_t* __restrict__ anc,
-                               const int32_t* __restrict__ dep, const int64_t* __restrict__ pre,
-                               const int32_t* __restrict__ top, const int32_t* __restrict__ bth,
-                               int32_t* __restrict__ anc2, int32_t* __restrict__ dep2,
-                               int64_t* __restrict__ pre2, int32_t* __restrict__ top2,
-                               int32_t* __restrict__ bth2) {
+// One doubling step.  A node's state covers the path from it up to (not
+// including) its ancestor; the root's own contribution is an identity for
+// dep, pre and top and a default for bth, so a state stops changing one step
+// after its ancestor has become the root.  `moving` (nullable) is set when
+// some node's ancestor was not yet the root: a step that leaves it clear has
+// finished every node.
+__global__ void pj_step_kernel(int64_t m, const PjRec* __restrict__ R, PjRec* __restrict__ R2,
+                               int* __restrict__ moving) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
-    const int32_t a = anc[i];
-    if (a == (int32_t)i) {  // already at the root: nothing left above
-        anc2[i] = a; dep2[i] = dep[i]; pre2[i] = pre[i]; top2[i] = top[i]; bth2[i] = bth[i];
+    const PjRec x = pj_load(R, i);
+    if (x.anc == (int32_t)i) {  // the root
+        pj_store(R2, i, x);
         return;
     }
-    anc2[i] = anc[a];
-    dep2[i] = dep[i] + dep[a];
-    pre2[i] = pre[i] + pre[a];
-    const int32_t ta = top[a];
-    top2[i] = ta != -1 ? ta : top[i];
-    const int32_t bi = bth[i];
-    bth2[i] = bi != -1 ? bi : bth[a];
+    if (moving && x.anc != (int32_t)(m - 1)) *moving = 1;
+    const PjRec y = pj_load(R, x.anc);
+    PjRec z;
+    z.anc = y.anc;
+    z.dep = x.dep + y.dep;
+    z.pre = x.pre + y.pre;
+    z.top = y.top != -1 ? y.top : x.top;
+    z.bth = x.bth != -1 ? x.bth : y.bth;
+    pj_store(R2, i, z);
+}
+
+__global__ void pj_split_kernel(int64_t m, const PjRec* __restrict__ R, int32_t* __restrict__ dep,
+                                int64_t* __restrict__ pre, int32_t* __restrict__ top,
+                                int32_t* __restrict__ bth) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const PjRec x = pj_load(R, i);
+    dep[i] = x.dep;
+    pre[i] = x.pre;
+    top[i] = x.top;
+    bth[i] = x.bth;
 }
 
 // Points: derive from the parent node; decide the emitting node and segment.
@@ -311,8 +349,8 @@ int condense_tree(Workspace& ws, const Linkage& lk, int64_t mcs, double max_cs, 
 
     int8_t *kase, *cont, *birth, *side, *emit_part;
     float* lam;
-    int32_t *par, *anc, *dep, *top, *bth, *anc2, *dep2, *top2, *bth2, *emit_u, *pdep;
-    int64_t *pre, *pre2, *ppre;
+    int32_t *par, *dep, *top, *bth, *emit_u, *pdep;
+    int64_t *pre, *ppre;
     FHG_TRY(ws.alloc(&kase, (size_t)m));
     FHG_TRY(ws.alloc(&lam, (size_t)m));
     FHG_TRY(ws.alloc(&par, (size_t)nodes));
@@ -323,35 +361,33 @@ int condense_tree(Workspace& ws, const Linkage& lk, int64_t mcs, double max_cs, 
            kase, lam,
            par, cont, birth, side);
 
-    FHG_TRY(ws.alloc(&anc, (size_t)m));
     FHG_TRY(ws.alloc(&dep, (size_t)m));
     FHG_TRY(ws.alloc(&pre, (size_t)m));
     FHG_TRY(ws.alloc(&top, (size_t)m));
     FHG_TRY(ws.alloc(&bth, (size_t)m));
     {
         Workspace tmp(s);
-        FHG_TRY(tmp.alloc(&anc2, (size_t)m));
-        FHG_TRY(tmp.alloc(&dep2, (size_t)m));
-        FHG_TRY(tmp.alloc(&pre2, (size_t)m));
-        FHG_TRY(tmp.alloc(&top2, (size_t)m));
-        FHG_TRY(tmp.alloc(&bth2, (size_t)m));
-        LAUNCH(pj_init_kernel, m, m, n, par, cont, birth, side, lk.left, lk.size, anc, dep, pre, top,
-               bth);
-        const int R = bits_for(m) + 1;
-        for (int r = 0; r < R; ++r) {
-            LAUNCH(pj_step_kernel, m, m, anc, dep, pre, top, bth, anc2, dep2, pre2, top2, bth2);
-            std::swap(anc, anc2); std::swap(dep, dep2); std::swap(pre, pre2);
-            std::swap(top, top2); std::swap(bth, bth2);
+        PjRec *R, *R2;
+        int* moving;
+        FHG_TRY(tmp.alloc(&R, (size_t)m));
+        FHG_TRY(tmp.alloc(&R2, (size_t)m));
+        FHG_TRY(tmp.alloc(&moving, 1));
+        LAUNCH(pj_init_kernel, m, m, n, par, cont, birth, side, lk.left, lk.size, R);
+        // log2(height) + 1 steps finish every node; the height is not known,
+        // so from step 12 on every fourth step reports whether it was the last
+        const int steps = bits_for(m) + 1;
+        for (int r = 0; r < steps; ++r) {
+            const bool check = r >= 11 && (r & 3) == 3 && r + 1 < steps;
+            if (check) FHG_CUDA(cudaMemsetAsync(moving, 0, sizeof(int), s));
+            LAUNCH(pj_step_kernel, m, m, R, R2, check ? moving : nullptr);
+            std::swap(R, R2);
+            if (check) {
+                int h_moving = 1;
+                FHG_TRY(read1(moving, &h_moving, s));
+                if (!h_moving) break;
+            }
         }
-        if (R & 1) {  // results live in the scratch buffers: copy back
-            FHG_CUDA(cudaMemcpyAsync(anc2, anc, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
-            FHG_CUDA(cudaMemcpyAsync(dep2, dep, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
-            FHG_CUDA(cudaMemcpyAsync(pre2, pre, sizeof(int64_t) * m, cudaMemcpyDeviceToDevice, s));
-            FHG_CUDA(cudaMemcpyAsync(top2, top, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
-            FHG_CUDA(cudaMemcpyAsync(bth2, bth, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
-            std::swap(anc, anc2); std::swap(dep, dep2); std::swap(pre, pre2);
-            std::swap(top, top2); std::swap(bth, bth2);
-        }
+        LAUNCH(pj_split_kernel, m, m, R, dep, pre, top, bth);
     }
 
     FHG_TRY(ws.alloc(&emit_u, (size_t)n));
