@@ -69,11 +69,20 @@ struct __align__(32) NodeRec {
     int32_t P, stamp, M, SUM, claim, SZ, pad0, pad1;
 };
 
-__device__ __forceinline__ int32_t rec_find(NodeRec* R, int32_t x) {
+// Union-find in which a parent is never younger than its child.  Age order:
+// cluster nodes (ids n + rank) by rank, then points by label (points are
+// renumbered by the rank of their first edge, so a smaller label is an older
+// point).  A union links the younger root under the older one, so the points
+// a cluster absorbs within an interval link under the cluster's node -- each
+// its own record, no contended update -- and paths stay short.
+__device__ __forceinline__ uint32_t age_key(int32_t x, int32_t n) {
+    return x >= n ? (uint32_t)(x - n) : (uint32_t)x + 0x80000000u;
+}
+__device__ __forceinline__ int32_t rec_find(NodeRec* R, int32_t x, int32_t n) {
     int32_t cur = R[x].P;
     if (cur != x) {
         int32_t prev = x, next;
-        while (cur > (next = R[cur].P)) {
+        while (age_key(cur, n) > age_key(next = R[cur].P, n)) {
             R[prev].P = next;
             prev = cur;
             cur = next;
@@ -82,16 +91,16 @@ __device__ __forceinline__ int32_t rec_find(NodeRec* R, int32_t x) {
     return cur;
 }
 
-__device__ __forceinline__ void rec_union(NodeRec* R, int32_t a, int32_t b) {
-    int32_t ra = rec_find(R, a), rb = rec_find(R, b);
+__device__ __forceinline__ void rec_union(NodeRec* R, int32_t a, int32_t b, int32_t n) {
+    int32_t ra = rec_find(R, a, n), rb = rec_find(R, b, n);
     while (ra != rb) {
-        if (ra < rb) {
+        if (age_key(ra, n) < age_key(rb, n)) {
             int32_t t = ra; ra = rb; rb = t;
         }
         int32_t old = atomicCAS(&R[ra].P, ra, rb);
         if (old == ra) return;
-        ra = rec_find(R, old);
-        rb = rec_find(R, rb);
+        ra = rec_find(R, old, n);
+        rb = rec_find(R, rb, n);
     }
 }
 
@@ -129,18 +138,20 @@ __global__ void lvl_init_kernel(int64_t m, int64_t s, int64_t half, const int32_
     *reinterpret_cast<int4*>(&R[a]) = make_int4(a, lev, -1, 0);
     *reinterpret_cast<int4*>(&R[b]) = make_int4(b, lev, -1, 0);
 }
-__global__ void lvl_union_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
-                                 const int32_t* __restrict__ B, NodeRec* R) {
+__global__ void lvl_union_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
+                                 const int32_t* __restrict__ A, const int32_t* __restrict__ B,
+                                 NodeRec* R) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
-    rec_union(R, A[i], B[i]);
+    rec_union(R, A[i], B[i], (int32_t)n);
 }
-__global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, const int32_t* __restrict__ A,
-                                  const int32_t* __restrict__ B, NodeRec* R, int lev) {
+__global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
+                                  const int32_t* __restrict__ A, const int32_t* __restrict__ B,
+                                  NodeRec* R, int lev) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
     const int32_t a = A[i], b = B[i];
-    const int32_t r = rec_find(R, a);
+    const int32_t r = rec_find(R, a, (int32_t)n);
     int32_t add = 0;
     if (atomicExch(&R[a].claim, lev) != lev) add += R[a].SZ;
     if (atomicExch(&R[b].claim, lev) != lev) add += R[b].SZ;
@@ -159,7 +170,7 @@ __global__ void lvl_size_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
                                 const int32_t* __restrict__ A, NodeRec* R) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
     if (i >= m) return;
-    const int32_t r = rec_find(R, A[i]);
+    const int32_t r = rec_find(R, A[i], (int32_t)n);
     if (R[r].M == (int32_t)i) R[n + i].SZ = R[r].SUM;
 }
 __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n, int32_t* A,
@@ -167,13 +178,14 @@ __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half) + half;
     if (i >= m) return;
     const int32_t a = A[i], b = B[i];
-    if (R[a].stamp == lev) A[i] = (int32_t)(n + R[rec_find(R, a)].M);
-    if (R[b].stamp == lev) B[i] = (int32_t)(n + R[rec_find(R, b)].M);
+    if (R[a].stamp == lev) A[i] = (int32_t)(n + R[rec_find(R, a, (int32_t)n)].M);
+    if (R[b].stamp == lev) B[i] = (int32_t)(n + R[rec_find(R, b, (int32_t)n)].M);
 }
-// Final levels: one block per interval of kLeafRanks consecutive ranks.  Every
-// endpoint label is already the root node at the interval's start, so the
-// block replays the reference's sequential union-find (cluster_trees.py:72-93)
-// over at most 2 * kLeafRanks distinct labels held in shared memory.
+// Final levels: one block per interval of L <= kLeafRanks consecutive ranks.
+// Every endpoint label is already the root node at the interval's start, so
+// the block replays the reference's sequential union-find
+// (cluster_trees.py:72-93) over at most 2 * L distinct labels held in shared
+// memory.
 constexpr int kLeafRanks = 512;
 constexpr int kLeafSlots = 4 * kLeafRanks;  // open-addressing table, load <= 1/2
 
@@ -186,13 +198,13 @@ __device__ __forceinline__ int32_t leaf_slot(int32_t* keys, int32_t label) {
     }
 }
 
-__global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n, int32_t* A,
-                                                            int32_t* B, NodeRec* R) {
+__global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n, int L,
+                                                            int32_t* A, int32_t* B, NodeRec* R) {
     __shared__ int32_t keys[kLeafSlots], par[kLeafSlots], node[kLeafSlots];
     __shared__ int32_t size[kLeafSlots];
     __shared__ int16_t sa[kLeafRanks], sb[kLeafRanks];
-    const int64_t a = (int64_t)blockIdx.x * kLeafRanks;
-    const int cnt = (int)(m - a < kLeafRanks ? m - a : kLeafRanks);
+    const int64_t a = (int64_t)blockIdx.x * L;
+    const int cnt = (int)(m - a < L ? m - a : L);
     for (int t = threadIdx.x; t < kLeafSlots; t += blockDim.x) keys[t] = -1;
     __syncthreads();
     for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
@@ -320,6 +332,33 @@ __global__ void sorted_mst_f64_kernel(int64_t m, const int32_t* __restrict__ ssr
         }                                                                   \
     } while (0)
 
+// The whole contraction over m > 0 sorted edges with endpoint labels A, B.
+// The leaf interval length L = ceil(m / 2^K) <= kLeafRanks makes the top
+// interval L * 2^K just cover m, so every level splits its intervals at their
+// middle: the lower halves hold about m / 2 ranks at every level.
+int contract_ranks(int64_t m, int64_t n, int32_t* A, int32_t* B, NodeRec* R, cudaStream_t s) {
+    int K = 0;
+    while (((m + (int64_t{1} << K) - 1) >> K) > kLeafRanks) ++K;
+    const int64_t L = (m + (int64_t{1} << K) - 1) >> K;
+    int lev = 0;
+    for (int64_t sz = L << K; sz >= 2 * L; sz /= 2, ++lev) {
+        const int64_t half = sz / 2;
+        const int64_t intervals = (m + sz - 1) / sz;
+        const int64_t lo_threads = intervals * half;
+        const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
+        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, R, lev);
+        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, n, A, B, R);
+        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, n, A, B, R, lev);
+        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, R);
+        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, R, lev);
+    }
+    const int64_t blocks = (m + L - 1) / L;
+    ::fhg::note_launch();
+    leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, (int)L, A, B, R);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
 }  // namespace
 
 int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* dst,
@@ -389,26 +428,7 @@ int sort_and_link(Workspace& ws, int64_t n, const int32_t* src, const int32_t* d
     }
 
     // ---- rank-halving contraction
-    int64_t S = 1;
-    while (S < m) S *= 2;
-    int lev = 0;
-    for (int64_t sz = S; sz >= 2 * kLeafRanks; sz /= 2, ++lev) {
-        const int64_t half = sz / 2;
-        const int64_t intervals = (m + sz - 1) / sz;
-        const int64_t lo_threads = intervals * half;
-        const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
-        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, R, lev);
-        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, R);
-        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, R, lev);
-        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, R);
-        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, R, lev);
-    }
-    {
-        const int64_t blocks = (m + kLeafRanks - 1) / kLeafRanks;
-        ::fhg::note_launch();
-        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, R);
-        FHG_CUDA(cudaGetLastError());
-    }
+    FHG_TRY(contract_ranks(m, n, A, B, R, s));
     FHG_TRY(ws.alloc(&out->left, (size_t)m));
     FHG_TRY(ws.alloc(&out->right, (size_t)m));
     LAUNCH(linkage_rows_kernel, m, m, n, A, B, inv, out->left, out->right);
@@ -567,26 +587,7 @@ int link_presorted_noalloc(const double* smst, int64_t m, double* out, cudaStrea
     LAUNCH(node_init_kernel, nodes, nodes, n, R);
     FHG_CUDA(cudaMemcpyAsync(A, src, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
     FHG_CUDA(cudaMemcpyAsync(B, dst, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
-    int64_t S = 1;
-    while (S < m) S *= 2;
-    int lev = 0;
-    for (int64_t sz = S; sz >= 2 * kLeafRanks; sz /= 2, ++lev) {
-        const int64_t half = sz / 2;
-        const int64_t intervals = (m + sz - 1) / sz;
-        const int64_t lo_threads = intervals * half;
-        const int64_t hi_threads = m > half ? ((m - half + sz - 1) / sz) * half : 0;
-        LAUNCH(lvl_init_kernel, lo_threads, m, sz, half, A, B, R, lev);
-        LAUNCH(lvl_union_kernel, lo_threads, m, sz, half, A, B, R);
-        LAUNCH(lvl_reduce_kernel, lo_threads, m, sz, half, A, B, R, lev);
-        LAUNCH(lvl_size_kernel, lo_threads, m, sz, half, n, A, R);
-        LAUNCH(lvl_relabel_kernel, hi_threads, m, sz, half, n, A, B, R, lev);
-    }
-    {
-        const int64_t blocks = (m + kLeafRanks - 1) / kLeafRanks;
-        ::fhg::note_launch();
-        leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, A, B, R);
-        FHG_CUDA(cudaGetLastError());
-    }
+    FHG_TRY(contract_ranks(m, n, A, B, R, s));
     LAUNCH(linkage_rows_kernel, m, m, n, A, B, (const int32_t*)nullptr, left, right);
     LAUNCH(node_sizes_kernel, nodes, nodes, R, size);
     LAUNCH(linkage_f64_kernel, m, m, left, right, w, size, (const float*)nullptr, n, out);
