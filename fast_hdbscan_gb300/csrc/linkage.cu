@@ -91,6 +91,24 @@ __device__ __forceinline__ int32_t rec_find(NodeRec* R, int32_t x, int32_t n) {
     return cur;
 }
 
+// Root of x without path compression, for the passes after the unions: a
+// large cluster's label is looked up by long runs of ranks, and compressing
+// writes from all of them would queue on one record.
+__device__ __forceinline__ int32_t rec_root(const NodeRec* R, int32_t x) {
+    int32_t cur = x, next;
+    while ((next = R[cur].P) != cur) cur = next;
+    return cur;
+}
+// rec_root of every lane's label, looked up once per distinct label in the
+// warp (the lanes in `act` call it together).
+__device__ __forceinline__ int32_t warp_root(const NodeRec* R, int32_t x, unsigned act) {
+    const unsigned peers = __match_any_sync(act, x);
+    const int lead = __ffs(peers) - 1;
+    int32_t r = 0;
+    if ((int)(threadIdx.x & 31) == lead) r = rec_root(R, x);
+    return __shfl_sync(act, r, lead);
+}
+
 __device__ __forceinline__ void rec_union(NodeRec* R, int32_t a, int32_t b, int32_t n) {
     int32_t ra = rec_find(R, a, n), rb = rec_find(R, b, n);
     while (ra != rb) {
@@ -145,23 +163,78 @@ __global__ void lvl_union_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
     if (i >= m) return;
     rec_union(R, A[i], B[i], (int32_t)n);
 }
-__global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
-                                  const int32_t* __restrict__ A, const int32_t* __restrict__ B,
-                                  NodeRec* R, int lev) {
+constexpr int kReduceThreads = 256;
+__global__ void __launch_bounds__(kReduceThreads) lvl_reduce_kernel(
+    int64_t m, int64_t s, int64_t half, int64_t n, const int32_t* __restrict__ A,
+    const int32_t* __restrict__ B, NodeRec* R, int lev) {
+    __shared__ int32_t s_root[kReduceThreads / 32], s_mx[kReduceThreads / 32];
+    __shared__ int32_t s_sum[kReduceThreads / 32];
+    __shared__ int s_uniform;
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
-    if (i >= m) return;
-    const int32_t a = A[i], b = B[i];
-    const int32_t r = rec_find(R, a, (int32_t)n);
-    int32_t add = 0;
-    if (atomicExch(&R[a].claim, lev) != lev) add += R[a].SZ;
-    if (atomicExch(&R[b].claim, lev) != lev) add += R[b].SZ;
+    const bool valid = i < m;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned act = __ballot_sync(kFull, valid);
+    int32_t r = -1, add = 0;
+    if (valid) {
+        // A label claims its size for its component once.  A large cluster's
+        // label is an endpoint of long runs of ranks: one lane per label per
+        // warp, and only while unclaimed, goes to the atomic.
+        const int32_t a = A[i], b = B[i];
+        const unsigned pa = __match_any_sync(act, a), pb = __match_any_sync(act, b);
+        r = warp_root(R, a, act);
+        if (lane == __ffs(pa) - 1 && R[a].claim != lev && atomicExch(&R[a].claim, lev) != lev)
+            add += R[a].SZ;
+        if (lane == __ffs(pb) - 1 && R[b].claim != lev && atomicExch(&R[b].claim, lev) != lev)
+            add += R[b].SZ;
+    }
     // Consecutive ranks mostly share a root (a large component absorbs long
-    // runs of edges): combine the lanes of each root first, then one atomic
-    // per root per warp instead of one per rank.
-    const unsigned peers = __match_any_sync(__activemask(), r);
-    const int32_t mx = __reduce_max_sync(peers, (int32_t)i);
-    const int32_t sum = (int32_t)__reduce_add_sync(peers, (unsigned)add);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) {
+    // runs of edges): combine the lanes of each root first, then the warps of
+    // the block when they all share one root, so that a large component takes
+    // one atomic per block rather than one per rank.
+    unsigned peers = 0;
+    int32_t mx = -1, sum = 0;
+    if (valid) {
+        peers = __match_any_sync(act, r);
+        mx = __reduce_max_sync(peers, (int32_t)i);
+        sum = (int32_t)__reduce_add_sync(peers, (unsigned)add);
+    }
+    const bool wuni = __all_sync(kFull, !valid || peers == act);
+    {
+        const int lead = act ? __ffs(act) - 1 : 0;
+        const int32_t rl = __shfl_sync(kFull, r, lead);
+        const int32_t ml = __shfl_sync(kFull, mx, lead);
+        const int32_t sl = __shfl_sync(kFull, sum, lead);
+        if (lane == 0) {
+            // -1: no edge in the warp; -3: several roots; else the warp's root
+            s_root[warp] = act == 0 ? -1 : (wuni ? rl : -3);
+            s_mx[warp] = ml;
+            s_sum[warp] = sl;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t root = -1, bm = -1, bs = 0;
+        int uni = 1;
+        for (int w = 0; w < kReduceThreads / 32; ++w) {
+            const int32_t x = s_root[w];
+            if (x == -1) continue;
+            if (x == -3 || (root >= 0 && x != root)) {
+                uni = 0;
+                break;
+            }
+            root = x;
+            bm = max(bm, s_mx[w]);
+            bs += s_sum[w];
+        }
+        if (uni && root >= 0) {
+            atomicMax(&R[root].M, bm);
+            if (bs) atomicAdd(&R[root].SUM, bs);
+        }
+        s_uniform = uni;
+    }
+    __syncthreads();
+    if (s_uniform || !valid) return;
+    if (lane == __ffs(peers) - 1) {
         atomicMax(&R[r].M, mx);
         if (sum) atomicAdd(&R[r].SUM, sum);
     }
@@ -169,8 +242,9 @@ __global__ void lvl_reduce_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
 __global__ void lvl_size_kernel(int64_t m, int64_t s, int64_t half, int64_t n,
                                 const int32_t* __restrict__ A, NodeRec* R) {
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half);
+    const unsigned act = __ballot_sync(kFull, i < m);
     if (i >= m) return;
-    const int32_t r = rec_find(R, A[i], (int32_t)n);
+    const int32_t r = warp_root(R, A[i], act);
     if (R[r].M == (int32_t)i) R[n + i].SZ = R[r].SUM;
 }
 __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n, int32_t* A,
@@ -178,8 +252,8 @@ __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n
     const int64_t i = low_rank((int64_t)blockIdx.x * blockDim.x + threadIdx.x, s, half) + half;
     if (i >= m) return;
     const int32_t a = A[i], b = B[i];
-    if (R[a].stamp == lev) A[i] = (int32_t)(n + R[rec_find(R, a, (int32_t)n)].M);
-    if (R[b].stamp == lev) B[i] = (int32_t)(n + R[rec_find(R, b, (int32_t)n)].M);
+    if (R[a].stamp == lev) A[i] = (int32_t)(n + R[rec_root(R, a)].M);
+    if (R[b].stamp == lev) B[i] = (int32_t)(n + R[rec_root(R, b)].M);
 }
 // Final levels: one block per interval of L <= kLeafRanks consecutive ranks.
 // Every endpoint label is already the root node at the interval's start, so
