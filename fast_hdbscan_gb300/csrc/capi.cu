@@ -677,8 +677,11 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
     int32_t* sel;
     FHG_TRY(ws.alloc(&sel, (size_t)(ct.n_clusters > 0 ? ct.n_clusters : 1)));
     int64_t k = 0;
-    if (selection_method == 0) FHG_TRY(select_eom(ws, ct, max_cluster_size, allow_single_cluster != 0, sel, &k));
-    else FHG_TRY(select_leaf(ws, ct, sel, &k));
+    LabelPre lpre;  // labelling work that overlaps the stabilities
+    if (selection_method == 0)
+        FHG_TRY(select_eom(ws, ct, max_cluster_size, allow_single_cluster != 0, sel, &k, &lpre));
+    else
+        FHG_TRY(select_leaf(ws, ct, sel, &k, &lpre));
     if (k > 1 && epsilon > 0.0) {  // hdbscan.py:555
         int32_t* searched;
         FHG_TRY(ws.alloc(&searched, (size_t)k));
@@ -699,7 +702,7 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
         FHG_CUDA(cudaGetLastError());
         return FHG_OK;
     }
-    return label_points(ws, ct, sel, k, epsilon, labels_dev, probs_dev);
+    return label_points(ws, ct, sel, k, epsilon, labels_dev, probs_dev, &lpre);
 }
 
 }  // namespace

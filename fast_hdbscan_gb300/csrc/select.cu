@@ -53,18 +53,26 @@ __global__ void products_kernel(int64_t rows, const int32_t* __restrict__ order,
 }
 // One thread per cluster: the float32 sum of its rows' products, strictly in
 // row order (a float32 sum is not associative, so the order is the result).
+// Clusters of kBigRows rows or more are summed by score_big_kernel.
+constexpr int32_t kBigRows = 8192;
+__device__ __forceinline__ float score_start(int64_t c, const int32_t* __restrict__ row_of_cluster,
+                                             const float* __restrict__ lam,
+                                             const float* __restrict__ csize) {
+    float s = 0.0f;
+    if (c > 0) {
+        int32_t r = row_of_cluster[c];
+        if (r >= 0 && csize[r] > 1.0f) s = __fmul_rn(-lam[r], csize[r]);
+    }
+    return s;
+}
 __global__ void score_kernel(int64_t C, const int64_t* __restrict__ start,
                              const int32_t* __restrict__ cnt, const float* __restrict__ prod,
                              const int32_t* __restrict__ row_of_cluster,
                              const float* __restrict__ lam, const float* __restrict__ csize,
                              float* __restrict__ score) {
     int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C) return;
-    float s = 0.0f;
-    if (c > 0) {
-        int32_t r = row_of_cluster[c];
-        if (r >= 0 && csize[r] > 1.0f) s = __fmul_rn(-lam[r], csize[r]);
-    }
+    if (c >= C || cnt[c] >= kBigRows) return;
+    float s = score_start(c, row_of_cluster, lam, csize);
     const int64_t b = start[c], e = b + cnt[c];
     int64_t j = b;
     for (; j + 8 <= e; j += 8) {
@@ -76,6 +84,51 @@ __global__ void score_kernel(int64_t C, const int64_t* __restrict__ start,
     }
     for (; j < e; ++j) s = __fadd_rn(s, __ldg(prod + j));
     score[c] = s;
+}
+// One block per cluster of kBigRows rows or more: the same sequential sum by
+// one thread, fed from shared memory -- the other warps stage the next chunk
+// of products while the current one is summed, so that the chain of
+// dependent additions never waits for memory.
+constexpr int kScoreThreads = 256;
+constexpr int kScoreChunk = 4096;
+__global__ void __launch_bounds__(kScoreThreads) score_big_kernel(
+    int64_t C, const int64_t* __restrict__ start, const int32_t* __restrict__ cnt,
+    const float* __restrict__ prod, const int32_t* __restrict__ row_of_cluster,
+    const float* __restrict__ lam, const float* __restrict__ csize, float* __restrict__ score) {
+    __shared__ float buf[2][kScoreChunk];
+    for (int64_t c = blockIdx.x; c < C; c += gridDim.x) {
+        if (cnt[c] < kBigRows) continue;  // uniform over the block
+        const int64_t b = start[c], len = cnt[c];
+        const int64_t chunks = (len + kScoreChunk - 1) / kScoreChunk;
+        for (int64_t j = threadIdx.x; j < kScoreChunk && j < len; j += blockDim.x)
+            buf[0][j] = __ldg(prod + b + j);
+        __syncthreads();
+        float s = threadIdx.x == 0 ? score_start(c, row_of_cluster, lam, csize) : 0.0f;
+        for (int64_t k = 0; k < chunks; ++k) {
+            const int cur = (int)(k & 1);
+            const int64_t base = k * kScoreChunk;
+            const int cl = (int)(len - base < kScoreChunk ? len - base : kScoreChunk);
+            if (threadIdx.x >= 32) {  // warps 1.. stage chunk k + 1
+                const int64_t nb = base + kScoreChunk;
+                for (int64_t j = threadIdx.x - 32; j < kScoreChunk && nb + j < len;
+                     j += blockDim.x - 32)
+                    buf[cur ^ 1][j] = __ldg(prod + b + nb + j);
+            } else if (threadIdx.x == 0) {
+                const float* v = buf[cur];
+                int t = 0;
+                for (; t + 8 <= cl; t += 8) {
+                    float x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) x[u] = v[t + u];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) s = __fadd_rn(s, x[u]);
+                }
+                for (; t < cl; ++t) s = __fadd_rn(s, v[t]);
+            }
+            __syncthreads();  // chunk k summed, chunk k + 1 staged
+        }
+        if (threadIdx.x == 0) score[c] = s;
+    }
 }
 
 // Cluster rows (child_size > 1) of every parent, kept in row order.
@@ -404,13 +457,35 @@ __global__ void fill_i32_kernel(int32_t* a, int64_t n, int32_t v) {
     } while (0)
 
 // Shared preparation: rows grouped by parent, scores, cluster tree.
+//
+// The scores are one sequential float32 sum per cluster, so a large cluster's
+// sum is a long chain of dependent additions on a single thread.  They are
+// computed on a side stream while the stream goes on with the work that does
+// not read them; join() (also run by the destructor) orders the stream after
+// them.  Every buffer the side stream touches belongs to the caller's
+// Workspace, which outlives the join.
 struct Prepared {
     int64_t C = 0;
     int32_t *order = nullptr, *cnt = nullptr, *row_of_cluster = nullptr, *cpar = nullptr;
     int32_t *corder = nullptr, *ccnt = nullptr;
     int64_t *start = nullptr, *cstart = nullptr;
-    float *score = nullptr, *nsize = nullptr;
+    float *score = nullptr, *nsize = nullptr, *prod = nullptr;
     int8_t* in_tree = nullptr;
+    cudaStream_t main = nullptr, side = nullptr;
+    cudaEvent_t done = nullptr;
+
+    Prepared() = default;
+    Prepared(const Prepared&) = delete;
+    Prepared& operator=(const Prepared&) = delete;
+    ~Prepared() { join(); }
+    void join() {
+        if (!side) return;
+        cudaStreamWaitEvent(main, done, 0);
+        cudaEventDestroy(done);
+        cudaStreamDestroy(side);  // released once its work has completed
+        side = nullptr;
+        done = nullptr;
+    }
 };
 
 int prepare(Workspace& ws, const Condensed& ct, Prepared* P) {
@@ -441,13 +516,42 @@ int prepare(Workspace& ws, const Condensed& ct, Prepared* P) {
         LAUNCH(widen_kernel, C, C, P->cnt, cnt64);
         FHG_TRY(scan_exclusive_i64(tmp, cnt64, P->start, C, nullptr));
     }
+    FHG_TRY(ws.alloc(&P->prod, (size_t)rows));
+    LAUNCH(products_kernel, rows, rows, P->order, ct.lambda, ct.csize, P->prod);
     {
-        Workspace tmp(s);
-        float* prod;
-        FHG_TRY(tmp.alloc(&prod, (size_t)rows));
-        LAUNCH(products_kernel, rows, rows, P->order, ct.lambda, ct.csize, prod);
-        LAUNCH(score_kernel, C, C, P->start, P->cnt, prod, P->row_of_cluster, ct.lambda,
-               ct.csize, P->score);
+        // the scores on a side stream (on the stream itself if none can be made)
+        cudaStream_t ss = s;
+        cudaEvent_t fork = nullptr;
+        if (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) == cudaSuccess) {
+            if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventRecord(fork, s) == cudaSuccess &&
+                cudaStreamWaitEvent(P->side, fork, 0) == cudaSuccess) {
+                ss = P->side;
+                P->main = s;
+            } else {
+                if (P->done) cudaEventDestroy(P->done);
+                P->done = nullptr;
+                cudaStreamDestroy(P->side);
+                P->side = nullptr;
+            }
+            if (fork) cudaEventDestroy(fork);
+        } else {
+            P->side = nullptr;
+            cudaGetLastError();
+        }
+        if (C > 0) {
+            ::fhg::note_launch();
+            score_big_kernel<<<(unsigned)(C < 1024 ? C : 1024), kScoreThreads, 0, ss>>>(
+                C, P->start, P->cnt, P->prod, P->row_of_cluster, ct.lambda, ct.csize, P->score);
+            FHG_CUDA(cudaGetLastError());
+            ::fhg::note_launch();
+            score_kernel<<<grid_for(C, 256), 256, 0, ss>>>(C, P->start, P->cnt, P->prod,
+                                                           P->row_of_cluster, ct.lambda,
+                                                           ct.csize, P->score);
+            FHG_CUDA(cudaGetLastError());
+        }
+        if (P->side) FHG_CUDA(cudaEventRecord(P->done, P->side));
     }
     FHG_TRY(ws.alloc(&P->corder, (size_t)rows));
     FHG_TRY(ws.alloc(&P->cstart, (size_t)C));
@@ -511,13 +615,15 @@ int condensed_from_arrays(Workspace& ws, const int64_t* parent, const int64_t* c
 }
 
 int select_eom(Workspace& ws, const Condensed& ct, double max_cs, bool allow_single, int32_t* sel,
-               int64_t* n_sel) {
+               int64_t* n_sel, LabelPre* pre) {
     cudaStream_t s = ws.stream();
     *n_sel = 0;
     if (ct.rows == 0) return FHG_OK;
     Stage stage(s, "select");
     Prepared P;
     FHG_TRY(prepare(ws, ct, &P));
+    if (pre) FHG_TRY(label_prework(ws, ct, pre));
+    P.join();
     const int64_t C = P.C;
     int32_t *depth, *depth2, *jmp, *jmp2, *dcount, *byd, *flags;
     double* ret;
@@ -545,12 +651,15 @@ int select_eom(Workspace& ws, const Condensed& ct, double max_cs, bool allow_sin
     return FHG_OK;
 }
 
-int select_leaf(Workspace& ws, const Condensed& ct, int32_t* sel, int64_t* n_sel) {
+int select_leaf(Workspace& ws, const Condensed& ct, int32_t* sel, int64_t* n_sel,
+                LabelPre* pre) {
     cudaStream_t s = ws.stream();
     *n_sel = 0;
     if (ct.rows == 0) return FHG_OK;
     Prepared P;
     FHG_TRY(prepare(ws, ct, &P));
+    if (pre) FHG_TRY(label_prework(ws, ct, pre));
+    P.join();
     int32_t* flags;
     int64_t* nsel_dev;
     FHG_TRY(ws.alloc(&flags, (size_t)P.C));
@@ -563,8 +672,33 @@ int select_leaf(Workspace& ws, const Condensed& ct, int32_t* sel, int64_t* n_sel
     return FHG_OK;
 }
 
+int label_prework(Workspace& ws, const Condensed& ct, LabelPre* pre) {
+    cudaStream_t s = ws.stream();
+    const int64_t n = ct.n, rows = ct.rows, C = ct.n_clusters;
+    *pre = LabelPre();
+    if (rows == 0) return FHG_OK;
+    FHG_TRY(ws.alloc(&pre->row_of_point, (size_t)n));
+    FHG_TRY(ws.alloc(&pre->row_of_cluster, (size_t)C));
+    FHG_TRY(ws.alloc(&pre->cpar, (size_t)C));
+    FHG_TRY(ws.alloc(&pre->nsize, (size_t)C));
+    FHG_TRY(ws.alloc(&pre->in_tree, (size_t)C));
+    FHG_TRY(ws.alloc(&pre->root_max, 1));
+    FHG_TRY(ws.alloc(&pre->death, (size_t)C));
+    FHG_CUDA(cudaMemsetAsync(pre->root_max, 0, sizeof(unsigned int), s));
+    FHG_CUDA(cudaMemsetAsync(pre->death, 0, sizeof(unsigned int) * C, s));
+    LAUNCH(fill_i32_kernel, n, pre->row_of_point, n, -1);
+    LAUNCH(fill_i32_kernel, C, pre->row_of_cluster, C, -1);
+    LAUNCH(row_of_child_kernel, rows, rows, n, ct.child, pre->row_of_cluster, pre->row_of_point);
+    LAUNCH(cluster_info_kernel, C, C, n, pre->row_of_cluster, ct.parent, ct.csize, pre->cpar,
+           pre->nsize, pre->in_tree);
+    LAUNCH(root_stats_kernel, rows, rows, n, ct.parent, ct.lambda, ct.csize, pre->root_max,
+           pre->death);
+    pre->ready = true;
+    return FHG_OK;
+}
+
 int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t n_sel,
-                 double eps, int64_t* labels, float* probs) {
+                 double eps, int64_t* labels, float* probs, const LabelPre* pre_in) {
     cudaStream_t s = ws.stream();
     const int64_t n = ct.n, rows = ct.rows, C = ct.n_clusters;
     Stage stage(s, "labels");
@@ -573,40 +707,34 @@ int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t
         LAUNCH(fill_i64_kernel, n, labels, n, (int64_t)-1);
         return FHG_OK;
     }
+    LabelPre own;
+    const LabelPre* pre = pre_in;
+    if (!pre || !pre->ready) {
+        FHG_TRY(label_prework(ws, ct, &own));
+        pre = &own;
+    }
+    const int32_t* row_of_point = pre->row_of_point;
+    const int32_t* cpar = pre->cpar;
+    unsigned int* root_max = pre->root_max;
+    unsigned int* death = pre->death;
     int8_t* is_sel;
-    int32_t *label_of, *by_label, *row_of_point, *row_of_cluster, *cpar, *jmp, *sa, *jmp2, *sa2;
-    float* nsize;
-    int8_t* in_tree;
+    int32_t *label_of, *by_label, *jmp, *sa, *jmp2, *sa2;
     uint32_t* key;
     int32_t* val;
-    unsigned int *root_max, *death;
     int* err;
     FHG_TRY(ws.alloc(&is_sel, (size_t)C));
     FHG_TRY(ws.alloc(&label_of, (size_t)C));
     FHG_TRY(ws.alloc(&by_label, (size_t)n_sel));
-    FHG_TRY(ws.alloc(&row_of_point, (size_t)n));
-    FHG_TRY(ws.alloc(&row_of_cluster, (size_t)C));
-    FHG_TRY(ws.alloc(&cpar, (size_t)C));
-    FHG_TRY(ws.alloc(&nsize, (size_t)C));
-    FHG_TRY(ws.alloc(&in_tree, (size_t)C));
     FHG_TRY(ws.alloc(&jmp, (size_t)C));
     FHG_TRY(ws.alloc(&sa, (size_t)C));
     FHG_TRY(ws.alloc(&jmp2, (size_t)C));
     FHG_TRY(ws.alloc(&sa2, (size_t)C));
     FHG_TRY(ws.alloc(&key, (size_t)n_sel));
     FHG_TRY(ws.alloc(&val, (size_t)n_sel));
-    FHG_TRY(ws.alloc(&root_max, 1));
-    FHG_TRY(ws.alloc(&death, (size_t)C));
     FHG_TRY(ws.alloc(&err, 1));
     FHG_CUDA(cudaMemsetAsync(is_sel, 0, C, s));
-    FHG_CUDA(cudaMemsetAsync(root_max, 0, sizeof(unsigned int), s));
-    FHG_CUDA(cudaMemsetAsync(death, 0, sizeof(unsigned int) * C, s));
     FHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
     LAUNCH(fill_i32_kernel, C, label_of, C, -1);
-    LAUNCH(fill_i32_kernel, n, row_of_point, n, -1);
-    LAUNCH(fill_i32_kernel, C, row_of_cluster, C, -1);
-    LAUNCH(row_of_child_kernel, rows, rows, n, ct.child, row_of_cluster, row_of_point);
-    LAUNCH(cluster_info_kernel, C, C, n, row_of_cluster, ct.parent, ct.csize, cpar, nsize, in_tree);
     LAUNCH(sel_flags_kernel, n_sel, n_sel, n, C, sel, is_sel, key, val);
     {
         Workspace tmp(s);
@@ -619,7 +747,6 @@ int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t
         std::swap(jmp, jmp2);
         std::swap(sa, sa2);
     }
-    LAUNCH(root_stats_kernel, rows, rows, n, ct.parent, ct.lambda, ct.csize, root_max, death);
     // distinct selected count
     int64_t n_distinct = 0;
     {

@@ -47,16 +47,32 @@ int condense_tree(Workspace& ws, const Linkage& lk, int64_t min_cluster_size,
 int condensed_from_arrays(Workspace& ws, const int64_t* parent, const int64_t* child,
                           const float* lambda, const float* csize, int64_t rows, Condensed* out);
 
+// The selection-independent part of label_points (row of every point and
+// cluster, cluster parents, the root's and every cluster's largest point
+// lambda), buffers owned by the Workspace it was computed in.
+struct LabelPre {
+    bool ready = false;
+    int32_t *row_of_point = nullptr, *row_of_cluster = nullptr, *cpar = nullptr;
+    float* nsize = nullptr;
+    int8_t* in_tree = nullptr;
+    unsigned int *root_max = nullptr, *death = nullptr;
+};
+int label_prework(Workspace& ws, const Condensed& ct, LabelPre* pre);
+
 // Cluster selection.  `sel` receives selected labels in the reference's
-// order; *n_sel its count (host).
+// order; *n_sel its count (host).  With `pre`, label_prework runs on the
+// stream while the cluster stabilities (a sequential float32 sum per
+// cluster) are computed beside it.
 int select_eom(Workspace& ws, const Condensed& ct, double max_cluster_size, bool allow_single,
-               int32_t* sel, int64_t* n_sel);
-int select_leaf(Workspace& ws, const Condensed& ct, int32_t* sel, int64_t* n_sel);
+               int32_t* sel, int64_t* n_sel, LabelPre* pre = nullptr);
+int select_leaf(Workspace& ws, const Condensed& ct, int32_t* sel, int64_t* n_sel,
+                LabelPre* pre = nullptr);
 
 // Labels and membership strengths (cluster_trees.py:944, :1011).  Returns
-// FHG_ERR_INVALID where the reference raises a KeyError.
+// FHG_ERR_INVALID where the reference raises a KeyError.  `pre`: the
+// label_prework of the same tree, or NULL.
 int label_points(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t n_sel,
-                 double epsilon, int64_t* labels, float* probs);
+                 double epsilon, int64_t* labels, float* probs, const LabelPre* pre = nullptr);
 // Membership strengths for given labels (cluster_trees.py:1011).
 int membership_strengths(Workspace& ws, const Condensed& ct, const int32_t* sel, int64_t n_sel,
                          const int64_t* labels, float* probs);
