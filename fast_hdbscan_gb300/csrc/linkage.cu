@@ -261,36 +261,45 @@ __global__ void lvl_relabel_kernel(int64_t m, int64_t s, int64_t half, int64_t n
 // (cluster_trees.py:72-93) over at most 2 * L distinct labels held in shared
 // memory.
 constexpr int kLeafRanks = 512;
-constexpr int kLeafSlots = 4 * kLeafRanks;  // open-addressing table, load <= 1/2
+constexpr int kLeafThreads = 128;
 
+// Open-addressing table of the interval's labels (SLOTS a power of two, at
+// least the 2L labels an interval can hold).
+template <int SLOTS>
 __device__ __forceinline__ int32_t leaf_slot(int32_t* keys, int32_t label) {
-    uint32_t h = ((uint32_t)label * 2654435761u) >> 21;  // 11 bits: 2048 slots
+    constexpr int kBits = SLOTS == 1024 ? 10 : 11;
+    uint32_t h = ((uint32_t)label * 2654435761u) >> (32 - kBits);
     for (;;) {
         int32_t prev = atomicCAS(&keys[h], -1, label);
         if (prev == -1 || prev == label) return (int32_t)h;
-        h = (h + 1) & (kLeafSlots - 1);
+        h = (h + 1) & (SLOTS - 1);
     }
 }
 
-__global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n, int L,
-                                                            int32_t* A, int32_t* B, NodeRec* R) {
-    __shared__ int32_t keys[kLeafSlots], par[kLeafSlots], node[kLeafSlots];
-    __shared__ int32_t size[kLeafSlots];
+// Small tables (L <= 384: 1024 slots, 16 KB) let 14 intervals share an SM,
+// each replayed by one thread.
+template <int SLOTS>
+__global__ void __launch_bounds__(kLeafThreads) leaf_interval_kernel(int64_t m, int64_t n, int L,
+                                                                     int32_t* A, int32_t* B,
+                                                                     NodeRec* R) {
+    static_assert(SLOTS == 1024 || SLOTS == 2048, "table size");
+    __shared__ int32_t keys[SLOTS], node[SLOTS], size[SLOTS];
+    __shared__ int16_t par[SLOTS];
     __shared__ int16_t sa[kLeafRanks], sb[kLeafRanks];
     const int64_t a = (int64_t)blockIdx.x * L;
     const int cnt = (int)(m - a < L ? m - a : L);
-    for (int t = threadIdx.x; t < kLeafSlots; t += blockDim.x) keys[t] = -1;
+    for (int t = threadIdx.x; t < SLOTS; t += blockDim.x) keys[t] = -1;
     __syncthreads();
     for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
         int32_t la = A[a + t], lb = B[a + t];
-        int32_t ha = leaf_slot(keys, la), hb = leaf_slot(keys, lb);
+        int32_t ha = leaf_slot<SLOTS>(keys, la), hb = leaf_slot<SLOTS>(keys, lb);
         sa[t] = (int16_t)ha;
         sb[t] = (int16_t)hb;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < kLeafSlots; t += blockDim.x) {
+    for (int t = threadIdx.x; t < SLOTS; t += blockDim.x) {
         int32_t k = keys[t];
-        par[t] = t;
+        par[t] = (int16_t)t;
         node[t] = k;
         size[t] = k >= 0 ? R[k].SZ : 0;
     }
@@ -305,7 +314,7 @@ __global__ void __launch_bounds__(256) leaf_interval_kernel(int64_t m, int64_t n
             B[i] = node[y];
             const int32_t sz = size[x] + size[y];
             R[n + i].SZ = sz;
-            par[y] = x;
+            par[y] = (int16_t)x;
             node[x] = (int32_t)(n + i);
             size[x] = sz;
         }
@@ -428,7 +437,10 @@ int contract_ranks(int64_t m, int64_t n, int32_t* A, int32_t* B, NodeRec* R, cud
     }
     const int64_t blocks = (m + L - 1) / L;
     ::fhg::note_launch();
-    leaf_interval_kernel<<<(unsigned)blocks, 256, 0, s>>>(m, n, (int)L, A, B, R);
+    if (L <= 384)
+        leaf_interval_kernel<1024><<<(unsigned)blocks, kLeafThreads, 0, s>>>(m, n, (int)L, A, B, R);
+    else
+        leaf_interval_kernel<2048><<<(unsigned)blocks, kLeafThreads, 0, s>>>(m, n, (int)L, A, B, R);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
