@@ -191,22 +191,25 @@ __global__ void cyc_drop_kernel(int64_t n, const int32_t* __restrict__ nxt,
     if (target[p] >= 0 && mx[nxt[p]] == orig[p]) target[p] = -1;
 }
 
+// `by` (nullable) numbers the points for the edge order: caller indices, or
+// NULL for the index positions themselves.
 __global__ void r0_flags_kernel(int64_t n, const int32_t* __restrict__ target,
-                                const int32_t* __restrict__ orig, uint32_t* __restrict__ flag) {
+                                const int32_t* __restrict__ by, uint32_t* __restrict__ flag) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    flag[orig[p]] = target[p] >= 0 ? 1u : 0u;
+    flag[by ? by[p] : p] = target[p] >= 0 ? 1u : 0u;
 }
 __global__ void r0_emit_kernel(int64_t n, const int32_t* __restrict__ target,
                                const float* __restrict__ w0, const int32_t* __restrict__ orig,
-                               const uint32_t* __restrict__ pos, int32_t* __restrict__ src,
-                               int32_t* __restrict__ dst, float* __restrict__ w2) {
+                               const int32_t* __restrict__ by, const uint32_t* __restrict__ pos,
+                               int32_t* __restrict__ src, int32_t* __restrict__ dst,
+                               float* __restrict__ w2) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     int32_t t = target[p];
     if (t < 0) return;
     int32_t op = orig[p];
-    uint32_t i = pos[op];
+    uint32_t i = pos[by ? by[p] : p];
     src[i] = op;
     dst[i] = orig[t];
     w2[i] = w0[p];
@@ -692,7 +695,8 @@ int finalize_edges(const MstResult& r, double* edges, cudaStream_t s) {
 }
 
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
-                float* core_o, int32_t* nbr_o, const float* weights, int weighted_k) {
+                float* core_o, int32_t* nbr_o, const float* weights, int weighted_k,
+                bool any_order) {
     cudaStream_t s = ws.stream();
     const int64_t n = ix.n;
     const bool weighted = weights != nullptr && n > 1;
@@ -789,9 +793,12 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         }
         LAUNCH(cyc_drop_kernel, n, n, nxt, mx, ix.orig, target);
     }
-    LAUNCH(r0_flags_kernel, n, n, target, ix.orig, flag);
+    // round-0 edges by caller index of the choosing point (the reference's
+    // order), or by index position when the order does not matter
+    const int32_t* by = any_order ? nullptr : ix.orig;
+    LAUNCH(r0_flags_kernel, n, n, target, by, flag);
     FHG_TRY(scan_exclusive_u32(ws, flag, pos, n, cnt));
-    LAUNCH(r0_emit_kernel, n, n, target, w0, ix.orig, pos, out->src, out->dst, out->w2);
+    LAUNCH(r0_emit_kernel, n, n, target, w0, ix.orig, by, pos, out->src, out->dst, out->w2);
     uint32_t h_cnt = 0;
     FHG_CUDA(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     LAUNCH(iota_kernel, n, par, n);

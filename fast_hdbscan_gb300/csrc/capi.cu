@@ -627,7 +627,7 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
     } guard{ix, s};
     MstResult mst;
     FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev, sample_weights_dev,
-                        weighted_k));
+                        weighted_k, /*any_order=*/true));  // sorted below
     if (neighbors_dev) {
         // the row width boruvka_mst writes: k - 1 for its k-neighbour query
         const int64_t kq = sample_weights_dev ? weighted_k : (min_samples > 1 ? min_samples + 1 : 2);

@@ -20,8 +20,12 @@ struct MstResult {
 // `ws` owns every returned buffer.  Optional outputs (nullable):
 //   core_o  [n]       sqrt core distance, caller order
 //   nbr_o   [n*(k-1)] neighbours without the point itself, caller order
+// The edge list comes in the reference's order (the round-0 edges by caller
+// index of the choosing point, then every round's by component); with
+// any_order the round-0 edges come in index order instead, for callers that
+// sort the edges anyway.
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
                 float* core_o, int32_t* nbr_o, const float* weights = nullptr,
-                int weighted_k = 0);
+                int weighted_k = 0, bool any_order = false);
 
 }  // namespace fhg
