@@ -213,6 +213,25 @@ FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples,
     return FHG_OK;
 }
 
+FHG_API int fhg_index_kruskal_knn(fhg_index* index, int32_t min_samples, int32_t query_k,
+                                  const float* sample_weights_dev, double* edges_dev,
+                                  int32_t* neighbors_dev, double* core_dev,
+                                  int64_t* n_components_host, void* stream) {
+    if (!index || !edges_dev || !core_dev) {
+        set_error("fhg_index_kruskal_knn: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (min_samples < 1) {
+        set_error("min_samples must be a positive integer");
+        return FHG_ERR_INVALID;
+    }
+    int64_t nc = 0;
+    FHG_TRY(kruskal_knn_mst(*index, min_samples, query_k, sample_weights_dev, edges_dev,
+                            neighbors_dev, core_dev, &nc, as_stream(stream)));
+    if (n_components_host) *n_components_host = nc;
+    return FHG_OK;
+}
+
 // ------------------------------------------------------------- tree passes
 namespace fhg {
 namespace capi {

@@ -1,0 +1,335 @@
+// kNN-graph Kruskal MST (kruskal.py:950 _kruskal_mst_knn, the
+// algorithm="kruskal" back-end with an integer knn_k, without cannot-link
+// constraints).
+//
+// The reference lists the mutual-reachability edges of every point's kNN list
+// (kruskal.py:456), drops self-loops and infinite weights, orders them by a
+// stable argsort of their float64 weights and runs Kruskal's union-find; a
+// disconnected kNN graph is then joined by +inf bridges between the smallest
+// points of its components (kruskal.py:723, precomputed.py:308).
+//
+// Here: the spatial index's kNN (rows in caller order), one thread per edge
+// for the weights, a stable LSD radix sort of the valid edges by their
+// float64 bits (non-negative doubles order like their bits), and -- in place
+// of the sequential scan -- Boruvka rounds over the sorted ranks: every
+// component takes its lowest-rank outgoing edge, the picked edges are hooked
+// with a lock-free union-find and intra-component edges leave the active list.
+// Ranks are distinct, so the forest is the one Kruskal accepts (the minimum
+// spanning forest of a strict order is unique); compacting the picked ranks
+// gives Kruskal's acceptance order.  The union-find keeps every root the
+// smallest point of its component, so the bridges join the roots in index
+// order.
+#include "index.cuh"
+#include "primitives.cuh"
+#include "uf.cuh"
+
+namespace fhg {
+namespace {
+
+#define LAUNCH(kernel, count, ...)                                        \
+    do {                                                                  \
+        if ((count) > 0) {                                                \
+            ::fhg::note_launch();                                         \
+            kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);   \
+            FHG_CUDA(cudaGetLastError());                                 \
+        }                                                                 \
+    } while (0)
+
+// kruskal.py:995-1015: float64 core distances from the kNN lists (rows of kq,
+// the point itself first).  min_samples <= 1: zero.
+__global__ void kr_core_kernel(int64_t n, int kq, int ms, const float* __restrict__ rd,
+                               double* __restrict__ core) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    core[i] = ms > 1 ? __dsqrt_rn((double)rd[i * kq + ms]) : 0.0;
+}
+// kruskal.py:981-990 with boruvka.py:528 sample_weight_core_distance: the
+// first list position at which the running float64 weight (the point's own
+// first) reaches min_samples; index -1 (padding) reads the last weight.  The
+// distances are the float32 square roots the reference's tree query returns.
+__global__ void kr_core_w_kernel(int64_t n, int kq, int ms, const float* __restrict__ rd,
+                                 const int32_t* __restrict__ ix, const float* __restrict__ w,
+                                 double* __restrict__ core) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double total = 0.0;
+    int j = 0;
+    while (total < (double)ms && j < kq) {
+        const int32_t q = ix[i * kq + j];
+        total += (double)w[q >= 0 ? q : n - 1];
+        ++j;
+    }
+    core[i] = (double)__fsqrt_rn(rd[i * kq + (j > 0 ? j - 1 : 0)]);
+}
+// kruskal.py:456 _build_mrd_edges_knn and the filter of :1022.  Edge e is the
+// (e % kk)-th neighbour of point e / kk (kk = kq - 1).
+__global__ void kr_edges_kernel(int64_t n, int kq, int weighted, const float* __restrict__ rd,
+                                const int32_t* __restrict__ ix, const double* __restrict__ core,
+                                double* __restrict__ w, uint32_t* __restrict__ flag) {
+    const int64_t kk = kq - 1;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * kk) return;
+    const int64_t i = e / kk, jp = e - i * kk;
+    const int32_t j = ix[i * kq + jp + 1];
+    double mrd = INFINITY;
+    if (j >= 0) {
+        const float r = rd[i * kq + jp + 1];
+        const double d = weighted ? (double)__fsqrt_rn(r) : __dsqrt_rn((double)r);
+        mrd = core[i];
+        if (core[j] > mrd) mrd = core[j];
+        if (d > mrd) mrd = d;
+    }
+    w[e] = mrd;
+    flag[e] = (j >= 0 && j != (int32_t)i && isfinite(mrd)) ? 1u : 0u;
+}
+__global__ void kr_compact_kernel(int64_t E, const uint32_t* __restrict__ flag,
+                                  const uint32_t* __restrict__ pos, const double* __restrict__ w,
+                                  uint64_t* __restrict__ key, int32_t* __restrict__ eid) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E || !flag[e]) return;
+    key[pos[e]] = (uint64_t)__double_as_longlong(w[e]);
+    eid[pos[e]] = (int32_t)e;
+}
+__device__ __forceinline__ void edge_ends(int64_t e, int kq, const int32_t* __restrict__ ix,
+                                          int32_t* u, int32_t* v) {
+    const int64_t kk = kq - 1;
+    const int64_t i = e / kk;
+    *u = (int32_t)i;
+    *v = ix[i * kq + (e - i * kk) + 1];
+}
+__global__ void kr_iota_kernel(int32_t* a, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (int32_t)i;
+}
+__global__ void kr_fill_u32_kernel(uint32_t* a, int64_t n, uint32_t v) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+// One Boruvka round, step 1: every component's lowest outgoing rank.  Active
+// ranks come in increasing order, so a component's best is mostly set by its
+// first edge and later ones only read it.
+__global__ void kr_best_kernel(int64_t na, const int32_t* __restrict__ act,
+                               const int32_t* __restrict__ eid, int kq,
+                               const int32_t* __restrict__ ix, int32_t* par,
+                               uint32_t* __restrict__ best, uint32_t* __restrict__ keep) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= na) return;
+    const int32_t r = act[t];
+    int32_t u, v;
+    edge_ends(eid[r], kq, ix, &u, &v);
+    const int32_t cu = uf_find(par, u), cv = uf_find(par, v);
+    keep[t] = cu != cv ? 1u : 0u;
+    if (cu == cv) return;
+    if ((uint32_t)r < *(volatile uint32_t*)&best[cu]) atomicMin(&best[cu], (uint32_t)r);
+    if ((uint32_t)r < *(volatile uint32_t*)&best[cv]) atomicMin(&best[cv], (uint32_t)r);
+}
+// Step 2 (no union yet, so the roots are those of step 1): an edge picked by
+// either of its components is marked with the round.
+__global__ void kr_pick_kernel(int64_t na, const int32_t* __restrict__ act,
+                               const int32_t* __restrict__ eid, int kq,
+                               const int32_t* __restrict__ ix, int32_t* par,
+                               const uint32_t* __restrict__ best,
+                               const uint32_t* __restrict__ keep, int32_t* __restrict__ mark,
+                               int round, uint32_t* __restrict__ picked) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= na || !keep[t]) return;
+    const int32_t r = act[t];
+    int32_t u, v;
+    edge_ends(eid[r], kq, ix, &u, &v);
+    const int32_t cu = uf_find(par, u), cv = uf_find(par, v);
+    if (best[cu] == (uint32_t)r || best[cv] == (uint32_t)r) {
+        mark[r] = round;
+        atomicAdd(picked, 1u);
+    }
+}
+// Step 3: hook the picked edges.
+__global__ void kr_hook_kernel(int64_t na, const int32_t* __restrict__ act,
+                               const int32_t* __restrict__ eid, int kq,
+                               const int32_t* __restrict__ ix, int32_t* par,
+                               const int32_t* __restrict__ mark, int round) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= na) return;
+    const int32_t r = act[t];
+    if (mark[r] != round) return;
+    int32_t u, v;
+    edge_ends(eid[r], kq, ix, &u, &v);
+    uf_union(par, u, v);
+}
+__global__ void kr_scatter_active_kernel(int64_t na, const int32_t* __restrict__ act,
+                                         const uint32_t* __restrict__ keep,
+                                         const uint32_t* __restrict__ pos,
+                                         int32_t* __restrict__ act2) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < na && keep[t]) act2[pos[t]] = act[t];
+}
+__global__ void kr_mark_flags_kernel(int64_t m, const int32_t* __restrict__ mark,
+                                     uint32_t* __restrict__ flag) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < m) flag[r] = mark[r] > 0 ? 1u : 0u;
+}
+// kruskal.py:104-107: picked edges in rank order as (row point, neighbour,
+// weight).
+__global__ void kr_emit_kernel(int64_t m, const uint32_t* __restrict__ flag,
+                               const uint32_t* __restrict__ pos, const int32_t* __restrict__ eid,
+                               const uint64_t* __restrict__ key, int kq,
+                               const int32_t* __restrict__ ix, double* __restrict__ edges) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m || !flag[r]) return;
+    int32_t u, v;
+    edge_ends(eid[r], kq, ix, &u, &v);
+    const int64_t o = pos[r];
+    edges[3 * o + 0] = (double)u;
+    edges[3 * o + 1] = (double)v;
+    edges[3 * o + 2] = __longlong_as_double((long long)key[r]);
+}
+__global__ void kr_root_flags_kernel(int64_t n, int32_t* par, uint32_t* __restrict__ flag) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flag[i] = uf_find(par, (int32_t)i) == (int32_t)i ? 1u : 0u;
+}
+// kruskal.py:723 / precomputed.py:308: +inf bridges between consecutive
+// component representatives (the roots, each its component's smallest point).
+__global__ void kr_bridge_kernel(int64_t n, int64_t nc, const uint32_t* __restrict__ flag,
+                                 const uint32_t* __restrict__ pos, int64_t base,
+                                 double* __restrict__ edges) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    const int64_t c = pos[i];  // this root's place among the roots
+    if (c > 0) {               // bridge c - 1 ends here
+        edges[3 * (base + c - 1) + 1] = (double)i;
+        edges[3 * (base + c - 1) + 2] = INFINITY;
+    }
+    if (c + 1 < nc) edges[3 * (base + c) + 0] = (double)i;  // bridge c starts here
+}
+__global__ void kr_neighbors_kernel(int64_t n, int kq, int cols, const int32_t* __restrict__ ix,
+                                    int32_t* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * cols) return;
+    const int64_t i = t / cols, c = t - i * cols;
+    out[t] = ix[i * kq + c + 1];
+}
+
+}  // namespace
+
+int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const float* weights,
+                    double* edges, int32_t* neighbors, double* core, int64_t* n_components,
+                    cudaStream_t s) {
+    const int64_t n = index.n;
+    const int kq = query_k;
+    const int64_t kk = kq - 1;
+    if (kq < 2 || kq > 64) {
+        set_error("kruskal: the kNN query size must be in [2, 64] (got %d)", kq);
+        return kq > 64 ? FHG_ERR_UNSUPPORTED : FHG_ERR_INVALID;
+    }
+    if (n * kk > 0x7fffffffLL) {
+        set_error("kruskal: %lld kNN edges exceed the int32 edge index", (long long)(n * kk));
+        return FHG_ERR_UNSUPPORTED;
+    }
+    if (!weights && min_samples > 1 && min_samples >= kq) {
+        set_error("kruskal: the kNN query size %d must exceed min_samples %d", kq, min_samples);
+        return FHG_ERR_INVALID;
+    }
+    *n_components = n > 0 ? 1 : 0;
+    if (n < 2) {
+        if (n == 1) FHG_CUDA(cudaMemsetAsync(core, 0, sizeof(double), s));
+        return FHG_OK;
+    }
+    Stage stage(s, "kruskal_knn");
+    Workspace ws(s);
+    float* rd;
+    int32_t* ix;
+    FHG_TRY(ws.alloc(&rd, (size_t)(n * kq)));
+    FHG_TRY(ws.alloc(&ix, (size_t)(n * kq)));
+    FHG_TRY(index_knn(index, kq, nullptr, nullptr, rd, ix, s));
+    if (weights) LAUNCH(kr_core_w_kernel, n, n, kq, min_samples, rd, ix, weights, core);
+    else LAUNCH(kr_core_kernel, n, n, kq, min_samples, rd, core);
+    if (neighbors) {
+        const int cols = weights ? kq - 1 : (min_samples > 1 ? min_samples : 1);
+        LAUNCH(kr_neighbors_kernel, n * cols, n, kq, cols, ix, neighbors);
+    }
+
+    // ---- valid edges, stably sorted by weight
+    const int64_t E = n * kk;
+    double* w;
+    uint32_t *flag, *pos, *cnt;
+    FHG_TRY(ws.alloc(&w, (size_t)E));
+    FHG_TRY(ws.alloc(&flag, (size_t)E));
+    FHG_TRY(ws.alloc(&pos, (size_t)E));
+    FHG_TRY(ws.alloc(&cnt, 2));
+    LAUNCH(kr_edges_kernel, E, n, kq, weights ? 1 : 0, rd, ix, core, w, flag);
+    FHG_TRY(scan_exclusive_u32(ws, flag, pos, E, cnt));
+    uint32_t h_m = 0;
+    FHG_CUDA(cudaMemcpyAsync(&h_m, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    const int64_t m = h_m;
+    uint64_t* key;
+    int32_t* eid;
+    FHG_TRY(ws.alloc(&key, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&eid, (size_t)(m > 0 ? m : 1)));
+    LAUNCH(kr_compact_kernel, E, E, flag, pos, w, key, eid);
+    if (m > 1) {
+        Workspace tmp(s);
+        FHG_TRY(radix_sort_u64(tmp, key, eid, m, 0, 64));
+    }
+
+    // ---- minimum spanning forest: Boruvka rounds over the ranks
+    int32_t *par, *act, *act2, *mark;
+    uint32_t *best, *keep, *picked;
+    FHG_TRY(ws.alloc(&par, (size_t)n));
+    FHG_TRY(ws.alloc(&best, (size_t)n));
+    FHG_TRY(ws.alloc(&act, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&act2, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&keep, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&mark, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&picked, 1));
+    LAUNCH(kr_iota_kernel, n, par, n);
+    LAUNCH(kr_iota_kernel, m, act, m);
+    if (m > 0) FHG_CUDA(cudaMemsetAsync(mark, 0, sizeof(int32_t) * m, s));
+    int64_t na = m;
+    for (int round = 1; na > 0; ++round) {
+        if (round > 64) {  // each round at least halves the components
+            set_error("kruskal: the spanning forest did not converge");
+            return FHG_ERR_NO_CONVERGENCE;
+        }
+        LAUNCH(kr_fill_u32_kernel, n, best, n, 0xffffffffu);
+        FHG_CUDA(cudaMemsetAsync(picked, 0, sizeof(uint32_t), s));
+        LAUNCH(kr_best_kernel, na, na, act, eid, kq, ix, par, best, keep);
+        LAUNCH(kr_pick_kernel, na, na, act, eid, kq, ix, par, best, keep, mark, round, picked);
+        LAUNCH(kr_hook_kernel, na, na, act, eid, kq, ix, par, mark, round);
+        // edges joining one component leave the list (the picked ones next round)
+        FHG_TRY(scan_exclusive_u32(ws, keep, pos, na, cnt));
+        LAUNCH(kr_scatter_active_kernel, na, na, act, keep, pos, act2);
+        uint32_t h[2] = {0, 0};
+        FHG_CUDA(cudaMemcpyAsync(&h[0], picked, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaMemcpyAsync(&h[1], cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        std::swap(act, act2);
+        na = h[0] == 0 ? 0 : (int64_t)h[1];
+    }
+
+    // ---- the forest in Kruskal's acceptance order, then the bridges
+    uint32_t *rflag, *rpos;
+    FHG_TRY(ws.alloc(&rflag, (size_t)n));
+    FHG_TRY(ws.alloc(&rpos, (size_t)n));
+    uint32_t h_f = 0, h_c = 0;
+    if (m > 0) {  // flag and pos (E >= m entries) are free again
+        LAUNCH(kr_mark_flags_kernel, m, m, mark, flag);
+        FHG_TRY(scan_exclusive_u32(ws, flag, pos, m, cnt));
+        FHG_CUDA(cudaMemcpyAsync(&h_f, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    }
+    LAUNCH(kr_root_flags_kernel, n, n, par, rflag);
+    FHG_TRY(scan_exclusive_u32(ws, rflag, rpos, n, cnt + 1));
+    FHG_CUDA(cudaMemcpyAsync(&h_c, cnt + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    const int64_t nf = h_f, nc = h_c;
+    if (nc < 1 || nf + nc != n) {  // a forest over n points in nc components
+        set_error("kruskal: %lld forest edges for %lld points in %lld components", (long long)nf,
+                  (long long)n, (long long)nc);
+        return FHG_ERR_NO_CONVERGENCE;
+    }
+    if (m > 0) LAUNCH(kr_emit_kernel, m, m, flag, pos, eid, key, kq, ix, edges);
+    if (nc > 1) LAUNCH(kr_bridge_kernel, n, n, nc, rflag, rpos, nf, edges);
+    *n_components = nc;
+    return FHG_OK;
+}
+
+}  // namespace fhg

@@ -24,6 +24,15 @@ struct MstResult {
 // index of the choosing point, then every round's by component); with
 // any_order the round-0 edges come in index order instead, for callers that
 // sort the edges anyway.
+// kNN-graph Kruskal MST (kruskal.py:950): query_k nearest points per point
+// (itself included), float64 mutual-reachability weights, the minimum
+// spanning forest in Kruskal's acceptance order followed by +inf bridges.
+// edges: (n-1) x 3 float64; neighbors (nullable): n x cols (query_k - 1
+// with weights, else max(min_samples, 1)); core: n float64.
+int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const float* weights,
+                    double* edges, int32_t* neighbors, double* core, int64_t* n_components,
+                    cudaStream_t s);
+
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
                 float* core_o, int32_t* nbr_o, const float* weights = nullptr,
                 int weighted_k = 0, bool any_order = false);

@@ -181,16 +181,23 @@ def _validate_params(min_samples, min_cluster_size, cluster_selection_epsilon,
 
 
 def _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data=None,
-                        cannot_link=None, cannot_link_groups=None):
+                        cannot_link=None, cannot_link_groups=None, knn_k=None):
     if metric != "euclidean":
         raise NotImplementedError(f"metric={metric!r} is outside the GPU engine's Euclidean path")
     if algorithm not in ("boruvka", "kruskal"):
         raise ValueError("algorithm must be 'boruvka' or 'kruskal'. Got: %s" % algorithm)
-    if algorithm != "boruvka":
-        raise NotImplementedError("algorithm='kruskal' is outside the GPU engine's Boruvka path")
-    if cannot_link is not None or cannot_link_groups is not None:
+    has_cl = cannot_link is not None or cannot_link_groups is not None
+    if has_cl and algorithm != "kruskal":
         raise ValueError("cannot_link constraints are only supported with algorithm='kruskal'. "
-                         "Got algorithm='boruvka'.")
+                         "Got algorithm=%r." % algorithm)
+    if algorithm == "kruskal":
+        if has_cl:
+            raise NotImplementedError("cannot-link constraints are not on the GPU path")
+        if knn_k is None:
+            raise NotImplementedError(
+                "algorithm='kruskal' with knn_k=None (exact MST from the full pairwise distance "
+                "matrix) is not on the GPU path; pass an integer knn_k or use "
+                "algorithm='boruvka'")
     if semi_supervised:
         raise NotImplementedError("semi-supervised selection is outside the GPU engine's path")
     if data is not None and data.shape[1] > 32:
@@ -361,7 +368,22 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
     if data.shape[0] < 2:
         return _degenerate(data.shape[0], return_trees)
     _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data, cannot_link,
-                        cannot_link_groups)
+                        cannot_link_groups, knn_k)
+    if algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
+        if _is_tensor(data):
+            data = data.detach().cpu().numpy()
+        ms = min_cluster_size if min_samples is None else min_samples
+        mst, neighbors, core = compute_minimum_spanning_tree(
+            data, min_samples=ms, sample_weights=sample_weights, algorithm="kruskal",
+            knn_k=knn_k)
+        result = (*clusters_from_spanning_tree(
+            mst, min_cluster_size=min_cluster_size,
+            cluster_selection_method=cluster_selection_method,
+            max_cluster_size=max_cluster_size, allow_single_cluster=allow_single_cluster,
+            cluster_selection_epsilon=cluster_selection_epsilon,
+            cluster_selection_persistence=cluster_selection_persistence,
+            sample_weights=sample_weights), neighbors, core)
+        return result[: (None if return_trees else 2)]
     fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
                  max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
                  cluster_selection_persistence, return_trees=return_trees,
@@ -383,8 +405,14 @@ def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, rep
                          "Provide one or the other, not both.")
     data = check_array(data)
     _unsupported_routes(metric, algorithm, sample_weights, False, data, cannot_link,
-                        cannot_link_groups)
+                        cannot_link_groups, knn_k)
     tree = build_kdtree(data)
+    if algorithm == "kruskal":
+        from .kruskal import kruskal_mst_from_feature_matrix
+
+        return kruskal_mst_from_feature_matrix(tree, min_samples, knn_k=knn_k,
+                                               sample_weights=sample_weights,
+                                               reproducible=reproducible)
     if sample_weights is None:
         return parallel_boruvka(tree, 1, min_samples=min_samples)
     return parallel_boruvka(tree, 1, min_samples=min_samples,

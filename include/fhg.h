@@ -97,6 +97,31 @@ int fhg_index_boruvka(fhg_index* index, int32_t min_samples, const float* sample
                       int32_t weighted_k, double* edges_dev, int32_t* neighbors_dev,
                       float* core_dev, int32_t* n_rounds_host, void* stream);
 
+/* Replaces kruskal.py:821 kruskal_mst_from_feature_matrix(tree, min_samples,
+ * knn_k=<int>, sample_weights) without cannot-link constraints
+ * (kruskal.py:950 _kruskal_mst_knn; the algorithm="kruskal" back-end of
+ * hdbscan.py:470): the minimum spanning forest of the mutual-reachability
+ * edges of every point's kNN list, in Kruskal's acceptance order (float64
+ * weight, then edge position: point-major, neighbour order), followed by +inf
+ * bridges between consecutive component representatives (the smallest point
+ * of each component) when the kNN graph is disconnected.
+ *   query_k       kNN query size, the point itself included, as the
+ *                 reference computes it: max(knn_k, min_samples) + 1
+ *                 (knn_k + 1 when min_samples == 1; with sample weights
+ *                 max(knn_k, int(2 * min_samples / float(np.mean(w)))) + 1).
+ *                 2 <= query_k <= 64.
+ *   sample_weights_dev NULL, or n float32 weights: the weighted core
+ *                 distance (boruvka.py:528) and float32 edge lengths.
+ *   edges_dev     (n-1) x 3 float64: src, dst, weight.
+ *   neighbors_dev optional, n x cols int32: cols = query_k - 1 with weights,
+ *                 else min_samples (1 when min_samples == 1).
+ *   core_dev      n float64 core distances.
+ *   n_components_host optional: components of the kNN graph. */
+int fhg_index_kruskal_knn(fhg_index* index, int32_t min_samples, int32_t query_k,
+                          const float* sample_weights_dev, double* edges_dev,
+                          int32_t* neighbors_dev, double* core_dev, int64_t* n_components_host,
+                          void* stream);
+
 /* Replaces the np.lexsort((mst[:,1], mst[:,0], mst[:,2])) of hdbscan.py:511:
  * rows of an m x 3 float64 edge list ordered by (weight, src, dst). */
 int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream);

@@ -1374,3 +1374,124 @@ void orc_get_cluster_labelling_at_cut(const double* lk, int64_t m, double cut, i
     for (int64_t p = 0; p < num_points; ++p) out[p] = map[out[p]];
     free(dp); free(dr); free(csize); free(map); free(seen);
 }
+
+/* ------------------------------------------------------------------------- */
+/* kNN-graph Kruskal MST: kruskal.py:950-1034 (_kruskal_mst_knn without       */
+/* cannot-link constraints), kruskal.py:456 _build_mrd_edges_knn, :32         */
+/* _kruskal_core, :723 _finish_mst + precomputed.py:308 bridge_forest_with_inf */
+/* ------------------------------------------------------------------------- */
+
+static const double* g_kr_w;
+/* kruskal.py:1028 np.argsort(weights, kind="stable"): by weight, then position */
+static int cmp_kr(const void* a, const void* b) {
+    const int64_t i = *(const int64_t*)a, j = *(const int64_t*)b;
+    const double wi = g_kr_w[i], wj = g_kr_w[j];
+    if (wi < wj) return -1;
+    if (wi > wj) return 1;
+    return (i > j) - (i < j);
+}
+
+int64_t orc_kruskal_knn(const float* rdist, const int32_t* idx, int64_t n, int64_t kq,
+                        int64_t min_samples, const float* weights, double* edges,
+                        double* core) {
+    const int64_t kk = kq - 1; /* neighbours per point without the point itself */
+    double* dist = (double*)malloc(sizeof(double) * (size_t)(n * (kk > 0 ? kk : 1)));
+    /* kruskal.py:981-1015: core distances and edge lengths */
+    for (int64_t i = 0; i < n; ++i) {
+        if (weights) {
+            /* boruvka.py:528 sample_weight_core_distance on the plain (float32
+             * sqrt) distances, self first; index -1 reads the last weight */
+            double total = 0.0;
+            int64_t j = 0;
+            while (total < (double)min_samples && j < kq) {
+                const int32_t q = idx[i * kq + j];
+                total += (double)weights[q >= 0 ? q : n - 1];
+                ++j;
+            }
+            core[i] = (double)sqrtf(rdist[i * kq + (j - 1)]);
+        } else if (min_samples > 1) {
+            core[i] = sqrt((double)rdist[i * kq + min_samples]);
+        } else {
+            core[i] = 0.0;
+        }
+        for (int64_t j = 1; j < kq; ++j)
+            dist[i * kk + j - 1] = weights ? (double)sqrtf(rdist[i * kq + j])
+                                           : sqrt((double)rdist[i * kq + j]);
+    }
+    /* kruskal.py:456 _build_mrd_edges_knn, then :1022 drop self-loops and
+     * infinite weights, keeping the edge order */
+    const int64_t total = n * kk;
+    double* w = (double*)malloc(sizeof(double) * (size_t)(total > 0 ? total : 1));
+    int32_t* row = (int32_t*)malloc(sizeof(int32_t) * (size_t)(total > 0 ? total : 1));
+    int32_t* col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(total > 0 ? total : 1));
+    int64_t m = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        for (int64_t jp = 0; jp < kk; ++jp) {
+            const int32_t j = idx[i * kq + jp + 1];
+            double mrd = INFINITY;
+            int32_t c = (int32_t)i;
+            if (j >= 0) {
+                mrd = core[i];
+                if (core[j] > mrd) mrd = core[j];
+                if (dist[i * kk + jp] > mrd) mrd = dist[i * kk + jp];
+                c = j;
+            }
+            if (c != (int32_t)i && isfinite(mrd)) {
+                w[m] = mrd;
+                row[m] = (int32_t)i;
+                col[m] = c;
+                ++m;
+            }
+        }
+    }
+    int64_t* order = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m > 0 ? m : 1));
+    for (int64_t e = 0; e < m; ++e) order[e] = e;
+    g_kr_w = w;
+    qsort(order, (size_t)m, sizeof(int64_t), cmp_kr);
+    /* kruskal.py:32 _kruskal_core: union by rank with full path compression */
+    int32_t* pred = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* rank = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+    for (int64_t i = 0; i < n; ++i) pred[i] = (int32_t)i;
+    int64_t n_mst = 0;
+    for (int64_t t = 0; t < m && n_mst < n - 1; ++t) {
+        const int64_t e = order[t];
+        int32_t u = row[e], v = col[e], ru = u, rv = v;
+        while (pred[ru] != ru) ru = pred[ru];
+        for (int32_t c = u; c != ru;) { const int32_t nx = pred[c]; pred[c] = ru; c = nx; }
+        while (pred[rv] != rv) rv = pred[rv];
+        for (int32_t c = v; c != rv;) { const int32_t nx = pred[c]; pred[c] = rv; c = nx; }
+        if (ru != rv) {
+            edges[3 * n_mst + 0] = (double)u;
+            edges[3 * n_mst + 1] = (double)v;
+            edges[3 * n_mst + 2] = w[e];
+            ++n_mst;
+            if (rank[ru] > rank[rv]) pred[rv] = ru;
+            else if (rank[ru] < rank[rv]) pred[ru] = rv;
+            else { pred[rv] = ru; rank[ru] += 1; }
+        }
+    }
+    /* kruskal.py:723 _finish_mst: one representative per component -- its
+     * smallest point -- in ascending order, joined by +inf bridges */
+    int32_t* rep = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) rep[i] = INT32_MAX;
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t r = (int32_t)i;
+        while (pred[r] != r) r = pred[r];
+        if ((int32_t)i < rep[r]) rep[r] = (int32_t)i;
+    }
+    int64_t prev = -1;
+    for (int64_t i = 0; i < n; ++i) { /* representatives are points: visit them in order */
+        int32_t r = (int32_t)i;
+        while (pred[r] != r) r = pred[r];
+        if (rep[r] != (int32_t)i) continue;
+        if (prev >= 0) {
+            edges[3 * n_mst + 0] = (double)prev;
+            edges[3 * n_mst + 1] = (double)i;
+            edges[3 * n_mst + 2] = INFINITY;
+            ++n_mst;
+        }
+        prev = i;
+    }
+    free(rep); free(rank); free(pred); free(order); free(col); free(row); free(w); free(dist);
+    return n_mst;
+}

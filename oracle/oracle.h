@@ -95,6 +95,17 @@ void orc_get_point_membership_strength_vector(const int64_t* parent, const int64
 void orc_get_cluster_labelling_at_cut(const double* linkage, int64_t m, double cut,
                                       int64_t min_cluster_size, int64_t* out);
 
+/* kruskal.py:950 _kruskal_mst_knn without cannot-link constraints, on kNN
+ * lists (rdist, idx: n x kq, the point itself first, as orc_tree_query
+ * returns them).  weights NULL: core = sqrt(rdist[:, min_samples]) in float64
+ * (0 when min_samples <= 1) and edge lengths sqrt(rdist) in float64; weights
+ * given: the weighted core (boruvka.py:528) and float32 sqrt lengths, widened.
+ * Writes the MST edges (src, dst, weight; +inf bridges join the components of
+ * a disconnected kNN graph) and core[n]; returns the edge count (n - 1). */
+int64_t orc_kruskal_knn(const float* rdist, const int32_t* idx, int64_t n, int64_t kq,
+                        int64_t min_samples, const float* weights, double* edges,
+                        double* core);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,6 +56,8 @@ def lib():
         L.orc_get_point_membership_strength_vector.argtypes = [
             _P, _P, _P, _P, _I64, _P, _I64, _P, _I64, _P]
         L.orc_get_cluster_labelling_at_cut.argtypes = [_P, _I64, _D, _I64, _P]
+        L.orc_kruskal_knn.restype = _I64
+        L.orc_kruskal_knn.argtypes = [_P, _P, _I64, _I64, _I64, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -130,6 +132,36 @@ def parallel_boruvka(tree, min_samples=10, mode=0, nthreads=1, sample_weights=No
     m = lib().orc_parallel_boruvka(tree._h, min_samples, mode, nthreads, _p(w), k, _p(edges),
                                    _p(nbrs), _p(core), _p(rounds))
     return edges[:m], nbrs, core, int(rounds[0])
+
+
+def kruskal_query_k(min_samples, knn_k, sample_weights=None):
+    """kruskal.py:981-1007: the kNN query size of _kruskal_mst_knn (the point
+    itself included)."""
+    if sample_weights is not None:
+        mean_sw = float(np.mean(np.asarray(sample_weights, np.float32)))
+        return max(knn_k, int(2 * min_samples / mean_sw)) + 1
+    if min_samples > 1:
+        return max(knn_k, min_samples) + 1
+    return knn_k + 1
+
+
+def kruskal_knn(tree, min_samples, knn_k, mode=0, nthreads=1, sample_weights=None):
+    """kruskal.py:950 _kruskal_mst_knn (no cannot-link constraints) ->
+    (mst_edges float64[n-1, 3], neighbors int32, core_distances float64)."""
+    n = tree.data.shape[0]
+    w = None if sample_weights is None else np.ascontiguousarray(sample_weights, np.float32)
+    kq = kruskal_query_k(min_samples, knn_k, w)
+    rd, ix = tree_query(tree, kq, mode, nthreads)
+    edges = np.zeros((max(n - 1, 0), 3), np.float64)
+    core = np.empty(n, np.float64)
+    m = lib().orc_kruskal_knn(_p(rd), _p(ix), n, kq, min_samples, _p(w), _p(edges), _p(core))
+    if w is not None:
+        nbrs = ix[:, 1:]
+    elif min_samples > 1:
+        nbrs = ix[:, 1:min_samples + 1]
+    else:
+        nbrs = ix[:, 1:2]
+    return edges[:m], np.ascontiguousarray(nbrs), core
 
 
 def sort_mst(mst):

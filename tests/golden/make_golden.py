@@ -237,15 +237,56 @@ def function_fixtures():
     np.savez_compressed(os.path.join(HERE, "fn_eps_search.npz"), **out)
 
 
+KRUSKAL_CASES = {
+    # name: (data factory, min_samples, min_cluster_size, knn_k, weights factory or None)
+    "kr_blobs200_k10": (lambda: _blobs200(), 5, 10, 10, None),
+    "kr_vd3d_5k_k8": (lambda: synthetic.varying_density(5000, seed=11), 10, 40, 8, None),
+    "kr_blobs2d_2k_ms1": (lambda: synthetic.blobs_2d(2000, seed=12), 1, 20, 3, None),
+    "kr_vd3d_3k_w": (lambda: synthetic.varying_density(3000, seed=13), 6, 30, 12,
+                     lambda n: _weights_sixty_fourths(n, 14)),
+}
+
+
+def kruskal_fixtures(only=None):
+    """The kNN-graph Kruskal MST (kruskal.py:950, algorithm='kruskal' with an
+    integer knn_k) and the fit on it, from the reference's public API."""
+    from fast_hdbscan.hdbscan import compute_minimum_spanning_tree, fast_hdbscan
+
+    for name, (factory, ms, mcs, knn_k, wf) in KRUSKAL_CASES.items():
+        if only and name not in only:
+            continue
+        X = np.ascontiguousarray(factory(), dtype=np.float32)
+        w = None if wf is None else wf(X.shape[0])
+        t0 = time.time()
+        mst, nbrs, core = compute_minimum_spanning_tree(
+            X, min_samples=ms, sample_weights=w, algorithm="kruskal", knn_k=knn_k)
+        labels, probs = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs,
+                                     sample_weights=w, algorithm="kruskal", knn_k=knn_k)
+        out = dict(X=X, min_samples=np.int64(ms), min_cluster_size=np.int64(mcs),
+                   knn_k=np.int64(knn_k), mst=np.asarray(mst, np.float64),
+                   neighbors=np.asarray(nbrs, np.int32), core=np.asarray(core, np.float64),
+                   labels=np.asarray(labels, np.int64), probabilities=np.asarray(probs))
+        if w is not None:
+            out["sample_weights"] = np.asarray(w, np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(f"{name}: n={X.shape[0]} bridges={int(np.isinf(mst[:, 2]).sum())} "
+              f"clusters={len(set(labels.tolist()) - {-1})} {time.time() - t0:.1f}s")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--cuts-only", action="store_true",
                     help="only add the DBSCAN-cut fields to existing fixtures")
+    ap.add_argument("--kruskal-only", action="store_true",
+                    help="only write the kNN-graph Kruskal fixtures")
     args = ap.parse_args()
     sys.path.insert(1, args.reference)
     import fast_hdbscan  # noqa: F401
+    if args.kruskal_only:
+        kruskal_fixtures(args.only)
+        return
     for name, (factory, kwargs) in CASES.items():
         if args.only and name not in args.only:
             continue
@@ -254,6 +295,7 @@ def main():
         add_cuts(name)
     if not args.only:
         function_fixtures()
+        kruskal_fixtures()
 
 
 if __name__ == "__main__":

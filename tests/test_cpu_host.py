@@ -96,8 +96,12 @@ def test_out_of_scope_routes_raise_not_implemented():
     X = np.random.default_rng(1).random((20, 2))
     with pytest.raises(NotImplementedError):
         fast_hdbscan(X, metric="cosine")
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(NotImplementedError):  # exact full-pairwise Kruskal (knn_k=None)
         fast_hdbscan(X, algorithm="kruskal")
+    with pytest.raises(NotImplementedError):  # cannot-link constraints
+        fast_hdbscan(X, algorithm="kruskal", knn_k=5, cannot_link_groups=np.zeros(20, np.int32))
+    with pytest.raises(ValueError):  # hdbscan.py:420: constraints need algorithm="kruskal"
+        fast_hdbscan(X, cannot_link_groups=np.zeros(20, np.int32))
     with pytest.raises(ValueError):
         compute_minimum_spanning_tree(X, algorithm="prim")
     with pytest.raises(NotImplementedError):  # hdbscan.py:447: NNDescent above 30 dims

@@ -15,9 +15,11 @@ import pytest
 from conftest import GOLDEN
 from oracle import oracle as O
 
-# fit fixtures; fn_*.npz hold function-level cases
+# fit fixtures; fn_*.npz hold function-level cases, kr_*.npz the kNN-graph
+# Kruskal back-end (algorithm="kruskal")
 FIXTURES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("fn_"))
+                  if not os.path.basename(p).startswith(("fn_", "kr_")))
+KRUSKAL = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "kr_*.npz")))
 # The reference indexes knn[-1] when min_samples >= n (k exceeds the point
 # count); its MST for that fixture has edges to "point -1".  Only its labels
 # and probabilities (all noise) are meaningful there.
@@ -148,3 +150,23 @@ def test_oracle_epsilon_search_crafted_tree():
         np.testing.assert_array_equal(got, g[f"out_{i}"])
         i += 1
     assert i >= 5
+
+
+@pytest.mark.parametrize("name", KRUSKAL)
+def test_oracle_kruskal_knn_bitexact(name):
+    """kruskal.py:950 _kruskal_mst_knn (algorithm="kruskal", integer knn_k):
+    the oracle's MST edges (acceptance order and +inf bridges included),
+    neighbours and float64 core distances equal the reference's, and the fit
+    on that MST gives the reference's labels and probabilities."""
+    g = _load(name)
+    X = g["X"]
+    ms, mcs, knn_k = int(g["min_samples"]), int(g["min_cluster_size"]), int(g["knn_k"])
+    w = g["sample_weights"] if "sample_weights" in g else None
+    mst, nbrs, core = O.kruskal_knn(O.build_kdtree(X), ms, knn_k, mode=0, sample_weights=w)
+    np.testing.assert_array_equal(mst, g["mst"])
+    np.testing.assert_array_equal(nbrs, g["neighbors"])
+    np.testing.assert_array_equal(core, g["core"])
+    labels, probs, *_ = O.clusters_from_spanning_tree(mst, min_cluster_size=mcs,
+                                                      sample_weights=w)
+    np.testing.assert_array_equal(labels, g["labels"])
+    np.testing.assert_array_equal(probs, g["probabilities"])
