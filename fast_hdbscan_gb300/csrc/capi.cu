@@ -620,7 +620,8 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
              int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
              int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
              int64_t* selected_dev, int64_t* n_selected_host, void* stream,
-             const FitExport& ex) {
+             const FitExport& ex, int32_t knn_k = 0, int32_t query_k = 0,
+             double* core64_dev = nullptr) {
     FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev, labels_dev, probs_dev}));
     if (min_samples < 1 || min_cluster_size < 1) {
         set_error("Min samples and min cluster size must be positive integers!");
@@ -644,23 +645,37 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
         cudaStream_t s;
         ~IndexGuard() { index_free(p, s); }
     } guard{ix, s};
-    MstResult mst;
-    FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev, sample_weights_dev,
-                        weighted_k, /*any_order=*/true));  // sorted below
-    if (neighbors_dev) {
-        // the row width boruvka_mst writes: k - 1 for its k-neighbour query
-        const int64_t kq = sample_weights_dev ? weighted_k : (min_samples > 1 ? min_samples + 1 : 2);
-        const int64_t kcols = kq > 1 ? kq - 1 : 0;
-        FHG_TRY(side.copy(ex.neighbors_host, neighbors_dev, sizeof(int32_t) * n * kcols));
-    }
-    if (core_dev) FHG_TRY(side.copy(ex.core_host, core_dev, sizeof(float) * n));
-    if (mst.m != n - 1) {
-        set_error("boruvka: spanning forest has %lld edges for %lld points", (long long)mst.m,
-                  (long long)n);
-        return FHG_ERR_NO_CONVERGENCE;
-    }
     Linkage lk;
-    FHG_TRY(sort_and_link(ws, n, mst.src, mst.dst, nullptr, mst.w2, &lk));
+    if (knn_k > 0) {  // the kNN-graph Kruskal back-end (kruskal.py:950)
+        double *kedges, *core64 = core64_dev;
+        FHG_TRY(ws.alloc(&kedges, (size_t)(3 * (n - 1))));
+        if (!core64) FHG_TRY(ws.alloc(&core64, (size_t)n));
+        int64_t nc = 0;
+        FHG_TRY(kruskal_knn_mst(*ix, min_samples, query_k, sample_weights_dev, kedges,
+                                neighbors_dev, core64, &nc, s));
+        int32_t *src, *dst;
+        double* w;
+        FHG_TRY(split_mst_f64(ws, kedges, n - 1, &src, &dst, &w));
+        FHG_TRY(sort_and_link(ws, n, src, dst, w, nullptr, &lk, false));
+    } else {
+        MstResult mst;
+        FHG_TRY(boruvka_mst(ws, *ix, min_samples, &mst, core_dev, neighbors_dev,
+                            sample_weights_dev, weighted_k, /*any_order=*/true));  // sorted below
+        if (neighbors_dev) {
+            // the row width boruvka_mst writes: k - 1 for its k-neighbour query
+            const int64_t kq =
+                sample_weights_dev ? weighted_k : (min_samples > 1 ? min_samples + 1 : 2);
+            const int64_t kcols = kq > 1 ? kq - 1 : 0;
+            FHG_TRY(side.copy(ex.neighbors_host, neighbors_dev, sizeof(int32_t) * n * kcols));
+        }
+        if (core_dev) FHG_TRY(side.copy(ex.core_host, core_dev, sizeof(float) * n));
+        if (mst.m != n - 1) {
+            set_error("boruvka: spanning forest has %lld edges for %lld points", (long long)mst.m,
+                      (long long)n);
+            return FHG_ERR_NO_CONVERGENCE;
+        }
+        FHG_TRY(sort_and_link(ws, n, mst.src, mst.dst, nullptr, mst.w2, &lk));
+    }
     if (sample_weights_dev) FHG_TRY(weighted_sizes(ws, lk, sample_weights_dev));
     {
         Stage stage(s, "outputs");
@@ -740,6 +755,26 @@ FHG_API int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t mi
                     sample_weights_dev, weighted_k, labels_dev, probs_dev, mst_dev, linkage_dev,
                     ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, ct_rows_host,
                     neighbors_dev, core_dev, selected_dev, n_selected_host, stream, FitExport());
+}
+
+FHG_API int fhg_hdbscan_fit_kruskal(
+    const float* X_dev, int64_t n, int32_t d, int32_t min_samples, int32_t knn_k,
+    int32_t query_k, int64_t min_cluster_size, int32_t selection_method, double max_cluster_size,
+    int allow_single_cluster, double epsilon, double persistence, const float* sample_weights_dev,
+    int64_t* labels_dev, float* probs_dev, double* mst_dev, double* linkage_dev,
+    int64_t* ct_parent_dev, int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+    int64_t* ct_rows_host, int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev,
+    int64_t* n_selected_host, void* stream) {
+    if (knn_k < 1) {
+        set_error("fhg_hdbscan_fit_kruskal: knn_k must be a positive integer (got %d)", knn_k);
+        return FHG_ERR_INVALID;
+    }
+    return fit_impl(X_dev, n, d, min_samples, min_cluster_size, selection_method,
+                    max_cluster_size, allow_single_cluster, epsilon, persistence,
+                    sample_weights_dev, 0, labels_dev, probs_dev, mst_dev, linkage_dev,
+                    ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, ct_rows_host,
+                    neighbors_dev, nullptr, selected_dev, n_selected_host, stream, FitExport(),
+                    knn_k, query_k, core_dev);
 }
 
 FHG_API int fhg_hdbscan_fit_export(

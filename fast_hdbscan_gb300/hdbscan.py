@@ -321,6 +321,62 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
     return FitResult(labels_h, host[1], host[4], ct, host[3], host[5], host[6], host[2])
 
 
+def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_method="eom",
+                    max_cluster_size=np.inf, allow_single_cluster=False,
+                    cluster_selection_epsilon=0.0, cluster_selection_persistence=0.0,
+                    return_trees=True, sample_weights=None):
+    """One call of fhg_hdbscan_fit_kruskal: the kNN-graph Kruskal MST
+    (kruskal.py:950) and the tree passes on the GPU, outputs copied back."""
+    from .kruskal import kruskal_query_k
+
+    torch = _native._torch()
+    if isinstance(X, torch.Tensor):
+        Xd = X.to(device="cuda", dtype=torch.float32, non_blocking=True).contiguous()
+    else:
+        Xd = _native.to_device(np.ascontiguousarray(X, dtype=np.float32), np.float32)
+    n, d = Xd.shape
+    ms = min_cluster_size if min_samples is None else min_samples
+    w = None if sample_weights is None else np.ascontiguousarray(sample_weights, np.float32)
+    kq = kruskal_query_k(int(ms), int(knn_k), w)
+    if kq > 64:
+        raise NotImplementedError(f"a kNN query of {kq} neighbours exceeds the GPU kNN's 64")
+    d_w = _native.to_device(w, np.float32) if w is not None else None
+    cols = kq - 1 if w is not None else (ms if ms > 1 else 1)
+    method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
+    if method is None:
+        raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+    E = _native.empty
+    labels, probs, sel = E(n, np.int64), E(n, np.float32), E(n, np.int64)
+    trees = return_trees
+    mst = E((n - 1, 3), np.float64) if trees else None
+    linkage = E((n - 1, 4), np.float64) if trees else None
+    ctp, ctc = (E(2 * n, np.int64), E(2 * n, np.int64)) if trees else (None, None)
+    ctl, cts = (E(2 * n, np.float32), E(2 * n, np.float32)) if trees else (None, None)
+    nbrs = E((n, cols), np.int32) if trees else None
+    core = E(n, np.float64) if trees else None
+    rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
+    V, lib = _native.vptr, _native.load()
+    rc = lib.fhg_hdbscan_fit_kruskal(
+        V(Xd), n, d, int(ms), int(knn_k), kq, int(min_cluster_size), method,
+        float(max_cluster_size), int(bool(allow_single_cluster)),
+        float(cluster_selection_epsilon), float(cluster_selection_persistence), V(d_w),
+        V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
+        ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel), _native.stream_ptr())
+    if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
+        raise KeyError(lib.fhg_last_error().decode())
+    _native.check(rc)
+    r, k = rows.value, nsel.value
+    labels_h = labels.cpu().numpy().astype(np.intp, copy=False)
+    if not trees:
+        return FitResult(labels_h, probs.cpu().numpy(), None, None, None, None, None,
+                         sel[:k].cpu().numpy())
+    ct = CondensedTree(ctp[:r].cpu().numpy(), ctc[:r].cpu().numpy(), ctl[:r].cpu().numpy(),
+                       cts[:r].cpu().numpy())
+    return FitResult(labels_h, probs.cpu().numpy(), linkage.cpu().numpy(), ct,
+                     mst.cpu().numpy(), nbrs.cpu().numpy(), core.cpu().numpy(),
+                     sel[:k].cpu().numpy())
+
+
 def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc",
                  min_samples=10, min_cluster_size=10, cluster_selection_method="eom",
                  max_cluster_size=np.inf, allow_single_cluster=False,
@@ -370,24 +426,15 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
     _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data, cannot_link,
                         cannot_link_groups, knn_k)
     if algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
-        if _is_tensor(data):
-            data = data.detach().cpu().numpy()
-        ms = min_cluster_size if min_samples is None else min_samples
-        mst, neighbors, core = compute_minimum_spanning_tree(
-            data, min_samples=ms, sample_weights=sample_weights, algorithm="kruskal",
-            knn_k=knn_k)
-        result = (*clusters_from_spanning_tree(
-            mst, min_cluster_size=min_cluster_size,
-            cluster_selection_method=cluster_selection_method,
-            max_cluster_size=max_cluster_size, allow_single_cluster=allow_single_cluster,
-            cluster_selection_epsilon=cluster_selection_epsilon,
-            cluster_selection_persistence=cluster_selection_persistence,
-            sample_weights=sample_weights), neighbors, core)
-        return result[: (None if return_trees else 2)]
-    fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
-                 max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
-                 cluster_selection_persistence, return_trees=return_trees,
-                 sample_weights=sample_weights, condensed_records=condensed_records)
+        fr = gpu_fit_kruskal(data, min_samples, min_cluster_size, knn_k,
+                             cluster_selection_method, max_cluster_size, allow_single_cluster,
+                             cluster_selection_epsilon, cluster_selection_persistence,
+                             return_trees=return_trees, sample_weights=sample_weights)
+    else:
+            fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
+                     max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
+                     cluster_selection_persistence, return_trees=return_trees,
+                     sample_weights=sample_weights, condensed_records=condensed_records)
     result = (fr.labels, fr.probabilities, fr.linkage, fr.condensed, fr.sorted_mst,
               fr.neighbors, fr.core_distances)
     return result[: (None if return_trees else 2)]

@@ -267,6 +267,23 @@ int fhg_hdbscan_fit(const float* X_dev, int64_t n, int32_t d, int32_t min_sample
                     float* core_dev, int64_t* selected_dev, int64_t* n_selected_host,
                     void* stream);
 
+/* fhg_hdbscan_fit on the kNN-graph Kruskal MST (hdbscan.py:306 with
+ * algorithm="kruskal" and an integer knn_k; the MST as fhg_index_kruskal_knn
+ * builds it, then the same tree passes).  query_k as for
+ * fhg_index_kruskal_knn; neighbors_dev (optional) takes its columns and
+ * core_dev (optional) is float64.  Sample weights (NULL or n float32) enter
+ * the core distances, the edge lengths and the tree sizes. */
+int fhg_hdbscan_fit_kruskal(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                            int32_t knn_k, int32_t query_k, int64_t min_cluster_size,
+                            int32_t selection_method, double max_cluster_size,
+                            int allow_single_cluster, double epsilon, double persistence,
+                            const float* sample_weights_dev, int64_t* labels_dev,
+                            float* probs_dev, double* mst_dev, double* linkage_dev,
+                            int64_t* ct_parent_dev, int64_t* ct_child_dev,
+                            float* ct_lambda_dev, float* ct_size_dev, int64_t* ct_rows_host,
+                            int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev,
+                            int64_t* n_selected_host, void* stream);
+
 /* fhg_hdbscan_fit, with the large outputs also copied to host memory while
  * the fit runs: each non-NULL *_host destination receives its output from a
  * side stream as soon as the fit has finished writing it (neighbours and
