@@ -48,6 +48,11 @@ OTHER_WORKLOADS = {
                    min_cluster_size=500, seed=1,
                    generator="40 blobs, std logU[0.2,2], Dirichlet weights, centres "
                              "U[-20,20]^5, 10% noise"),
+    # the metric's data through the algorithm="kruskal" back-end (kNN graph, knn_k=16)
+    "kruskal10m": dict(workload="varying_density_10M_3d_kruskal_knn16", n=10_000_000, d=3,
+                       min_samples=15, min_cluster_size=500, seed=3, algorithm="kruskal",
+                       knn_k=16,
+                       generator="200 Gaussians, std lognormal(0,1), centres U[-100,100]^3"),
 }
 CPU_SAMPLE_N = 1_000_000
 
@@ -64,7 +69,8 @@ def parse_args():
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--workload", default="fit", choices=["fit", "batched", *OTHER_WORKLOADS],
                     help="fit: the metric's 10M x 3-D fit; batched: many independent fits; "
-                         "umap2m: the 2M x 5-D fit")
+                         "umap2m: the 2M x 5-D fit; kruskal10m: the 10M x 3-D fit on the "
+                         "kNN-graph Kruskal back-end")
     ap.add_argument("--instances", type=int, default=4096, help="batched workload size")
     return ap.parse_args()
 
@@ -209,6 +215,8 @@ def run_gb300(args):
 
     n = args.n
     ms, mcs = WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"]
+    kruskal = WORKLOAD.get("algorithm") == "kruskal"
+    knn_k = WORKLOAD.get("knn_k", 0)
     Xh = make_data(n, WORKLOAD["seed"] + rank)
     d = Xh.shape[1]
     Xd = torch.from_numpy(Xh).cuda()
@@ -217,12 +225,20 @@ def run_gb300(args):
     mst, linkage = E((n - 1, 3), np.float64), E((n - 1, 4), np.float64)
     ctp, ctc, ctl, cts = (E(2 * n, np.int64), E(2 * n, np.int64), E(2 * n, np.float32),
                           E(2 * n, np.float32))
-    nbrs, core, sel = E((n, ms), np.int32), E(n, np.float32), E(n, np.int64)
+    nbrs, sel = E((n, ms), np.int32), E(n, np.int64)
+    core = E(n, np.float64 if kruskal else np.float32)
     rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
     V = _native.vptr
     stream = torch.cuda.current_stream()
 
     def step():
+        if kruskal:
+            _native.check(lib.fhg_hdbscan_fit_kruskal(
+                V(Xd), n, d, ms, knn_k, max(knn_k, ms) + 1, mcs, 0, float("inf"), 0, 0.0, 0.0,
+                None, V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
+                ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
+                _native.stream_ptr()))
+            return
         _native.check(lib.fhg_hdbscan_fit(
             V(Xd), n, d, ms, mcs, 0, float("inf"), 0, 0.0, 0.0, None, 0, V(labels), V(probs), V(mst),
             V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows), V(nbrs), V(core),
@@ -275,9 +291,11 @@ def run_gb300(args):
     if dom:
         tot_ms, cnt = kernel_stages[dom]
         per_launch_ms = tot_ms / cnt
-        alg = algorithmic_bytes(dom, n, ms + 1, 4 if d <= 4 else 8)
+        alg = algorithmic_bytes(dom, n, (max(knn_k, ms) if kruskal else ms) + 1,
+                                4 if d <= 4 else 8)
         achieved = alg / (per_launch_ms / 1e3) / 1e9
-        tpp = traffic_per_point(dom)
+        # the ncu traffic per point was measured for the Boruvka fit's kNN (k = 16)
+        tpp = None if kruskal else traffic_per_point(dom)
         traffic = round(tpp * n) if tpp is not None else None
         roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak,
                     "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 5),
@@ -290,7 +308,8 @@ def run_gb300(args):
     e2e = None
     if not args.no_e2e:
         Xp = torch.from_numpy(Xh).pin_memory()
-        est = HDBSCAN(min_cluster_size=mcs, min_samples=ms)
+        est = (HDBSCAN(min_cluster_size=mcs, min_samples=ms, algorithm="kruskal", knn_k=knn_k)
+               if kruskal else HDBSCAN(min_cluster_size=mcs, min_samples=ms))
         # warm-up fits: the estimator holds one fit's outputs while the next
         # runs, so the pinned host buffers reach their steady state (two sets
         # in PyTorch's caching host allocator) before the timed fits
@@ -305,8 +324,9 @@ def run_gb300(args):
                                torch.device("cuda", local))
         rows_out = est._condensed_tree.shape[0]
         # labels i64, probabilities f32, sorted MST (n-1) x 3 f64, linkage (n-1) x 4 f64,
-        # condensed records 28 B/row, neighbours n x ms i32, core distances f32, selection
-        d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 28 + n * ms * 4 + n * 4)
+        # condensed tree 28 B/row, neighbours n x ms i32, core distances f32 (Kruskal: f64)
+        d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 28 + n * ms * 4
+               + n * (8 if kruskal else 4))
         e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",
                "h2d_bytes_per_step": int(n * d * 4), "d2h_bytes_per_step": int(d2h),
                "s_per_step": round(e2e_s, 4)}
@@ -342,7 +362,13 @@ def _oracle_fit_time(n, nthreads):
 
     X = make_data(n, WORKLOAD["seed"])
     t0 = time.perf_counter()
-    O.fit(X, WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"], mode=0, nthreads=nthreads)
+    if WORKLOAD.get("algorithm") == "kruskal":  # hdbscan.py:306 with algorithm="kruskal"
+        mst, _, _ = O.kruskal_knn(O.build_kdtree(X), WORKLOAD["min_samples"], WORKLOAD["knn_k"],
+                                  mode=0, nthreads=nthreads)
+        O.clusters_from_spanning_tree(mst, WORKLOAD["min_cluster_size"])
+    else:
+        O.fit(X, WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"], mode=0,
+              nthreads=nthreads)
     return time.perf_counter() - t0
 
 
@@ -461,6 +487,8 @@ def main():
             args.n = WORKLOAD["n"]
         global METRIC
         METRIC = f"HDBSCAN fit points/s at {WORKLOAD['n'] // 1_000_000}M x {WORKLOAD['d']}-D"
+        if WORKLOAD.get("algorithm") == "kruskal":
+            METRIC += f" (algorithm='kruskal', knn_k={WORKLOAD['knn_k']})"
         args.workload = "fit"
     if args.impl == "reference":
         run_reference(args)

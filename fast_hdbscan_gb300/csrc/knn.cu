@@ -252,6 +252,7 @@ int dispatch_k(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o,
                int8_t* tie_s, int ios, int iok, cudaStream_t s) {
     if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
     if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
+    if (k <= 24) return launch_knn<DIM, 24>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
     if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
     return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
 }

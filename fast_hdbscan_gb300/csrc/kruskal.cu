@@ -9,16 +9,25 @@
 // points of its components (kruskal.py:723, precomputed.py:308).
 //
 // Here: the spatial index's kNN (rows in caller order), one thread per edge
-// for the weights, a stable LSD radix sort of the valid edges by their
-// float64 bits (non-negative doubles order like their bits), and -- in place
+// for the weights, a stable LSD radix sort of the valid edges, and -- in place
 // of the sequential scan -- Boruvka rounds over the sorted ranks: every
 // component takes its lowest-rank outgoing edge, the picked edges are hooked
-// with a lock-free union-find and intra-component edges leave the active list.
-// Ranks are distinct, so the forest is the one Kruskal accepts (the minimum
-// spanning forest of a strict order is unique); compacting the picked ranks
-// gives Kruskal's acceptance order.  The union-find keeps every root the
+// with a lock-free union-find and edges inside one component leave the active
+// list.  Ranks are distinct, so the forest is the one Kruskal accepts (the
+// minimum spanning forest of a strict order is unique); compacting the picked
+// ranks gives Kruskal's acceptance order.  The union-find keeps every root the
 // smallest point of its component, so the bridges join the roots in index
 // order.
+//
+// Every float64 weight is a monotone image of one float32 value -- without
+// sample weights sqrt(double(max(core2_i, core2_j, rdist_ij))) (core2 the
+// squared core distance, a kNN rdist entry), with them
+// double(max(core_i, core_j, sqrtf(rdist_ij))) -- and distinct float32 values
+// give distinct weights (a correctly rounded double square root keeps the
+// strict order of float32 inputs), so the sort runs on the 32-bit pattern of
+// that value (non-negative floats order like their bits).
+#include <memory>
+
 #include "index.cuh"
 #include "primitives.cuh"
 #include "uf.cuh"
@@ -36,12 +45,15 @@ namespace {
     } while (0)
 
 // kruskal.py:995-1015: float64 core distances from the kNN lists (rows of kq,
-// the point itself first).  min_samples <= 1: zero.
+// the point itself first; min_samples <= 1: zero) and the float32 value the
+// edge keys take the maximum of (the squared core distance).
 __global__ void kr_core_kernel(int64_t n, int kq, int ms, const float* __restrict__ rd,
-                               double* __restrict__ core) {
+                               double* __restrict__ core, float* __restrict__ ck) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    core[i] = ms > 1 ? __dsqrt_rn((double)rd[i * kq + ms]) : 0.0;
+    const float c2 = ms > 1 ? rd[i * kq + ms] : 0.0f;
+    core[i] = ms > 1 ? __dsqrt_rn((double)c2) : 0.0;
+    ck[i] = c2;
 }
 // kruskal.py:981-990 with boruvka.py:528 sample_weight_core_distance: the
 // first list position at which the running float64 weight (the point's own
@@ -49,7 +61,7 @@ __global__ void kr_core_kernel(int64_t n, int kq, int ms, const float* __restric
 // distances are the float32 square roots the reference's tree query returns.
 __global__ void kr_core_w_kernel(int64_t n, int kq, int ms, const float* __restrict__ rd,
                                  const int32_t* __restrict__ ix, const float* __restrict__ w,
-                                 double* __restrict__ core) {
+                                 double* __restrict__ core, float* __restrict__ ck) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double total = 0.0;
@@ -59,43 +71,48 @@ __global__ void kr_core_w_kernel(int64_t n, int kq, int ms, const float* __restr
         total += (double)w[q >= 0 ? q : n - 1];
         ++j;
     }
-    core[i] = (double)__fsqrt_rn(rd[i * kq + (j > 0 ? j - 1 : 0)]);
+    const float c = __fsqrt_rn(rd[i * kq + (j > 0 ? j - 1 : 0)]);
+    core[i] = (double)c;
+    ck[i] = c;
 }
-// kruskal.py:456 _build_mrd_edges_knn and the filter of :1022.  Edge e is the
-// (e % kk)-th neighbour of point e / kk (kk = kq - 1).
+// kruskal.py:456 _build_mrd_edges_knn and the filter of :1022, as each edge's
+// float32 key.  Edge e is the (e % kk)-th neighbour of point e / kk
+// (kk = kq - 1).
 __global__ void kr_edges_kernel(int64_t n, int kq, int weighted, const float* __restrict__ rd,
-                                const int32_t* __restrict__ ix, const double* __restrict__ core,
-                                double* __restrict__ w, uint32_t* __restrict__ flag) {
+                                const int32_t* __restrict__ ix, const float* __restrict__ ck,
+                                uint32_t* __restrict__ key, uint32_t* __restrict__ flag) {
     const int64_t kk = kq - 1;
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n * kk) return;
     const int64_t i = e / kk, jp = e - i * kk;
     const int32_t j = ix[i * kq + jp + 1];
-    double mrd = INFINITY;
+    float v = INFINITY;
     if (j >= 0) {
         const float r = rd[i * kq + jp + 1];
-        const double d = weighted ? (double)__fsqrt_rn(r) : __dsqrt_rn((double)r);
-        mrd = core[i];
-        if (core[j] > mrd) mrd = core[j];
-        if (d > mrd) mrd = d;
+        v = fmaxf(fmaxf(ck[i], ck[j]), weighted ? __fsqrt_rn(r) : r);
     }
-    w[e] = mrd;
-    flag[e] = (j >= 0 && j != (int32_t)i && isfinite(mrd)) ? 1u : 0u;
+    key[e] = __float_as_uint(v);
+    flag[e] = (j >= 0 && j != (int32_t)i && isfinite(v)) ? 1u : 0u;
 }
 __global__ void kr_compact_kernel(int64_t E, const uint32_t* __restrict__ flag,
-                                  const uint32_t* __restrict__ pos, const double* __restrict__ w,
-                                  uint64_t* __restrict__ key, int32_t* __restrict__ eid) {
+                                  const uint32_t* __restrict__ pos, const uint32_t* __restrict__ k0,
+                                  uint32_t* __restrict__ key, int32_t* __restrict__ eid) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E || !flag[e]) return;
-    key[pos[e]] = (uint64_t)__double_as_longlong(w[e]);
+    key[pos[e]] = k0[e];
     eid[pos[e]] = (int32_t)e;
 }
-__device__ __forceinline__ void edge_ends(int64_t e, int kq, const int32_t* __restrict__ ix,
-                                          int32_t* u, int32_t* v) {
-    const int64_t kk = kq - 1;
-    const int64_t i = e / kk;
-    *u = (int32_t)i;
-    *v = ix[i * kq + (e - i * kk) + 1];
+// Endpoints of every sorted edge, and the initial active list (all ranks).
+__global__ void kr_ends_kernel(int64_t m, int kq, const int32_t* __restrict__ eid,
+                               const int32_t* __restrict__ ix, int2* __restrict__ uv,
+                               int32_t* __restrict__ act, int2* __restrict__ act_uv) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    const int64_t kk = kq - 1, e = eid[r], i = e / kk;
+    const int2 p = make_int2((int32_t)i, ix[i * kq + (e - i * kk) + 1]);
+    uv[r] = p;
+    act[r] = (int32_t)r;
+    act_uv[r] = p;
 }
 __global__ void kr_iota_kernel(int32_t* a, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -109,58 +126,60 @@ __global__ void kr_fill_u32_kernel(uint32_t* a, int64_t n, uint32_t v) {
 // ranks come in increasing order, so a component's best is mostly set by its
 // first edge and later ones only read it.
 __global__ void kr_best_kernel(int64_t na, const int32_t* __restrict__ act,
-                               const int32_t* __restrict__ eid, int kq,
-                               const int32_t* __restrict__ ix, int32_t* par,
-                               uint32_t* __restrict__ best, uint32_t* __restrict__ keep) {
+                               const int2* __restrict__ act_uv, int32_t* par,
+                               uint32_t* __restrict__ best) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= na) return;
-    const int32_t r = act[t];
-    int32_t u, v;
-    edge_ends(eid[r], kq, ix, &u, &v);
-    const int32_t cu = uf_find(par, u), cv = uf_find(par, v);
-    keep[t] = cu != cv ? 1u : 0u;
+    const uint32_t r = (uint32_t)act[t];
+    const int2 p = act_uv[t];
+    const int32_t cu = uf_find(par, p.x), cv = uf_find(par, p.y);
     if (cu == cv) return;
-    if ((uint32_t)r < *(volatile uint32_t*)&best[cu]) atomicMin(&best[cu], (uint32_t)r);
-    if ((uint32_t)r < *(volatile uint32_t*)&best[cv]) atomicMin(&best[cv], (uint32_t)r);
+    if (r < *(volatile uint32_t*)&best[cu]) atomicMin(&best[cu], r);
+    if (r < *(volatile uint32_t*)&best[cv]) atomicMin(&best[cv], r);
 }
 // Step 2 (no union yet, so the roots are those of step 1): an edge picked by
 // either of its components is marked with the round.
 __global__ void kr_pick_kernel(int64_t na, const int32_t* __restrict__ act,
-                               const int32_t* __restrict__ eid, int kq,
-                               const int32_t* __restrict__ ix, int32_t* par,
-                               const uint32_t* __restrict__ best,
-                               const uint32_t* __restrict__ keep, int32_t* __restrict__ mark,
+                               const int2* __restrict__ act_uv, int32_t* par,
+                               const uint32_t* __restrict__ best, int32_t* __restrict__ mark,
                                int round, uint32_t* __restrict__ picked) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= na || !keep[t]) return;
-    const int32_t r = act[t];
-    int32_t u, v;
-    edge_ends(eid[r], kq, ix, &u, &v);
-    const int32_t cu = uf_find(par, u), cv = uf_find(par, v);
-    if (best[cu] == (uint32_t)r || best[cv] == (uint32_t)r) {
+    if (t >= na) return;
+    const uint32_t r = (uint32_t)act[t];
+    const int2 p = act_uv[t];
+    const int32_t cu = uf_find(par, p.x), cv = uf_find(par, p.y);
+    if (cu != cv && (best[cu] == r || best[cv] == r)) {
         mark[r] = round;
         atomicAdd(picked, 1u);
     }
 }
 // Step 3: hook the picked edges.
 __global__ void kr_hook_kernel(int64_t na, const int32_t* __restrict__ act,
-                               const int32_t* __restrict__ eid, int kq,
-                               const int32_t* __restrict__ ix, int32_t* par,
+                               const int2* __restrict__ act_uv, int32_t* par,
                                const int32_t* __restrict__ mark, int round) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= na) return;
-    const int32_t r = act[t];
-    if (mark[r] != round) return;
-    int32_t u, v;
-    edge_ends(eid[r], kq, ix, &u, &v);
-    uf_union(par, u, v);
+    if (mark[act[t]] != round) return;
+    const int2 p = act_uv[t];
+    uf_union(par, p.x, p.y);
+}
+// Step 4: edges now inside one component leave the list.
+__global__ void kr_keep_kernel(int64_t na, const int2* __restrict__ act_uv, int32_t* par,
+                               uint32_t* __restrict__ keep) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= na) return;
+    const int2 p = act_uv[t];
+    keep[t] = uf_find(par, p.x) != uf_find(par, p.y) ? 1u : 0u;
 }
 __global__ void kr_scatter_active_kernel(int64_t na, const int32_t* __restrict__ act,
+                                         const int2* __restrict__ act_uv,
                                          const uint32_t* __restrict__ keep,
                                          const uint32_t* __restrict__ pos,
-                                         int32_t* __restrict__ act2) {
+                                         int32_t* __restrict__ act2, int2* __restrict__ act_uv2) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < na && keep[t]) act2[pos[t]] = act[t];
+    if (t >= na || !keep[t]) return;
+    act2[pos[t]] = act[t];
+    act_uv2[pos[t]] = act_uv[t];
 }
 __global__ void kr_mark_flags_kernel(int64_t m, const int32_t* __restrict__ mark,
                                      uint32_t* __restrict__ flag) {
@@ -168,19 +187,17 @@ __global__ void kr_mark_flags_kernel(int64_t m, const int32_t* __restrict__ mark
     if (r < m) flag[r] = mark[r] > 0 ? 1u : 0u;
 }
 // kruskal.py:104-107: picked edges in rank order as (row point, neighbour,
-// weight).
-__global__ void kr_emit_kernel(int64_t m, const uint32_t* __restrict__ flag,
-                               const uint32_t* __restrict__ pos, const int32_t* __restrict__ eid,
-                               const uint64_t* __restrict__ key, int kq,
-                               const int32_t* __restrict__ ix, double* __restrict__ edges) {
+// float64 weight).
+__global__ void kr_emit_kernel(int64_t m, int weighted, const uint32_t* __restrict__ flag,
+                               const uint32_t* __restrict__ pos, const int2* __restrict__ uv,
+                               const uint32_t* __restrict__ key, double* __restrict__ edges) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= m || !flag[r]) return;
-    int32_t u, v;
-    edge_ends(eid[r], kq, ix, &u, &v);
     const int64_t o = pos[r];
-    edges[3 * o + 0] = (double)u;
-    edges[3 * o + 1] = (double)v;
-    edges[3 * o + 2] = __longlong_as_double((long long)key[r]);
+    const float v = __uint_as_float(key[r]);
+    edges[3 * o + 0] = (double)uv[r].x;
+    edges[3 * o + 1] = (double)uv[r].y;
+    edges[3 * o + 2] = weighted ? (double)v : __dsqrt_rn((double)v);
 }
 __global__ void kr_root_flags_kernel(int64_t n, int32_t* par, uint32_t* __restrict__ flag) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,54 +252,62 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
     }
     Stage stage(s, "kruskal_knn");
     Workspace ws(s);
-    float* rd;
+    float *rd, *ck;
     int32_t* ix;
     FHG_TRY(ws.alloc(&rd, (size_t)(n * kq)));
     FHG_TRY(ws.alloc(&ix, (size_t)(n * kq)));
+    FHG_TRY(ws.alloc(&ck, (size_t)n));
     FHG_TRY(index_knn(index, kq, nullptr, nullptr, rd, ix, s));
-    if (weights) LAUNCH(kr_core_w_kernel, n, n, kq, min_samples, rd, ix, weights, core);
-    else LAUNCH(kr_core_kernel, n, n, kq, min_samples, rd, core);
+    if (weights) LAUNCH(kr_core_w_kernel, n, n, kq, min_samples, rd, ix, weights, core, ck);
+    else LAUNCH(kr_core_kernel, n, n, kq, min_samples, rd, core, ck);
     if (neighbors) {
         const int cols = weights ? kq - 1 : (min_samples > 1 ? min_samples : 1);
         LAUNCH(kr_neighbors_kernel, n * cols, n, kq, cols, ix, neighbors);
     }
 
     // ---- valid edges, stably sorted by weight
+    std::unique_ptr<Stage> sub(new Stage(s, "kruskal_edges"));
     const int64_t E = n * kk;
-    double* w;
-    uint32_t *flag, *pos, *cnt;
-    FHG_TRY(ws.alloc(&w, (size_t)E));
+    uint32_t *k0, *flag, *pos, *cnt;
+    FHG_TRY(ws.alloc(&k0, (size_t)E));
     FHG_TRY(ws.alloc(&flag, (size_t)E));
     FHG_TRY(ws.alloc(&pos, (size_t)E));
     FHG_TRY(ws.alloc(&cnt, 2));
-    LAUNCH(kr_edges_kernel, E, n, kq, weights ? 1 : 0, rd, ix, core, w, flag);
+    LAUNCH(kr_edges_kernel, E, n, kq, weights ? 1 : 0, rd, ix, ck, k0, flag);
     FHG_TRY(scan_exclusive_u32(ws, flag, pos, E, cnt));
     uint32_t h_m = 0;
     FHG_CUDA(cudaMemcpyAsync(&h_m, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     FHG_CUDA(cudaStreamSynchronize(s));
     const int64_t m = h_m;
-    uint64_t* key;
+    const size_t mm = (size_t)(m > 0 ? m : 1);
+    uint32_t* key;
     int32_t* eid;
-    FHG_TRY(ws.alloc(&key, (size_t)(m > 0 ? m : 1)));
-    FHG_TRY(ws.alloc(&eid, (size_t)(m > 0 ? m : 1)));
-    LAUNCH(kr_compact_kernel, E, E, flag, pos, w, key, eid);
+    FHG_TRY(ws.alloc(&key, mm));
+    FHG_TRY(ws.alloc(&eid, mm));
+    LAUNCH(kr_compact_kernel, E, E, flag, pos, k0, key, eid);
+    sub.reset(new Stage(s, "kruskal_sort"));
     if (m > 1) {
         Workspace tmp(s);
-        FHG_TRY(radix_sort_u64(tmp, key, eid, m, 0, 64));
+        FHG_TRY(radix_sort_u32(tmp, key, eid, m, 0, 32));
     }
 
     // ---- minimum spanning forest: Boruvka rounds over the ranks
+    sub.reset(new Stage(s, "kruskal_forest"));
     int32_t *par, *act, *act2, *mark;
+    int2 *uv, *act_uv, *act_uv2;
     uint32_t *best, *keep, *picked;
     FHG_TRY(ws.alloc(&par, (size_t)n));
     FHG_TRY(ws.alloc(&best, (size_t)n));
-    FHG_TRY(ws.alloc(&act, (size_t)(m > 0 ? m : 1)));
-    FHG_TRY(ws.alloc(&act2, (size_t)(m > 0 ? m : 1)));
-    FHG_TRY(ws.alloc(&keep, (size_t)(m > 0 ? m : 1)));
-    FHG_TRY(ws.alloc(&mark, (size_t)(m > 0 ? m : 1)));
+    FHG_TRY(ws.alloc(&uv, mm));
+    FHG_TRY(ws.alloc(&act, mm));
+    FHG_TRY(ws.alloc(&act2, mm));
+    FHG_TRY(ws.alloc(&act_uv, mm));
+    FHG_TRY(ws.alloc(&act_uv2, mm));
+    FHG_TRY(ws.alloc(&keep, mm));
+    FHG_TRY(ws.alloc(&mark, mm));
     FHG_TRY(ws.alloc(&picked, 1));
     LAUNCH(kr_iota_kernel, n, par, n);
-    LAUNCH(kr_iota_kernel, m, act, m);
+    LAUNCH(kr_ends_kernel, m, m, kq, eid, ix, uv, act, act_uv);
     if (m > 0) FHG_CUDA(cudaMemsetAsync(mark, 0, sizeof(int32_t) * m, s));
     int64_t na = m;
     for (int round = 1; na > 0; ++round) {
@@ -292,21 +317,23 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
         }
         LAUNCH(kr_fill_u32_kernel, n, best, n, 0xffffffffu);
         FHG_CUDA(cudaMemsetAsync(picked, 0, sizeof(uint32_t), s));
-        LAUNCH(kr_best_kernel, na, na, act, eid, kq, ix, par, best, keep);
-        LAUNCH(kr_pick_kernel, na, na, act, eid, kq, ix, par, best, keep, mark, round, picked);
-        LAUNCH(kr_hook_kernel, na, na, act, eid, kq, ix, par, mark, round);
-        // edges joining one component leave the list (the picked ones next round)
+        LAUNCH(kr_best_kernel, na, na, act, act_uv, par, best);
+        LAUNCH(kr_pick_kernel, na, na, act, act_uv, par, best, mark, round, picked);
+        LAUNCH(kr_hook_kernel, na, na, act, act_uv, par, mark, round);
+        LAUNCH(kr_keep_kernel, na, na, act_uv, par, keep);
         FHG_TRY(scan_exclusive_u32(ws, keep, pos, na, cnt));
-        LAUNCH(kr_scatter_active_kernel, na, na, act, keep, pos, act2);
+        LAUNCH(kr_scatter_active_kernel, na, na, act, act_uv, keep, pos, act2, act_uv2);
         uint32_t h[2] = {0, 0};
         FHG_CUDA(cudaMemcpyAsync(&h[0], picked, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         FHG_CUDA(cudaMemcpyAsync(&h[1], cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         FHG_CUDA(cudaStreamSynchronize(s));
         std::swap(act, act2);
+        std::swap(act_uv, act_uv2);
         na = h[0] == 0 ? 0 : (int64_t)h[1];
     }
 
     // ---- the forest in Kruskal's acceptance order, then the bridges
+    sub.reset(new Stage(s, "kruskal_emit"));
     uint32_t *rflag, *rpos;
     FHG_TRY(ws.alloc(&rflag, (size_t)n));
     FHG_TRY(ws.alloc(&rpos, (size_t)n));
@@ -326,7 +353,7 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
                   (long long)n, (long long)nc);
         return FHG_ERR_NO_CONVERGENCE;
     }
-    if (m > 0) LAUNCH(kr_emit_kernel, m, m, flag, pos, eid, key, kq, ix, edges);
+    if (m > 0) LAUNCH(kr_emit_kernel, m, m, weights ? 1 : 0, flag, pos, uv, key, edges);
     if (nc > 1) LAUNCH(kr_bridge_kernel, n, n, nc, rflag, rpos, nf, edges);
     *n_components = nc;
     return FHG_OK;
