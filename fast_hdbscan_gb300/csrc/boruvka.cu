@@ -293,34 +293,46 @@ __global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
                             int32_t* __restrict__ cand_q, int8_t* __restrict__ exhausted) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    if (exhausted[p]) {
-        cand_w[p] = INFINITY;
-        cand_q[p] = -1;
-        return;
-    }
     const int32_t c = comp[p];
-    const float cp = core2[p];
+    // The previous round's candidate of this point is still an edge out of
+    // its component when its target has not been merged in: it seeds the
+    // point's best (when it beats the kNN seed) and its component's key
+    // before any point searches.  The search still finds every edge within
+    // that bound, so the point's final candidate is its exact best.  (Its
+    // weight equals the core distance only for a target inside the kNN
+    // radius, which the kNN seed has already met, so the seed-finality rule
+    // below is unaffected.)
+    const int32_t oq = cand_q[p];
+    const float ow = cand_w[p];
+    const int32_t oo = (oq >= 0 && comp[oq] != c) ? orig[oq] : -1;
     float bw = INFINITY;
     int32_t bq = -1, bo = INT32_MAX;
-    for (int j = 1; j < k; ++j) {
-        int32_t qs = knn_s[p * k + j];
-        if (qs < 0) break;
-        if (comp[qs] == c) continue;
-        float w = fmaxf(fmaxf(knn_d[p * k + j], cp), core2[qs]);
-        int32_t oq = orig[qs];
-        if (w < bw || (w == bw && oq < bo)) {
-            bw = w;
-            bq = qs;
-            bo = oq;
+    if (!exhausted[p]) {
+        const float cp = core2[p];
+        for (int j = 1; j < k; ++j) {
+            int32_t qs = knn_s[p * k + j];
+            if (qs < 0) break;
+            if (comp[qs] == c) continue;
+            float w = fmaxf(fmaxf(knn_d[p * k + j], cp), core2[qs]);
+            int32_t o = orig[qs];
+            if (w < bw || (w == bw && o < bo)) {
+                bw = w;
+                bq = qs;
+                bo = o;
+            }
         }
+        if (bq < 0) exhausted[p] = 1;  // no other component in the kNN list
+    }
+    if (oo >= 0 && (ow < bw || (ow == bw && oo < bo))) {
+        bw = ow;
+        bq = oq;
+        bo = oo;
     }
     cand_w[p] = bw;
     cand_q[p] = bq;
     if (bq >= 0) {
         unsigned long long key = pack_key(bw, min(orig[p], bo));
         if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
-    } else {
-        exhausted[p] = 1;
     }
 }
 
@@ -828,6 +840,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&nc, (size_t)ix.nnodes));
     FHG_TRY(ws.alloc(&cand_w, (size_t)n));
     FHG_TRY(ws.alloc(&cand_q, (size_t)n));
+    FHG_CUDA(cudaMemsetAsync(cand_q, 0xff, sizeof(int32_t) * n, s));  // no candidate yet (-1)
     int8_t* exhausted;
     FHG_TRY(ws.alloc(&exhausted, (size_t)n));
     FHG_CUDA(cudaMemsetAsync(exhausted, 0, (size_t)n, s));
