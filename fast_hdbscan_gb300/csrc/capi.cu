@@ -232,6 +232,32 @@ FHG_API int fhg_index_kruskal_knn(fhg_index* index, int32_t min_samples, int32_t
     return FHG_OK;
 }
 
+FHG_API int fhg_precomputed_mst(const int32_t* rows_dev, const int32_t* cols_dev,
+                                const double* data_dev, int64_t nnz, int64_t n,
+                                int32_t min_samples, int32_t algorithm, double* edges_dev,
+                                int32_t* neighbors_dev, double* core_dev,
+                                int64_t* n_components_host, void* stream) {
+    if (n < 0 || nnz < 0 || (nnz > 0 && (!rows_dev || !cols_dev || !data_dev)) ||
+        (n > 0 && (!neighbors_dev || !core_dev)) || (n > 1 && !edges_dev)) {
+        set_error("fhg_precomputed_mst: invalid sizes or null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (algorithm != 0 && algorithm != 1) {
+        set_error("fhg_precomputed_mst: algorithm must be 0 (boruvka) or 1 (kruskal)");
+        return FHG_ERR_INVALID;
+    }
+    if (n > 0x7fffffffLL) {
+        set_error("fhg_precomputed_mst: %lld points exceed int32 indices", (long long)n);
+        return FHG_ERR_UNSUPPORTED;
+    }
+    int64_t nc = 0;
+    FHG_TRY(precomputed_mst(rows_dev, cols_dev, data_dev, nnz, n,
+                            min_samples > 0 ? min_samples : 1, edges_dev, neighbors_dev,
+                            core_dev, &nc, as_stream(stream)));
+    if (n_components_host) *n_components_host = nc;
+    return FHG_OK;
+}
+
 // ------------------------------------------------------------- tree passes
 namespace fhg {
 namespace capi {

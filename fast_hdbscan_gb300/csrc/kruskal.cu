@@ -29,6 +29,7 @@
 #include <memory>
 
 #include "index.cuh"
+#include "mst.cuh"
 #include "primitives.cuh"
 #include "uf.cuh"
 
@@ -187,17 +188,23 @@ __global__ void kr_mark_flags_kernel(int64_t m, const int32_t* __restrict__ mark
     if (r < m) flag[r] = mark[r] > 0 ? 1u : 0u;
 }
 // kruskal.py:104-107: picked edges in rank order as (row point, neighbour,
-// float64 weight).
+// float64 weight); the weight is the rank's float32 key (kNN graph) or its
+// float64 weight.
 __global__ void kr_emit_kernel(int64_t m, int weighted, const uint32_t* __restrict__ flag,
                                const uint32_t* __restrict__ pos, const int2* __restrict__ uv,
-                               const uint32_t* __restrict__ key, double* __restrict__ edges) {
+                               const uint32_t* __restrict__ key, const double* __restrict__ w64,
+                               double* __restrict__ edges) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= m || !flag[r]) return;
     const int64_t o = pos[r];
-    const float v = __uint_as_float(key[r]);
     edges[3 * o + 0] = (double)uv[r].x;
     edges[3 * o + 1] = (double)uv[r].y;
-    edges[3 * o + 2] = weighted ? (double)v : __dsqrt_rn((double)v);
+    if (w64) {
+        edges[3 * o + 2] = w64[r];
+    } else {
+        const float v = __uint_as_float(key[r]);
+        edges[3 * o + 2] = weighted ? (double)v : __dsqrt_rn((double)v);
+    }
 }
 __global__ void kr_root_flags_kernel(int64_t n, int32_t* par, uint32_t* __restrict__ flag) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -291,11 +298,23 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
         FHG_TRY(radix_sort_u32(tmp, key, eid, m, 0, 32));
     }
 
+    sub.reset();
+    FHG_TRY(sorted_forest_edges(ws, n, m, kq, eid, ix, nullptr, key, weights ? 1 : 0, edges,
+                                n_components));
+    return FHG_OK;
+}
+
+int sorted_forest_edges(Workspace& ws, int64_t n, int64_t m, int kq, const int32_t* eid,
+                        const int32_t* ix, const int2* uv_in, const uint32_t* key32,
+                        int key_weighted, double* edges, int64_t* n_components,
+                        const double* w64) {
+    cudaStream_t s = ws.stream();
+    const size_t mm = (size_t)(m > 0 ? m : 1);
     // ---- minimum spanning forest: Boruvka rounds over the ranks
-    sub.reset(new Stage(s, "kruskal_forest"));
+    std::unique_ptr<Stage> sub(new Stage(s, "kruskal_forest"));
     int32_t *par, *act, *act2, *mark;
     int2 *uv, *act_uv, *act_uv2;
-    uint32_t *best, *keep, *picked;
+    uint32_t *best, *keep, *picked, *pos, *cnt;
     FHG_TRY(ws.alloc(&par, (size_t)n));
     FHG_TRY(ws.alloc(&best, (size_t)n));
     FHG_TRY(ws.alloc(&uv, mm));
@@ -304,10 +323,18 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
     FHG_TRY(ws.alloc(&act_uv, mm));
     FHG_TRY(ws.alloc(&act_uv2, mm));
     FHG_TRY(ws.alloc(&keep, mm));
+    FHG_TRY(ws.alloc(&pos, mm));
     FHG_TRY(ws.alloc(&mark, mm));
     FHG_TRY(ws.alloc(&picked, 1));
+    FHG_TRY(ws.alloc(&cnt, 2));
     LAUNCH(kr_iota_kernel, n, par, n);
-    LAUNCH(kr_ends_kernel, m, m, kq, eid, ix, uv, act, act_uv);
+    if (uv_in) {
+        FHG_CUDA(cudaMemcpyAsync(uv, uv_in, sizeof(int2) * m, cudaMemcpyDeviceToDevice, s));
+        FHG_CUDA(cudaMemcpyAsync(act_uv, uv_in, sizeof(int2) * m, cudaMemcpyDeviceToDevice, s));
+        LAUNCH(kr_iota_kernel, m, act, m);
+    } else {
+        LAUNCH(kr_ends_kernel, m, m, kq, eid, ix, uv, act, act_uv);
+    }
     if (m > 0) FHG_CUDA(cudaMemsetAsync(mark, 0, sizeof(int32_t) * m, s));
     int64_t na = m;
     for (int round = 1; na > 0; ++round) {
@@ -334,11 +361,12 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
 
     // ---- the forest in Kruskal's acceptance order, then the bridges
     sub.reset(new Stage(s, "kruskal_emit"));
-    uint32_t *rflag, *rpos;
+    uint32_t *flag, *rflag, *rpos;
+    FHG_TRY(ws.alloc(&flag, mm));
     FHG_TRY(ws.alloc(&rflag, (size_t)n));
     FHG_TRY(ws.alloc(&rpos, (size_t)n));
     uint32_t h_f = 0, h_c = 0;
-    if (m > 0) {  // flag and pos (E >= m entries) are free again
+    if (m > 0) {
         LAUNCH(kr_mark_flags_kernel, m, m, mark, flag);
         FHG_TRY(scan_exclusive_u32(ws, flag, pos, m, cnt));
         FHG_CUDA(cudaMemcpyAsync(&h_f, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -353,7 +381,7 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
                   (long long)n, (long long)nc);
         return FHG_ERR_NO_CONVERGENCE;
     }
-    if (m > 0) LAUNCH(kr_emit_kernel, m, m, weights ? 1 : 0, flag, pos, uv, key, edges);
+    if (m > 0) LAUNCH(kr_emit_kernel, m, m, key_weighted, flag, pos, uv, key32, w64, edges);
     if (nc > 1) LAUNCH(kr_bridge_kernel, n, n, nc, rflag, rpos, nf, edges);
     *n_components = nc;
     return FHG_OK;

@@ -33,6 +33,26 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
                     double* edges, int32_t* neighbors, double* core, int64_t* n_components,
                     cudaStream_t s);
 
+// The minimum spanning forest of n points over m edges given in rank order
+// (strictly increasing weight), in Kruskal's acceptance order, then +inf
+// bridges between consecutive component representatives (each component's
+// smallest point): (n-1) x 3 float64 rows (src, dst, weight).  Edge r's
+// endpoints are uv[r], or -- with uv NULL -- point eid[r] / (kq-1) and its
+// kNN column eid[r] % (kq-1) + 1 in the rows ix of kq entries.  Weights: w64
+// when given, else the float32 keys key32 (their square roots in float64
+// unless key_weighted).
+int sorted_forest_edges(Workspace& ws, int64_t n, int64_t m, int kq, const int32_t* eid,
+                        const int32_t* ix, const int2* uv, const uint32_t* key32,
+                        int key_weighted, double* edges, int64_t* n_components,
+                        const double* w64 = nullptr);
+
+// Minimum spanning forest of a precomputed sparse graph given as COO entries
+// (precomputed.py:479 / :410; see precomputed.cu): edges (n-1) x 3 float64,
+// neighbors n x max(1, min_samples) int32 (-1 padded), core n float64.
+int precomputed_mst(const int32_t* rows, const int32_t* cols, const double* data, int64_t nnz,
+                    int64_t n, int min_samples, double* edges, int32_t* neighbors, double* core,
+                    int64_t* n_components, cudaStream_t s);
+
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
                 float* core_o, int32_t* nbr_o, const float* weights = nullptr,
                 int weighted_k = 0, bool any_order = false);

@@ -182,17 +182,24 @@ def _validate_params(min_samples, min_cluster_size, cluster_selection_epsilon,
 
 def _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data=None,
                         cannot_link=None, cannot_link_groups=None, knn_k=None):
-    if metric != "euclidean":
-        raise NotImplementedError(f"metric={metric!r} is outside the GPU engine's Euclidean path")
+    if metric not in ("euclidean", "precomputed"):
+        raise NotImplementedError(f"metric={metric!r} is outside the GPU engine's Euclidean and "
+                                  "precomputed paths")
     if algorithm not in ("boruvka", "kruskal"):
         raise ValueError("algorithm must be 'boruvka' or 'kruskal'. Got: %s" % algorithm)
     has_cl = cannot_link is not None or cannot_link_groups is not None
     if has_cl and algorithm != "kruskal":
         raise ValueError("cannot_link constraints are only supported with algorithm='kruskal'. "
                          "Got algorithm=%r." % algorithm)
+    if has_cl:
+        raise NotImplementedError("cannot-link constraints are not on the GPU path")
+    if metric == "precomputed":
+        if sample_weights is not None:
+            raise NotImplementedError("sample_weights is not supported with metric='precomputed'.")
+        if semi_supervised:
+            raise NotImplementedError("semi-supervised selection is outside the GPU engine's path")
+        return
     if algorithm == "kruskal":
-        if has_cl:
-            raise NotImplementedError("cannot-link constraints are not on the GPU path")
         if knn_k is None:
             raise NotImplementedError(
                 "algorithm='kruskal' with knn_k=None (exact MST from the full pairwise distance "
@@ -425,6 +432,17 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
         return _degenerate(data.shape[0], return_trees)
     _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data, cannot_link,
                         cannot_link_groups, knn_k)
+    if metric == "precomputed":  # hdbscan.py:306-337 on a precomputed sparse graph
+        ms = min_cluster_size if min_samples is None else min_samples
+        mst, neighbors, core = compute_minimum_spanning_tree(
+            data, min_samples=ms, metric="precomputed", algorithm=algorithm)
+        result = (*clusters_from_spanning_tree(
+            mst, min_cluster_size=min_cluster_size,
+            cluster_selection_method=cluster_selection_method,
+            max_cluster_size=max_cluster_size, allow_single_cluster=allow_single_cluster,
+            cluster_selection_epsilon=cluster_selection_epsilon,
+            cluster_selection_persistence=cluster_selection_persistence), neighbors, core)
+        return result[: (None if return_trees else 2)]
     if algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
         fr = gpu_fit_kruskal(data, min_samples, min_cluster_size, knn_k,
                              cluster_selection_method, max_cluster_size, allow_single_cluster,
@@ -450,6 +468,15 @@ def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, rep
     if cannot_link is not None and cannot_link_groups is not None:
         raise ValueError("cannot_link and cannot_link_groups are mutually exclusive. "
                          "Provide one or the other, not both.")
+    if metric == "precomputed":  # hdbscan.py:427-442
+        _unsupported_routes(metric, algorithm, sample_weights, False, None, cannot_link,
+                            cannot_link_groups, knn_k)
+        from .precomputed import (compute_mst_from_precomputed_sparse,
+                                  compute_mst_from_precomputed_sparse_kruskal)
+
+        if algorithm == "kruskal":
+            return compute_mst_from_precomputed_sparse_kruskal(data, min_samples)
+        return compute_mst_from_precomputed_sparse(data, min_samples)
     data = check_array(data)
     _unsupported_routes(metric, algorithm, sample_weights, False, data, cannot_link,
                         cannot_link_groups, knn_k)
@@ -545,8 +572,23 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
 
     def fit(self, X, y=None, sample_weight=None, **fit_params):
         """hdbscan.py:686: validation, non-finite row filter, GPU fit, remap."""
-        if self.metric == "precomputed" or self.semi_supervised:
-            raise NotImplementedError("precomputed and semi-supervised fits are not on the GPU path")
+        if self.semi_supervised:
+            raise NotImplementedError("semi-supervised fits are not on the GPU path")
+        if self.metric == "precomputed":  # hdbscan.py:688-697: a scipy sparse graph
+            from .precomputed import validate_precomputed_sparse_graph
+
+            validate_precomputed_sparse_graph(X)
+            if sample_weight is not None:
+                raise NotImplementedError(
+                    "sample_weights is not supported with metric='precomputed'.")
+            self._raw_data = None
+            self._all_finite = True
+            kwargs = self.get_params()
+            (self.labels_, self.probabilities_, self._single_linkage_tree,
+             self._condensed_tree, self._min_spanning_tree, self._neighbors,
+             self._core_distances) = _fast_hdbscan(X, None, return_trees=True, **kwargs)
+            self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
+            return self
         if _is_tensor(X):
             Xd, finite = _tensor_input(X)
             if finite and sample_weight is None:

@@ -122,6 +122,28 @@ int fhg_index_kruskal_knn(fhg_index* index, int32_t min_samples, int32_t query_k
                           int32_t* neighbors_dev, double* core_dev, int64_t* n_components_host,
                           void* stream);
 
+/* Replaces precomputed.py:479 compute_mst_from_precomputed_sparse_kruskal
+ * (algorithm 1) and :410 compute_mst_from_precomputed_sparse (algorithm 0),
+ * without cannot-link constraints: the metric="precomputed" back-ends of
+ * hdbscan.py:427.  Input: a sparse graph as COO entries (the reference's
+ * X.tocoo(); finite, non-negative float64 weights; duplicates and the
+ * diagonal allowed).  The graph is symmetrised by the least weight per pair
+ * without its diagonal, core distances are the min_samples-th smallest
+ * weight of each row, and the minimum spanning forest of the float64
+ * mutual-reachability weights comes in Kruskal's acceptance order (weight,
+ * then position in the symmetrised CSR), followed by +inf bridges between
+ * consecutive component representatives (each component's smallest point).
+ * Both algorithms return that forest: the reference's Boruvka finds a forest
+ * of the same weights whose equal-weight choices and order are its own.
+ *   edges_dev      (n-1) x 3 float64 (src, dst, weight)
+ *   neighbors_dev  n x max(1, min_samples) int32, -1 where a row is short
+ *   core_dev       n float64 (+inf for rows shorter than min_samples)
+ *   n_components_host optional: components of the graph. */
+int fhg_precomputed_mst(const int32_t* rows_dev, const int32_t* cols_dev, const double* data_dev,
+                        int64_t nnz, int64_t n, int32_t min_samples, int32_t algorithm,
+                        double* edges_dev, int32_t* neighbors_dev, double* core_dev,
+                        int64_t* n_components_host, void* stream);
+
 /* Replaces the np.lexsort((mst[:,1], mst[:,0], mst[:,2])) of hdbscan.py:511:
  * rows of an m x 3 float64 edge list ordered by (weight, src, dst). */
 int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream);

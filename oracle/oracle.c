@@ -1495,3 +1495,145 @@ int64_t orc_kruskal_knn(const float* rdist, const int32_t* idx, int64_t n, int64
     free(rep); free(rank); free(pred); free(order); free(col); free(row); free(w); free(dist);
     return n_mst;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Precomputed sparse graphs: precomputed.py:479                               */
+/* compute_mst_from_precomputed_sparse_kruskal (no cannot-link constraints):   */
+/* :70 _symmetrize_min_csr, :148 _core_distances_csr, kruskal.py:755           */
+/* kruskal_mst_from_csr (:421 _compute_mrd_csr_flat), :723 _finish_mst.        */
+/* ------------------------------------------------------------------------- */
+
+typedef struct { int32_t u, v; double d; int64_t pos; } pc_ent;
+static int cmp_pc_uv(const void* a, const void* b) { /* lexsort((v, u)), stable */
+    const pc_ent *x = (const pc_ent*)a, *y = (const pc_ent*)b;
+    if (x->u != y->u) return x->u < y->u ? -1 : 1;
+    if (x->v != y->v) return x->v < y->v ? -1 : 1;
+    return (x->pos > y->pos) - (x->pos < y->pos);
+}
+static int cmp_pc_row(const void* a, const void* b) { /* argsort(rows, kind="stable") */
+    const pc_ent *x = (const pc_ent*)a, *y = (const pc_ent*)b;
+    if (x->u != y->u) return x->u < y->u ? -1 : 1;
+    return (x->pos > y->pos) - (x->pos < y->pos);
+}
+static const double* g_pc_d;
+static int cmp_pc_val(const void* a, const void* b) { /* by value, then position */
+    const int64_t i = *(const int64_t*)a, j = *(const int64_t*)b;
+    if (g_pc_d[i] != g_pc_d[j]) return g_pc_d[i] < g_pc_d[j] ? -1 : 1;
+    return (i > j) - (i < j);
+}
+
+int64_t orc_precomputed_kruskal(const int32_t* rows, const int32_t* cols, const double* data,
+                                int64_t nnz, int64_t n, int64_t min_samples, double* edges,
+                                int32_t* neighbors, double* core) {
+    /* _symmetrize_min_csr: min weight per undirected pair, no diagonal */
+    pc_ent* e = (pc_ent*)malloc(sizeof(pc_ent) * (size_t)(nnz > 0 ? nnz : 1));
+    int64_t m0 = 0;
+    for (int64_t t = 0; t < nnz; ++t) {
+        if (rows[t] == cols[t]) continue;
+        e[m0].u = rows[t] < cols[t] ? rows[t] : cols[t];
+        e[m0].v = rows[t] < cols[t] ? cols[t] : rows[t];
+        e[m0].d = data[t];
+        e[m0].pos = m0;
+        ++m0;
+    }
+    qsort(e, (size_t)m0, sizeof(pc_ent), cmp_pc_uv);
+    int64_t m = 0;
+    for (int64_t t = 0; t < m0; ++t) {
+        if (m > 0 && e[m - 1].u == e[t].u && e[m - 1].v == e[t].v) {
+            if (e[t].d < e[m - 1].d) e[m - 1].d = e[t].d; /* np.minimum.reduceat */
+        } else {
+            e[m++] = e[t];
+        }
+    }
+    const int64_t M = 2 * m;
+    pc_ent* sym = (pc_ent*)malloc(sizeof(pc_ent) * (size_t)(M > 0 ? M : 1));
+    for (int64_t t = 0; t < m; ++t) {
+        sym[t].u = e[t].u; sym[t].v = e[t].v; sym[t].d = e[t].d; sym[t].pos = t;
+        sym[m + t].u = e[t].v; sym[m + t].v = e[t].u; sym[m + t].d = e[t].d; sym[m + t].pos = m + t;
+    }
+    qsort(sym, (size_t)M, sizeof(pc_ent), cmp_pc_row);
+    int64_t* indptr = (int64_t*)calloc((size_t)(n + 1), sizeof(int64_t));
+    for (int64_t t = 0; t < M; ++t) indptr[sym[t].u + 1] += 1;
+    for (int64_t i = 0; i < n; ++i) indptr[i + 1] += indptr[i];
+    double* sd = (double*)malloc(sizeof(double) * (size_t)(M > 0 ? M : 1));
+    int32_t* sc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(M > 0 ? M : 1));
+    for (int64_t t = 0; t < M; ++t) { sd[t] = sym[t].d; sc[t] = sym[t].v; }
+    /* _core_distances_csr: rows ordered by weight (ties by position) */
+    const int64_t k = min_samples > 1 ? min_samples : 1;
+    int64_t* order = (int64_t*)malloc(sizeof(int64_t) * (size_t)(M > 0 ? M : 1));
+    g_pc_d = sd;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t s0 = indptr[i], deg = indptr[i + 1] - s0;
+        for (int64_t j = 0; j < k; ++j) neighbors[i * k + j] = -1;
+        core[i] = 0.0;
+        if (deg == 0) {
+            if (min_samples > 1) core[i] = INFINITY;
+            continue;
+        }
+        for (int64_t j = 0; j < deg; ++j) order[j] = s0 + j;
+        qsort(order, (size_t)deg, sizeof(int64_t), cmp_pc_val);
+        const int64_t fill = k < deg ? k : deg;
+        for (int64_t j = 0; j < fill; ++j) neighbors[i * k + j] = sc[order[j]];
+        if (min_samples > 1) core[i] = deg >= min_samples ? sd[order[min_samples - 1]] : INFINITY;
+    }
+    /* kruskal.py:421 _compute_mrd_csr_flat, stable argsort, :32 _kruskal_core */
+    double* w = (double*)malloc(sizeof(double) * (size_t)(M > 0 ? M : 1));
+    for (int64_t i = 0; i < n; ++i) {
+        for (int64_t p = indptr[i]; p < indptr[i + 1]; ++p) {
+            double mrd = core[i];
+            if (core[sc[p]] > mrd) mrd = core[sc[p]];
+            if (sd[p] > mrd) mrd = sd[p];
+            w[p] = mrd;
+        }
+    }
+    for (int64_t p = 0; p < M; ++p) order[p] = p;
+    g_pc_d = w;
+    qsort(order, (size_t)M, sizeof(int64_t), cmp_pc_val);
+    int32_t* pred = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    int32_t* rank = (int32_t*)calloc((size_t)(n > 0 ? n : 1), sizeof(int32_t));
+    for (int64_t i = 0; i < n; ++i) pred[i] = (int32_t)i;
+    int64_t n_mst = 0;
+    for (int64_t t = 0; t < M && n_mst < n - 1; ++t) {
+        const int64_t p = order[t];
+        const int32_t u = sym[p].u, v = sc[p];
+        if (u == v) continue;
+        int32_t ru = u, rv = v;
+        while (pred[ru] != ru) ru = pred[ru];
+        for (int32_t c = u; c != ru;) { const int32_t nx = pred[c]; pred[c] = ru; c = nx; }
+        while (pred[rv] != rv) rv = pred[rv];
+        for (int32_t c = v; c != rv;) { const int32_t nx = pred[c]; pred[c] = rv; c = nx; }
+        if (ru != rv) {
+            edges[3 * n_mst + 0] = (double)u;
+            edges[3 * n_mst + 1] = (double)v;
+            edges[3 * n_mst + 2] = w[p];
+            ++n_mst;
+            if (rank[ru] > rank[rv]) pred[rv] = ru;
+            else if (rank[ru] < rank[rv]) pred[ru] = rv;
+            else { pred[rv] = ru; rank[ru] += 1; }
+        }
+    }
+    /* _finish_mst: +inf bridges between the smallest points of the components */
+    int32_t* rep = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    for (int64_t i = 0; i < n; ++i) rep[i] = INT32_MAX;
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t r = (int32_t)i;
+        while (pred[r] != r) r = pred[r];
+        if ((int32_t)i < rep[r]) rep[r] = (int32_t)i;
+    }
+    int64_t prev = -1;
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t r = (int32_t)i;
+        while (pred[r] != r) r = pred[r];
+        if (rep[r] != (int32_t)i) continue;
+        if (prev >= 0) {
+            edges[3 * n_mst + 0] = (double)prev;
+            edges[3 * n_mst + 1] = (double)i;
+            edges[3 * n_mst + 2] = INFINITY;
+            ++n_mst;
+        }
+        prev = i;
+    }
+    free(rep); free(rank); free(pred); free(w); free(order); free(sc); free(sd); free(indptr);
+    free(sym); free(e);
+    return n_mst;
+}

@@ -106,6 +106,17 @@ int64_t orc_kruskal_knn(const float* rdist, const int32_t* idx, int64_t n, int64
                         int64_t min_samples, const float* weights, double* edges,
                         double* core);
 
+/* precomputed.py:479 compute_mst_from_precomputed_sparse_kruskal without
+ * cannot-link constraints, on a COO graph (rows, cols, float64 data; the
+ * reference's X.tocoo()): the min-symmetrised graph without its diagonal,
+ * core distances = the min_samples-th smallest weight of a row (rows ordered
+ * by weight, ties by position), float64 mutual-reachability weights, Kruskal
+ * with +inf bridges.  neighbors: n x max(1, min_samples) (-1 padded).
+ * Returns the edge count (n - 1). */
+int64_t orc_precomputed_kruskal(const int32_t* rows, const int32_t* cols, const double* data,
+                                int64_t nnz, int64_t n, int64_t min_samples, double* edges,
+                                int32_t* neighbors, double* core);
+
 #ifdef __cplusplus
 }
 #endif

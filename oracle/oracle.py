@@ -56,6 +56,8 @@ def lib():
         L.orc_get_point_membership_strength_vector.argtypes = [
             _P, _P, _P, _P, _I64, _P, _I64, _P, _I64, _P]
         L.orc_get_cluster_labelling_at_cut.argtypes = [_P, _I64, _D, _I64, _P]
+        L.orc_precomputed_kruskal.restype = _I64
+        L.orc_precomputed_kruskal.argtypes = [_P, _P, _P, _I64, _I64, _I64, _P, _P, _P]
         L.orc_kruskal_knn.restype = _I64
         L.orc_kruskal_knn.argtypes = [_P, _P, _I64, _I64, _I64, _P, _P, _P]
         _lib = L
@@ -162,6 +164,24 @@ def kruskal_knn(tree, min_samples, knn_k, mode=0, nthreads=1, sample_weights=Non
     else:
         nbrs = ix[:, 1:2]
     return edges[:m], np.ascontiguousarray(nbrs), core
+
+
+def precomputed_kruskal(X, min_samples):
+    """precomputed.py:479 compute_mst_from_precomputed_sparse_kruskal (no
+    cannot-link constraints) on a scipy sparse matrix -> (mst_edges,
+    neighbors, core_distances)."""
+    coo = X.tocoo()
+    n = X.shape[0]
+    rows = np.ascontiguousarray(coo.row, np.int32)
+    cols = np.ascontiguousarray(coo.col, np.int32)
+    data = np.ascontiguousarray(coo.data, np.float64)
+    k = max(1, int(min_samples))
+    edges = np.zeros((max(n - 1, 0), 3), np.float64)
+    nbrs = np.empty((n, k), np.int32)
+    core = np.empty(n, np.float64)
+    m = lib().orc_precomputed_kruskal(_p(rows), _p(cols), _p(data), len(data), n, min_samples,
+                                      _p(edges), _p(nbrs), _p(core))
+    return edges[:m], nbrs, core
 
 
 def sort_mst(mst):

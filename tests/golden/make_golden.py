@@ -273,6 +273,84 @@ def kruskal_fixtures(only=None):
               f"clusters={len(set(labels.tolist()) - {-1})} {time.time() - t0:.1f}s")
 
 
+def _knn_graph(X, k, seed):
+    """A directed kNN distance graph (float64 CSR, asymmetric), as a user
+    would build one for metric="precomputed"."""
+    import scipy.sparse
+    from scipy.spatial import cKDTree
+
+    X = np.asarray(X, np.float64)
+    d, ix = cKDTree(X).query(X, k=k + 1)
+    n = X.shape[0]
+    rows = np.repeat(np.arange(n), k)
+    return scipy.sparse.csr_matrix((d[:, 1:].ravel(), (rows, ix[:, 1:].ravel())), shape=(n, n))
+
+
+def _blob_graph_disconnected():
+    import scipy.sparse
+
+    g1 = _knn_graph(synthetic.blobs_2d(600, seed=41), 6, 0)
+    g2 = _knn_graph(synthetic.blobs_2d(400, seed=42) + 100.0, 6, 0)
+    return scipy.sparse.block_diag([g1, g2], format="csr")
+
+
+def _coo_with_duplicates():
+    """Duplicate (i, j) entries, both orientations, explicit zeros and a
+    diagonal: the min-symmetrisation keeps the least weight per pair."""
+    import scipy.sparse
+
+    rng = np.random.default_rng(43)
+    n, m = 300, 2400
+    rows = rng.integers(0, n, m)
+    cols = rng.integers(0, n, m)
+    data = rng.random(m) * 10.0
+    # explicit zeros on pairs of distinct points: no row holds two equal
+    # weights (the reference orders a row with np.argsort's default sort, whose
+    # order of equal weights is not specified)
+    rows = np.concatenate([rows, np.arange(8)])
+    cols = np.concatenate([cols, 100 + np.arange(8)])
+    data = np.concatenate([data, np.zeros(8)])
+    return scipy.sparse.coo_matrix((data, (rows, cols)), shape=(n, n))
+
+
+PRECOMPUTED_CASES = {
+    # name: (graph factory, min_samples, min_cluster_size, algorithm)
+    "pc_knn3d_kr": (lambda: _knn_graph(synthetic.varying_density(3000, seed=44), 10, 0), 5, 30,
+                    "kruskal"),
+    "pc_knn3d_bo": (lambda: _knn_graph(synthetic.varying_density(3000, seed=44), 10, 0), 5, 30,
+                    "boruvka"),
+    "pc_disconnected_kr": (_blob_graph_disconnected, 3, 20, "kruskal"),
+    "pc_disconnected_bo": (_blob_graph_disconnected, 3, 20, "boruvka"),
+    "pc_coo_dups_kr": (_coo_with_duplicates, 1, 5, "kruskal"),
+}
+
+
+def precomputed_fixtures(only=None):
+    """metric="precomputed" on scipy sparse graphs (precomputed.py:410 Boruvka,
+    :479 Kruskal), from the reference's public API."""
+    from fast_hdbscan.hdbscan import compute_minimum_spanning_tree, fast_hdbscan
+
+    for name, (factory, ms, mcs, algo) in PRECOMPUTED_CASES.items():
+        if only and name not in only:
+            continue
+        G = factory()
+        t0 = time.time()
+        mst, nbrs, core = compute_minimum_spanning_tree(G, min_samples=ms, metric="precomputed",
+                                                        algorithm=algo)
+        labels, probs = fast_hdbscan(G, min_samples=ms, min_cluster_size=mcs,
+                                     metric="precomputed", algorithm=algo)
+        coo = G.tocoo()
+        out = dict(rows=np.asarray(coo.row, np.int32), cols=np.asarray(coo.col, np.int32),
+                   data=np.asarray(coo.data, np.float64), n=np.int64(G.shape[0]),
+                   min_samples=np.int64(ms), min_cluster_size=np.int64(mcs),
+                   algorithm=np.array(algo), mst=np.asarray(mst, np.float64),
+                   neighbors=np.asarray(nbrs, np.int32), core=np.asarray(core, np.float64),
+                   labels=np.asarray(labels, np.int64), probabilities=np.asarray(probs))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(f"{name}: n={G.shape[0]} nnz={G.nnz} bridges={int(np.isinf(mst[:, 2]).sum())} "
+              f"clusters={len(set(labels.tolist()) - {-1})} {time.time() - t0:.1f}s")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -281,11 +359,16 @@ def main():
                     help="only add the DBSCAN-cut fields to existing fixtures")
     ap.add_argument("--kruskal-only", action="store_true",
                     help="only write the kNN-graph Kruskal fixtures")
+    ap.add_argument("--precomputed-only", action="store_true",
+                    help="only write the metric='precomputed' fixtures")
     args = ap.parse_args()
     sys.path.insert(1, args.reference)
     import fast_hdbscan  # noqa: F401
     if args.kruskal_only:
         kruskal_fixtures(args.only)
+        return
+    if args.precomputed_only:
+        precomputed_fixtures(args.only)
         return
     for name, (factory, kwargs) in CASES.items():
         if args.only and name not in args.only:
@@ -296,6 +379,7 @@ def main():
     if not args.only:
         function_fixtures()
         kruskal_fixtures()
+        precomputed_fixtures()
 
 
 if __name__ == "__main__":

@@ -18,8 +18,11 @@ from oracle import oracle as O
 # fit fixtures; fn_*.npz hold function-level cases, kr_*.npz the kNN-graph
 # Kruskal back-end (algorithm="kruskal")
 FIXTURES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("fn_", "kr_")))
+                  if not os.path.basename(p).startswith(("fn_", "kr_", "pc_")))
 KRUSKAL = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "kr_*.npz")))
+# metric="precomputed" on sparse graphs (precomputed.py:410 Boruvka, :479 Kruskal)
+PRECOMPUTED = sorted(os.path.basename(p)[:-4]
+                     for p in glob.glob(os.path.join(GOLDEN, "pc_*.npz")))
 # The reference indexes knn[-1] when min_samples >= n (k exceeds the point
 # count); its MST for that fixture has edges to "point -1".  Only its labels
 # and probabilities (all noise) are meaningful there.
@@ -170,3 +173,42 @@ def test_oracle_kruskal_knn_bitexact(name):
                                                       sample_weights=w)
     np.testing.assert_array_equal(labels, g["labels"])
     np.testing.assert_array_equal(probs, g["probabilities"])
+
+
+@pytest.mark.parametrize("name", PRECOMPUTED)
+def test_oracle_precomputed_bitexact(name):
+    """precomputed.py:479 (algorithm="kruskal"): MST edges in acceptance order
+    with their bridges, neighbours and core distances equal the reference's.
+    precomputed.py:410 (algorithm="boruvka"): its float32 Boruvka finds a
+    spanning forest of the same weights (restored to the same float64 values)
+    -- mutual-reachability weights tie wherever a core distance dominates, and
+    its tie choices are its own -- in another order.  Labels and
+    probabilities equal the reference's for both."""
+    import scipy.sparse
+
+    g = _load(name)
+    n = int(g["n"])
+    G = scipy.sparse.coo_matrix((g["data"], (g["rows"], g["cols"])), shape=(n, n))
+    ms, mcs = int(g["min_samples"]), int(g["min_cluster_size"])
+    mst, nbrs, core = O.precomputed_kruskal(G, ms)
+    np.testing.assert_array_equal(nbrs, g["neighbors"])
+    np.testing.assert_array_equal(core, g["core"])
+    if str(g["algorithm"]) == "kruskal":
+        np.testing.assert_array_equal(mst, g["mst"])
+    else:
+        np.testing.assert_array_equal(np.sort(mst[:, 2]), np.sort(g["mst"][:, 2]))
+    labels, probs, *_ = O.clusters_from_spanning_tree(mst, min_cluster_size=mcs)
+    if str(g["algorithm"]) == "kruskal":
+        np.testing.assert_array_equal(labels, g["labels"])
+        np.testing.assert_array_equal(probs, g["probabilities"])
+    else:  # same partition; equal-weight edges may number the clusters otherwise
+        assert_same_partition(labels, g["labels"])
+        np.testing.assert_array_equal(probs, g["probabilities"])
+
+
+def assert_same_partition(a, b):
+    """Labels equal up to renaming the clusters (noise stays noise)."""
+    a, b = np.asarray(a), np.asarray(b)
+    assert np.array_equal(a == -1, b == -1)
+    pairs = set(zip(a[a >= 0].tolist(), b[b >= 0].tolist()))
+    assert len(pairs) == len({x for x, _ in pairs}) == len({y for _, y in pairs})
