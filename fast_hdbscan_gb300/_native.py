@@ -59,6 +59,10 @@ SIGNATURES = {
                                        _D, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                        ctypes.POINTER(_I64), _P, _P, _P, ctypes.POINTER(_I64),
                                        _P]),
+    "fhg_hdbscan_fit_precomputed": (_INT, [_P, _P, _P, _I64, _I64, _I32, _I32, _I64, _I32, _D,
+                                           _INT, _D, _D, _P, _P, _P, _P, _P, _P, _P, _P,
+                                           ctypes.POINTER(_I64), _P, _P, _P,
+                                           ctypes.POINTER(_I64), _P]),
     "fhg_precomputed_mst": (_INT, [_P, _P, _P, _I64, _I64, _I32, _I32, _P, _P, _P,
                                    ctypes.POINTER(_I64), _P]),
     "fhg_index_kruskal_knn": (_INT, [_P, _I32, _I32, _P, _P, _P, _P, ctypes.POINTER(_I64), _P]),

@@ -587,6 +587,14 @@ FHG_API int fhg_labelling_at_cut(const double* linkage_dev, int64_t m, double cu
 // ---------------------------------------------------------------- fused fit
 namespace {
 
+// A precomputed sparse graph as the fit's input (metric="precomputed").
+struct GraphInput {
+    const int32_t* rows = nullptr;
+    const int32_t* cols = nullptr;
+    const double* data = nullptr;
+    int64_t nnz = 0;
+};
+
 // Host destinations of the large fit outputs, each copied on a side stream as
 // soon as the fit has finished writing it, so that the transfers overlap the
 // later stages.  NULL members are not copied.
@@ -647,8 +655,9 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
              int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
              int64_t* selected_dev, int64_t* n_selected_host, void* stream,
              const FitExport& ex, int32_t knn_k = 0, int32_t query_k = 0,
-             double* core64_dev = nullptr) {
-    FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev, labels_dev, probs_dev}));
+             double* core64_dev = nullptr, const GraphInput* graph = nullptr) {
+    FHG_TRY(check_ptrs("fhg_hdbscan_fit", {labels_dev, probs_dev}));
+    if (!graph) FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev}));
     if (min_samples < 1 || min_cluster_size < 1) {
         set_error("Min samples and min cluster size must be positive integers!");
         return FHG_ERR_INVALID;
@@ -665,14 +674,27 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
     SideCopies side(s);  // declared before the workspace: joins after its frees are queued
     Workspace ws(s);
     fhg_index* ix = nullptr;
-    FHG_TRY(index_build(X_dev, n, d, s, &ix));
+    if (!graph) FHG_TRY(index_build(X_dev, n, d, s, &ix));
     struct IndexGuard {
         fhg_index* p;
         cudaStream_t s;
         ~IndexGuard() { index_free(p, s); }
     } guard{ix, s};
     Linkage lk;
-    if (knn_k > 0) {  // the kNN-graph Kruskal back-end (kruskal.py:950)
+    if (graph) {  // a precomputed sparse graph (precomputed.py:410 / :479)
+        double *kedges, *core64 = core64_dev;
+        int32_t* nb = neighbors_dev;
+        FHG_TRY(ws.alloc(&kedges, (size_t)(3 * (n - 1))));
+        if (!core64) FHG_TRY(ws.alloc(&core64, (size_t)n));
+        if (!nb) FHG_TRY(ws.alloc(&nb, (size_t)(n * (min_samples > 1 ? min_samples : 1))));
+        int64_t nc = 0;
+        FHG_TRY(precomputed_mst(graph->rows, graph->cols, graph->data, graph->nnz, n,
+                                min_samples, kedges, nb, core64, &nc, s));
+        int32_t *src, *dst;
+        double* w;
+        FHG_TRY(split_mst_f64(ws, kedges, n - 1, &src, &dst, &w));
+        FHG_TRY(sort_and_link(ws, n, src, dst, w, nullptr, &lk, false));
+    } else if (knn_k > 0) {  // the kNN-graph Kruskal back-end (kruskal.py:950)
         double *kedges, *core64 = core64_dev;
         FHG_TRY(ws.alloc(&kedges, (size_t)(3 * (n - 1))));
         if (!core64) FHG_TRY(ws.alloc(&core64, (size_t)n));
@@ -801,6 +823,34 @@ FHG_API int fhg_hdbscan_fit_kruskal(
                     ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, ct_rows_host,
                     neighbors_dev, nullptr, selected_dev, n_selected_host, stream, FitExport(),
                     knn_k, query_k, core_dev);
+}
+
+FHG_API int fhg_hdbscan_fit_precomputed(
+    const int32_t* rows_dev, const int32_t* cols_dev, const double* data_dev, int64_t nnz,
+    int64_t n, int32_t min_samples, int32_t algorithm, int64_t min_cluster_size,
+    int32_t selection_method, double max_cluster_size, int allow_single_cluster, double epsilon,
+    double persistence, int64_t* labels_dev, float* probs_dev, double* mst_dev,
+    double* linkage_dev, int64_t* ct_parent_dev, int64_t* ct_child_dev, float* ct_lambda_dev,
+    float* ct_size_dev, int64_t* ct_rows_host, int32_t* neighbors_dev, double* core_dev,
+    int64_t* selected_dev, int64_t* n_selected_host, void* stream) {
+    if (nnz < 0 || (nnz > 0 && (!rows_dev || !cols_dev || !data_dev))) {
+        set_error("fhg_hdbscan_fit_precomputed: invalid graph entries");
+        return FHG_ERR_INVALID;
+    }
+    if (algorithm != 0 && algorithm != 1) {
+        set_error("fhg_hdbscan_fit_precomputed: algorithm must be 0 (boruvka) or 1 (kruskal)");
+        return FHG_ERR_INVALID;
+    }
+    GraphInput g;
+    g.rows = rows_dev;
+    g.cols = cols_dev;
+    g.data = data_dev;
+    g.nnz = nnz;
+    return fit_impl(nullptr, n, 0, min_samples, min_cluster_size, selection_method,
+                    max_cluster_size, allow_single_cluster, epsilon, persistence, nullptr, 0,
+                    labels_dev, probs_dev, mst_dev, linkage_dev, ct_parent_dev, ct_child_dev,
+                    ct_lambda_dev, ct_size_dev, ct_rows_host, neighbors_dev, nullptr,
+                    selected_dev, n_selected_host, stream, FitExport(), 0, 0, core_dev, &g);
 }
 
 FHG_API int fhg_hdbscan_fit_export(

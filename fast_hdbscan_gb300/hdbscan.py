@@ -384,6 +384,59 @@ def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_m
                      sel[:k].cpu().numpy())
 
 
+def gpu_fit_precomputed(G, min_samples, min_cluster_size, algorithm="boruvka",
+                        cluster_selection_method="eom", max_cluster_size=np.inf,
+                        allow_single_cluster=False, cluster_selection_epsilon=0.0,
+                        cluster_selection_persistence=0.0, return_trees=True):
+    """One call of fhg_hdbscan_fit_precomputed on a scipy sparse graph's COO
+    entries (metric="precomputed"), outputs copied back."""
+    from .precomputed import validate_precomputed_sparse_graph
+
+    validate_precomputed_sparse_graph(G)
+    coo = G.tocoo()
+    n = G.shape[0]
+    ms = min_cluster_size if min_samples is None else min_samples
+    k = max(1, int(ms))
+    method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
+    if method is None:
+        raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+    to_dev = _native.to_device
+    rows = to_dev(np.ascontiguousarray(coo.row, np.int32), np.int32)
+    cols = to_dev(np.ascontiguousarray(coo.col, np.int32), np.int32)
+    data = to_dev(np.ascontiguousarray(coo.data, np.float64), np.float64)
+    E = _native.empty
+    labels, probs, sel = E(n, np.int64), E(n, np.float32), E(n, np.int64)
+    trees = return_trees
+    mst = E((n - 1, 3), np.float64) if trees else None
+    linkage = E((n - 1, 4), np.float64) if trees else None
+    ctp, ctc = (E(2 * n, np.int64), E(2 * n, np.int64)) if trees else (None, None)
+    ctl, cts = (E(2 * n, np.float32), E(2 * n, np.float32)) if trees else (None, None)
+    nbrs = E((n, k), np.int32) if trees else None
+    core = E(n, np.float64) if trees else None
+    rows_c, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
+    V, lib = _native.vptr, _native.load()
+    rc = lib.fhg_hdbscan_fit_precomputed(
+        V(rows), V(cols), V(data), int(coo.nnz), n, int(ms),
+        1 if algorithm == "kruskal" else 0, int(min_cluster_size), method,
+        float(max_cluster_size), int(bool(allow_single_cluster)),
+        float(cluster_selection_epsilon), float(cluster_selection_persistence), V(labels),
+        V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows_c),
+        V(nbrs), V(core), V(sel), ctypes.byref(nsel), _native.stream_ptr())
+    if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
+        raise KeyError(lib.fhg_last_error().decode())
+    _native.check(rc)
+    r, kk = rows_c.value, nsel.value
+    labels_h = labels.cpu().numpy().astype(np.intp, copy=False)
+    if not trees:
+        return FitResult(labels_h, probs.cpu().numpy(), None, None, None, None, None,
+                         sel[:kk].cpu().numpy())
+    ct = CondensedTree(ctp[:r].cpu().numpy(), ctc[:r].cpu().numpy(), ctl[:r].cpu().numpy(),
+                       cts[:r].cpu().numpy())
+    return FitResult(labels_h, probs.cpu().numpy(), linkage.cpu().numpy(), ct,
+                     mst.cpu().numpy(), nbrs.cpu().numpy(), core.cpu().numpy(),
+                     sel[:kk].cpu().numpy())
+
+
 def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc",
                  min_samples=10, min_cluster_size=10, cluster_selection_method="eom",
                  max_cluster_size=np.inf, allow_single_cluster=False,
@@ -433,23 +486,17 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
     _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data, cannot_link,
                         cannot_link_groups, knn_k)
     if metric == "precomputed":  # hdbscan.py:306-337 on a precomputed sparse graph
-        ms = min_cluster_size if min_samples is None else min_samples
-        mst, neighbors, core = compute_minimum_spanning_tree(
-            data, min_samples=ms, metric="precomputed", algorithm=algorithm)
-        result = (*clusters_from_spanning_tree(
-            mst, min_cluster_size=min_cluster_size,
-            cluster_selection_method=cluster_selection_method,
-            max_cluster_size=max_cluster_size, allow_single_cluster=allow_single_cluster,
-            cluster_selection_epsilon=cluster_selection_epsilon,
-            cluster_selection_persistence=cluster_selection_persistence), neighbors, core)
-        return result[: (None if return_trees else 2)]
-    if algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
+        fr = gpu_fit_precomputed(data, min_samples, min_cluster_size, algorithm,
+                                 cluster_selection_method, max_cluster_size,
+                                 allow_single_cluster, cluster_selection_epsilon,
+                                 cluster_selection_persistence, return_trees=return_trees)
+    elif algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
         fr = gpu_fit_kruskal(data, min_samples, min_cluster_size, knn_k,
                              cluster_selection_method, max_cluster_size, allow_single_cluster,
                              cluster_selection_epsilon, cluster_selection_persistence,
                              return_trees=return_trees, sample_weights=sample_weights)
     else:
-            fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
+        fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
                      max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
                      cluster_selection_persistence, return_trees=return_trees,
                      sample_weights=sample_weights, condensed_records=condensed_records)

@@ -306,6 +306,22 @@ int fhg_hdbscan_fit_kruskal(const float* X_dev, int64_t n, int32_t d, int32_t mi
                             int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev,
                             int64_t* n_selected_host, void* stream);
 
+/* The whole fit (hdbscan.py:306) on a precomputed sparse graph
+ * (metric="precomputed"): the forest of fhg_precomputed_mst, then the tree
+ * passes of fhg_hdbscan_fit.  neighbors_dev (optional, n x max(1,
+ * min_samples)) and core_dev (optional, float64) as fhg_precomputed_mst. */
+int fhg_hdbscan_fit_precomputed(const int32_t* rows_dev, const int32_t* cols_dev,
+                                const double* data_dev, int64_t nnz, int64_t n,
+                                int32_t min_samples, int32_t algorithm,
+                                int64_t min_cluster_size, int32_t selection_method,
+                                double max_cluster_size, int allow_single_cluster,
+                                double epsilon, double persistence, int64_t* labels_dev,
+                                float* probs_dev, double* mst_dev, double* linkage_dev,
+                                int64_t* ct_parent_dev, int64_t* ct_child_dev,
+                                float* ct_lambda_dev, float* ct_size_dev, int64_t* ct_rows_host,
+                                int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev,
+                                int64_t* n_selected_host, void* stream);
+
 /* fhg_hdbscan_fit, with the large outputs also copied to host memory while
  * the fit runs: each non-NULL *_host destination receives its output from a
  * side stream as soon as the fit has finished writing it (neighbours and
