@@ -48,6 +48,12 @@ OTHER_WORKLOADS = {
                    min_cluster_size=500, seed=1,
                    generator="40 blobs, std logU[0.2,2], Dirichlet weights, centres "
                              "U[-20,20]^5, 10% noise"),
+    # a 15-NN distance graph of 1M points of the metric's generator, metric="precomputed"
+    "precomputed1m": dict(workload="knn15_graph_1M_3d_precomputed", n=1_000_000, d=3,
+                          min_samples=10, min_cluster_size=100, seed=3, metric="precomputed",
+                          graph_k=15, algorithm="kruskal",
+                          generator="15-NN float64 distance graph (scipy sparse) of 200 "
+                                    "Gaussians, std lognormal(0,1), centres U[-100,100]^3"),
     # the metric's data through the algorithm="kruskal" back-end (kNN graph, knn_k=16)
     "kruskal10m": dict(workload="varying_density_10M_3d_kruskal_knn16", n=10_000_000, d=3,
                        min_samples=15, min_cluster_size=500, seed=3, algorithm="kruskal",
@@ -215,23 +221,40 @@ def run_gb300(args):
 
     n = args.n
     ms, mcs = WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"]
-    kruskal = WORKLOAD.get("algorithm") == "kruskal"
+    pre = WORKLOAD.get("metric") == "precomputed"
+    kruskal = WORKLOAD.get("algorithm") == "kruskal" and not pre
     knn_k = WORKLOAD.get("knn_k", 0)
     Xh = make_data(n, WORKLOAD["seed"] + rank)
     d = Xh.shape[1]
     Xd = torch.from_numpy(Xh).cuda()
+    if pre:  # the input graph: every point's graph_k nearest points, float64 distances
+        from fast_hdbscan_gb300.numba_kdtree import build_kdtree, parallel_tree_query
+
+        gk = WORKLOAD["graph_k"]
+        rd, gi = parallel_tree_query(build_kdtree(Xh), Xh, k=gk + 1, output_rdist=True)
+        g_rows = torch.arange(n, dtype=torch.int32).repeat_interleave(gk).cuda()
+        g_cols = torch.from_numpy(np.ascontiguousarray(gi[:, 1:])).reshape(-1).cuda()
+        g_data = torch.from_numpy(np.sqrt(rd[:, 1:].astype(np.float64))).reshape(-1).cuda()
+        nnz = n * gk
     E = _native.empty
     labels, probs = E(n, np.int64), E(n, np.float32)
     mst, linkage = E((n - 1, 3), np.float64), E((n - 1, 4), np.float64)
     ctp, ctc, ctl, cts = (E(2 * n, np.int64), E(2 * n, np.int64), E(2 * n, np.float32),
                           E(2 * n, np.float32))
     nbrs, sel = E((n, ms), np.int32), E(n, np.int64)
-    core = E(n, np.float64 if kruskal else np.float32)
+    core = E(n, np.float64 if (kruskal or pre) else np.float32)
     rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
     V = _native.vptr
     stream = torch.cuda.current_stream()
 
     def step():
+        if pre:
+            _native.check(lib.fhg_hdbscan_fit_precomputed(
+                V(g_rows), V(g_cols), V(g_data), nnz, n, ms, 1, mcs, 0, float("inf"), 0, 0.0,
+                0.0, V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
+                ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
+                _native.stream_ptr()))
+            return
         if kruskal:
             _native.check(lib.fhg_hdbscan_fit_kruskal(
                 V(Xd), n, d, ms, knn_k, max(knn_k, ms) + 1, mcs, 0, float("inf"), 0, 0.0, 0.0,
@@ -308,8 +331,19 @@ def run_gb300(args):
     e2e = None
     if not args.no_e2e:
         Xp = torch.from_numpy(Xh).pin_memory()
-        est = (HDBSCAN(min_cluster_size=mcs, min_samples=ms, algorithm="kruskal", knn_k=knn_k)
-               if kruskal else HDBSCAN(min_cluster_size=mcs, min_samples=ms))
+        if pre:  # the caller's scipy graph on the host
+            import scipy.sparse
+
+            Xp = scipy.sparse.csr_matrix(
+                (g_data.cpu().numpy(), g_cols.cpu().numpy(),
+                 np.arange(0, nnz + 1, WORKLOAD["graph_k"], dtype=np.int64)), shape=(n, n))
+            est = HDBSCAN(min_cluster_size=mcs, min_samples=ms, metric="precomputed",
+                          algorithm=WORKLOAD["algorithm"])
+        elif kruskal:
+            est = HDBSCAN(min_cluster_size=mcs, min_samples=ms, algorithm="kruskal",
+                          knn_k=knn_k)
+        else:
+            est = HDBSCAN(min_cluster_size=mcs, min_samples=ms)
         # warm-up fits: the estimator holds one fit's outputs while the next
         # runs, so the pinned host buffers reach their steady state (two sets
         # in PyTorch's caching host allocator) before the timed fits
@@ -326,9 +360,10 @@ def run_gb300(args):
         # labels i64, probabilities f32, sorted MST (n-1) x 3 f64, linkage (n-1) x 4 f64,
         # condensed tree 28 B/row, neighbours n x ms i32, core distances f32 (Kruskal: f64)
         d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 28 + n * ms * 4
-               + n * (8 if kruskal else 4))
+               + n * (8 if (kruskal or pre) else 4))
+        h2d = n * WORKLOAD["graph_k"] * 16 if pre else n * d * 4  # graph: rows, cols, f64
         e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",
-               "h2d_bytes_per_step": int(n * d * 4), "d2h_bytes_per_step": int(d2h),
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "s_per_step": round(e2e_s, 4)}
 
     cpu = None
@@ -362,7 +397,18 @@ def _oracle_fit_time(n, nthreads):
 
     X = make_data(n, WORKLOAD["seed"])
     t0 = time.perf_counter()
-    if WORKLOAD.get("algorithm") == "kruskal":  # hdbscan.py:306 with algorithm="kruskal"
+    if WORKLOAD.get("metric") == "precomputed":  # hdbscan.py:306 on the kNN graph
+        import scipy.sparse
+
+        gk = WORKLOAD["graph_k"]
+        rd, gi = O.tree_query(O.build_kdtree(X), gk + 1, 0, nthreads)
+        G = scipy.sparse.csr_matrix(
+            (np.sqrt(rd[:, 1:].astype(np.float64)).ravel(), gi[:, 1:].ravel(),
+             np.arange(0, n * gk + 1, gk)), shape=(n, n))
+        t0 = time.perf_counter()
+        mst, _, _ = O.precomputed_kruskal(G, WORKLOAD["min_samples"])
+        O.clusters_from_spanning_tree(mst, WORKLOAD["min_cluster_size"])
+    elif WORKLOAD.get("algorithm") == "kruskal":  # hdbscan.py:306 with algorithm="kruskal"
         mst, _, _ = O.kruskal_knn(O.build_kdtree(X), WORKLOAD["min_samples"], WORKLOAD["knn_k"],
                                   mode=0, nthreads=nthreads)
         O.clusters_from_spanning_tree(mst, WORKLOAD["min_cluster_size"])
@@ -487,7 +533,10 @@ def main():
             args.n = WORKLOAD["n"]
         global METRIC
         METRIC = f"HDBSCAN fit points/s at {WORKLOAD['n'] // 1_000_000}M x {WORKLOAD['d']}-D"
-        if WORKLOAD.get("algorithm") == "kruskal":
+        if WORKLOAD.get("metric") == "precomputed":
+            METRIC += (f" (metric='precomputed', {WORKLOAD['graph_k']}-NN graph, "
+                       f"algorithm='{WORKLOAD['algorithm']}')")
+        elif WORKLOAD.get("algorithm") == "kruskal":
             METRIC += f" (algorithm='kruskal', knn_k={WORKLOAD['knn_k']})"
         args.workload = "fit"
     if args.impl == "reference":
