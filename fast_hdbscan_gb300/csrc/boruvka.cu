@@ -35,6 +35,9 @@ namespace fhg {
 namespace {
 
 constexpr int kSW = 4;        // warps per block, search kernel
+// The global search pass runs on a list of the searching points when they are
+// fewer than one in kSparseFraction.
+constexpr int64_t kSparseFraction = 4;
 constexpr int kStack = 64;
 constexpr int kMaxRounds = 64;
 constexpr int kLocalLevels = 4;  // first search pass: subtrees of up to 16 buckets
@@ -354,16 +357,22 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     IndexView ix, const int8_t* __restrict__ knn_open,
     const float* __restrict__ core2, const int32_t* __restrict__ comp,
     const int2* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
-    int32_t* __restrict__ cand_q, int lvl_lo, int lvl_hi) {
+    int32_t* __restrict__ cand_q, int lvl_lo, int lvl_hi, const int32_t* __restrict__ plist,
+    int64_t plen) {
     __shared__ int32_t s_stack[kSW][kStack];
     __shared__ float4 s_xyz[kSW][32 * (SP / 4)];
     __shared__ int2 s_cc[kSW][32];      // (component, core bits)
     __shared__ int32_t s_orig[kSW][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Dense: warp = bucket, lane = point.  Sparse (plist): warp = 32
+    // consecutive entries of a list of the points still searching (in index
+    // order), each searching from the root.
+    const bool sparse = plist != nullptr;
     const int64_t leaf = (int64_t)blockIdx.x * kSW + warp;
-    if (leaf >= ix.nleaves) return;
-    const int64_t p = leaf * kLeaf + lane;
-    const bool valid = p < ix.n;
+    if (sparse ? leaf * 32 >= plen : leaf >= ix.nleaves) return;
+    const int64_t li = leaf * 32 + lane;
+    const int64_t p = sparse ? (li < plen ? plist[li] : 0) : leaf * kLeaf + lane;
+    const bool valid = sparse ? li < plen : p < ix.n;
     int32_t c = -3;
     float cp = 0.0f, bw = INFINITY;
     int32_t bq = -1, bo = INT32_MAX;
@@ -440,10 +449,9 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     };
 
     const int64_t first_leaf_node = ix.slots - 1;
-    const int64_t home_node = first_leaf_node + leaf;
+    const int64_t home_node = first_leaf_node + (sparse ? 0 : leaf);
     // A home bucket spanning several components holds the nearest candidates.
-    const int32_t home_nc = nc[home_node].x;
-    const bool home_first = lvl_lo == 0 && home_nc == kMixed;
+    const bool home_first = !sparse && lvl_lo == 0 && nc[home_node].x == kMixed;
     if (home_first && __any_sync(kFull, active)) scan_leaf(leaf, active);
 
     // Walk up from the home bucket to the root, searching the sibling subtree
@@ -455,13 +463,16 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     // needed when the key is within the lane's threshold.
     int32_t* st = s_stack[warp];
     auto other = [&](int2 ncn) { return ncn.x != c && ncn.x != kEmpty; };
+    // (Sparse: one pass over the whole tree from the root, children of least
+    // bound over the searching lanes first.)
     int64_t x = home_node;
-    for (int lv = 0; lv < lvl_lo && x > 0; ++lv) x = (x - 1) >> 1;
-    for (int lv = lvl_lo; lv < lvl_hi && x > 0; ++lv) {
-        const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+    if (!sparse)
+        for (int lv = 0; lv < lvl_lo && x > 0; ++lv) x = (x - 1) >> 1;
+    for (int lv = lvl_lo; sparse ? lv == lvl_lo : (lv < lvl_hi && x > 0); ++lv) {
+        const int32_t sib = sparse ? 0 : (int32_t)((x & 1) ? x + 1 : x - 1);
         // children nearer the home bucket in Morton order first
         const bool right_side = (x & 1) != 0;
-        x = (x - 1) >> 1;
+        if (!sparse) x = (x - 1) >> 1;
         {
             const int2 ncn = nc[sib];
             bool need = active && other(ncn) && !(__int_as_float(ncn.y) > thr);
@@ -503,7 +514,10 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
             }
             const bool al = __any_sync(kFull, nl), ar = __any_sync(kFull, nr);
             if (!al && !ar) continue;
-            const bool left_first = !(al && ar) ? al : right_side;
+            bool left_first = !(al && ar) ? al : right_side;
+            if (sparse && al && ar)  // non-negative floats order like their bits
+                left_first = __reduce_min_sync(kFull, nl ? __float_as_uint(kl) : 0x7f800000u) <=
+                             __reduce_min_sync(kFull, nr ? __float_as_uint(kr) : 0x7f800000u);
             if (l >= first_leaf_node) {
                 // thresholds may shrink while the first bucket is scanned
                 const int32_t n1 = left_first ? l : r, n2 = left_first ? r : l;
@@ -530,6 +544,27 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     cand_q[p] = bq;
     unsigned long long key = pack_key(bw, min(ix.orig[p], bo));
     if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
+}
+
+// The points that start the global pass searching (as search_kernel decides).
+__global__ void searching_flags_kernel(int64_t n, const int8_t* __restrict__ knn_open,
+                                       const float* __restrict__ core2,
+                                       const int32_t* __restrict__ comp,
+                                       const unsigned long long* __restrict__ keyA,
+                                       const float* __restrict__ cand_w,
+                                       const int32_t* __restrict__ cand_q,
+                                       uint32_t* __restrict__ flag) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float cp = core2[p], bw = cand_w[p];
+    const bool settled = cand_q[p] >= 0 && bw == cp && !knn_open[p];
+    const float thr0 = fminf(bw, key_weight(keyA[comp[p]]));
+    flag[p] = (!settled && !(cp > thr0)) ? 1u : 0u;
+}
+__global__ void iota_list_kernel(int64_t n, const uint32_t* __restrict__ flag,
+                                 const uint32_t* __restrict__ pos, int32_t* __restrict__ list) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n && flag[p]) list[pos[p]] = (int32_t)p;
 }
 
 __global__ void stage_b_kernel(int64_t n, const int32_t* __restrict__ comp,
@@ -645,20 +680,66 @@ __global__ void finalize_edges_kernel(int64_t m, const int32_t* __restrict__ src
 template <int DIM>
 int launch_search(const fhg_index& ix, const int8_t* knn_open,
                   const float* core2, const int32_t* comp, const int2* nc,
-                  unsigned long long* keyA, float* cand_w, int32_t* cand_q, cudaStream_t s) {
+                  unsigned long long* keyA, float* cand_w, int32_t* cand_q, bool* try_sparse,
+                  cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);  // as in the kNN kernel
     // Local pass (home bucket and the kLocalLevels nearest sibling subtrees),
     // then the rest of the walk: every component's bound from its nearby
     // candidates is published before any point searches far away.
-    const int spans[2][2] = {{0, kLocalLevels}, {kLocalLevels, 64}};
-    for (const auto& sp : spans) {
+    {
         Stage stage(s, "search_kernel");
         ::fhg::note_launch();
         search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
-            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, sp[0],
-            sp[1]);
+            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, 0, kLocalLevels,
+            nullptr, 0);
         FHG_CUDA(cudaGetLastError());
     }
+    // When few points still search (early rounds: most points' best edge is
+    // settled by the seeds and the local pass), the global pass runs on a
+    // list of them, 32 to a warp, each from the root -- instead of a warp per
+    // bucket walking for one or two of its lanes.  Searching only grows with
+    // the components, so after the first dense round the list is not made.
+    const int64_t n = ix.n;
+    if (!*try_sparse) {
+        Stage stage(s, "search_kernel");
+        ::fhg::note_launch();
+        search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
+            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, kLocalLevels, 64,
+            nullptr, 0);
+        FHG_CUDA(cudaGetLastError());
+        return FHG_OK;
+    }
+    Workspace tmp(s);
+    uint32_t *flag, *pos, *cnt;
+    int32_t* list;
+    FHG_TRY(tmp.alloc(&flag, (size_t)n));
+    FHG_TRY(tmp.alloc(&pos, (size_t)n));
+    FHG_TRY(tmp.alloc(&list, (size_t)n));
+    FHG_TRY(tmp.alloc(&cnt, 1));
+    ::fhg::note_launch();
+    searching_flags_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, knn_open, core2, comp, keyA,
+                                                              cand_w, cand_q, flag);
+    FHG_CUDA(cudaGetLastError());
+    FHG_TRY(scan_exclusive_u32(tmp, flag, pos, n, cnt));
+    uint32_t h_cnt = 0;
+    FHG_CUDA(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    const int64_t ns = h_cnt;
+    if (ns == 0) return FHG_OK;
+    const bool sparse = ns * kSparseFraction < n;
+    *try_sparse = sparse;
+    if (sparse) {
+        ::fhg::note_launch();
+        iota_list_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, flag, pos, list);
+        FHG_CUDA(cudaGetLastError());
+    }
+    Stage stage(s, "search_kernel");
+    ::fhg::note_launch();
+    const int64_t units = sparse ? (ns + 31) / 32 : ix.nleaves;
+    search_kernel<DIM, SP><<<grid_for(units, kSW), kSW * 32, 0, s>>>(
+        view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, kLocalLevels, 64,
+        sparse ? list : nullptr, ns);
+    FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
@@ -666,7 +747,7 @@ int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* 
                  const int8_t* knn_open, int8_t* exhausted, const float* core2,
                  const int32_t* comp,
                  const int2* nc, unsigned long long* keyA, float* cand_w, int32_t* cand_q,
-                 cudaStream_t s) {
+                 bool* try_sparse, cudaStream_t s) {
     const int64_t n = ix.n;
     if (n > 0) {
         ::fhg::note_launch();
@@ -675,18 +756,18 @@ int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* 
         FHG_CUDA(cudaGetLastError());
     }
     switch (ix.d) {
-        case 1: return launch_search<1>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 2: return launch_search<2>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 3: return launch_search<3>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 4: return launch_search<4>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 5: return launch_search<5>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 6: return launch_search<6>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 7: return launch_search<7>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-        case 8: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+        case 1: return launch_search<1>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 2: return launch_search<2>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 3: return launch_search<3>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 4: return launch_search<4>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 5: return launch_search<5>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 6: return launch_search<6>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 7: return launch_search<7>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 8: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
         default:
             if (ix.d <= 16)
-                return launch_search<16>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
-            return launch_search<32>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, s);
+                return launch_search<16>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+            return launch_search<32>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
     }
 }
 
@@ -849,6 +930,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t) * n, s));
 
     int rounds = 0;
+    bool try_sparse = true;  // until a round's global pass is dense
     while (ncomp > 1) {
         if (rounds >= kMaxRounds) {
             set_error("boruvka: no convergence after %d rounds (%lld components left)", rounds,
@@ -865,7 +947,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         {
             Stage stage(s, "boruvka_search");
             FHG_TRY(search_round(ix, k, knn_s, knn_d, knn_open, exhausted, core2, comp, nc, keyA,
-                                 cand_w, cand_q, s));
+                                 cand_w, cand_q, &try_sparse, s));
         }
         Stage merge_stage(s, "boruvka_merge");
         LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);
