@@ -683,63 +683,55 @@ int launch_search(const fhg_index& ix, const int8_t* knn_open,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, bool* try_sparse,
                   cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);  // as in the kNN kernel
-    // Local pass (home bucket and the kLocalLevels nearest sibling subtrees),
-    // then the rest of the walk: every component's bound from its nearby
-    // candidates is published before any point searches far away.
-    {
-        Stage stage(s, "search_kernel");
-        ::fhg::note_launch();
-        search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
-            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, 0, kLocalLevels,
-            nullptr, 0);
-        FHG_CUDA(cudaGetLastError());
-    }
-    // When few points still search (early rounds: most points' best edge is
-    // settled by the seeds and the local pass), the global pass runs on a
-    // list of them, 32 to a warp, each from the root -- instead of a warp per
-    // bucket walking for one or two of its lanes.  Searching only grows with
-    // the components, so after the first dense round the list is not made.
     const int64_t n = ix.n;
-    if (!*try_sparse) {
+    // When few points search (early rounds: most points' best edge is settled
+    // by the seeds), one pass runs on a list of them, 32 to a warp, each from
+    // the root -- instead of a warp per bucket walking for one or two of its
+    // lanes.  Searching only grows with the components, so after the first
+    // dense round the list is not made again.
+    if (*try_sparse) {
+        Workspace tmp(s);
+        uint32_t *flag, *pos, *cnt;
+        int32_t* list;
+        FHG_TRY(tmp.alloc(&flag, (size_t)n));
+        FHG_TRY(tmp.alloc(&pos, (size_t)n));
+        FHG_TRY(tmp.alloc(&list, (size_t)n));
+        FHG_TRY(tmp.alloc(&cnt, 1));
+        ::fhg::note_launch();
+        searching_flags_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, knn_open, core2, comp, keyA,
+                                                                  cand_w, cand_q, flag);
+        FHG_CUDA(cudaGetLastError());
+        FHG_TRY(scan_exclusive_u32(tmp, flag, pos, n, cnt));
+        uint32_t h_cnt = 0;
+        FHG_CUDA(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        const int64_t ns = h_cnt;
+        if (ns == 0) return FHG_OK;
+        *try_sparse = ns * kSparseFraction < n;
+        if (*try_sparse) {
+            ::fhg::note_launch();
+            iota_list_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, flag, pos, list);
+            FHG_CUDA(cudaGetLastError());
+            Stage stage(s, "search_kernel");
+            ::fhg::note_launch();
+            search_kernel<DIM, SP><<<grid_for((ns + 31) / 32, kSW), kSW * 32, 0, s>>>(
+                view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, 0, 64, list, ns);
+            FHG_CUDA(cudaGetLastError());
+            return FHG_OK;
+        }
+    }
+    // Dense: a local pass (home bucket and the kLocalLevels nearest sibling
+    // subtrees), then the rest of the walk -- every component's bound from
+    // its nearby candidates is published before any point searches far away.
+    const int spans[2][2] = {{0, kLocalLevels}, {kLocalLevels, 64}};
+    for (const auto& sp : spans) {
         Stage stage(s, "search_kernel");
         ::fhg::note_launch();
         search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
-            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, kLocalLevels, 64,
+            view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, sp[0], sp[1],
             nullptr, 0);
         FHG_CUDA(cudaGetLastError());
-        return FHG_OK;
     }
-    Workspace tmp(s);
-    uint32_t *flag, *pos, *cnt;
-    int32_t* list;
-    FHG_TRY(tmp.alloc(&flag, (size_t)n));
-    FHG_TRY(tmp.alloc(&pos, (size_t)n));
-    FHG_TRY(tmp.alloc(&list, (size_t)n));
-    FHG_TRY(tmp.alloc(&cnt, 1));
-    ::fhg::note_launch();
-    searching_flags_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, knn_open, core2, comp, keyA,
-                                                              cand_w, cand_q, flag);
-    FHG_CUDA(cudaGetLastError());
-    FHG_TRY(scan_exclusive_u32(tmp, flag, pos, n, cnt));
-    uint32_t h_cnt = 0;
-    FHG_CUDA(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    FHG_CUDA(cudaStreamSynchronize(s));
-    const int64_t ns = h_cnt;
-    if (ns == 0) return FHG_OK;
-    const bool sparse = ns * kSparseFraction < n;
-    *try_sparse = sparse;
-    if (sparse) {
-        ::fhg::note_launch();
-        iota_list_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, flag, pos, list);
-        FHG_CUDA(cudaGetLastError());
-    }
-    Stage stage(s, "search_kernel");
-    ::fhg::note_launch();
-    const int64_t units = sparse ? (ns + 31) / 32 : ix.nleaves;
-    search_kernel<DIM, SP><<<grid_for(units, kSW), kSW * 32, 0, s>>>(
-        view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, kLocalLevels, 64,
-        sparse ? list : nullptr, ns);
-    FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
