@@ -35,9 +35,9 @@ namespace fhg {
 namespace {
 
 constexpr int kSW = 4;        // warps per block, search kernel
-// The global search pass runs on a list of the searching points when they are
-// fewer than one in kSparseFraction.
-constexpr int64_t kSparseFraction = 4;
+// A round's search runs on a list of the searching points when they are fewer
+// than kSparseNum / kSparseDen of all points.
+constexpr int64_t kSparseNum = 1, kSparseDen = 4;
 constexpr int kStack = 64;
 constexpr int kMaxRounds = 64;
 constexpr int kLocalLevels = 4;  // first search pass: subtrees of up to 16 buckets
@@ -707,7 +707,7 @@ int launch_search(const fhg_index& ix, const int8_t* knn_open,
         FHG_CUDA(cudaStreamSynchronize(s));
         const int64_t ns = h_cnt;
         if (ns == 0) return FHG_OK;
-        *try_sparse = ns * kSparseFraction < n;
+        *try_sparse = ns * kSparseDen < n * kSparseNum;
         if (*try_sparse) {
             ::fhg::note_launch();
             iota_list_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, flag, pos, list);
