@@ -244,6 +244,9 @@ KRUSKAL_CASES = {
     "kr_blobs2d_2k_ms1": (lambda: synthetic.blobs_2d(2000, seed=12), 1, 20, 3, None),
     "kr_vd3d_3k_w": (lambda: synthetic.varying_density(3000, seed=13), 6, 30, 12,
                      lambda n: _weights_sixty_fourths(n, 14)),
+    # edge cases: knn_k above the point count, and min_samples above knn_k
+    "kr_edge_n3": (lambda: np.array([[0.0, 0.0], [1.0, 0.5], [3.0, -1.0]]), 2, 2, 5, None),
+    "kr_edge_ms_gt_k": (lambda: _rand(15, 60, 2), 8, 5, 3, None),
 }
 
 
@@ -313,6 +316,20 @@ def _coo_with_duplicates():
     return scipy.sparse.coo_matrix((data, (rows, cols)), shape=(n, n))
 
 
+def _sparse_empty(n):
+    import scipy.sparse
+
+    return scipy.sparse.csr_matrix((n, n), dtype=np.float64)
+
+
+def _graph_with_isolated():
+    """A 5-NN graph of 40 points plus 5 points with no stored edge."""
+    import scipy.sparse
+
+    g = _knn_graph(_rand(16, 40, 2), 5, 0)
+    return scipy.sparse.block_diag([g, scipy.sparse.csr_matrix((5, 5))], format="csr")
+
+
 PRECOMPUTED_CASES = {
     # name: (graph factory, min_samples, min_cluster_size, algorithm)
     "pc_knn3d_kr": (lambda: _knn_graph(synthetic.varying_density(3000, seed=44), 10, 0), 5, 30,
@@ -322,7 +339,12 @@ PRECOMPUTED_CASES = {
     "pc_disconnected_kr": (_blob_graph_disconnected, 3, 20, "kruskal"),
     "pc_disconnected_bo": (_blob_graph_disconnected, 3, 20, "boruvka"),
     "pc_coo_dups_kr": (_coo_with_duplicates, 1, 5, "kruskal"),
+    # edge cases: no stored edge at all, and isolated points beside a component
+    "pc_edge_empty_kr": (lambda: _sparse_empty(6), 2, 2, "kruskal"),
+    "pc_edge_isolated_kr": (_graph_with_isolated, 2, 3, "kruskal"),
+    "pc_edge_isolated_bo": (_graph_with_isolated, 2, 3, "boruvka"),
 }
+
 
 
 def precomputed_fixtures(only=None):

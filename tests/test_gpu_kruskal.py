@@ -18,7 +18,8 @@ from fast_hdbscan_gb300 import synthetic
 
 pytestmark = pytest.mark.gpu
 
-KRUSKAL = ["kr_blobs200_k10", "kr_vd3d_5k_k8", "kr_blobs2d_2k_ms1", "kr_vd3d_3k_w"]
+KRUSKAL = ["kr_blobs200_k10", "kr_vd3d_5k_k8", "kr_blobs2d_2k_ms1", "kr_vd3d_3k_w",
+           "kr_edge_n3", "kr_edge_ms_gt_k"]
 
 
 def _golden(name):

@@ -20,7 +20,8 @@ from fast_hdbscan_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 PRECOMPUTED = ["pc_knn3d_kr", "pc_knn3d_bo", "pc_disconnected_kr", "pc_disconnected_bo",
-               "pc_coo_dups_kr"]
+               "pc_coo_dups_kr", "pc_edge_empty_kr", "pc_edge_isolated_kr",
+               "pc_edge_isolated_bo"]
 
 
 def _graph(g):
