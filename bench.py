@@ -72,6 +72,7 @@ def parse_args():
     ap.add_argument("--n", type=int, default=WORKLOAD["n"], help="points (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-radius", action="store_true", help="skip the learned-radius arm")
     ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N)
     ap.add_argument("--workload", default="fit", choices=["fit", "batched", *OTHER_WORKLOADS],
                     help="fit: the metric's 10M x 3-D fit; batched: many independent fits; "
@@ -327,6 +328,41 @@ def run_gb300(args):
                     "ms_per_launch": round(per_launch_ms, 4),
                     "kernel_share_of_stage_time": round(tot_ms / total_stage, 4)}
 
+    # the learned-radius arm: the same fit with the kNN radius proposed by a
+    # network trained on a 2M-point draw of the generator with another seed
+    # (training untimed), labels checked identical to the plain fit's
+    learned = None
+    if not (pre or kruskal or args.no_radius):
+        from fast_hdbscan_gb300.radius import RadiusModel
+
+        lab_plain, prob_plain = labels.clone(), probs.clone()
+        t0 = time.perf_counter()
+        model = RadiusModel.train(make_data(2_000_000, WORKLOAD["seed"] + 100), min_samples=ms,
+                                  steps=1500, batch=4096, seed=7)
+        train_s = time.perf_counter() - t0
+        with model.active():
+            for _ in range(args.warmup):
+                step()
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                step()
+            e1.record(stream)
+            barrier()
+            fallbacks = model.last_fallbacks()
+        ms_learned = max_over_ranks(e0.elapsed_time(e1) / args.steps,
+                                    torch.device("cuda", local))
+        learned = {"value": round(n * world / (ms_learned / 1e3), 1), "unit": "points/s",
+                   "ms_per_step": round(ms_learned, 3),
+                   "vs_plain": round(ms_step_max / ms_learned, 4),
+                   "fallback_rate": round(fallbacks / n, 6), "margin": round(model.margin, 4),
+                   "train_s": round(train_s, 3), "train_points": 2_000_000,
+                   "train_rmse_log": round(model.train_rmse, 4),
+                   "identical_labels": bool(torch.equal(labels, lab_plain)
+                                            and torch.equal(probs, prob_plain))}
+
     # e2e through the public estimator, pinned host input, outputs to host
     e2e = None
     if not args.no_e2e:
@@ -385,6 +421,7 @@ def run_gb300(args):
             "stage_share": {k: round(v[0] / total_stage, 4) for k, v in stages.items()
                             if k not in nested},
             "boruvka_rounds": rounds,
+            "learned_radius": learned,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -70,6 +70,20 @@ SIGNATURES = {
                                       _I32, _P, _P, _P, _P, _P, _P, _P, _P,
                                       ctypes.POINTER(_I64), _P, _P, _P, ctypes.POINTER(_I64),
                                       _P, _P, _P, _P, _P, _P, _P]),
+    "fhg_radius_param_count": (_INT, []),
+    "fhg_radius_features": (_INT, [_P, _P, _P]),
+    "fhg_radius_targets": (_INT, [_P, _I32, _P, _P]),
+    "fhg_radius_init": (_INT, [_P, _P, _P, _I64, ctypes.c_uint64, _P]),
+    "fhg_radius_forward": (_INT, [_P, _P, _I64, _P, _P]),
+    "fhg_radius_backward": (_INT, [_P, _P, _P, _P, _I64, _P, _P, _P]),
+    "fhg_radius_train": (_INT, [_P, _P, _P, _I64, _I32, _I32, ctypes.c_float, ctypes.c_uint64,
+                                _P, _P]),
+    "fhg_radius_use": (_INT, [_P, ctypes.c_float]),
+    "fhg_radius_fallbacks": (_INT, [ctypes.POINTER(_I64), _P]),
+    "fhg_index_knn_radius": (_INT, [_P, _I32, _P, ctypes.c_float, _P, _P, ctypes.POINTER(_I64),
+                                    _P]),
+    "fhg_knn_scan_count": (_INT, [_P, _I32, _P, ctypes.c_float, ctypes.POINTER(_I64),
+                                  ctypes.POINTER(_I64), _P]),
 }
 
 _lib = None

@@ -26,6 +26,7 @@
 // in order of each component's lowest point index (the reference's dict
 // insertion order).
 #include "mst.cuh"
+#include "radius.cuh"
 #include "primitives.cuh"
 #include "uf.cuh"
 
@@ -817,7 +818,10 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     int8_t* knn_open;  // the kNN kernel's tie flags, then "seed not provably final"
     FHG_TRY(ws.alloc(&knn_open, (size_t)n));
     // the neighbours[:, 1:] matrix (kq - 1 columns) straight from the kNN kernel
-    FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
+    if (const RadiusUse* ru = radius_in_use())
+        FHG_TRY(knn_with_radius(ix, k, *ru, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
+    else
+        FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
     FHG_TRY(ws.alloc(&core2, (size_t)n));
     if (weighted) {
         float* w_s;

@@ -6,6 +6,7 @@
 
 #include "index.cuh"
 #include "mst.cuh"
+#include "radius.cuh"
 #include "trees.cuh"
 
 #include <initializer_list>
@@ -184,6 +185,121 @@ FHG_API int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t
         return FHG_ERR_INVALID;
     }
     return index_knn(*index, k, nullptr, nullptr, rdist_dev, idx_dev, as_stream(stream));
+}
+
+// ------------------------------------------------------ learned radius
+FHG_API int fhg_radius_param_count(void) { return kRadiusParams; }
+
+FHG_API int fhg_radius_features(fhg_index* index, float* feat_dev, void* stream) {
+    if (!index || !feat_dev) {
+        set_error("fhg_radius_features: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return radius_features(*index, index->orig, feat_dev, as_stream(stream));
+}
+
+FHG_API int fhg_radius_targets(fhg_index* index, int32_t k, float* target_dev, void* stream) {
+    if (!index || !target_dev) {
+        set_error("fhg_radius_targets: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (k < 1 || k > 64) {
+        set_error("fhg_radius_targets: k must be in [1, 64] (got %d)", k);
+        return FHG_ERR_INVALID;
+    }
+    return radius_targets(*index, k, target_dev, as_stream(stream));
+}
+
+FHG_API int fhg_radius_init(float* params_dev, const float* feat_dev, const float* target_dev,
+                            int64_t n, uint64_t seed, void* stream) {
+    if (!params_dev || !feat_dev || !target_dev) {
+        set_error("fhg_radius_init: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return radius_init(params_dev, feat_dev, target_dev, n, seed, as_stream(stream));
+}
+
+FHG_API int fhg_radius_forward(const float* params_dev, const float* feat_dev, int64_t n,
+                               float* log_radius_dev, void* stream) {
+    if (!params_dev || !feat_dev || !log_radius_dev) {
+        set_error("fhg_radius_forward: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return radius_predict(params_dev, feat_dev, n, 1.0f, log_radius_dev, nullptr,
+                          as_stream(stream));
+}
+
+FHG_API int fhg_radius_backward(const float* params_dev, const float* feat_dev,
+                                const float* target_dev, const int32_t* rows_dev, int64_t batch,
+                                float* grad_dev, float* loss_dev, void* stream) {
+    if (!params_dev || !feat_dev || !target_dev || !rows_dev || !grad_dev || !loss_dev) {
+        set_error("fhg_radius_backward: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return radius_grad(params_dev, feat_dev, target_dev, rows_dev, batch, grad_dev, loss_dev,
+                       as_stream(stream));
+}
+
+FHG_API int fhg_radius_train(float* params_dev, const float* feat_dev, const float* target_dev,
+                             int64_t n, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                             float* loss_curve_dev, void* stream) {
+    if (!params_dev || !feat_dev || !target_dev) {
+        set_error("fhg_radius_train: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return radius_train(params_dev, feat_dev, target_dev, n, steps, batch, lr, seed,
+                        loss_curve_dev, as_stream(stream));
+}
+
+FHG_API int fhg_radius_use(const float* params_dev, float margin) {
+    if (params_dev && !(margin > 0.0f)) {
+        set_error("fhg_radius_use: margin must be positive");
+        return FHG_ERR_INVALID;
+    }
+    radius_set_use(params_dev, margin);
+    return FHG_OK;
+}
+
+FHG_API int fhg_radius_fallbacks(int64_t* count_host, void* stream) {
+    if (!count_host) {
+        set_error("fhg_radius_fallbacks: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return radius_last_fallbacks(count_host, as_stream(stream));
+}
+
+FHG_API int fhg_index_knn_radius(fhg_index* index, int32_t k, const float* params_dev,
+                                 float margin, float* rdist_dev, int32_t* idx_dev,
+                                 int64_t* fallbacks_host, void* stream) {
+    if (!index || !params_dev || !rdist_dev || !idx_dev) {
+        set_error("fhg_index_knn_radius: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (!(margin > 0.0f)) {
+        set_error("fhg_index_knn_radius: margin must be positive");
+        return FHG_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    RadiusUse use;
+    use.params = params_dev;
+    use.margin = margin;
+    FHG_TRY(knn_with_radius(*index, k, use, nullptr, nullptr, rdist_dev, idx_dev, s));
+    if (fallbacks_host) return radius_last_fallbacks(fallbacks_host, s);
+    return FHG_OK;
+}
+
+FHG_API int fhg_knn_scan_count(fhg_index* index, int32_t k, const float* params_dev, float margin,
+                               int64_t* scans_host, int64_t* fallbacks_host, void* stream) {
+    if (!index || !scans_host) {
+        set_error("fhg_knn_scan_count: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (k < 1 || k > 64) {
+        set_error("knn: k must be in [1, 64] (got %d)", k);
+        return FHG_ERR_INVALID;
+    }
+    return knn_scan_count(*index, k, params_dev, margin, scans_host, fallbacks_host,
+                          as_stream(stream));
 }
 
 FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples,

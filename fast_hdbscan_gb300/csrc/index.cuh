@@ -114,7 +114,20 @@ int index_free(fhg_index* ix, cudaStream_t s);
 //             matrix of the fit)
 //   tie_s   : per point (Morton order), 1 when some point outside its list
 //             lies at exactly its k-th distance
+// A capped kNN pass (all members nullable, Morton order): cap2 = every
+// query's squared search radius; queries with fewer than k points within it
+// get fail = 1 (and fail_count, if given, counts them) and no output.
+// redo: only these queries search (uncapped).  scan_count (nullable, any
+// pass): adds the number of buckets the pass scanned.
+struct KnnCap {
+    const float* cap2 = nullptr;
+    const uint8_t* redo = nullptr;
+    uint8_t* fail = nullptr;
+    unsigned long long* fail_count = nullptr;
+    unsigned long long* scan_count = nullptr;
+};
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-              cudaStream_t s, int8_t* tie_s = nullptr, int io_stride = 0, int io_skip = 0);
+              cudaStream_t s, int8_t* tie_s = nullptr, int io_stride = 0, int io_skip = 0,
+              const KnnCap& cap = KnnCap());
 
 }  // namespace fhg

@@ -47,7 +47,12 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
                                                               float* __restrict__ d_o,
                                                               int32_t* __restrict__ i_o,
                                                               int8_t* __restrict__ tie_s,
-                                                              int io_stride, int io_skip) {
+                                                              int io_stride, int io_skip,
+                                                              const float* __restrict__ cap2,
+                                                              const uint8_t* __restrict__ redo,
+                                                              uint8_t* __restrict__ fail,
+                                                              unsigned long long* fail_count,
+                                                              unsigned long long* scan_count) {
     __shared__ int32_t s_stack[kKnnWarps][kStack];
     __shared__ float4 s_cand[kKnnWarps][32 * (SP / 4)];
     __shared__ int32_t s_corig[kKnnWarps][32];
@@ -55,7 +60,11 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
     const int64_t leaf = (int64_t)blockIdx.x * kKnnWarps + warp;
     if (leaf >= ix.nleaves) return;
     const int64_t qi = leaf * kLeaf + lane;
-    const bool valid = qi < ix.n;
+    // redo (nullable): only these queries search (the fallback of a capped
+    // pass); cap2 (nullable): every query's list starts full of sentinels at
+    // its squared search radius, so only points within it are considered.
+    const bool valid = qi < ix.n && (!redo || redo[qi]);
+    if (redo && !__any_sync(kFull, valid)) return;
     float q[DIM];
     {
         float t[SP];
@@ -72,7 +81,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
     // Slots [0, K-k) hold a 0 sentinel so that the live list has length k;
     // empty live slots hold (+inf, INT32_MAX).
     unsigned long long key[K];
-    const unsigned long long kEmptyKey = pack_entry(INFINITY, INT32_MAX);
+    const unsigned long long kEmptyKey =
+        pack_entry(cap2 && valid ? cap2[qi] : INFINITY, INT32_MAX);
 #pragma unroll
     for (int j = 0; j < K; ++j) key[j] = (j < K - k) ? 0ull : kEmptyKey;
     float4* cand = s_cand[warp];
@@ -92,7 +102,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
             rejmin = fminf(rejmin, dd);
             return;
         }
-        rejmin = fminf(rejmin, entry_dist(key[K - 1]));
+        // (a sentinel of a capped list leaving is no point)
+        if (entry_orig(key[K - 1]) != INT32_MAX) rejmin = fminf(rejmin, entry_dist(key[K - 1]));
         bool gt_hi = true;
 #pragma unroll
         for (int j = K - 1; j > 0; --j) {
@@ -107,7 +118,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
     // k-th distance (one bit each), then each lane inserts only its own
     // marked candidates -- the warp pays for the busiest lane, not for every
     // candidate some lane wants.
+    int scans = 0;  // buckets this warp scanned
     auto scan_leaf = [&](int64_t lf, bool need) {
+        ++scans;
         const int64_t base = lf * kLeaf;
         const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
         float own[SP];  // this lane's candidate (lane t holds candidate t)
@@ -213,7 +226,17 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
         }
         x = (x - 1) >> 1;
     }
+    if (scan_count && lane == 0) atomicAdd(scan_count, (unsigned long long)scans);
     if (!valid) return;
+    // Certification: a capped list whose k-th slot still holds a sentinel had
+    // fewer than k points within the radius -- its query is searched again
+    // without a cap.  A full list is the exact answer: every point closer than
+    // its k-th entry lies within the radius and was considered.
+    if (cap2 && entry_orig(key[K - 1]) == INT32_MAX) {
+        fail[qi] = 1;
+        if (fail_count) atomicAdd(fail_count, 1ull);
+        return;
+    }
     if (tie_s) tie_s[qi] = rejmin == entry_dist(key[K - 1]) ? 1 : 0;
     const int64_t o_row = orig[qi];
 #pragma unroll
@@ -234,7 +257,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
 
 template <int DIM, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-               int8_t* tie_s, int io_stride, int io_skip, cudaStream_t s) {
+               int8_t* tie_s, int io_stride, int io_skip, const KnnCap& cap, cudaStream_t s) {
     // padded width; for d > 8 the kernels run over all SP = DIM padded
     // coordinates (the padding is zero and adds exact zeros to distances)
     constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);
@@ -242,25 +265,27 @@ int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o,
     Stage stage(s, "knn_kernel");
     ::fhg::note_launch();
     knn_kernel<DIM, SP, K><<<g, kKnnWarps * 32, 0, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o,
-                                                         tie_s, io_stride, io_skip);
+                                                         tie_s, io_stride, io_skip, cap.cap2,
+                                                         cap.redo, cap.fail, cap.fail_count,
+                                                         cap.scan_count);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
 template <int DIM>
 int dispatch_k(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-               int8_t* tie_s, int ios, int iok, cudaStream_t s) {
-    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
-    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
-    if (k <= 24) return launch_knn<DIM, 24>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
-    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
-    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, s);
+               int8_t* tie_s, int ios, int iok, const KnnCap& c, cudaStream_t s) {
+    if (k <= 8) return launch_knn<DIM, 8>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, c, s);
+    if (k <= 16) return launch_knn<DIM, 16>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, c, s);
+    if (k <= 24) return launch_knn<DIM, 24>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, c, s);
+    if (k <= 32) return launch_knn<DIM, 32>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, c, s);
+    return launch_knn<DIM, 64>(ix, k, d_s, i_s, d_o, i_o, tie_s, ios, iok, c, s);
 }
 
 }  // namespace
 
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
-              cudaStream_t s, int8_t* tie_s, int io_stride, int io_skip) {
+              cudaStream_t s, int8_t* tie_s, int io_stride, int io_skip, const KnnCap& cap) {
     if (io_stride <= 0) io_stride = k;
     if (k < 1 || k > 64) {
         set_error("knn: k must be in [1, 64] (got %d)", k);
@@ -273,18 +298,18 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
     }
     Stage stage(s, "knn");
     switch (ix.d) {
-        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-        case 8: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+        case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 3: return dispatch_k<3>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 4: return dispatch_k<4>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 5: return dispatch_k<5>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 6: return dispatch_k<6>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 7: return dispatch_k<7>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+        case 8: return dispatch_k<8>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
         default:
             if (ix.d <= 16)
-                return dispatch_k<16>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
-            return dispatch_k<32>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, s);
+                return dispatch_k<16>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
+            return dispatch_k<32>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
     }
 }
 

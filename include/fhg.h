@@ -349,6 +349,57 @@ int fhg_hdbscan_fit_export(const float* X_dev, int64_t n, int32_t d, int32_t min
                            double* linkage_host, void* ct_records_dev, void* ct_records_host,
                            void* stream);
 
+/* ---- Learned kNN search radius (no reference counterpart: a network that
+ * proposes each query's search radius for the kNN of core_distances /
+ * parallel_tree_query, boruvka.py:561-585; the certified search keeps every
+ * kNN output identical to fhg_index_knn's).
+ * The model is a float32 block of fhg_radius_param_count() parameters:
+ * W1[64][11] b1[64] W2[64][64] b2[64] w3[64] b3 mu[11] sigma[11], the network
+ * 11 -> 64 -> 64 -> 1 (ReLU, bfloat16 operands, float32 accumulation) on
+ * standardised features, predicting the log core distance. */
+int fhg_radius_param_count(void);
+/* 11 features per point (caller order, row-major n x 11): the first three
+ * coordinates scaled to the bounding box and the log point density of the
+ * point's bucket and its 7 ancestor nodes. */
+int fhg_radius_features(fhg_index* index, float* feat_dev, void* stream);
+/* Training targets: log of every point's k-th neighbour distance (caller
+ * order), the point itself counted. */
+int fhg_radius_targets(fhg_index* index, int32_t k, float* target_dev, void* stream);
+/* Initial parameters: He-normal weights from `seed`, zero biases, b3 = the
+ * target mean, mu / sigma the feature means and deviations of the n rows. */
+int fhg_radius_init(float* params_dev, const float* feat_dev, const float* target_dev,
+                    int64_t n, uint64_t seed, void* stream);
+/* Forward pass (tensor-core kernel): log radius of n feature rows. */
+int fhg_radius_forward(const float* params_dev, const float* feat_dev, int64_t n,
+                       float* log_radius_dev, void* stream);
+/* Backward pass over the batch rows_dev[0..batch): grad_dev (the trained
+ * parameters, everything before mu) = gradient of the mean squared error,
+ * *loss_dev = that error. */
+int fhg_radius_backward(const float* params_dev, const float* feat_dev, const float* target_dev,
+                        const int32_t* rows_dev, int64_t batch, float* grad_dev, float* loss_dev,
+                        void* stream);
+/* `steps` Adam steps (learning rate lr) on random batches of `batch` rows;
+ * loss_curve_dev (optional, `steps` floats) receives every step's loss. */
+int fhg_radius_train(float* params_dev, const float* feat_dev, const float* target_dev,
+                     int64_t n, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                     float* loss_curve_dev, void* stream);
+/* Fits made afterwards by the calling thread search their kNN with this
+ * model (radius = exp(prediction) * margin); NULL returns to the plain
+ * search.  The parameters must stay alive while in use. */
+int fhg_radius_use(const float* params_dev, float margin);
+/* Queries the calling thread's last radius search had to search again. */
+int fhg_radius_fallbacks(int64_t* count_host, void* stream);
+/* fhg_index_knn with the model's radius and the certified fallback: the same
+ * outputs; *fallbacks_host (optional) = queries searched again. */
+int fhg_index_knn_radius(fhg_index* index, int32_t k, const float* params_dev, float margin,
+                         float* rdist_dev, int32_t* idx_dev, int64_t* fallbacks_host,
+                         void* stream);
+/* Work measure of the kNN of every point: *scans_host = buckets scanned,
+ * with the model (params_dev non-NULL) or by the plain search (NULL);
+ * *fallbacks_host (optional) = queries searched again. */
+int fhg_knn_scan_count(fhg_index* index, int32_t k, const float* params_dev, float margin,
+                       int64_t* scans_host, int64_t* fallbacks_host, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
