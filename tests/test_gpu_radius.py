@@ -111,32 +111,34 @@ def test_fit_with_radius_identical(trained):
 
 
 def test_training_gain_and_certification_cost(trained):
-    """What training buys: at the trained margin, the trained network leaves
-    far fewer queries to the fallback pass than the same network untrained
-    (initial weights), and the certified search scans at most 10 % more
-    buckets than the plain search.  (On this index the plain search already
-    starts every query from its own bucket's k-th distance, so the learned
-    bound prunes little beyond it -- measured and reported, not assumed.)"""
+    """What training buys, on held-out points: the trained network's log
+    radius is far closer to the true log core distance than the best constant
+    (the target mean) and than the untrained network; and the certified
+    search with it scans at most 10 % more buckets than the plain search.
+    (The plain search already starts every query from its own bucket's k-th
+    distance, so on this index the learned bound prunes little beyond it:
+    the printed bucket counts are the measured gain.)"""
     import ctypes
 
     from fast_hdbscan_gb300 import _native
-    from fast_hdbscan_gb300.numba_kdtree import build_kdtree
     from fast_hdbscan_gb300.radius import RadiusModel
 
-    X = synthetic.varying_density(n=1_000_000, seed=15)
-    tree = build_kdtree(X)
+    tree, f, t = _feat_target(n=1_000_000, seed=15)
+    t = t.cpu().numpy().astype(np.float64)
     untrained = RadiusModel.train(synthetic.varying_density(n=100_000, seed=16),
                                   min_samples=15, steps=1, seed=5)
+    rmse = {"constant": float(np.std(t))}
+    for name, m in (("trained", trained), ("untrained", untrained)):
+        rmse[name] = float(np.sqrt(np.mean((m.predict_log(feat=f) - t) ** 2)))
     lib = _native.load()
-    res = {}
-    for name, prm in (("plain", None), ("trained", trained.params),
-                      ("untrained", untrained.params)):
+    scans = {}
+    for name, prm in (("plain", None), ("trained", trained.params)):
         sc, fb = ctypes.c_int64(0), ctypes.c_int64(0)
         _native.check(lib.fhg_knn_scan_count(tree.index.handle, 16, _native.vptr(prm),
                                              ctypes.c_float(trained.margin), ctypes.byref(sc),
                                              ctypes.byref(fb), _native.stream_ptr()))
-        res[name] = (sc.value, fb.value)
-    print("bucket scans / fallbacks:", res)
-    assert res["trained"][1] < 0.2 * res["untrained"][1]
-    assert res["trained"][0] < res["untrained"][0]
-    assert res["trained"][0] <= 1.10 * res["plain"][0]
+        scans[name] = (sc.value, fb.value)
+    print("log-radius rmse:", rmse, "bucket scans / fallbacks:", scans)
+    assert rmse["trained"] < 0.6 * rmse["constant"]
+    assert rmse["trained"] < rmse["untrained"]
+    assert scans["trained"][0] <= 1.10 * scans["plain"][0]
