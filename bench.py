@@ -59,6 +59,13 @@ OTHER_WORKLOADS = {
                        min_samples=15, min_cluster_size=500, seed=3, algorithm="kruskal",
                        knn_k=16,
                        generator="200 Gaussians, std lognormal(0,1), centres U[-100,100]^3"),
+    # the high-dimensional route (d > 30 without weights: the kNN-graph
+    # back-end, nndescent.py:179) on the exact tensor-core kNN, knn_k = 30
+    "highd1m": dict(workload="aniso_highdim_1M_64d_knn_graph", n=1_000_000, d=64,
+                    min_samples=10, min_cluster_size=500, seed=2, algorithm="knn_graph",
+                    knn_k=30, cpu_sample=30_000,
+                    generator="50 anisotropic Gaussians (covariance A A^T, A_ij ~ N(0, 0.3^2)),"
+                              " centres N(0, 4 I)"),
 }
 CPU_SAMPLE_N = 1_000_000
 
@@ -77,7 +84,8 @@ def parse_args():
     ap.add_argument("--workload", default="fit", choices=["fit", "batched", *OTHER_WORKLOADS],
                     help="fit: the metric's 10M x 3-D fit; batched: many independent fits; "
                          "umap2m: the 2M x 5-D fit; kruskal10m: the 10M x 3-D fit on the "
-                         "kNN-graph Kruskal back-end")
+                         "kNN-graph Kruskal back-end; highd1m: the 1M x 64-D fit on the "
+                         "kNN-graph route with the tensor-core kNN")
     ap.add_argument("--instances", type=int, default=4096, help="batched workload size")
     return ap.parse_args()
 
@@ -105,6 +113,8 @@ def make_data(n, seed):
 
     if WORKLOAD["workload"].startswith("umap_like"):
         return synthetic.umap_like(n, seed=seed, dim=WORKLOAD["d"])
+    if WORKLOAD["workload"].startswith("aniso_highdim"):
+        return synthetic.aniso_highdim(n, seed=seed, dim=WORKLOAD["d"])
     return synthetic.varying_density(n, seed=seed)
 
 
@@ -224,6 +234,7 @@ def run_gb300(args):
     ms, mcs = WORKLOAD["min_samples"], WORKLOAD["min_cluster_size"]
     pre = WORKLOAD.get("metric") == "precomputed"
     kruskal = WORKLOAD.get("algorithm") == "kruskal" and not pre
+    kgraph = WORKLOAD.get("algorithm") == "knn_graph"
     knn_k = WORKLOAD.get("knn_k", 0)
     Xh = make_data(n, WORKLOAD["seed"] + rank)
     d = Xh.shape[1]
@@ -243,7 +254,7 @@ def run_gb300(args):
     ctp, ctc, ctl, cts = (E(2 * n, np.int64), E(2 * n, np.int64), E(2 * n, np.float32),
                           E(2 * n, np.float32))
     nbrs, sel = E((n, ms), np.int32), E(n, np.int64)
-    core = E(n, np.float64 if (kruskal or pre) else np.float32)
+    core = E(n, np.float64 if (kruskal or pre or kgraph) else np.float32)
     rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
     V = _native.vptr
     stream = torch.cuda.current_stream()
@@ -255,6 +266,12 @@ def run_gb300(args):
                 0.0, V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
                 ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
                 _native.stream_ptr()))
+            return
+        if kgraph:
+            _native.check(lib.fhg_hdbscan_fit_knn_graph(
+                V(Xd), n, d, ms, knn_k, mcs, 0, float("inf"), 0, 0.0, 0.0, V(labels), V(probs),
+                V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows),
+                V(nbrs), V(core), V(sel), ctypes.byref(nsel), _native.stream_ptr()))
             return
         if kruskal:
             _native.check(lib.fhg_hdbscan_fit_kruskal(
@@ -300,9 +317,11 @@ def run_gb300(args):
 
     # per-stage share and the dominant kernel's roofline
     # kernel records nest inside the stage records: shares are over stages
-    nested = ("knn_kernel", "search_kernel")
+    nested = ("knn_kernel", "search_kernel", "hd_cand_kernel", "hd_rerank_kernel",
+              "hd_exact_kernel")
     total_stage = sum(v[0] for k, v in stages.items() if k not in nested) or 1.0
-    kernel_stages = {k: v for k, v in stages.items() if k in ("knn_kernel", "search_kernel")}
+    kernel_stages = {k: v for k, v in stages.items()
+                     if k in ("knn_kernel", "search_kernel", "hd_cand_kernel")}
     dom = max(kernel_stages, key=lambda k: kernel_stages[k][0]) if kernel_stages else None
     peaks = {}
     try:
@@ -312,7 +331,27 @@ def run_gb300(args):
         peak, peak_src = 6800.0, "fallback"
     roofline = None
     rounds = max(1, stages.get("boruvka_search", [0, 1])[1] // max(args.steps, 1))
-    if dom:
+    if dom == "hd_cand_kernel":
+        # tensor-bound: 2 n^2 K flops per launch, K = 3 x 64 (two-term bf16
+        # split) for d = 64; against the measured cuBLAS bf16 burst peak
+        tot_ms, cnt = kernel_stages[dom]
+        per_launch_ms = tot_ms / cnt
+        kdepth = 3 * (32 if d <= 32 else (64 if d <= 64 else 96))
+        flops = 2.0 * n * n * kdepth
+        achieved = flops / (per_launch_ms / 1e3) / 1e12
+        try:
+            tpeak, tsrc = float(peaks["bf16_tflops"]), "measured cuBLAS bf16 burst"
+        except (KeyError, ValueError, TypeError):
+            tpeak, tsrc = 1900.0, "fallback"
+        roofline = {"bound": "tensor", "kernel": dom, "achieved": round(achieved, 2),
+                    "peak": tpeak, "peak_source": tsrc, "unit": "TFLOP/s",
+                    "frac": round(achieved / tpeak, 5), "traffic": None,
+                    "algorithmic_flops_per_launch": flops,
+                    "launches_per_step": cnt // max(args.steps, 1),
+                    "ms_per_launch": round(per_launch_ms, 4),
+                    "kernel_share_of_stage_time": round(tot_ms / total_stage, 4),
+                    "note": "mma.sync m16n8k16 bf16 (legacy tensor path)"}
+    elif dom:
         tot_ms, cnt = kernel_stages[dom]
         per_launch_ms = tot_ms / cnt
         alg = algorithmic_bytes(dom, n, (max(knn_k, ms) if kruskal else ms) + 1,
@@ -332,7 +371,7 @@ def run_gb300(args):
     # network trained on a 2M-point draw of the generator with another seed
     # (training untimed), labels checked identical to the plain fit's
     learned = None
-    if not (pre or kruskal or args.no_radius):
+    if not (pre or kruskal or kgraph or args.no_radius):
         from fast_hdbscan_gb300.radius import RadiusModel
 
         lab_plain, prob_plain = labels.clone(), probs.clone()
@@ -396,7 +435,7 @@ def run_gb300(args):
         # labels i64, probabilities f32, sorted MST (n-1) x 3 f64, linkage (n-1) x 4 f64,
         # condensed tree 28 B/row, neighbours n x ms i32, core distances f32 (Kruskal: f64)
         d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 28 + n * ms * 4
-               + n * (8 if (kruskal or pre) else 4))
+               + n * (8 if (kruskal or pre or kgraph) else 4))
         h2d = n * WORKLOAD["graph_k"] * 16 if pre else n * d * 4  # graph: rows, cols, f64
         e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -444,6 +483,10 @@ def _oracle_fit_time(n, nthreads):
              np.arange(0, n * gk + 1, gk)), shape=(n, n))
         t0 = time.perf_counter()
         mst, _, _ = O.precomputed_kruskal(G, WORKLOAD["min_samples"])
+        O.clusters_from_spanning_tree(mst, WORKLOAD["min_cluster_size"])
+    elif WORKLOAD.get("algorithm") == "knn_graph":  # hdbscan.py:446 -> nndescent.py:179
+        mst, _, _ = O.kruskal_knn(O.build_kdtree(X), WORKLOAD["min_samples"], WORKLOAD["knn_k"],
+                                  mode=0, nthreads=nthreads)
         O.clusters_from_spanning_tree(mst, WORKLOAD["min_cluster_size"])
     elif WORKLOAD.get("algorithm") == "kruskal":  # hdbscan.py:306 with algorithm="kruskal"
         mst, _, _ = O.kruskal_knn(O.build_kdtree(X), WORKLOAD["min_samples"], WORKLOAD["knn_k"],
@@ -575,6 +618,10 @@ def main():
                        f"algorithm='{WORKLOAD['algorithm']}')")
         elif WORKLOAD.get("algorithm") == "kruskal":
             METRIC += f" (algorithm='kruskal', knn_k={WORKLOAD['knn_k']})"
+        elif WORKLOAD.get("algorithm") == "knn_graph":
+            METRIC += f" (kNN-graph route, exact tensor-core kNN, knn_k={WORKLOAD['knn_k']})"
+        if args.cpu_sample == CPU_SAMPLE_N and "cpu_sample" in WORKLOAD:
+            args.cpu_sample = WORKLOAD["cpu_sample"]
         args.workload = "fit"
     if args.impl == "reference":
         run_reference(args)

@@ -82,6 +82,13 @@ SIGNATURES = {
     "fhg_radius_fallbacks": (_INT, [ctypes.POINTER(_I64), _P]),
     "fhg_index_knn_radius": (_INT, [_P, _I32, _P, ctypes.c_float, _P, _P, ctypes.POINTER(_I64),
                                     _P]),
+    "fhg_highd_knn": (_INT, [_P, _I64, _I32, _I32, _P, _P, ctypes.POINTER(_I64), _P]),
+    "fhg_knn_graph_mst": (_INT, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, ctypes.POINTER(_I64),
+                                 _P]),
+    "fhg_hdbscan_fit_knn_graph": (_INT, [_P, _I64, _I32, _I32, _I32, _I64, _I32, _D, _INT, _D,
+                                         _D, _P, _P, _P, _P, _P, _P, _P, _P,
+                                         ctypes.POINTER(_I64), _P, _P, _P,
+                                         ctypes.POINTER(_I64), _P]),
     "fhg_knn_scan_count": (_INT, [_P, _I32, _P, ctypes.c_float, ctypes.POINTER(_I64),
                                   ctypes.POINTER(_I64), _P]),
 }

@@ -5,6 +5,7 @@
 #include <mutex>
 
 #include "index.cuh"
+#include "highd.cuh"
 #include "mst.cuh"
 #include "radius.cuh"
 #include "trees.cuh"
@@ -300,6 +301,31 @@ FHG_API int fhg_knn_scan_count(fhg_index* index, int32_t k, const float* params_
     }
     return knn_scan_count(*index, k, params_dev, margin, scans_host, fallbacks_host,
                           as_stream(stream));
+}
+
+FHG_API int fhg_highd_knn(const float* X_dev, int64_t n, int32_t d, int32_t k, float* rdist_dev,
+                          int32_t* idx_dev, int64_t* fallbacks_host, void* stream) {
+    if (n > 0 && (!X_dev || !rdist_dev || !idx_dev)) {
+        set_error("fhg_highd_knn: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return highd_knn(X_dev, n, d, k, rdist_dev, idx_dev, fallbacks_host, as_stream(stream));
+}
+
+FHG_API int fhg_knn_graph_mst(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                              int32_t knn_k, double* edges_dev, int32_t* neighbors_dev,
+                              double* core_dev, int64_t* n_components_host, void* stream) {
+    if (n > 0 && (!X_dev || !edges_dev || !core_dev || !n_components_host)) {
+        set_error("fhg_knn_graph_mst: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (min_samples < 1 || knn_k < min_samples) {
+        set_error("fhg_knn_graph_mst: needs 1 <= min_samples <= knn_k (got %d, %d)", min_samples,
+                  knn_k);
+        return FHG_ERR_INVALID;
+    }
+    return kruskal_mst_of_lists(n, min_samples, knn_k + 1, nullptr, nullptr, X_dev, d, edges_dev,
+                                neighbors_dev, core_dev, n_components_host, as_stream(stream));
 }
 
 FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples,
@@ -771,7 +797,8 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
              int64_t* ct_rows_host, int32_t* neighbors_dev, float* core_dev,
              int64_t* selected_dev, int64_t* n_selected_host, void* stream,
              const FitExport& ex, int32_t knn_k = 0, int32_t query_k = 0,
-             double* core64_dev = nullptr, const GraphInput* graph = nullptr) {
+             double* core64_dev = nullptr, const GraphInput* graph = nullptr,
+             bool brute_knn = false) {
     FHG_TRY(check_ptrs("fhg_hdbscan_fit", {labels_dev, probs_dev}));
     if (!graph) FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev}));
     if (min_samples < 1 || min_cluster_size < 1) {
@@ -790,7 +817,7 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
     SideCopies side(s);  // declared before the workspace: joins after its frees are queued
     Workspace ws(s);
     fhg_index* ix = nullptr;
-    if (!graph) FHG_TRY(index_build(X_dev, n, d, s, &ix));
+    if (!graph && !brute_knn) FHG_TRY(index_build(X_dev, n, d, s, &ix));
     struct IndexGuard {
         fhg_index* p;
         cudaStream_t s;
@@ -815,8 +842,12 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
         FHG_TRY(ws.alloc(&kedges, (size_t)(3 * (n - 1))));
         if (!core64) FHG_TRY(ws.alloc(&core64, (size_t)n));
         int64_t nc = 0;
-        FHG_TRY(kruskal_knn_mst(*ix, min_samples, query_k, sample_weights_dev, kedges,
-                                neighbors_dev, core64, &nc, s));
+        if (brute_knn)  // the high-dimensional kNN graph (nndescent.py:179)
+            FHG_TRY(kruskal_mst_of_lists(n, min_samples, query_k, nullptr, nullptr, X_dev, d,
+                                         kedges, neighbors_dev, core64, &nc, s));
+        else
+            FHG_TRY(kruskal_knn_mst(*ix, min_samples, query_k, sample_weights_dev, kedges,
+                                    neighbors_dev, core64, &nc, s));
         int32_t *src, *dst;
         double* w;
         FHG_TRY(split_mst_f64(ws, kedges, n - 1, &src, &dst, &w));
@@ -939,6 +970,27 @@ FHG_API int fhg_hdbscan_fit_kruskal(
                     ct_parent_dev, ct_child_dev, ct_lambda_dev, ct_size_dev, ct_rows_host,
                     neighbors_dev, nullptr, selected_dev, n_selected_host, stream, FitExport(),
                     knn_k, query_k, core_dev);
+}
+
+FHG_API int fhg_hdbscan_fit_knn_graph(
+    const float* X_dev, int64_t n, int32_t d, int32_t min_samples, int32_t knn_k,
+    int64_t min_cluster_size, int32_t selection_method, double max_cluster_size,
+    int allow_single_cluster, double epsilon, double persistence, int64_t* labels_dev,
+    float* probs_dev, double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+    int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev, int64_t* ct_rows_host,
+    int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev, int64_t* n_selected_host,
+    void* stream) {
+    if (knn_k < 1 || knn_k < min_samples) {
+        set_error("fhg_hdbscan_fit_knn_graph: knn_k must be at least max(1, min_samples) "
+                  "(got %d)", knn_k);
+        return FHG_ERR_INVALID;
+    }
+    return fit_impl(X_dev, n, d, min_samples, min_cluster_size, selection_method,
+                    max_cluster_size, allow_single_cluster, epsilon, persistence, nullptr, 0,
+                    labels_dev, probs_dev, mst_dev, linkage_dev, ct_parent_dev, ct_child_dev,
+                    ct_lambda_dev, ct_size_dev, ct_rows_host, neighbors_dev, nullptr,
+                    selected_dev, n_selected_host, stream, FitExport(), knn_k, knn_k + 1,
+                    core_dev, nullptr, /*brute_knn=*/true);
 }
 
 FHG_API int fhg_hdbscan_fit_precomputed(

@@ -1,0 +1,503 @@
+// Exact kNN for high-dimensional points (d up to 96) by brute force on the
+// tensor cores, behind the reference's d > 30 route (hdbscan.py:447 ->
+// nndescent.py:179 compute_mst_from_knn_graph, whose kNN graph pynndescent
+// approximates; here it is exact).
+//
+// 1. Candidates.  The centred points c = x - mean are split into two
+//    bfloat16 terms, hi = bf16(c) and lo = bf16(c - hi), and every query's
+//    squared distance to every point is estimated as
+//        D~ = |y_i|^2 + |y_j|^2 - 2 (hi_i.hi_j + hi_i.lo_j + lo_i.hi_j)
+//    (y = hi + lo) with one bf16 GEMM of depth 3 * dp (mma.sync m16n8k16,
+//    float32 accumulation).  A CTA holds 64 queries (16 per warp, operands in
+//    registers) and streams all points through shared memory in chunks of
+//    64 (cp.async, double-buffered).  Each query keeps the L = k + 32 points
+//    of smallest D~ in a shared-memory buffer: an estimate below the query's
+//    current L-th value is appended, and a buffer that fills is cut back to
+//    its L smallest by ranking.
+// 2. Re-rank and certificate.  The L candidates' exact float32 squared
+//    distances (each difference, square and sum rounded in dimension order,
+//    as every kNN of the engine computes them) give the k nearest in
+//    (distance, index) order.  Every other point has D~ >= T, the L-th
+//    estimate, and the rounding analysis bounds the estimate's error:
+//      |c - y| <= (2^-16 + 2^-23) |c|  per point (two bf16 terms),
+//      |D~ - |y_i - y_j|^2| <= eta_i = (2 K + 4 dp + 16) 2^-24 (|y_i| + Ymax)^2
+//                                    + 2^-15 |c_i| Cmax
+//    (K = 3 dp float32 accumulations, which may truncate; the dropped
+//    lo_i.lo_j term).  So every non-candidate lies at true distance at least
+//      lb = sqrt(T - eta_i) - (2^-16 + 2^-23)(|c_i| + Cmax),
+//    and its float32 squared distance at least lb^2 (1 - (d + 8) 2^-23).  A
+//    query whose k-th exact candidate distance is below that bound is
+//    certified; the others (and none is assumed rare) are searched again.
+// 3. Fallback.  A warp per uncertified query scans every point in exact
+//    float32 with the same buffer-and-rank selection.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "highd.cuh"
+
+namespace fhg {
+namespace {
+
+constexpr int kHdWarps = 4;
+constexpr int kHdRows = 16;                    // queries per warp
+constexpr int kHdQ = kHdWarps * kHdRows;       // queries per CTA
+constexpr int kHdChunk = 64;                   // points per streamed chunk
+constexpr int kHdCap = 192;                    // candidate buffer per query
+constexpr int kHdTrigger = kHdCap - kHdChunk;  // cut back when fuller
+constexpr int kHdMaxL = 128;                   // candidates kept (k + 32)
+
+__device__ __forceinline__ unsigned long long hd_key(float dist, int32_t j) {
+    return ((unsigned long long)__float_as_uint(dist) << 32) | (uint32_t)j;
+}
+__device__ __forceinline__ float hd_dist(unsigned long long key) {
+    return __uint_as_float((uint32_t)(key >> 32));
+}
+
+// Column means (one block per dimension, a fixed summation order).
+__global__ void __launch_bounds__(256) hd_mean_kernel(const float* __restrict__ X, int64_t n,
+                                                      int d, float* __restrict__ mu) {
+    __shared__ double part[256];
+    const int col = blockIdx.x;
+    double a = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) a += X[i * d + col];
+    part[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) mu[col] = (float)(part[0] / (double)n);
+}
+
+// Per point: the operand rows A = [hi, hi, lo] and B = [hi, lo, hi] (dp
+// columns each, zero-padded), |y|^2 (float32, dimension order), |c|, and the
+// running maxima of |y| and |c| (float bit patterns, non-negative).
+__global__ void hd_split_kernel(const float* __restrict__ X, int64_t n, int d, int dp,
+                                const float* __restrict__ mu, __nv_bfloat16* __restrict__ A,
+                                __nv_bfloat16* __restrict__ B, float* __restrict__ ny,
+                                float* __restrict__ cn, unsigned* __restrict__ maxes) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int kw = 3 * dp;
+    float y2 = 0.0f, c2 = 0.0f;
+    for (int k = 0; k < dp; ++k) {
+        __nv_bfloat16 hi = __float2bfloat16_rn(0.0f), lo = hi;
+        if (k < d) {
+            const float c = __fsub_rn(X[i * d + k], mu[k]);
+            hi = __float2bfloat16_rn(c);
+            lo = __float2bfloat16_rn(__fsub_rn(c, __bfloat162float(hi)));
+            const float y = __fadd_rn(__bfloat162float(hi), __bfloat162float(lo));
+            y2 = __fadd_rn(y2, __fmul_rn(y, y));
+            c2 = __fadd_rn(c2, __fmul_rn(c, c));
+        }
+        A[i * kw + k] = hi;
+        A[i * kw + dp + k] = hi;
+        A[i * kw + 2 * dp + k] = lo;
+        B[i * kw + k] = hi;
+        B[i * kw + dp + k] = lo;
+        B[i * kw + 2 * dp + k] = hi;
+    }
+    ny[i] = y2;
+    const float c = sqrtf(c2);
+    cn[i] = c;
+    atomicMax(maxes, __float_as_uint(sqrtf(y2)));
+    atomicMax(maxes + 1, __float_as_uint(c));
+}
+
+__device__ __forceinline__ void hd_mma(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
+                                       uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Cuts a buffer of cnt unique keys back to its `keep` smallest, sorted: every
+// lane ranks its keys against the whole buffer, then writes the kept ones at
+// their ranks.  Returns the new count.
+__device__ __forceinline__ int hd_cut(unsigned long long* buf, int cnt, int keep, int lane) {
+    constexpr int kPer = kHdCap / 32;
+    unsigned long long mine[kPer];
+    int rank[kPer];
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int e = lane + 32 * m;
+        mine[m] = e < cnt ? buf[e] : ~0ull;
+        rank[m] = 0;
+    }
+    for (int e = 0; e < cnt; ++e) {
+        const unsigned long long o = buf[e];
+#pragma unroll
+        for (int m = 0; m < kPer; ++m) rank[m] += o < mine[m] ? 1 : 0;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < kPer; ++m)
+        if (lane + 32 * m < cnt && rank[m] < keep) buf[rank[m]] = mine[m];
+    __syncwarp();
+    return cnt < keep ? cnt : keep;
+}
+
+template <int KB>  // k-blocks of 16 in the operand depth 3 * dp
+__global__ void __launch_bounds__(kHdWarps * 32) hd_cand_kernel(
+    int64_t n, int L, const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B,
+    const float* __restrict__ ny, int32_t* __restrict__ cand, float* __restrict__ T) {
+    constexpr int KW = KB * 16;
+    constexpr int RS = KW + 8;  // shared row stride (bf16): conflict-free fragment loads
+    extern __shared__ __align__(16) unsigned char hd_smem[];
+    __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(hd_smem);  // [2][kHdChunk][RS]
+    unsigned long long* bufs =
+        reinterpret_cast<unsigned long long*>(Bs + 2 * kHdChunk * RS);  // [kHdQ][kHdCap]
+    float* npj = reinterpret_cast<float*>(bufs + kHdQ * kHdCap);       // [2][kHdChunk]
+    int* cnt = reinterpret_cast<int*>(npj + 2 * kHdChunk);              // [kHdQ]
+    float* tau = reinterpret_cast<float*>(cnt + kHdQ);                  // [kHdQ]
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int64_t q0 = (int64_t)blockIdx.x * kHdQ + warp * kHdRows;
+    if (threadIdx.x < kHdQ) {
+        cnt[threadIdx.x] = 0;
+        tau[threadIdx.x] = INFINITY;
+    }
+    // this warp's 16 query rows as A fragments
+    uint32_t a[KB][4];
+    const int64_t ra = q0 + g, rb = q0 + g + 8;
+#pragma unroll
+    for (int kb = 0; kb < KB; ++kb) {
+        const int c0 = kb * 16 + 2 * t;
+        a[kb][0] = ra < n ? *reinterpret_cast<const uint32_t*>(A + ra * KW + c0) : 0u;
+        a[kb][1] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0) : 0u;
+        a[kb][2] = ra < n ? *reinterpret_cast<const uint32_t*>(A + ra * KW + c0 + 8) : 0u;
+        a[kb][3] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0 + 8) : 0u;
+    }
+    const float nqa = ra < n ? ny[ra] : 0.0f, nqb = rb < n ? ny[rb] : 0.0f;
+    unsigned long long* bufa = bufs + (warp * kHdRows + g) * kHdCap;
+    unsigned long long* bufb = bufs + (warp * kHdRows + g + 8) * kHdCap;
+    int* cnta = cnt + warp * kHdRows + g;
+    int* cntb = cnt + warp * kHdRows + g + 8;
+
+    const int64_t nchunks = (n + kHdChunk - 1) / kHdChunk;
+    constexpr int kSeg = KW * 2 / 16;  // 16-byte segments per point row
+    auto stage = [&](int64_t chunk, int slot) {
+        __nv_bfloat16* dst = Bs + slot * kHdChunk * RS;
+        for (int e = threadIdx.x; e < kHdChunk * kSeg; e += blockDim.x) {
+            const int r = e / kSeg, sgm = e % kSeg;
+            const int64_t j = chunk * kHdChunk + r;
+            __nv_bfloat16* d16 = dst + r * RS + sgm * 8;
+            if (j < n) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(d16);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+                             "l"(B + j * KW + sgm * 8));
+            } else {
+                *reinterpret_cast<uint4*>(d16) = make_uint4(0u, 0u, 0u, 0u);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+        if (threadIdx.x < kHdChunk) {
+            const int64_t j = chunk * kHdChunk + threadIdx.x;
+            npj[slot * kHdChunk + threadIdx.x] = j < n ? ny[j] : 0.0f;
+        }
+    };
+    stage(0, 0);
+    float ta = INFINITY, tb = INFINITY;
+    for (int64_t c = 0; c < nchunks; ++c) {
+        const int slot = (int)(c & 1);
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        __syncthreads();  // chunk c visible; every warp is done with chunk c - 1
+        if (c + 1 < nchunks) stage(c + 1, slot ^ 1);
+        const __nv_bfloat16* bs = Bs + slot * kHdChunk * RS;
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+        for (int kb = 0; kb < KB; ++kb) {
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const __nv_bfloat16* row = bs + (nt * 8 + g) * RS + kb * 16 + 2 * t;
+                const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
+                const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
+                hd_mma(acc[nt], a[kb], b0, b1);
+            }
+        }
+        // estimates below the row's current L-th value join its buffer
+        const int64_t jb = c * kHdChunk;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int col = nt * 8 + 2 * t + (e & 1);
+                const int64_t j = jb + col;
+                if (j >= n) continue;
+                const bool hi = e >= 2;
+                const float dd =
+                    fmaxf(__fsub_rn(__fadd_rn(hi ? nqb : nqa, npj[slot * kHdChunk + col]),
+                                    __fmul_rn(2.0f, acc[nt][e])),
+                          0.0f);
+                if (dd < (hi ? tb : ta)) {
+                    const int p = atomicAdd(hi ? cntb : cnta, 1);
+                    (hi ? bufb : bufa)[p] = hd_key(dd, (int32_t)j);
+                }
+            }
+        }
+        __syncwarp();
+        // cut full buffers back to their L smallest
+        for (int r = 0; r < kHdRows; ++r) {
+            const int qr = warp * kHdRows + r;
+            const int cr = cnt[qr];
+            if (cr > kHdTrigger) {
+                unsigned long long* b = bufs + qr * kHdCap;
+                const int kept = hd_cut(b, cr, L, lane);
+                if (lane == 0) {
+                    cnt[qr] = kept;
+                    tau[qr] = kept >= L ? hd_dist(b[L - 1]) : INFINITY;
+                }
+                __syncwarp();
+            }
+        }
+        ta = tau[warp * kHdRows + g];
+        tb = tau[warp * kHdRows + g + 8];
+        __syncwarp();
+    }
+    // final cut: the L smallest estimates of every row, and the L-th estimate
+    for (int r = 0; r < kHdRows; ++r) {
+        const int qr = warp * kHdRows + r;
+        const int64_t q = q0 + r;
+        unsigned long long* b = bufs + qr * kHdCap;
+        const int kept = hd_cut(b, cnt[qr], L, lane);
+        if (q < n) {
+            for (int e = lane; e < L; e += 32)
+                cand[q * L + e] = e < kept ? (int32_t)(uint32_t)b[e] : -1;
+            if (lane == 0) T[q] = kept >= L ? hd_dist(b[L - 1]) : INFINITY;
+        }
+        __syncwarp();
+    }
+}
+
+// Exact float32 squared distance in dimension order (each difference, square
+// and sum rounded), from shared-memory query coordinates.
+__device__ __forceinline__ float hd_rdist(const float* __restrict__ q,
+                                          const float* __restrict__ x, int d) {
+    float r = 0.0f;
+    for (int k = 0; k < d; ++k) {
+        const float df = __fsub_rn(q[k], x[k]);
+        r = __fadd_rn(r, __fmul_rn(df, df));
+    }
+    return r;
+}
+
+// Re-rank: a warp per query.  Writes the certified queries' k nearest (rows
+// of k, (distance, index) order) and lists the others.
+__global__ void __launch_bounds__(128) hd_rerank_kernel(
+    int64_t n, int d, int dp, int k, int L, const float* __restrict__ X,
+    const int32_t* __restrict__ cand, const float* __restrict__ T, const float* __restrict__ ny,
+    const float* __restrict__ cn, const unsigned* __restrict__ maxes, float* __restrict__ rd_o,
+    int32_t* __restrict__ ix_o, int32_t* __restrict__ fail_list,
+    unsigned long long* __restrict__ fail_count) {
+    __shared__ float qs[4][96];
+    __shared__ unsigned long long keys[4][kHdMaxL];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t q = (int64_t)blockIdx.x * 4 + warp;
+    if (q >= n) return;
+    for (int e = lane; e < d; e += 32) qs[warp][e] = X[q * d + e];
+    __syncwarp();
+    int cntc = 0;
+    for (int e = lane; e < L; e += 32) {
+        const int32_t j = cand[q * L + e];
+        keys[warp][e] = j >= 0 ? hd_key(hd_rdist(qs[warp], X + (int64_t)j * d, d), j) : ~0ull;
+    }
+    __syncwarp();
+    for (int e = 0; e < L; ++e) cntc += keys[warp][e] != ~0ull ? 1 : 0;
+    // ranks of this lane's keys among the L
+    constexpr int kPer = kHdMaxL / 32;
+    unsigned long long mine[kPer];
+    int rank[kPer];
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+        const int e = lane + 32 * m;
+        mine[m] = e < L ? keys[warp][e] : ~0ull;
+        rank[m] = 0;
+    }
+    for (int e = 0; e < L; ++e) {
+        const unsigned long long o = keys[warp][e];
+#pragma unroll
+        for (int m = 0; m < kPer; ++m) rank[m] += o < mine[m] ? 1 : 0;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < kPer; ++m)
+        if (lane + 32 * m < L && rank[m] < L) keys[warp][rank[m]] = mine[m];
+    __syncwarp();
+    // certificate
+    const float Tq = T[q];
+    bool ok = true;
+    if (cntc < k) {
+        ok = !(Tq < INFINITY);  // fewer than k points exist only when every point is a candidate
+    } else if (Tq < INFINITY) {
+        const float dk = hd_dist(keys[warp][k - 1]);
+        const float ymax = __uint_as_float(maxes[0]), cmax = __uint_as_float(maxes[1]);
+        const float yq = sqrtf(ny[q]), cq = cn[q];
+        const float kw = 3.0f * (float)dp;
+        const float eta = (2.0f * kw + 4.0f * (float)dp + 16.0f) * 5.9604645e-8f *
+                              (yq + ymax) * (yq + ymax) * 1.0001f +
+                          3.0517578e-5f * cq * cmax * 1.0001f;
+        const float a2 = Tq - eta;
+        if (!(a2 > 0.0f)) {
+            ok = false;
+        } else {
+            const float aa = sqrtf(a2) * (1.0f - 9.5367432e-7f);
+            const float E = (1.5258789e-5f + 1.1920929e-7f) * (cq + cmax) * 1.0001f;
+            const float lb = aa - E;
+            ok = lb > 0.0f && lb * lb * (1.0f - (float)(d + 8) * 1.1920929e-7f) > dk;
+        }
+    }
+    if (!ok) {
+        if (lane == 0) {
+            const unsigned long long p = atomicAdd(fail_count, 1ull);
+            fail_list[p] = (int32_t)q;
+        }
+        return;
+    }
+    for (int e = lane; e < k; e += 32) {
+        const unsigned long long key = keys[warp][e];
+        const bool have = e < cntc;
+        rd_o[q * k + e] = have ? hd_dist(key) : INFINITY;
+        ix_o[q * k + e] = have ? (int32_t)(uint32_t)key : -1;
+    }
+}
+
+// Fallback: a warp per listed query scans every point in exact float32.
+__global__ void __launch_bounds__(128) hd_exact_kernel(
+    int64_t n, int d, int k, const float* __restrict__ X, const int32_t* __restrict__ list,
+    const unsigned long long* __restrict__ count, float* __restrict__ rd_o,
+    int32_t* __restrict__ ix_o) {
+    __shared__ float qs[4][96];
+    __shared__ unsigned long long bufs[4][kHdCap];
+    __shared__ int cnts[4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t total = (int64_t)*count;
+    for (int64_t w = (int64_t)blockIdx.x * 4 + warp; w < total; w += (int64_t)gridDim.x * 4) {
+        const int64_t q = list[w];
+        for (int e = lane; e < d; e += 32) qs[warp][e] = X[q * d + e];
+        if (lane == 0) cnts[warp] = 0;
+        __syncwarp();
+        unsigned long long* buf = bufs[warp];
+        float tau = INFINITY;
+        for (int64_t j0 = 0; j0 < n; j0 += 32) {
+            const int64_t j = j0 + lane;
+            if (j < n) {
+                const float r = hd_rdist(qs[warp], X + j * d, d);
+                if (r <= tau) {
+                    const int p = atomicAdd(&cnts[warp], 1);
+                    buf[p] = hd_key(r, (int32_t)j);
+                }
+            }
+            __syncwarp();
+            const int c = cnts[warp];
+            if (c > kHdCap - 32) {
+                const int kept = hd_cut(buf, c, k, lane);
+                tau = kept >= k ? hd_dist(buf[k - 1]) : INFINITY;
+                __syncwarp();
+                if (lane == 0) cnts[warp] = kept;
+            }
+            __syncwarp();
+        }
+        const int kept = hd_cut(buf, cnts[warp], k, lane);
+        for (int e = lane; e < k; e += 32) {
+            const bool have = e < kept;
+            rd_o[q * k + e] = have ? hd_dist(buf[e]) : INFINITY;
+            ix_o[q * k + e] = have ? (int32_t)(uint32_t)buf[e] : -1;
+        }
+        __syncwarp();
+    }
+}
+
+template <int KB>
+int launch_cand(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
+                const float* ny, int32_t* cand, float* T, cudaStream_t s) {
+    constexpr int KW = KB * 16, RS = KW + 8;
+    const size_t smem = (size_t)2 * kHdChunk * RS * sizeof(__nv_bfloat16) +
+                        (size_t)kHdQ * kHdCap * sizeof(unsigned long long) +
+                        2 * kHdChunk * sizeof(float) + kHdQ * (sizeof(int) + sizeof(float));
+    FHG_CUDA(cudaFuncSetAttribute(hd_cand_kernel<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    const int64_t blocks = (n + kHdQ - 1) / kHdQ;
+    Stage stage(s, "hd_cand_kernel");
+    ::fhg::note_launch();
+    hd_cand_kernel<KB><<<(unsigned)blocks, kHdWarps * 32, smem, s>>>(n, L, A, B, ny, cand, T);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
+}  // namespace
+
+int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_o,
+              int64_t* fallbacks, cudaStream_t s) {
+    if (d < 1 || d > kHighdMaxDim) {
+        set_error("high-dimensional kNN: d must be in [1, %d] (got %d)", kHighdMaxDim, d);
+        return d < 1 ? FHG_ERR_INVALID : FHG_ERR_UNSUPPORTED;
+    }
+    if (k < 1 || k + 32 > kHdMaxL) {
+        set_error("high-dimensional kNN: k must be in [1, %d] (got %d)", kHdMaxL - 32, k);
+        return FHG_ERR_INVALID;
+    }
+    if (n > 0x7fffffffLL) {
+        set_error("high-dimensional kNN: more than 2^31 - 1 points");
+        return FHG_ERR_UNSUPPORTED;
+    }
+    if (fallbacks) *fallbacks = 0;
+    if (n <= 0) return FHG_OK;
+    Stage stage(s, "highd_knn");
+    const int dp = d <= 32 ? 32 : (d <= 64 ? 64 : 96);
+    const int kw = 3 * dp;
+    const int L = k + 32;
+    Workspace ws(s);
+    float *mu, *ny, *cn, *T;
+    unsigned* maxes;
+    __nv_bfloat16 *A, *B;
+    int32_t *cand, *flist;
+    unsigned long long* fcount;
+    FHG_TRY(ws.alloc(&mu, (size_t)d));
+    FHG_TRY(ws.alloc(&ny, (size_t)n));
+    FHG_TRY(ws.alloc(&cn, (size_t)n));
+    FHG_TRY(ws.alloc(&T, (size_t)n));
+    FHG_TRY(ws.alloc(&maxes, 2));
+    FHG_TRY(ws.alloc(&A, (size_t)(n * kw)));
+    FHG_TRY(ws.alloc(&B, (size_t)(n * kw)));
+    FHG_TRY(ws.alloc(&cand, (size_t)(n * L)));
+    FHG_TRY(ws.alloc(&flist, (size_t)n));
+    FHG_TRY(ws.alloc(&fcount, 1));
+    FHG_CUDA(cudaMemsetAsync(maxes, 0, 2 * sizeof(unsigned), s));
+    FHG_CUDA(cudaMemsetAsync(fcount, 0, sizeof(unsigned long long), s));
+    ::fhg::note_launch();
+    hd_mean_kernel<<<d, 256, 0, s>>>(X, n, d, mu);
+    ::fhg::note_launch();
+    hd_split_kernel<<<grid_for(n, 128), 128, 0, s>>>(X, n, d, dp, mu, A, B, ny, cn, maxes);
+    FHG_CUDA(cudaGetLastError());
+    switch (dp) {
+        case 32: FHG_TRY(launch_cand<6>(n, L, A, B, ny, cand, T, s)); break;
+        case 64: FHG_TRY(launch_cand<12>(n, L, A, B, ny, cand, T, s)); break;
+        default: FHG_TRY(launch_cand<18>(n, L, A, B, ny, cand, T, s)); break;
+    }
+    {
+        Stage st(s, "hd_rerank_kernel");
+        ::fhg::note_launch();
+        hd_rerank_kernel<<<(unsigned)((n + 3) / 4), 128, 0, s>>>(
+            n, d, dp, k, L, X, cand, T, ny, cn, maxes, rd_o, ix_o, flist, fcount);
+        FHG_CUDA(cudaGetLastError());
+    }
+    unsigned long long nf = 0;
+    FHG_CUDA(cudaMemcpyAsync(&nf, fcount, sizeof(nf), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    if (nf > 0) {
+        Stage st(s, "hd_exact_kernel");
+        const int64_t blocks = std::min<int64_t>(((int64_t)nf + 3) / 4, 152 * 16);
+        ::fhg::note_launch();
+        hd_exact_kernel<<<(unsigned)blocks, 128, 0, s>>>(n, d, k, X, flist, fcount, rd_o, ix_o);
+        FHG_CUDA(cudaGetLastError());
+    }
+    if (fallbacks) *fallbacks = (int64_t)nf;
+    return FHG_OK;
+}
+
+}  // namespace fhg

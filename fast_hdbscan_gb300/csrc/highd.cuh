@@ -1,0 +1,17 @@
+// Exact brute-force kNN for high-dimensional points (highd.cu).
+#pragma once
+#include "fhg_common.cuh"
+
+namespace fhg {
+
+constexpr int kHighdMaxDim = 96;
+
+// kNN of every point of X (n x d float32, row-major, caller order), itself
+// included: rows of k (squared float32 distance, index) in (distance, index)
+// order, as index_knn writes them.  k + 32 <= 128.  *fallbacks (nullable) =
+// queries whose tensor-core candidates could not be certified and were
+// searched again exactly.
+int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_o,
+              int64_t* fallbacks, cudaStream_t s);
+
+}  // namespace fhg

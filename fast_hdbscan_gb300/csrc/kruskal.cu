@@ -28,6 +28,7 @@
 // that value (non-negative floats order like their bits).
 #include <memory>
 
+#include "highd.cuh"
 #include "index.cuh"
 #include "mst.cuh"
 #include "primitives.cuh"
@@ -237,7 +238,14 @@ __global__ void kr_neighbors_kernel(int64_t n, int kq, int cols, const int32_t* 
 int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const float* weights,
                     double* edges, int32_t* neighbors, double* core, int64_t* n_components,
                     cudaStream_t s) {
-    const int64_t n = index.n;
+    return kruskal_mst_of_lists(index.n, min_samples, query_k, weights, &index, nullptr, 0,
+                                edges, neighbors, core, n_components, s);
+}
+
+int kruskal_mst_of_lists(int64_t n, int min_samples, int query_k, const float* weights,
+                         const fhg_index* index, const float* X, int d, double* edges,
+                         int32_t* neighbors, double* core, int64_t* n_components,
+                         cudaStream_t s) {
     const int kq = query_k;
     const int64_t kk = kq - 1;
     if (kq < 2 || kq > 64) {
@@ -264,7 +272,8 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
     FHG_TRY(ws.alloc(&rd, (size_t)(n * kq)));
     FHG_TRY(ws.alloc(&ix, (size_t)(n * kq)));
     FHG_TRY(ws.alloc(&ck, (size_t)n));
-    FHG_TRY(index_knn(index, kq, nullptr, nullptr, rd, ix, s));
+    if (index) FHG_TRY(index_knn(*index, kq, nullptr, nullptr, rd, ix, s));
+    else FHG_TRY(highd_knn(X, n, d, kq, rd, ix, nullptr, s));
     if (weights) LAUNCH(kr_core_w_kernel, n, n, kq, min_samples, rd, ix, weights, core, ck);
     else LAUNCH(kr_core_kernel, n, n, kq, min_samples, rd, core, ck);
     if (neighbors) {

@@ -32,6 +32,13 @@ struct MstResult {
 int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const float* weights,
                     double* edges, int32_t* neighbors, double* core, int64_t* n_components,
                     cudaStream_t s);
+// The same on kNN lists from the spatial index (index given) or from the
+// brute-force high-dimensional kNN of X (n x d, index NULL) -- the latter is
+// nndescent.py:179 compute_mst_from_knn_graph with an exact kNN graph.
+int kruskal_mst_of_lists(int64_t n, int min_samples, int query_k, const float* weights,
+                         const fhg_index* index, const float* X, int d, double* edges,
+                         int32_t* neighbors, double* core, int64_t* n_components,
+                         cudaStream_t s);
 
 // The minimum spanning forest of n points over m edges given in rank order
 // (strictly increasing weight), in Kruskal's acceptance order, then +inf

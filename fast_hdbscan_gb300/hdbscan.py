@@ -207,13 +207,33 @@ def _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data
                 "algorithm='boruvka'")
     if semi_supervised:
         raise NotImplementedError("semi-supervised selection is outside the GPU engine's path")
+    if data is not None and _knn_graph_route(metric, data, sample_weights):
+        if data.shape[1] > KNN_GRAPH_MAX_DIM:
+            raise NotImplementedError(
+                f"{data.shape[1]}-dimensional data: the GPU kNN graph supports up to "
+                f"{KNN_GRAPH_MAX_DIM} dimensions")
+        return
     if data is not None and data.shape[1] > 32:
         raise NotImplementedError(
             f"{data.shape[1]}-dimensional data: the GPU spatial path supports up to 32 dimensions")
-    if data is not None and data.shape[1] > 30 and sample_weights is None:
-        raise NotImplementedError(
-            "the reference routes data with more than 30 dimensions (and no sample weights) to "
-            "its approximate NNDescent back-end (hdbscan.py:447), which is not on the GPU path")
+
+
+KNN_GRAPH_MAX_DIM = 96
+
+
+def _knn_graph_route(metric, data, sample_weights):
+    """hdbscan.py:446-449: Euclidean data with more than 30 dimensions and no
+    sample weights takes the kNN-graph back-end (nndescent.py:179), here on
+    the GPU's exact high-dimensional kNN."""
+    return metric == "euclidean" and data.shape[1] > 30 and sample_weights is None
+
+
+def resolve_knn_graph_k(min_samples, knn_k):
+    """nndescent.py:214-217: knn_k None -> max(3 min_samples, 15); at least
+    min_samples."""
+    if knn_k is None:
+        knn_k = max(3 * min_samples, 15)
+    return max(int(knn_k), int(min_samples))
 
 
 def _degenerate(n, return_trees):
@@ -331,9 +351,12 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
 def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_method="eom",
                     max_cluster_size=np.inf, allow_single_cluster=False,
                     cluster_selection_epsilon=0.0, cluster_selection_persistence=0.0,
-                    return_trees=True, sample_weights=None):
+                    return_trees=True, sample_weights=None, knn_graph=False):
     """One call of fhg_hdbscan_fit_kruskal: the kNN-graph Kruskal MST
-    (kruskal.py:950) and the tree passes on the GPU, outputs copied back."""
+    (kruskal.py:950) and the tree passes on the GPU, outputs copied back.
+    knn_graph: fhg_hdbscan_fit_knn_graph instead, the d > 30 route
+    (nndescent.py:179) on the exact brute-force kNN; knn_k as resolved by
+    resolve_knn_graph_k."""
     from .kruskal import kruskal_query_k
 
     torch = _native._torch()
@@ -344,9 +367,10 @@ def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_m
     n, d = Xd.shape
     ms = min_cluster_size if min_samples is None else min_samples
     w = None if sample_weights is None else np.ascontiguousarray(sample_weights, np.float32)
-    kq = kruskal_query_k(int(ms), int(knn_k), w)
-    if kq > 64:
-        raise NotImplementedError(f"a kNN query of {kq} neighbours exceeds the GPU kNN's 64")
+    kq = int(knn_k) + 1 if knn_graph else kruskal_query_k(int(ms), int(knn_k), w)
+    if kq > (96 if knn_graph else 64):
+        raise NotImplementedError(f"a kNN query of {kq} neighbours exceeds the GPU kNN's "
+                                  f"{96 if knn_graph else 64}")
     d_w = _native.to_device(w, np.float32) if w is not None else None
     cols = kq - 1 if w is not None else (ms if ms > 1 else 1)
     method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
@@ -363,12 +387,22 @@ def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_m
     core = E(n, np.float64) if trees else None
     rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
     V, lib = _native.vptr, _native.load()
-    rc = lib.fhg_hdbscan_fit_kruskal(
-        V(Xd), n, d, int(ms), int(knn_k), kq, int(min_cluster_size), method,
-        float(max_cluster_size), int(bool(allow_single_cluster)),
-        float(cluster_selection_epsilon), float(cluster_selection_persistence), V(d_w),
-        V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
-        ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel), _native.stream_ptr())
+    if knn_graph:
+        rc = lib.fhg_hdbscan_fit_knn_graph(
+            V(Xd), n, d, int(ms), int(knn_k), int(min_cluster_size), method,
+            float(max_cluster_size), int(bool(allow_single_cluster)),
+            float(cluster_selection_epsilon), float(cluster_selection_persistence),
+            V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
+            ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
+            _native.stream_ptr())
+    else:
+        rc = lib.fhg_hdbscan_fit_kruskal(
+            V(Xd), n, d, int(ms), int(knn_k), kq, int(min_cluster_size), method,
+            float(max_cluster_size), int(bool(allow_single_cluster)),
+            float(cluster_selection_epsilon), float(cluster_selection_persistence), V(d_w),
+            V(labels), V(probs), V(mst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts),
+            ctypes.byref(rows), V(nbrs), V(core), V(sel), ctypes.byref(nsel),
+            _native.stream_ptr())
     if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
         raise KeyError(lib.fhg_last_error().decode())
     _native.check(rc)
@@ -490,6 +524,13 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
                                  cluster_selection_method, max_cluster_size,
                                  allow_single_cluster, cluster_selection_epsilon,
                                  cluster_selection_persistence, return_trees=return_trees)
+    elif _knn_graph_route(metric, data, sample_weights):  # hdbscan.py:446 -> nndescent.py:179
+        ms = min_cluster_size if min_samples is None else min_samples
+        fr = gpu_fit_kruskal(data, min_samples, min_cluster_size,
+                             resolve_knn_graph_k(ms, knn_k), cluster_selection_method,
+                             max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
+                             cluster_selection_persistence, return_trees=return_trees,
+                             knn_graph=True)
     elif algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
         fr = gpu_fit_kruskal(data, min_samples, min_cluster_size, knn_k,
                              cluster_selection_method, max_cluster_size, allow_single_cluster,
@@ -527,6 +568,11 @@ def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, rep
     data = check_array(data)
     _unsupported_routes(metric, algorithm, sample_weights, False, data, cannot_link,
                         cannot_link_groups, knn_k)
+    if _knn_graph_route(metric, data, sample_weights):  # hdbscan.py:446-463
+        from .nndescent import compute_mst_from_knn_graph
+
+        return compute_mst_from_knn_graph(data, min_samples=min_samples, metric=metric,
+                                          metric_kwds=metric_kwds, knn_k=knn_k)
     tree = build_kdtree(data)
     if algorithm == "kruskal":
         from .kruskal import kruskal_mst_from_feature_matrix

@@ -322,6 +322,39 @@ int fhg_hdbscan_fit_precomputed(const int32_t* rows_dev, const int32_t* cols_dev
                                 int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev,
                                 int64_t* n_selected_host, void* stream);
 
+/* Exact kNN of every point of X (n x d float32, 1 <= d <= 96) by brute force:
+ * bfloat16 tensor-core candidates (k + 32 per query, from a two-term bf16
+ * split of the centred points), re-ranked in exact float32 and certified by
+ * a rounding bound; uncertified queries are searched again exactly.  Rows of
+ * k (squared distance, index), the point itself included, in (distance,
+ * index) order -- fhg_index_knn's output for any d.  k + 32 <= 128.
+ * *fallbacks_host (optional) = queries searched again.  Replaces the kNN
+ * graph of nndescent.py:41 build_knn_graph (pynndescent, approximate). */
+int fhg_highd_knn(const float* X_dev, int64_t n, int32_t d, int32_t k, float* rdist_dev,
+                  int32_t* idx_dev, int64_t* fallbacks_host, void* stream);
+
+/* nndescent.py:179 compute_mst_from_knn_graph (the d > 30 route of
+ * hdbscan.py:447) on the exact kNN graph of fhg_highd_knn with knn_k
+ * neighbours besides the point itself (the caller resolves knn_k: None ->
+ * max(3 min_samples, 15), then max(knn_k, min_samples)): float64 core
+ * distances (the min_samples-th neighbour; 0 for min_samples 1), neighbours
+ * n x min_samples, the Kruskal forest of the mutual-reachability kNN edges
+ * with +inf bridges (edges (n-1) x 3 float64). */
+int fhg_knn_graph_mst(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                      int32_t knn_k, double* edges_dev, int32_t* neighbors_dev, double* core_dev,
+                      int64_t* n_components_host, void* stream);
+
+/* The whole fit on fhg_knn_graph_mst's forest (hdbscan.py:306 with
+ * d > 30 and no sample weights); outputs as fhg_hdbscan_fit_kruskal. */
+int fhg_hdbscan_fit_knn_graph(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
+                              int32_t knn_k, int64_t min_cluster_size, int32_t selection_method,
+                              double max_cluster_size, int allow_single_cluster, double epsilon,
+                              double persistence, int64_t* labels_dev, float* probs_dev,
+                              double* mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+                              int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+                              int64_t* ct_rows_host, int32_t* neighbors_dev, double* core_dev,
+                              int64_t* selected_dev, int64_t* n_selected_host, void* stream);
+
 /* fhg_hdbscan_fit, with the large outputs also copied to host memory while
  * the fit runs: each non-NULL *_host destination receives its output from a
  * side stream as soon as the fit has finished writing it (neighbours and

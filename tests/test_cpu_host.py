@@ -104,11 +104,25 @@ def test_out_of_scope_routes_raise_not_implemented():
         fast_hdbscan(X, cannot_link_groups=np.zeros(20, np.int32))
     with pytest.raises(ValueError):
         compute_minimum_spanning_tree(X, algorithm="prim")
-    with pytest.raises(NotImplementedError):  # hdbscan.py:447: NNDescent above 30 dims
-        fast_hdbscan(np.random.default_rng(2).random((20, 31)))
+    with pytest.raises(NotImplementedError):  # hdbscan.py:447's kNN-graph route: up to 96 dims
+        fast_hdbscan(np.random.default_rng(2).random((20, 97)))
     with pytest.raises(NotImplementedError):
         fast_hdbscan(np.random.default_rng(2).random((20, 40)),
                      sample_weights=np.ones(20, np.float32))
+
+
+def test_knn_graph_route_and_k():
+    """hdbscan.py:446-449 routes Euclidean data above 30 dimensions without
+    sample weights to the kNN-graph back-end; nndescent.py:214-217 resolves
+    its k."""
+    from fast_hdbscan_gb300.hdbscan import _knn_graph_route, resolve_knn_graph_k
+
+    X31, X30 = np.zeros((5, 31)), np.zeros((5, 30))
+    assert _knn_graph_route("euclidean", X31, None)
+    assert not _knn_graph_route("euclidean", X30, None)
+    assert not _knn_graph_route("euclidean", X31, np.ones(5))
+    assert resolve_knn_graph_k(10, None) == 30 and resolve_knn_graph_k(3, None) == 15
+    assert resolve_knn_graph_k(10, 5) == 10 and resolve_knn_graph_k(2, 40) == 40
 
 
 def test_estimator_params_roundtrip():
