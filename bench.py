@@ -318,7 +318,7 @@ def run_gb300(args):
     # per-stage share and the dominant kernel's roofline
     # kernel records nest inside the stage records: shares are over stages
     nested = ("knn_kernel", "search_kernel", "hd_cand_kernel", "hd_rerank_kernel",
-              "hd_exact_kernel")
+              "hd_exact_kernel", "highd_knn")
     total_stage = sum(v[0] for k, v in stages.items() if k not in nested) or 1.0
     kernel_stages = {k: v for k, v in stages.items()
                      if k in ("knn_kernel", "search_kernel", "hd_cand_kernel")}

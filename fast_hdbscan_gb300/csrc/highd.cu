@@ -8,9 +8,10 @@
 //    squared distance to every point is estimated as
 //        D~ = |y_i|^2 + |y_j|^2 - 2 (hi_i.hi_j + hi_i.lo_j + lo_i.hi_j)
 //    (y = hi + lo) with one bf16 GEMM of depth 3 * dp (mma.sync m16n8k16,
-//    float32 accumulation).  A CTA holds 64 queries (16 per warp, operands in
-//    registers) and streams all points through shared memory in chunks of
-//    64 (cp.async, double-buffered).  Each query keeps the L = k + 32 points
+//    float32 accumulation).  A CTA holds 128 queries (8 warps of 16, operands
+//    in registers; 64 when the buffers below need the room) and streams all
+//    points through shared memory in chunks of 64 (cp.async,
+//    double-buffered).  Each query keeps the L = k + 32 points
 //    of smallest D~ in a shared-memory buffer: an estimate below the query's
 //    current L-th value is appended, and a buffer that fills is cut back to
 //    its L smallest by ranking.
@@ -39,13 +40,11 @@
 namespace fhg {
 namespace {
 
-constexpr int kHdWarps = 4;
-constexpr int kHdRows = 16;                    // queries per warp
-constexpr int kHdQ = kHdWarps * kHdRows;       // queries per CTA
-constexpr int kHdChunk = 64;                   // points per streamed chunk
-constexpr int kHdCap = 192;                    // candidate buffer per query
-constexpr int kHdTrigger = kHdCap - kHdChunk;  // cut back when fuller
-constexpr int kHdMaxL = 128;                   // candidates kept (k + 32)
+constexpr int kHdRows = 16;     // queries per warp
+constexpr int kHdChunk = 64;    // points per streamed chunk
+constexpr int kHdCap = 192;     // largest candidate buffer per query (L + kHdChunk)
+constexpr int kHdMaxL = 128;    // candidates kept (k + 32)
+constexpr int kHdSmemMax = 227 * 1024;
 
 __device__ __forceinline__ unsigned long long hd_key(float dist, int32_t j) {
     return ((unsigned long long)__float_as_uint(dist) << 32) | (uint32_t)j;
@@ -140,17 +139,22 @@ __device__ __forceinline__ int hd_cut(unsigned long long* buf, int cnt, int keep
     return cnt < keep ? cnt : keep;
 }
 
-template <int KB>  // k-blocks of 16 in the operand depth 3 * dp
-__global__ void __launch_bounds__(kHdWarps * 32) hd_cand_kernel(
-    int64_t n, int L, const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B,
-    const float* __restrict__ ny, int32_t* __restrict__ cand, float* __restrict__ T) {
+// KB: k-blocks of 16 in the operand depth 3 * dp; W warps of 16 queries.
+// cap: candidate buffer entries per query (L + kHdChunk rounded up, <= kHdCap):
+// after a cut to L a buffer always has room for one chunk's estimates.
+template <int KB, int W>
+__global__ void __launch_bounds__(W * 32) hd_cand_kernel(
+    int64_t n, int L, int cap, const __nv_bfloat16* __restrict__ A,
+    const __nv_bfloat16* __restrict__ B, const float* __restrict__ ny, int32_t* __restrict__ cand,
+    float* __restrict__ T) {
+    constexpr int kHdQ = W * kHdRows;
     constexpr int KW = KB * 16;
     constexpr int RS = KW + 8;  // shared row stride (bf16): conflict-free fragment loads
     extern __shared__ __align__(16) unsigned char hd_smem[];
     __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(hd_smem);  // [2][kHdChunk][RS]
     unsigned long long* bufs =
-        reinterpret_cast<unsigned long long*>(Bs + 2 * kHdChunk * RS);  // [kHdQ][kHdCap]
-    float* npj = reinterpret_cast<float*>(bufs + kHdQ * kHdCap);       // [2][kHdChunk]
+        reinterpret_cast<unsigned long long*>(Bs + 2 * kHdChunk * RS);  // [kHdQ][cap]
+    float* npj = reinterpret_cast<float*>(bufs + kHdQ * cap);          // [2][kHdChunk]
     int* cnt = reinterpret_cast<int*>(npj + 2 * kHdChunk);              // [kHdQ]
     float* tau = reinterpret_cast<float*>(cnt + kHdQ);                  // [kHdQ]
 
@@ -172,8 +176,8 @@ __global__ void __launch_bounds__(kHdWarps * 32) hd_cand_kernel(
         a[kb][3] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0 + 8) : 0u;
     }
     const float nqa = ra < n ? ny[ra] : 0.0f, nqb = rb < n ? ny[rb] : 0.0f;
-    unsigned long long* bufa = bufs + (warp * kHdRows + g) * kHdCap;
-    unsigned long long* bufb = bufs + (warp * kHdRows + g + 8) * kHdCap;
+    unsigned long long* bufa = bufs + (warp * kHdRows + g) * cap;
+    unsigned long long* bufb = bufs + (warp * kHdRows + g + 8) * cap;
     int* cnta = cnt + warp * kHdRows + g;
     int* cntb = cnt + warp * kHdRows + g + 8;
 
@@ -220,50 +224,78 @@ __global__ void __launch_bounds__(kHdWarps * 32) hd_cand_kernel(
                 hd_mma(acc[nt], a[kb], b0, b1);
             }
         }
-        // estimates below the row's current L-th value join its buffer
+        // estimates below the row's current L-th value join its buffer; a row
+        // whose buffer cannot take this chunk's passing estimates is first cut
+        // back to its L smallest (which can only tighten its threshold)
         const int64_t jb = c * kHdChunk;
+        int pa = 0, pb = 0;
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const int col = nt * 8 + 2 * t + (e & 1);
-                const int64_t j = jb + col;
-                if (j >= n) continue;
                 const bool hi = e >= 2;
                 const float dd =
-                    fmaxf(__fsub_rn(__fadd_rn(hi ? nqb : nqa, npj[slot * kHdChunk + col]),
-                                    __fmul_rn(2.0f, acc[nt][e])),
-                          0.0f);
-                if (dd < (hi ? tb : ta)) {
-                    const int p = atomicAdd(hi ? cntb : cnta, 1);
-                    (hi ? bufb : bufa)[p] = hd_key(dd, (int32_t)j);
-                }
+                    jb + col < n
+                        ? fmaxf(__fsub_rn(__fadd_rn(hi ? nqb : nqa, npj[slot * kHdChunk + col]),
+                                          __fmul_rn(2.0f, acc[nt][e])),
+                                0.0f)
+                        : INFINITY;
+                acc[nt][e] = dd;
+                if (hi) pb += dd < tb ? 1 : 0;
+                else pa += dd < ta ? 1 : 0;
             }
         }
-        __syncwarp();
-        // cut full buffers back to their L smallest
-        for (int r = 0; r < kHdRows; ++r) {
-            const int qr = warp * kHdRows + r;
-            const int cr = cnt[qr];
-            if (cr > kHdTrigger) {
-                unsigned long long* b = bufs + qr * kHdCap;
-                const int kept = hd_cut(b, cr, L, lane);
+        pa += __shfl_xor_sync(0xffffffffu, pa, 1);
+        pa += __shfl_xor_sync(0xffffffffu, pa, 2);
+        pb += __shfl_xor_sync(0xffffffffu, pb, 1);
+        pb += __shfl_xor_sync(0xffffffffu, pb, 2);
+        // lane 4g answers for rows g (low half of the mask) and g + 8
+        const unsigned over_a = __ballot_sync(0xffffffffu, t == 0 && *cnta + pa > cap);
+        const unsigned over_b = __ballot_sync(0xffffffffu, t == 0 && *cntb + pb > cap);
+        unsigned rows = 0;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            rows |= ((over_a >> (4 * r)) & 1u) << r;
+            rows |= ((over_b >> (4 * r)) & 1u) << (r + 8);
+        }
+        if (rows) {
+            while (rows) {
+                const int r = __ffs(rows) - 1;
+                rows &= rows - 1u;
+                const int qr = warp * kHdRows + r;
+                unsigned long long* b = bufs + qr * cap;
+                const int kept = hd_cut(b, cnt[qr], L, lane);
                 if (lane == 0) {
                     cnt[qr] = kept;
                     tau[qr] = kept >= L ? hd_dist(b[L - 1]) : INFINITY;
                 }
                 __syncwarp();
             }
+            ta = tau[warp * kHdRows + g];
+            tb = tau[warp * kHdRows + g + 8];
         }
-        ta = tau[warp * kHdRows + g];
-        tb = tau[warp * kHdRows + g + 8];
+        if (pa + pb > 0) {  // quad-uniform: the quad's rows have passing estimates
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const bool hi = e >= 2;
+                    const float dd = acc[nt][e];
+                    if (dd < (hi ? tb : ta)) {
+                        const int p = atomicAdd(hi ? cntb : cnta, 1);
+                        (hi ? bufb : bufa)[p] = hd_key(dd, (int32_t)(jb + nt * 8 + 2 * t + (e & 1)));
+                    }
+                }
+            }
+        }
         __syncwarp();
     }
     // final cut: the L smallest estimates of every row, and the L-th estimate
     for (int r = 0; r < kHdRows; ++r) {
         const int qr = warp * kHdRows + r;
         const int64_t q = q0 + r;
-        unsigned long long* b = bufs + qr * kHdCap;
+        unsigned long long* b = bufs + qr * cap;
         const int kept = hd_cut(b, cnt[qr], L, lane);
         if (q < n) {
             for (int e = lane; e < L; e += 32)
@@ -412,21 +444,37 @@ __global__ void __launch_bounds__(128) hd_exact_kernel(
     }
 }
 
+size_t cand_smem(int kb, int warps, int cap) {
+    const int rs = kb * 16 + 8;
+    const int q = warps * kHdRows;
+    return (size_t)2 * kHdChunk * rs * sizeof(__nv_bfloat16) +
+           (size_t)q * cap * sizeof(unsigned long long) + 2 * kHdChunk * sizeof(float) +
+           q * (sizeof(int) + sizeof(float));
+}
+
+template <int KB, int W>
+int launch_cand_w(int64_t n, int L, int cap, const __nv_bfloat16* A, const __nv_bfloat16* B,
+                  const float* ny, int32_t* cand, float* T, cudaStream_t s) {
+    const size_t smem = cand_smem(KB, W, cap);
+    FHG_CUDA(cudaFuncSetAttribute(hd_cand_kernel<KB, W>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t blocks = (n + W * kHdRows - 1) / (W * kHdRows);
+    Stage stage(s, "hd_cand_kernel");
+    ::fhg::note_launch();
+    hd_cand_kernel<KB, W><<<(unsigned)blocks, W * 32, smem, s>>>(n, L, cap, A, B, ny, cand, T);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
+// Eight warps (128 queries share every staged chunk) when their buffers fit
+// in shared memory, else four.
 template <int KB>
 int launch_cand(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
                 const float* ny, int32_t* cand, float* T, cudaStream_t s) {
-    constexpr int KW = KB * 16, RS = KW + 8;
-    const size_t smem = (size_t)2 * kHdChunk * RS * sizeof(__nv_bfloat16) +
-                        (size_t)kHdQ * kHdCap * sizeof(unsigned long long) +
-                        2 * kHdChunk * sizeof(float) + kHdQ * (sizeof(int) + sizeof(float));
-    FHG_CUDA(cudaFuncSetAttribute(hd_cand_kernel<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    const int64_t blocks = (n + kHdQ - 1) / kHdQ;
-    Stage stage(s, "hd_cand_kernel");
-    ::fhg::note_launch();
-    hd_cand_kernel<KB><<<(unsigned)blocks, kHdWarps * 32, smem, s>>>(n, L, A, B, ny, cand, T);
-    FHG_CUDA(cudaGetLastError());
-    return FHG_OK;
+    const int cap = std::min(kHdCap, (L + kHdChunk + 31) / 32 * 32);
+    if (cand_smem(KB, 8, cap) <= (size_t)kHdSmemMax)
+        return launch_cand_w<KB, 8>(n, L, cap, A, B, ny, cand, T, s);
+    return launch_cand_w<KB, 4>(n, L, cap, A, B, ny, cand, T, s);
 }
 
 }  // namespace
