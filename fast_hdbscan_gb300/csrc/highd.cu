@@ -185,7 +185,11 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
     constexpr int kSeg = KW * 2 / 16;  // 16-byte segments per point row
     auto stage = [&](int64_t chunk, int slot) {
         __nv_bfloat16* dst = Bs + slot * kHdChunk * RS;
-        for (int e = threadIdx.x; e < kHdChunk * kSeg; e += blockDim.x) {
+        constexpr int kPerThr = (kHdChunk * kSeg + W * 32 - 1) / (W * 32);
+#pragma unroll
+        for (int i = 0; i < kPerThr; ++i) {
+            const int e = threadIdx.x + i * W * 32;
+            if (kHdChunk * kSeg % (W * 32) != 0 && e >= kHdChunk * kSeg) break;
             const int r = e / kSeg, sgm = e % kSeg;
             const int64_t j = chunk * kHdChunk + r;
             __nv_bfloat16* d16 = dst + r * RS + sgm * 8;
@@ -228,6 +232,7 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
         // whose buffer cannot take this chunk's passing estimates is first cut
         // back to its L smallest (which can only tighten its threshold)
         const int64_t jb = c * kHdChunk;
+        const bool whole = jb + kHdChunk <= n;
         int pa = 0, pb = 0;
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) {
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
                 const int col = nt * 8 + 2 * t + (e & 1);
                 const bool hi = e >= 2;
                 const float dd =
-                    jb + col < n
+                    (whole || jb + col < n)
                         ? fmaxf(__fsub_rn(__fadd_rn(hi ? nqb : nqa, npj[slot * kHdChunk + col]),
                                           __fmul_rn(2.0f, acc[nt][e])),
                                 0.0f)
