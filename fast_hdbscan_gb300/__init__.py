@@ -7,6 +7,9 @@ Every stage (spatial index, kNN core distances, Boruvka MST, linkage tree,
 condensed tree, cluster selection, labels) runs as hand-written sm_103a CUDA
 kernels in libfhg.so, called through the C ABI of include/fhg.h.
 """
+from .branches import BranchDetector, find_branch_sub_clusters  # noqa: F401
 from .hdbscan import HDBSCAN, fast_hdbscan  # noqa: F401
+from .sub_clusters import SubClusterDetector, find_sub_clusters  # noqa: F401
 
-__all__ = ["HDBSCAN", "fast_hdbscan"]
+__all__ = ["HDBSCAN", "fast_hdbscan", "BranchDetector", "find_branch_sub_clusters",
+           "SubClusterDetector", "find_sub_clusters"]

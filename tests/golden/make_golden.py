@@ -373,6 +373,104 @@ def precomputed_fixtures(only=None):
               f"clusters={len(set(labels.tolist()) - {-1})} {time.time() - t0:.1f}s")
 
 
+def _flares():
+    """Three noisy arms from the origin (a Y) and a separate blob, 2-D."""
+    rng = np.random.default_rng(0)
+    arms = []
+    for ang in (0.0, 2.1, 4.2):
+        t = rng.uniform(0, 5, 200)
+        arms.append(np.c_[t * np.cos(ang), t * np.sin(ang)] + rng.normal(0, 0.15, (200, 2)))
+    X = np.concatenate(arms + [rng.normal((12, 0), 0.5, (150, 2))])
+    return X[rng.permutation(len(X))].astype(np.float32)
+
+
+def _flares_nonfinite():
+    X = _flares().astype(np.float64)
+    X[[3, 77, 400]] = np.nan
+    X[500, 1] = np.inf
+    return X
+
+
+def _blobs_lens():
+    rng = np.random.default_rng(5)
+    X = np.concatenate([rng.normal(c, 1.0, (250, 2)) for c in ((0, 0), (9, 1), (3, 9))])
+    return X[rng.permutation(len(X))].astype(np.float32)
+
+
+# name -> (data factory, HDBSCAN kwargs, detector, detector kwargs)
+SUBCLUSTER_CASES = {
+    "sc_branches_flares": (_flares, dict(min_cluster_size=30, min_samples=5), "branch",
+                           dict(min_cluster_size=15)),
+    "sc_branches_flares_leaf": (_flares, dict(min_cluster_size=30, min_samples=5), "branch",
+                                dict(min_cluster_size=10, cluster_selection_method="leaf",
+                                     label_sides_as_branches=True)),
+    "sc_branches_nonfinite": (_flares_nonfinite, dict(min_cluster_size=30, min_samples=5),
+                              "branch", dict(min_cluster_size=15)),
+    "sc_lens_x_propagate": (_blobs_lens, dict(min_cluster_size=40, min_samples=8), "lens",
+                            dict(min_cluster_size=20, propagate_labels=True)),
+}
+
+
+def subcluster_fixtures(only=None):
+    """Sub-cluster and branch detection (sub_clusters.py:245, branches.py:70)
+    on fits of the reference's own HDBSCAN, plus the core graph of the first
+    cluster (core_graph.py:19) for the host-side check."""
+    from fast_hdbscan import HDBSCAN, BranchDetector
+    from fast_hdbscan.core_graph import knn_mst_union, flatten_to_csr
+    from fast_hdbscan.sub_clusters import SubClusterDetector
+
+    for name, (factory, hkw, kind, dkw) in SUBCLUSTER_CASES.items():
+        if only and name not in only:
+            continue
+        X = factory()
+        t0 = time.time()
+        c = HDBSCAN(**hkw).fit(X)
+        if kind == "branch":
+            det = BranchDetector(**dkw).fit(c)
+            lens = None
+        else:
+            lens = np.ascontiguousarray(X[:, 0], dtype=np.float64)
+            det = SubClusterDetector(lens_values=lens, **dkw).fit(c)
+        prop_labels, prop_sub = det.propagated_labels()
+        pts = list(det.cluster_points_)
+        out = dict(X=X, hdbscan_kwargs=np.array(repr(hkw)), kind=np.array(kind),
+                   detector_kwargs=np.array(repr(dkw)),
+                   fit_labels=np.asarray(c.labels_, np.int64),
+                   labels=np.asarray(det.labels_, np.int64),
+                   probabilities=np.asarray(det.probabilities_, np.float64),
+                   sub_labels=np.asarray(det.sub_cluster_labels_, np.int64),
+                   sub_probabilities=np.asarray(det.sub_cluster_probabilities_, np.float64),
+                   lens_out=np.asarray(det.lens_values_, np.float64),
+                   points=np.concatenate(pts).astype(np.int64),
+                   points_offsets=np.cumsum([0] + [len(p) for p in pts]).astype(np.int64),
+                   prop_labels=np.asarray(prop_labels, np.int64),
+                   prop_sub_labels=np.asarray(prop_sub, np.int64))
+        if lens is not None:
+            out["lens"] = lens
+        # the first cluster's core graph, from the reference's own inputs
+        points = np.nonzero(det.cluster_labels_ == 0)[0]
+        if not np.all(np.isfinite(X)):
+            out["core_graph_skipped"] = np.array(True)
+        else:
+            ids = np.full(X.shape[0], -1, np.int32)
+            ids[points] = np.arange(len(points))
+            nb = ids[c._neighbors[points, :]]
+            core = c._core_distances[points]
+            mst = c._min_spanning_tree
+            keep = (c.labels_[mst[:, 0].astype(np.int64)] == 0) & \
+                   (c.labels_[mst[:, 1].astype(np.int64)] == 0)
+            mst = mst[keep].copy()
+            mst[:, :2] = ids[mst[:, :2].astype(np.int64)]
+            lens0 = np.asarray(det.lens_values_, np.float64)[points]
+            g = flatten_to_csr(knn_mst_union(nb, core, mst, lens0))
+            out.update(cg_neighbors=nb, cg_core=np.asarray(core), cg_mst=mst, cg_lens=lens0,
+                       cg_weights=g.weights, cg_distances=g.distances, cg_indices=g.indices,
+                       cg_indptr=g.indptr)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(f"{name}: n={len(X)} clusters={len(pts)} labels={len(np.unique(det.labels_))} "
+              f"{time.time() - t0:.1f}s")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -383,6 +481,8 @@ def main():
                     help="only write the kNN-graph Kruskal fixtures")
     ap.add_argument("--precomputed-only", action="store_true",
                     help="only write the metric='precomputed' fixtures")
+    ap.add_argument("--subclusters-only", action="store_true",
+                    help="only write the sub-cluster / branch detection fixtures")
     args = ap.parse_args()
     sys.path.insert(1, args.reference)
     import fast_hdbscan  # noqa: F401
@@ -391,6 +491,9 @@ def main():
         return
     if args.precomputed_only:
         precomputed_fixtures(args.only)
+        return
+    if args.subclusters_only:
+        subcluster_fixtures(args.only)
         return
     for name, (factory, kwargs) in CASES.items():
         if args.only and name not in args.only:
@@ -402,6 +505,7 @@ def main():
         function_fixtures()
         kruskal_fixtures()
         precomputed_fixtures()
+        subcluster_fixtures()
 
 
 if __name__ == "__main__":

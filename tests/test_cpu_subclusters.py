@@ -1,0 +1,50 @@
+"""Host side of sub-cluster / branch detection: the core graph of a cluster
+(core_graph.py:19 knn_mst_union + :47 flatten_to_csr) against the
+reference's own graph stored in the fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+CASES = ["sc_branches_flares", "sc_branches_flares_leaf", "sc_lens_x_propagate"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_core_graph_matches_reference(name):
+    from fast_hdbscan_gb300.core_graph import core_graph_to_edge_list, knn_mst_union
+
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ours = knn_mst_union(g["cg_neighbors"], g["cg_core"], g["cg_mst"], g["cg_lens"])
+    assert np.array_equal(ours.indptr, g["cg_indptr"])
+    n = len(ours.indptr) - 1
+    rows = np.repeat(np.arange(n), np.diff(g["cg_indptr"]))
+    ref = sorted(zip(rows.tolist(), g["cg_indices"].tolist(), g["cg_weights"].tolist(),
+                     g["cg_distances"].tolist()))
+    mine = sorted(map(tuple, core_graph_to_edge_list(ours).tolist()))
+    mine = [(int(a), int(b), float(c), float(d)) for a, b, c, d in mine]
+    assert mine == [(int(a), int(b), float(c), float(d)) for a, b, c, d in ref]
+    # rows sorted by weight
+    for i in range(n):
+        w = ours.weights[ours.indptr[i]:ours.indptr[i + 1]]
+        assert np.all(np.diff(w) >= 0)
+
+
+def test_branch_threshold_and_label_merge():
+    """branches.py:14 and sub_clusters.py:98 on a hand-made two-cluster case."""
+    from fast_hdbscan_gb300.branches import apply_branch_threshold
+    from fast_hdbscan_gb300.sub_clusters import update_labels
+
+    pts = [np.array([0, 1, 2, 3]), np.array([4, 5, 6])]
+    sub = [np.array([0, 1, 2, -1]), np.array([0, 0, 0])]
+    probs = [np.ones(4, np.float32), np.full(3, 0.5, np.float32)]
+    lens = [np.arange(4, dtype=np.float32), np.arange(3, dtype=np.float32)]
+    cp = np.full(7, 0.8, np.float32)
+    labels, p, sl, sp, lv = update_labels(cp, sub, probs, lens, pts, 7)
+    assert labels.tolist() == [1, 2, 3, 0, 4, 4, 4]
+    assert np.allclose(p, [0.9, 0.9, 0.9, 0.9, 0.65, 0.65, 0.65])
+    apply_branch_threshold(labels, sl, p, cp, pts, [np.zeros((3, 4)), np.zeros((2, 4))])
+    # three branches in the first cluster stay; one in the second merges to one label
+    assert labels.tolist() == [1, 2, 3, 0, 4, 4, 4]
+    assert np.allclose(p[4:], 0.8)

@@ -1,0 +1,75 @@
+"""Sub-cluster and branch detection (sub_clusters.py:245, branches.py:70) on
+the GPU engine's fits, against the reference's results on the same inputs
+(fixtures written by tests/golden/make_golden.py from the reference's own
+HDBSCAN, BranchDetector and SubClusterDetector).  The per-cluster core-graph
+forests and cluster hierarchies run on the GPU."""
+import ast
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["sc_branches_flares", "sc_branches_flares_leaf", "sc_branches_nonfinite",
+         "sc_lens_x_propagate"]
+
+
+def _same_partition(a, b):
+    """Equal up to a renaming of the labels (noise -1 kept as noise)."""
+    a, b = np.asarray(a), np.asarray(b)
+    if not np.array_equal(a == -1, b == -1):
+        return False
+    pairs = set(zip(a.tolist(), b.tolist()))
+    return len(pairs) == len(set(a.tolist())) == len(set(b.tolist()))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_detector_matches_reference(engine, name):
+    from fast_hdbscan_gb300 import HDBSCAN, BranchDetector, SubClusterDetector
+
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    hkw = ast.literal_eval(str(g["hdbscan_kwargs"]))
+    dkw = ast.literal_eval(str(g["detector_kwargs"]))
+    c = HDBSCAN(**hkw).fit(g["X"])
+    np.testing.assert_array_equal(c.labels_, g["fit_labels"])
+    if str(g["kind"]) == "branch":
+        det = BranchDetector(**dkw).fit(c)
+    else:
+        det = SubClusterDetector(lens_values=g["lens"], **dkw).fit(c)
+    pts = [g["points"][a:b] for a, b in zip(g["points_offsets"][:-1], g["points_offsets"][1:])]
+    assert len(pts) == len(det.cluster_points_)
+    for p, q in zip(pts, det.cluster_points_):
+        np.testing.assert_array_equal(p, q)
+    np.testing.assert_allclose(det.lens_values_, g["lens_out"], rtol=1e-6)
+    np.testing.assert_array_equal(det.labels_, g["labels"])
+    np.testing.assert_array_equal(det.sub_cluster_labels_, g["sub_labels"])
+    np.testing.assert_allclose(det.probabilities_, g["probabilities"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(det.sub_cluster_probabilities_, g["sub_probabilities"],
+                               rtol=1e-5, atol=1e-6)
+    prop_labels, prop_sub = det.propagated_labels()
+    assert _same_partition(prop_labels, g["prop_labels"])
+
+
+def test_find_branch_sub_clusters_function(engine):
+    from fast_hdbscan_gb300 import HDBSCAN, find_branch_sub_clusters
+
+    g = np.load(os.path.join(GOLDEN, "sc_branches_flares.npz"))
+    c = HDBSCAN(**ast.literal_eval(str(g["hdbscan_kwargs"]))).fit(g["X"])
+    res = find_branch_sub_clusters(c, min_cluster_size=15)
+    np.testing.assert_array_equal(res[0], g["labels"])
+
+
+def test_detector_input_errors(engine):
+    from fast_hdbscan_gb300 import HDBSCAN, BranchDetector
+
+    g = np.load(os.path.join(GOLDEN, "sc_branches_flares.npz"))
+    c = HDBSCAN(min_cluster_size=30, min_samples=5).fit(g["X"])
+    with pytest.raises(ValueError):
+        BranchDetector(min_cluster_size=1).fit(c)
+    with pytest.raises(ValueError):
+        BranchDetector(cluster_selection_method="other").fit(c)
+    with pytest.raises(ValueError):
+        BranchDetector().fit(c, labels=np.full(len(g["X"]), -1))
