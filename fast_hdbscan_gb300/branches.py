@@ -48,7 +48,9 @@ def find_branch_sub_clusters(clusterer, cluster_labels=None, cluster_probabiliti
         cluster_selection_method=cluster_selection_method,
         cluster_selection_epsilon=cluster_selection_epsilon,
         cluster_selection_persistence=cluster_selection_persistence)
-    apply_branch_threshold(result[0], result[4], result[1], result[3], result[-1],
+    # the reference's call here leaves out the linkage trees (result[8]),
+    # which apply_branch_threshold requires
+    apply_branch_threshold(result[0], result[4], result[1], result[3], result[-1], result[8],
                            label_sides_as_branches=label_sides_as_branches)
     return result
 

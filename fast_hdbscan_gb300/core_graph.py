@@ -5,16 +5,14 @@ A cluster's core graph joins each point to its in-cluster kNN neighbours and
 to its in-cluster MST children; an edge's weight is the larger lens value of
 its two ends and its distance the larger core distance (MST edges keep their
 MST distance).  The graph is laid out on the host (a few numpy passes over
-n * k entries, as cheap as the lens itself); its minimum spanning forest --
-Kruskal's, with +inf bridges -- and the cluster hierarchy of that forest run
-on the GPU (``fhg_precomputed_mst`` with min_samples 1, then the tree passes
-of ``clusters_from_spanning_tree``).
+n * k entries, as cheap as the lens itself); its spanning forest
+(``fhg_core_graph_mst``: the reference's Boruvka, including its choices
+among the many equal lens weights, which shape the cluster hierarchy) and
+the hierarchy's tree passes (``clusters_from_spanning_tree``) run on the GPU.
 
-The reference builds the forest with a Boruvka pass whose equal-weight
-choices follow numba's unstable argsort; lens weights tie wherever an edge's
-larger lens belongs to a shared end, so the forest's equal-weight edges may
-differ while its weights, and the single-linkage merge heights, are the
-same.
+Rows are ordered by weight with ties in insertion order (the kNN children in
+neighbour order, then the MST children): the order of the reference's sort
+for rows of up to 15 entries, where its quicksort is an insertion sort.
 """
 import ctypes
 from collections import namedtuple
@@ -58,50 +56,56 @@ def knn_mst_union(neighbors, core_distances, min_spanning_tree, lens_values):
     return CoreGraph(weights[order], distances[order], cols[order].astype(np.int32), indptr)
 
 
+def _root_labels(n, edges):
+    """The reference's component labels for a disconnected core graph: the
+    union-by-rank roots (disjoint_set.py:30, edges merged in forest order),
+    numbered in increasing root order (core_graph.py:251)."""
+    parent = np.arange(n)
+    rank = np.zeros(n, np.int64)
+
+    def find(x):
+        while parent[x] != x:
+            x = parent[x]
+        return x
+
+    for a, b in edges[:, :2].astype(np.int64):
+        x, y = find(a), find(b)
+        if x == y:
+            continue
+        if rank[x] < rank[y]:
+            x, y = y, x
+        parent[y] = x
+        if rank[x] == rank[y]:
+            rank[x] += 1
+    roots = np.array([find(i) for i in range(n)])
+    return np.unique(roots, return_inverse=True)[1].astype(np.int64)
+
+
 def core_graph_spanning_tree(neighbors, core_distances, min_spanning_tree, lens):
     """core_graph.py:234: ``(n_components, component_labels, lensed_mst,
-    graph)`` -- the minimum spanning forest of the core graph on its lens
-    weights (component labels number the components by their smallest
-    point)."""
+    graph)`` -- the core graph's spanning forest on its lens weights, built on
+    the GPU with the reference's Boruvka choices (``fhg_core_graph_mst``)."""
     torch = _native._torch()
     graph = knn_mst_union(neighbors, core_distances, min_spanning_tree, lens)
     n = len(graph.indptr) - 1
-    if n == 0:
-        return 0, np.zeros(0, np.int64), np.zeros((0, 3)), graph
-    w = graph.weights.astype(np.float64)
-    if np.any(np.isnan(w)):
+    if np.any(np.isnan(graph.weights)):
         raise ValueError("lens values must not be NaN")
-    # the GPU forest orders non-negative float64 weights; a constant shift
-    # (exact in float64 for float32 weights of similar magnitude) keeps their
-    # order, and the forest's weights are recomputed from the lens below
-    shift = -float(w.min()) if len(w) and w.min() < 0 else 0.0
-    rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(graph.indptr))
-    d_rows = torch.from_numpy(rows).cuda()
-    d_cols = torch.from_numpy(np.ascontiguousarray(graph.indices)).cuda()
-    d_w = torch.from_numpy(w + shift).cuda()
-    edges = torch.empty((max(n - 1, 0), 3), dtype=torch.float64, device="cuda")
-    nbrs = torch.empty((n, 1), dtype=torch.int32, device="cuda")
-    core = torch.empty((n,), dtype=torch.float64, device="cuda")
-    ncomp = ctypes.c_int64(0)
+    if n <= 1:
+        return n, np.zeros(n, np.int64), np.zeros((0, 3)), graph
     V = _native.vptr
-    _native.check(_native.load().fhg_precomputed_mst(
-        V(d_rows), V(d_cols), V(d_w), int(d_w.numel()), n, 1, 1, V(edges), V(nbrs), V(core),
-        ctypes.byref(ncomp), _native.stream_ptr()))
-    nc = int(ncomp.value)
-    # Kruskal's forest first, then the nc - 1 bridges between its components
-    forest = edges.cpu().numpy()[: n - nc].copy()
-    a, b = forest[:, 0].astype(np.int64), forest[:, 1].astype(np.int64)
-    lv = np.asarray(lens)
-    forest[:, 2] = np.maximum(lv[a], lv[b]).astype(np.float32).astype(np.float64)
+    d_indptr = torch.from_numpy(np.ascontiguousarray(graph.indptr, np.int32)).cuda()
+    d_indices = torch.from_numpy(np.ascontiguousarray(graph.indices, np.int32)).cuda()
+    d_weights = torch.from_numpy(np.ascontiguousarray(graph.weights, np.float32)).cuda()
+    edges = torch.empty((n - 1, 3), dtype=torch.float64, device="cuda")
+    m = ctypes.c_int64(0)
+    _native.check(_native.load().fhg_core_graph_mst(V(d_indptr), V(d_indices), V(d_weights), n,
+                                                    V(edges), ctypes.byref(m),
+                                                    _native.stream_ptr()))
+    forest = edges[: m.value].cpu().numpy()
+    nc = n - int(m.value)
     if nc <= 1:
         return 1, np.zeros(n, np.int64), forest, graph
-    # the forest's components, numbered by their smallest point
-    import scipy.sparse
-    from scipy.sparse.csgraph import connected_components
-
-    adj = scipy.sparse.coo_matrix((np.ones(len(forest)), (a, b)), shape=(n, n))
-    _, comp = connected_components(adj, directed=False)
-    return nc, comp.astype(np.int64), forest, graph
+    return nc, _root_labels(n, forest), forest, graph
 
 
 def core_graph_clusters(lens, neighbors, core_distances, min_spanning_tree, **kwargs):

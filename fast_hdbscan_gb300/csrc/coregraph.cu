@@ -1,0 +1,231 @@
+// Spanning forest of a cluster's core graph (core_graph.py:198 boruvka_mst,
+// the sub-cluster / branch detection back-end) with the reference's choices
+// among equal weights, so that the forest -- and the cluster hierarchy built
+// from it -- is the reference's own.
+//
+// The graph is CSR, every row sorted by weight (ties in insertion order).
+// A Boruvka round of the reference:
+//   * every point's candidate is the first entry of its row that leaves its
+//     component (the reference deletes the other entries, keeping order);
+//   * a component keeps the candidate of smallest weight, ties to the
+//     smallest point, and components come in the order of their smallest
+//     point that has a candidate ("pos");
+//   * the candidates are added in that order, each unless its ends are
+//     already joined.
+// The candidates form a functional graph on components (each points at the
+// component its edge enters); processed in pos order, an edge is rejected
+// exactly when it closes that graph's cycle, i.e. the cycle edge of largest
+// pos.  So a round is: select (atomicMin on (ordered weight, point) and on
+// pos), find every cycle and its largest pos by pointer doubling, drop that
+// edge, emit the others in pos order (a scan over pos slots) and hook them
+// with the lock-free union-find.
+#include <utility>
+
+#include "fhg_common.cuh"
+#include "primitives.cuh"
+#include "uf.cuh"
+
+namespace fhg {
+namespace {
+
+#define LAUNCH(kernel, count, ...)                                        \
+    do {                                                                  \
+        if ((count) > 0) {                                                \
+            ::fhg::note_launch();                                         \
+            kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);   \
+            FHG_CUDA(cudaGetLastError());                                 \
+        }                                                                 \
+    } while (0)
+
+constexpr unsigned long long kNone = ~0ull;
+
+// float32 bits -> unsigned key in the float order (negatives included; -0
+// compares equal to +0, as in the reference's float comparisons)
+__device__ __forceinline__ uint32_t ordered(float w) {
+    const uint32_t u = __float_as_uint(w == 0.0f ? 0.0f : w);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void cg_init_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                               int32_t* __restrict__ comp, int32_t* __restrict__ par,
+                               int32_t* __restrict__ ptr) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    comp[p] = (int32_t)p;
+    par[p] = (int32_t)p;
+    ptr[p] = indptr[p];
+}
+
+__global__ void cg_reset_kernel(int64_t n, unsigned long long* __restrict__ best,
+                                int32_t* __restrict__ pos, uint32_t* __restrict__ take) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    best[c] = kNone;
+    pos[c] = INT32_MAX;
+    take[c] = 0u;
+}
+
+// Each point's first row entry outside its component; the component's
+// smallest (weight, point) and its smallest point with a candidate.
+__global__ void cg_select_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                 const int32_t* __restrict__ indices,
+                                 const float* __restrict__ weights,
+                                 const int32_t* __restrict__ comp, int32_t* __restrict__ ptr,
+                                 unsigned long long* __restrict__ best,
+                                 int32_t* __restrict__ pos) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t c = comp[p], end = indptr[p + 1];
+    int32_t e = ptr[p];
+    while (e < end && comp[indices[e]] == c) ++e;
+    ptr[p] = e;
+    if (e >= end) return;
+    atomicMin(best + c, ((unsigned long long)ordered(weights[e]) << 32) | (uint32_t)p);
+    atomicMin(pos + c, (int32_t)p);
+}
+
+// succ / mx of every component slot: the component its candidate enters and
+// its pos (self and -1 for slots without a candidate).
+__global__ void cg_succ_kernel(int64_t n, const int32_t* __restrict__ indices,
+                               const int32_t* __restrict__ comp,
+                               const int32_t* __restrict__ ptr,
+                               const unsigned long long* __restrict__ best,
+                               const int32_t* __restrict__ pos, int32_t* __restrict__ succ,
+                               int32_t* __restrict__ mx) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const unsigned long long b = best[c];
+    if (b == kNone) {
+        succ[c] = (int32_t)c;
+        mx[c] = -1;
+        return;
+    }
+    const int32_t p = (int32_t)(uint32_t)b;
+    succ[c] = comp[indices[ptr[p]]];
+    mx[c] = pos[c];
+}
+
+__global__ void cg_double_kernel(int64_t n, const int32_t* __restrict__ succ,
+                                 const int32_t* __restrict__ mx, int32_t* __restrict__ succ2,
+                                 int32_t* __restrict__ mx2) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int32_t t = succ[c];
+    succ2[c] = succ[t];
+    mx2[c] = max(mx[c], mx[t]);
+}
+
+// A slot reached after 2^K >= n steps lies on its part's cycle.
+__global__ void cg_mark_kernel(int64_t n, const unsigned long long* __restrict__ best,
+                               const int32_t* __restrict__ succK, uint32_t* __restrict__ cyc) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || best[c] == kNone) return;
+    cyc[succK[c]] = 1u;
+}
+
+// Candidates kept: all but each cycle's largest-pos edge; take[pos] = 1 and
+// slot[pos] = component, so that a scan over pos emits them in pos order.
+__global__ void cg_keep_kernel(int64_t n, const unsigned long long* __restrict__ best,
+                               const int32_t* __restrict__ pos, const uint32_t* __restrict__ cyc,
+                               const int32_t* __restrict__ mxK, uint32_t* __restrict__ take,
+                               int32_t* __restrict__ slot) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || best[c] == kNone) return;
+    if (cyc[c] && pos[c] == mxK[c]) return;
+    take[pos[c]] = 1u;
+    slot[pos[c]] = (int32_t)c;
+}
+
+__global__ void cg_emit_kernel(int64_t n, int64_t base, const uint32_t* __restrict__ take,
+                               const uint32_t* __restrict__ rank,
+                               const int32_t* __restrict__ slot,
+                               const unsigned long long* __restrict__ best,
+                               const int32_t* __restrict__ ptr,
+                               const int32_t* __restrict__ indices,
+                               const float* __restrict__ weights, const int32_t* __restrict__ comp,
+                               double* __restrict__ edges, int32_t* __restrict__ par) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n || !take[q]) return;
+    const int32_t c = slot[q];
+    const int32_t p = (int32_t)(uint32_t)best[c];
+    const int32_t e = ptr[p];
+    const int32_t j = indices[e];
+    double* row = edges + 3 * (base + rank[q]);
+    row[0] = (double)p;
+    row[1] = (double)j;
+    row[2] = (double)weights[e];
+    uf_union(par, c, comp[j]);
+}
+
+__global__ void cg_relabel_kernel(int64_t n, int32_t* __restrict__ comp, int32_t* __restrict__ par) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    comp[p] = uf_find(par, comp[p]);
+}
+
+}  // namespace
+
+int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
+                       const float* weights, double* edges, int64_t* n_edges, cudaStream_t s) {
+    *n_edges = 0;
+    if (n <= 1) return FHG_OK;
+    if (n > 0x7ffffffeLL) {
+        set_error("core graph: more than 2^31 - 2 points");
+        return FHG_ERR_UNSUPPORTED;
+    }
+    Stage stage(s, "core_graph_boruvka");
+    Workspace ws(s);
+    int32_t *comp, *par, *ptr, *pos, *succ, *mx, *succ2, *mx2, *slot;
+    unsigned long long* best;
+    uint32_t *take, *rank, *cyc, *total;
+    FHG_TRY(ws.alloc(&comp, (size_t)n));
+    FHG_TRY(ws.alloc(&par, (size_t)n));
+    FHG_TRY(ws.alloc(&ptr, (size_t)n));
+    FHG_TRY(ws.alloc(&pos, (size_t)n));
+    FHG_TRY(ws.alloc(&succ, (size_t)n));
+    FHG_TRY(ws.alloc(&mx, (size_t)n));
+    FHG_TRY(ws.alloc(&succ2, (size_t)n));
+    FHG_TRY(ws.alloc(&mx2, (size_t)n));
+    FHG_TRY(ws.alloc(&slot, (size_t)n));
+    FHG_TRY(ws.alloc(&best, (size_t)n));
+    FHG_TRY(ws.alloc(&take, (size_t)n));
+    FHG_TRY(ws.alloc(&rank, (size_t)n));
+    FHG_TRY(ws.alloc(&cyc, (size_t)n));
+    FHG_TRY(ws.alloc(&total, 1));
+    LAUNCH(cg_init_kernel, n, n, indptr, comp, par, ptr);
+    int K = 1;
+    while (((int64_t)1 << K) < n) ++K;
+    int64_t m = 0, components = n;
+    while (components > 1) {
+        LAUNCH(cg_reset_kernel, n, n, best, pos, take);
+        FHG_CUDA(cudaMemsetAsync(cyc, 0, sizeof(uint32_t) * n, s));
+        LAUNCH(cg_select_kernel, n, n, indptr, indices, weights, comp, ptr, best, pos);
+        LAUNCH(cg_succ_kernel, n, n, indices, comp, ptr, best, pos, succ, mx);
+        int32_t *a = succ, *am = mx, *b = succ2, *bm = mx2;
+        for (int k = 0; k < K; ++k) {
+            LAUNCH(cg_double_kernel, n, n, a, am, b, bm);
+            std::swap(a, b);
+            std::swap(am, bm);
+        }
+        LAUNCH(cg_mark_kernel, n, n, best, a, cyc);
+        LAUNCH(cg_keep_kernel, n, n, best, pos, cyc, am, take, slot);
+        FHG_TRY(scan_exclusive_u32(ws, take, rank, n, total));
+        uint32_t added = 0;
+        FHG_CUDA(cudaMemcpyAsync(&added, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        if (added == 0) break;
+        if (m + (int64_t)added > n - 1) {
+            set_error("core graph: spanning forest overflow");
+            return FHG_ERR_NO_CONVERGENCE;
+        }
+        LAUNCH(cg_emit_kernel, n, n, m, take, rank, slot, best, ptr, indices, weights, comp,
+               edges, par);
+        LAUNCH(cg_relabel_kernel, n, n, comp, par);
+        m += added;
+        components -= added;
+    }
+    *n_edges = m;
+    return FHG_OK;
+}
+
+}  // namespace fhg

@@ -32,6 +32,12 @@ struct MstResult {
 int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const float* weights,
                     double* edges, int32_t* neighbors, double* core, int64_t* n_components,
                     cudaStream_t s);
+// Spanning forest of a core graph (CSR, rows sorted by weight) with the
+// reference's Boruvka choices (core_graph.py:198): edges (p, neighbour,
+// weight) float64 in the reference's order; *n_edges of them.
+int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
+                       const float* weights, double* edges, int64_t* n_edges, cudaStream_t s);
+
 // The same on kNN lists from the spatial index (index given) or from the
 // brute-force high-dimensional kNN of X (n x d, index NULL) -- the latter is
 // nndescent.py:179 compute_mst_from_knn_graph with an exact kNN graph.

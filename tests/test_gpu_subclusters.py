@@ -73,3 +73,37 @@ def test_detector_input_errors(engine):
         BranchDetector(cluster_selection_method="other").fit(c)
     with pytest.raises(ValueError):
         BranchDetector().fit(c, labels=np.full(len(g["X"]), -1))
+
+
+def _random_core_graph_inputs(seed, n, lens_kind):
+    rng = np.random.default_rng(seed)
+    k = 5
+    nb = rng.integers(0, n, size=(n, k)).astype(np.int32)
+    nb[rng.random((n, k)) < (0.6 if lens_kind == "sparse" else 0.1)] = -1
+    core = rng.random(n).astype(np.float32)
+    perm = rng.permutation(n)
+    parents = perm[rng.integers(0, np.arange(1, n))]  # a random tree over perm
+    mst = np.c_[parents, perm[1:], rng.random(n - 1)].astype(np.float64)
+    if lens_kind == "sparse":
+        mst = mst[rng.random(n - 1) < 0.3]
+    lens = {"float": rng.random(n), "int": rng.integers(0, 6, n).astype(np.float64),
+            "neg": rng.normal(0, 1, n), "sparse": rng.random(n)}[lens_kind]
+    return nb, core, mst, lens
+
+
+@pytest.mark.parametrize("seed,kind", [(0, "float"), (1, "int"), (2, "neg"), (3, "sparse")])
+def test_core_graph_forest_matches_oracle(engine, seed, kind):
+    """The GPU forest equals the restated reference Boruvka edge for edge,
+    including its choices among equal weights (integer lens: heavy ties) and
+    a disconnected graph."""
+    from fast_hdbscan_gb300.core_graph import core_graph_spanning_tree
+    from oracle import core_graph_boruvka as CB
+
+    nb, core, mst, lens = _random_core_graph_inputs(seed, 3000, kind)
+    nc, comp, forest, graph = core_graph_spanning_tree(nb, core, mst, lens)
+    nc_o, comp_o, edges_o = CB.boruvka_mst(graph.weights, graph.indices, graph.indptr)
+    assert nc == nc_o
+    np.testing.assert_array_equal(forest, edges_o)
+    if nc > 1:
+        _, ref_labels = np.unique(comp_o, return_inverse=True)
+        np.testing.assert_array_equal(comp, ref_labels)
