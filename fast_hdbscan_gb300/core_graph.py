@@ -38,12 +38,20 @@ def knn_mst_union(neighbors, core_distances, min_spanning_tree, lens_values):
     cols_k = nb.reshape(-1).astype(np.int64)
     valid = cols_k >= 0
     rows_k, cols_k = rows_k[valid], cols_k[valid]
+    # a child enters a row once (the reference's per-row dict keeps the first)
+    _, first = np.unique(rows_k * n + cols_k, return_index=True)
+    first.sort()
+    rows_k, cols_k = rows_k[first], cols_k[first]
     w_k = np.maximum(lens[rows_k], lens[cols_k])
     d_k = np.maximum(core[rows_k], core[cols_k])
     mst = np.asarray(min_spanning_tree, dtype=np.float64).reshape(-1, 3)
     rows_m = mst[:, 0].astype(np.int64)
     cols_m = mst[:, 1].astype(np.int64)
-    new = ~np.isin(rows_m * n + cols_m, rows_k * n + cols_k)
+    keys_m = rows_m * n + cols_m
+    _, first = np.unique(keys_m, return_index=True)
+    new = np.zeros(len(keys_m), bool)
+    new[first] = True
+    new &= ~np.isin(keys_m, rows_k * n + cols_k)
     rows_m, cols_m, d_m = rows_m[new], cols_m[new], mst[new, 2]
     w_m = np.maximum(lens[rows_m], lens[cols_m])
     rows = np.concatenate([rows_k, rows_m])

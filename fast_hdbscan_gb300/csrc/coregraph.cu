@@ -12,6 +12,11 @@
 //     point that has a candidate ("pos");
 //   * the candidates are added in that order, each unless its ends are
 //     already joined.
+// The reference reads a point's candidate at its row's first slot, so a
+// point with an empty row takes the first remaining entry of the next
+// non-empty row (own[p]); such an entry may lie inside the point's own
+// component, where it still counts as the component's candidate and is
+// then skipped (a one-edge cycle below).
 // The candidates form a functional graph on components (each points at the
 // component its edge enters); processed in pos order, an edge is rejected
 // exactly when it closes that graph's cycle, i.e. the cycle edge of largest
@@ -48,12 +53,28 @@ __device__ __forceinline__ uint32_t ordered(float w) {
 
 __global__ void cg_init_kernel(int64_t n, const int32_t* __restrict__ indptr,
                                int32_t* __restrict__ comp, int32_t* __restrict__ par,
-                               int32_t* __restrict__ ptr) {
+                               int32_t* __restrict__ ptr, int32_t* __restrict__ own) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     comp[p] = (int32_t)p;
     par[p] = (int32_t)p;
     ptr[p] = indptr[p];
+    int64_t r = p;  // the row owning slot indptr[p]: p, or the next non-empty row
+    while (r < n && indptr[r + 1] == indptr[r]) ++r;
+    own[p] = r < n ? (int32_t)r : -1;
+}
+
+// Every row's first entry outside its component (the reference's rows after
+// update_graph_components, :143).
+__global__ void cg_advance_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                  const int32_t* __restrict__ indices,
+                                  const int32_t* __restrict__ comp, int32_t* __restrict__ ptr) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t c = comp[p], end = indptr[p + 1];
+    int32_t e = ptr[p];
+    while (e < end && comp[indices[e]] == c) ++e;
+    ptr[p] = e;
 }
 
 __global__ void cg_reset_kernel(int64_t n, unsigned long long* __restrict__ best,
@@ -65,21 +86,22 @@ __global__ void cg_reset_kernel(int64_t n, unsigned long long* __restrict__ best
     take[c] = 0u;
 }
 
-// Each point's first row entry outside its component; the component's
-// smallest (weight, point) and its smallest point with a candidate.
+// Each point's candidate (the entry at its row's first slot); the
+// component's smallest (weight, point) and its smallest point with one.
 __global__ void cg_select_kernel(int64_t n, const int32_t* __restrict__ indptr,
-                                 const int32_t* __restrict__ indices,
                                  const float* __restrict__ weights,
-                                 const int32_t* __restrict__ comp, int32_t* __restrict__ ptr,
+                                 const int32_t* __restrict__ comp,
+                                 const int32_t* __restrict__ ptr,
+                                 const int32_t* __restrict__ own,
                                  unsigned long long* __restrict__ best,
                                  int32_t* __restrict__ pos) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const int32_t c = comp[p], end = indptr[p + 1];
-    int32_t e = ptr[p];
-    while (e < end && comp[indices[e]] == c) ++e;
-    ptr[p] = e;
-    if (e >= end) return;
+    const int32_t r = own[p];
+    if (r < 0) return;
+    const int32_t e = ptr[r];
+    if (e >= indptr[r + 1]) return;
+    const int32_t c = comp[p];
     atomicMin(best + c, ((unsigned long long)ordered(weights[e]) << 32) | (uint32_t)p);
     atomicMin(pos + c, (int32_t)p);
 }
@@ -89,6 +111,7 @@ __global__ void cg_select_kernel(int64_t n, const int32_t* __restrict__ indptr,
 __global__ void cg_succ_kernel(int64_t n, const int32_t* __restrict__ indices,
                                const int32_t* __restrict__ comp,
                                const int32_t* __restrict__ ptr,
+                               const int32_t* __restrict__ own,
                                const unsigned long long* __restrict__ best,
                                const int32_t* __restrict__ pos, int32_t* __restrict__ succ,
                                int32_t* __restrict__ mx) {
@@ -101,7 +124,7 @@ __global__ void cg_succ_kernel(int64_t n, const int32_t* __restrict__ indices,
         return;
     }
     const int32_t p = (int32_t)(uint32_t)b;
-    succ[c] = comp[indices[ptr[p]]];
+    succ[c] = comp[indices[ptr[own[p]]]];
     mx[c] = pos[c];
 }
 
@@ -141,6 +164,7 @@ __global__ void cg_emit_kernel(int64_t n, int64_t base, const uint32_t* __restri
                                const int32_t* __restrict__ slot,
                                const unsigned long long* __restrict__ best,
                                const int32_t* __restrict__ ptr,
+                               const int32_t* __restrict__ own,
                                const int32_t* __restrict__ indices,
                                const float* __restrict__ weights, const int32_t* __restrict__ comp,
                                double* __restrict__ edges, int32_t* __restrict__ par) {
@@ -148,7 +172,7 @@ __global__ void cg_emit_kernel(int64_t n, int64_t base, const uint32_t* __restri
     if (q >= n || !take[q]) return;
     const int32_t c = slot[q];
     const int32_t p = (int32_t)(uint32_t)best[c];
-    const int32_t e = ptr[p];
+    const int32_t e = ptr[own[p]];
     const int32_t j = indices[e];
     double* row = edges + 3 * (base + rank[q]);
     row[0] = (double)p;
@@ -175,12 +199,13 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
     }
     Stage stage(s, "core_graph_boruvka");
     Workspace ws(s);
-    int32_t *comp, *par, *ptr, *pos, *succ, *mx, *succ2, *mx2, *slot;
+    int32_t *comp, *par, *ptr, *own, *pos, *succ, *mx, *succ2, *mx2, *slot;
     unsigned long long* best;
     uint32_t *take, *rank, *cyc, *total;
     FHG_TRY(ws.alloc(&comp, (size_t)n));
     FHG_TRY(ws.alloc(&par, (size_t)n));
     FHG_TRY(ws.alloc(&ptr, (size_t)n));
+    FHG_TRY(ws.alloc(&own, (size_t)n));
     FHG_TRY(ws.alloc(&pos, (size_t)n));
     FHG_TRY(ws.alloc(&succ, (size_t)n));
     FHG_TRY(ws.alloc(&mx, (size_t)n));
@@ -192,15 +217,18 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
     FHG_TRY(ws.alloc(&rank, (size_t)n));
     FHG_TRY(ws.alloc(&cyc, (size_t)n));
     FHG_TRY(ws.alloc(&total, 1));
-    LAUNCH(cg_init_kernel, n, n, indptr, comp, par, ptr);
+    LAUNCH(cg_init_kernel, n, n, indptr, comp, par, ptr, own);
     int K = 1;
     while (((int64_t)1 << K) < n) ++K;
     int64_t m = 0, components = n;
     while (components > 1) {
         LAUNCH(cg_reset_kernel, n, n, best, pos, take);
         FHG_CUDA(cudaMemsetAsync(cyc, 0, sizeof(uint32_t) * n, s));
-        LAUNCH(cg_select_kernel, n, n, indptr, indices, weights, comp, ptr, best, pos);
-        LAUNCH(cg_succ_kernel, n, n, indices, comp, ptr, best, pos, succ, mx);
+        // rows are compacted after each round's merges: the first round reads
+        // them as given (an entry may point into its own one-point component)
+        if (m > 0 || components < n) LAUNCH(cg_advance_kernel, n, n, indptr, indices, comp, ptr);
+        LAUNCH(cg_select_kernel, n, n, indptr, weights, comp, ptr, own, best, pos);
+        LAUNCH(cg_succ_kernel, n, n, indices, comp, ptr, own, best, pos, succ, mx);
         int32_t *a = succ, *am = mx, *b = succ2, *bm = mx2;
         for (int k = 0; k < K; ++k) {
             LAUNCH(cg_double_kernel, n, n, a, am, b, bm);
@@ -218,8 +246,8 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
             set_error("core graph: spanning forest overflow");
             return FHG_ERR_NO_CONVERGENCE;
         }
-        LAUNCH(cg_emit_kernel, n, n, m, take, rank, slot, best, ptr, indices, weights, comp,
-               edges, par);
+        LAUNCH(cg_emit_kernel, n, n, m, take, rank, slot, best, ptr, own, indices, weights,
+               comp, edges, par);
         LAUNCH(cg_relabel_kernel, n, n, comp, par);
         m += added;
         components -= added;
