@@ -32,26 +32,29 @@ def knn_mst_union(neighbors, core_distances, min_spanning_tree, lens_values):
     n = len(core_distances)
     lens = np.asarray(lens_values)
     core = np.asarray(core_distances)
-    nb = np.asarray(neighbors)
-    k = nb.shape[1] if nb.ndim == 2 else 0
-    rows_k = np.repeat(np.arange(n, dtype=np.int64), k)
-    cols_k = nb.reshape(-1).astype(np.int64)
-    valid = cols_k >= 0
-    rows_k, cols_k = rows_k[valid], cols_k[valid]
+    nb = np.asarray(neighbors).reshape(n, -1)
+    k = nb.shape[1]
+    valid = nb >= 0
     # a child enters a row once (the reference's per-row dict keeps the first)
-    _, first = np.unique(rows_k * n + cols_k, return_index=True)
-    first.sort()
-    rows_k, cols_k = rows_k[first], cols_k[first]
+    if k > 1:
+        srt = np.sort(nb, axis=1)
+        if np.any((srt[:, 1:] == srt[:, :-1]) & (srt[:, 1:] >= 0)):
+            for j in range(1, k):
+                valid[:, j] &= ~np.any(nb[:, :j] == nb[:, j:j + 1], axis=1)
+    rows_k, jk = np.nonzero(valid)  # row-major: each row's children in neighbour order
+    cols_k = nb[rows_k, jk].astype(np.int64)
     w_k = np.maximum(lens[rows_k], lens[cols_k])
     d_k = np.maximum(core[rows_k], core[cols_k])
     mst = np.asarray(min_spanning_tree, dtype=np.float64).reshape(-1, 3)
     rows_m = mst[:, 0].astype(np.int64)
     cols_m = mst[:, 1].astype(np.int64)
+    new = ~np.any(nb[rows_m] == cols_m[:, None], axis=1) if k > 0 else np.ones(len(rows_m), bool)
     keys_m = rows_m * n + cols_m
-    _, first = np.unique(keys_m, return_index=True)
-    new = np.zeros(len(keys_m), bool)
-    new[first] = True
-    new &= ~np.isin(keys_m, rows_k * n + cols_k)
+    if len(np.unique(keys_m)) != len(keys_m):  # repeated MST pairs: the first counts
+        _, first = np.unique(keys_m, return_index=True)
+        once = np.zeros(len(keys_m), bool)
+        once[first] = True
+        new &= once
     rows_m, cols_m, d_m = rows_m[new], cols_m[new], mst[new, 2]
     w_m = np.maximum(lens[rows_m], lens[cols_m])
     rows = np.concatenate([rows_k, rows_m])
