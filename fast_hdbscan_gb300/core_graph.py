@@ -109,8 +109,8 @@ def core_graph_spanning_tree(neighbors, core_distances, min_spanning_tree, lens)
     d_weights = torch.from_numpy(np.ascontiguousarray(graph.weights, np.float32)).cuda()
     edges = torch.empty((n - 1, 3), dtype=torch.float64, device="cuda")
     m = ctypes.c_int64(0)
-    _native.check(_native.load().fhg_core_graph_mst(V(d_indptr), V(d_indices), V(d_weights), n,
-                                                    V(edges), ctypes.byref(m),
+    _native.check(_native.load().fhg_core_graph_mst(V(d_indptr), V(d_indices), V(d_weights),
+                                                    None, n, V(edges), ctypes.byref(m),
                                                     _native.stream_ptr()))
     forest = edges[: m.value].cpu().numpy()
     nc = n - int(m.value)
@@ -119,17 +119,62 @@ def core_graph_spanning_tree(neighbors, core_distances, min_spanning_tree, lens)
     return nc, _root_labels(n, forest), forest, graph
 
 
-def core_graph_clusters(lens, neighbors, core_distances, min_spanning_tree, **kwargs):
-    """core_graph.py:244: the cluster hierarchy of the lens-weighted core
-    graph's spanning tree, or its components when it is disconnected."""
+def core_graph_forests(graphs):
+    """Spanning forests of several core graphs in one GPU launch (their rows
+    as disjoint blocks of one CSR): ``[(n_components, component_labels,
+    forest), ...]``, each as ``core_graph_spanning_tree`` returns it."""
+    torch = _native._torch()
+    sizes = np.array([len(g.indptr) - 1 for g in graphs], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    n = int(offs[-1])
+    if n <= 1:
+        return [(int(sz), np.zeros(int(sz), np.int64), np.zeros((0, 3))) for sz in sizes]
+    nnz = np.concatenate([[0], np.cumsum([g.indptr[-1] for g in graphs])])
+    indptr = np.concatenate([g.indptr[:-1].astype(np.int64) + nnz[i]
+                             for i, g in enumerate(graphs)] + [[nnz[-1]]]).astype(np.int32)
+    indices = np.concatenate([g.indices.astype(np.int64) + offs[i]
+                              for i, g in enumerate(graphs)]).astype(np.int32)
+    weights = np.concatenate([g.weights for g in graphs]).astype(np.float32)
+    if np.any(np.isnan(weights)):
+        raise ValueError("lens values must not be NaN")
+    seg_end = np.repeat(offs[1:], sizes).astype(np.int32)
+    V = _native.vptr
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    d_indptr, d_indices, d_weights, d_seg = T(indptr), T(indices), T(weights), T(seg_end)
+    edges = torch.empty((n - 1, 3), dtype=torch.float64, device="cuda")
+    m = ctypes.c_int64(0)
+    _native.check(_native.load().fhg_core_graph_mst(V(d_indptr), V(d_indices), V(d_weights),
+                                                    V(d_seg), n, V(edges), ctypes.byref(m),
+                                                    _native.stream_ptr()))
+    all_edges = edges[: m.value].cpu().numpy()
+    owner = np.searchsorted(offs, all_edges[:, 0].astype(np.int64), side="right") - 1
+    order = np.argsort(owner, kind="stable")
+    bounds = np.searchsorted(owner[order], np.arange(len(graphs) + 1))
+    out = []
+    for i, sz in enumerate(sizes):
+        f = all_edges[order[bounds[i]:bounds[i + 1]]].copy()
+        f[:, :2] -= offs[i]
+        nc = int(sz) - len(f)
+        comp = np.zeros(int(sz), np.int64) if nc <= 1 else _root_labels(int(sz), f)
+        out.append((max(nc, 1) if sz > 0 else 0, comp, f))
+    return out
+
+
+def _clusters_of_forest(num_components, component_labels, lensed_mst, graph, **kwargs):
     from .hdbscan import clusters_from_spanning_tree
 
-    num_components, component_labels, lensed_mst, graph = core_graph_spanning_tree(
-        neighbors, core_distances, min_spanning_tree, lens)
     if num_components > 1:
         return (component_labels, np.ones(len(component_labels), dtype=np.float32),
                 np.empty((0, 4)), empty_condensed_tree(), lensed_mst, graph)
     return (*clusters_from_spanning_tree(lensed_mst, **kwargs), graph)
+
+
+def core_graph_clusters(lens, neighbors, core_distances, min_spanning_tree, **kwargs):
+    """core_graph.py:244: the cluster hierarchy of the lens-weighted core
+    graph's spanning tree, or its components when it is disconnected."""
+    num_components, component_labels, lensed_mst, graph = core_graph_spanning_tree(
+        neighbors, core_distances, min_spanning_tree, lens)
+    return _clusters_of_forest(num_components, component_labels, lensed_mst, graph, **kwargs)
 
 
 def core_graph_to_rec_array(graph):

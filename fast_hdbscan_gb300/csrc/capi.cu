@@ -329,14 +329,14 @@ FHG_API int fhg_knn_graph_mst(const float* X_dev, int64_t n, int32_t d, int32_t 
 }
 
 FHG_API int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices_dev,
-                               const float* weights_dev, int64_t n, double* edges_dev,
-                               int64_t* n_edges_host, void* stream) {
+                               const float* weights_dev, const int32_t* seg_end_dev, int64_t n,
+                               double* edges_dev, int64_t* n_edges_host, void* stream) {
     if (!n_edges_host || (n > 1 && (!indptr_dev || !indices_dev || !weights_dev || !edges_dev))) {
         set_error("fhg_core_graph_mst: null pointer");
         return FHG_ERR_INVALID;
     }
-    return core_graph_boruvka(n, indptr_dev, indices_dev, weights_dev, edges_dev, n_edges_host,
-                              as_stream(stream));
+    return core_graph_boruvka(n, indptr_dev, indices_dev, weights_dev, seg_end_dev, edges_dev,
+                              n_edges_host, as_stream(stream));
 }
 
 FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples,

@@ -1,5 +1,6 @@
 // Spanning forest of a cluster's core graph (core_graph.py:198 boruvka_mst,
-// the sub-cluster / branch detection back-end) with the reference's choices
+// the sub-cluster / branch detection back-end) -- or of many clusters' graphs
+// side by side, as disjoint blocks of one CSR -- with the reference's choices
 // among equal weights, so that the forest -- and the cluster hierarchy built
 // from it -- is the reference's own.
 //
@@ -52,16 +53,19 @@ __device__ __forceinline__ uint32_t ordered(float w) {
 }
 
 __global__ void cg_init_kernel(int64_t n, const int32_t* __restrict__ indptr,
-                               int32_t* __restrict__ comp, int32_t* __restrict__ par,
-                               int32_t* __restrict__ ptr, int32_t* __restrict__ own) {
+                               const int32_t* __restrict__ seg_end, int32_t* __restrict__ comp,
+                               int32_t* __restrict__ par, int32_t* __restrict__ ptr,
+                               int32_t* __restrict__ own) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     comp[p] = (int32_t)p;
     par[p] = (int32_t)p;
     ptr[p] = indptr[p];
-    int64_t r = p;  // the row owning slot indptr[p]: p, or the next non-empty row
-    while (r < n && indptr[r + 1] == indptr[r]) ++r;
-    own[p] = r < n ? (int32_t)r : -1;
+    // the row owning slot indptr[p]: p, or the next non-empty row of p's graph
+    const int64_t lim = seg_end ? (int64_t)seg_end[p] : n;
+    int64_t r = p;
+    while (r < lim && indptr[r + 1] == indptr[r]) ++r;
+    own[p] = r < lim ? (int32_t)r : -1;
 }
 
 // Every row's first entry outside its component (the reference's rows after
@@ -190,7 +194,8 @@ __global__ void cg_relabel_kernel(int64_t n, int32_t* __restrict__ comp, int32_t
 }  // namespace
 
 int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
-                       const float* weights, double* edges, int64_t* n_edges, cudaStream_t s) {
+                       const float* weights, const int32_t* seg_end, double* edges,
+                       int64_t* n_edges, cudaStream_t s) {
     *n_edges = 0;
     if (n <= 1) return FHG_OK;
     if (n > 0x7ffffffeLL) {
@@ -217,7 +222,7 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
     FHG_TRY(ws.alloc(&rank, (size_t)n));
     FHG_TRY(ws.alloc(&cyc, (size_t)n));
     FHG_TRY(ws.alloc(&total, 1));
-    LAUNCH(cg_init_kernel, n, n, indptr, comp, par, ptr, own);
+    LAUNCH(cg_init_kernel, n, n, indptr, seg_end, comp, par, ptr, own);
     int K = 1;
     while (((int64_t)1 << K) < n) ++K;
     int64_t m = 0, components = n;

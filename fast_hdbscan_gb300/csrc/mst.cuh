@@ -35,8 +35,11 @@ int kruskal_knn_mst(const fhg_index& index, int min_samples, int query_k, const 
 // Spanning forest of a core graph (CSR, rows sorted by weight) with the
 // reference's Boruvka choices (core_graph.py:198): edges (p, neighbour,
 // weight) float64 in the reference's order; *n_edges of them.
+// seg_end (nullable): per row, the end of its graph's block of rows, when
+// several disjoint graphs share the CSR (each then evolves as alone).
 int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
-                       const float* weights, double* edges, int64_t* n_edges, cudaStream_t s);
+                       const float* weights, const int32_t* seg_end, double* edges,
+                       int64_t* n_edges, cudaStream_t s);
 
 // The same on kNN lists from the spatial index (index given) or from the
 // brute-force high-dimensional kNN of X (n x d, index NULL) -- the latter is

@@ -7,7 +7,8 @@ noise propagation and non-finite remapping -- follows the reference step for
 step."""
 import numpy as np
 
-from .core_graph import core_graph_clusters, core_graph_to_edge_list
+from .core_graph import (_clusters_of_forest, core_graph_clusters, core_graph_forests,
+                         core_graph_to_edge_list, knn_mst_union)
 from .hdbscan import _BaseEstimator as BaseEstimator
 from .hdbscan import _check_sample_weight, to_numpy_rec_array
 from .hdbscan import _ClusterMixin as ClusterMixin
@@ -46,14 +47,45 @@ def compute_sub_clusters_in_cluster(cluster, data, labels, probabilities, neighb
 
 
 def compute_sub_clusters_per_cluster(data, labels, probabilities, neighbors, core_distances,
-                                     min_spanning_tree, lens_callback, num_clusters, **kwargs):
-    """sub_clusters.py:64."""
+                                     min_spanning_tree, lens_callback, num_clusters,
+                                     sample_weights=None, **kwargs):
+    """sub_clusters.py:64: compute_sub_clusters_in_cluster for every cluster.
+    The per-cluster inputs come from one grouping pass (points and in-cluster
+    MST edges in their original order, in-cluster ids in one array) instead
+    of a scan of all points and edges per cluster; they are the same arrays."""
+    labels = np.asarray(labels)
     parent_labels = labels[min_spanning_tree[:, 0].astype(np.int64)]
     child_labels = labels[min_spanning_tree[:, 1].astype(np.int64)]
-    return [compute_sub_clusters_in_cluster(cluster, data, labels, probabilities, neighbors,
-                                            core_distances, min_spanning_tree, parent_labels,
-                                            child_labels, lens_callback, **kwargs)
-            for cluster in range(num_clusters)]
+    order = np.argsort(labels, kind="stable")
+    bounds = np.searchsorted(labels[order], np.arange(num_clusters + 1))
+    same = parent_labels == child_labels
+    e_idx = np.nonzero(same)[0]
+    e_order = e_idx[np.argsort(parent_labels[e_idx], kind="stable")]
+    e_bounds = np.searchsorted(parent_labels[e_order], np.arange(num_clusters + 1))
+    local = np.empty(len(labels), dtype=np.int32)
+    for cluster in range(num_clusters):
+        pts = order[bounds[cluster]:bounds[cluster + 1]]
+        local[pts] = np.arange(len(pts), dtype=np.int32)
+    per = []
+    for cluster in range(num_clusters):
+        points = order[bounds[cluster]:bounds[cluster + 1]]
+        nb = neighbors[points, :]
+        cl_nb = np.where(nb >= 0, labels[np.maximum(nb, 0)], -2) == cluster
+        nb_local = np.where(cl_nb, local[np.maximum(nb, 0)], -1).astype(np.int32)
+        mst = min_spanning_tree[e_order[e_bounds[cluster]:e_bounds[cluster + 1]]].copy()
+        mst[:, :2] = local[mst[:, :2].astype(np.int64)]
+        core = core_distances[points]
+        lens_values = lens_callback(data, probabilities, nb_local, core, mst, points)
+        per.append((points, lens_values, knn_mst_union(nb_local, core, mst, lens_values)))
+    # every cluster's forest in one launch, then each cluster's hierarchy
+    forests = core_graph_forests([g for _, _, g in per])
+    out = []
+    for (points, lens_values, graph), (nc, comp, forest) in zip(per, forests):
+        out.append((*_clusters_of_forest(
+            nc, comp, forest, graph,
+            sample_weights=(sample_weights[points] if sample_weights is not None else None),
+            **kwargs), lens_values, points))
+    return out
 
 
 def update_labels(cluster_probabilities, sub_labels_list, sub_probabilities_list,

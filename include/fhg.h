@@ -358,11 +358,14 @@ int fhg_hdbscan_fit_knn_graph(const float* X_dev, int64_t n, int32_t d, int32_t 
 /* core_graph.py:198 boruvka_mst: the spanning forest of a cluster's core
  * graph (CSR of n rows, each sorted by float32 weight, ties in insertion
  * order; nnz = indptr[n]) with the reference's choices among equal weights.
- * Writes *n_edges_host <= n - 1 edges (point, neighbour, weight) float64 in
- * the reference's order; n - *n_edges_host components remain. */
+ * Several clusters' graphs may share the CSR as disjoint blocks of rows:
+ * seg_end_dev (optional, n int32) gives each row the end of its block, and
+ * every block evolves as if alone.  Writes *n_edges_host <= n - 1 edges
+ * (point, neighbour, weight) float64; each block's edges appear in the
+ * reference's order for that block. */
 int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices_dev,
-                       const float* weights_dev, int64_t n, double* edges_dev,
-                       int64_t* n_edges_host, void* stream);
+                       const float* weights_dev, const int32_t* seg_end_dev, int64_t n,
+                       double* edges_dev, int64_t* n_edges_host, void* stream);
 
 /* fhg_hdbscan_fit, with the large outputs also copied to host memory while
  * the fit runs: each non-NULL *_host destination receives its output from a

@@ -107,3 +107,22 @@ def test_core_graph_forest_matches_oracle(engine, seed, kind):
     if nc > 1:
         _, ref_labels = np.unique(comp_o, return_inverse=True)
         np.testing.assert_array_equal(comp, ref_labels)
+
+
+def test_batched_forests_equal_single(engine):
+    """Several clusters' graphs in one launch (disjoint blocks, empty rows at
+    block ends included) give each graph's own forest."""
+    from fast_hdbscan_gb300.core_graph import (core_graph_forests, core_graph_spanning_tree,
+                                               knn_mst_union)
+
+    graphs, singles = [], []
+    for seed, kind, n in [(5, "float", 700), (6, "sparse", 500), (7, "int", 900), (8, "sparse", 40)]:
+        nb, core, mst, lens = _random_core_graph_inputs(seed, n, kind)
+        nb[-3:] = -1  # the block's last rows: no kNN children ...
+        mst = mst[~np.isin(mst[:, 0], [n - 1, n - 2, n - 3])]  # ... and no MST children
+        graphs.append(knn_mst_union(nb, core, mst, lens))
+        singles.append(core_graph_spanning_tree(nb, core, mst, lens))
+    for (nc, comp, forest), (nc1, comp1, forest1, _) in zip(core_graph_forests(graphs), singles):
+        assert nc == nc1
+        np.testing.assert_array_equal(forest, forest1)
+        np.testing.assert_array_equal(comp, comp1)
