@@ -570,8 +570,12 @@ def run_batched(args):
         torch.cuda.synchronize()
         return time.perf_counter() - t0
 
+    from fast_hdbscan_gb300.batch import autotune_workers
+
+    best, tune_times = autotune_workers(Xs, ms, mcs, sample=256)
     with ClockSampler(local) as clocks:
-        t_batch = timed(16)
+        t_batch = timed(best)
+    t_16 = timed(16)
     t_one = timed(1)
     cpu = None
     if not args.no_cpu_baseline:
@@ -595,11 +599,14 @@ def run_batched(args):
         "config": {"workload": "batched_uneven_instances", "instances": len(Xs),
                    "points": total, "sizes": "log-uniform 200..200000", "d": "2..8",
                    "min_samples": "{5,10,20}", "min_cluster_size": "max(10, n/100)",
-                   "workers": 16},
+                   "workers": best, "workers_source": "autotune_workers on 256 sampled "
+                   "instances", "autotune_s": {str(k): round(v, 3) for k, v in tune_times.items()}},
         "points_per_s": round(total / t_batch, 1), "s_total": round(t_batch, 3),
         "one_at_a_time": {"value": round(len(Xs) / t_one, 2), "unit": "instances/s",
                           "s_total": round(t_one, 3)},
         "speedup_vs_one_at_a_time": round(t_one / t_batch, 2),
+        "workers_16": {"value": round(len(Xs) / t_16, 2), "unit": "instances/s",
+                       "s_total": round(t_16, 3)},
         "cpu_baseline": cpu, "clocks": clocks.summary(),
         "e2e_note": "host arrays in, host labels/probabilities out (fit_many)",
     }

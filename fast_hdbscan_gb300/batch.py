@@ -5,9 +5,12 @@
 
 Every instance gets exactly the labels and probabilities of a single fit
 (fast_hdbscan(X, min_samples, min_cluster_size)); the fits run concurrently on
-a pool of worker streams inside the engine.
+a pool of worker streams inside the engine, largest instances first.  The
+number of streams can be tuned per batch size signature (autotune_workers,
+fit_many(workers="auto")).
 """
 import ctypes
+import time
 
 import numpy as np
 
@@ -23,14 +26,62 @@ def _per_instance(v, count, name):
     return v
 
 
+WORKER_CANDIDATES = (4, 8, 16, 32, 64)
+_TUNED = {}  # size signature -> worker count
+
+
+def _signature(instances):
+    """Size bucket of a batch: log2 of its median instance size and of its
+    instance count."""
+    sizes = np.array([np.shape(X)[0] for X in instances], dtype=np.float64)
+    return (int(np.log2(max(np.median(sizes), 1.0))), int(np.log2(max(len(sizes), 1))))
+
+
+def autotune_workers(instances, min_samples=10, min_cluster_size=10, candidates=None,
+                     sample=256, seed=0, **kwargs):
+    """Pick the number of worker streams for batches like ``instances``: time
+    fit_many on a random sample of them (a warm-up pass, then one timed pass
+    per candidate) and keep the fastest for the batch's size signature.
+    Returns ``(workers, {candidate: seconds})``."""
+    torch = _native._torch()
+    count = len(instances)
+    ms = _per_instance(min_samples, count, "min_samples")
+    mcs = _per_instance(min_cluster_size, count, "min_cluster_size")
+    rng = np.random.default_rng(seed)
+    pick = np.sort(rng.choice(count, min(sample, count), replace=False))
+    Xs, m1, m2 = [instances[i] for i in pick], [ms[i] for i in pick], [mcs[i] for i in pick]
+    candidates = tuple(candidates or WORKER_CANDIDATES)
+    fit_many(Xs, m1, m2, workers=max(candidates), **kwargs)
+    times = {}
+    for w in candidates:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fit_many(Xs, m1, m2, workers=w, **kwargs)
+        torch.cuda.synchronize()
+        times[w] = time.perf_counter() - t0
+    best = min(times, key=times.get)
+    _TUNED[_signature(instances)] = best
+    return best, times
+
+
 def fit_many(instances, min_samples=10, min_cluster_size=10, cluster_selection_method="eom",
              max_cluster_size=np.inf, allow_single_cluster=False, workers=16):
     """Returns [(labels intp[n_i], probabilities float32[n_i]), ...].
 
     ``min_samples`` / ``min_cluster_size``: one value, or one per instance
-    (min_samples None means min_cluster_size, as in fast_hdbscan)."""
+    (min_samples None means min_cluster_size, as in fast_hdbscan).
+    ``workers="auto"``: the count autotune_workers found for batches of this
+    size signature (tuned on a sample of this batch when there is none)."""
     torch = _native._torch()
     count = len(instances)
+    if workers == "auto":
+        sig = _signature(instances)
+        if sig not in _TUNED:
+            autotune_workers(instances, min_samples, min_cluster_size,
+                             cluster_selection_method=cluster_selection_method,
+                             max_cluster_size=max_cluster_size,
+                             allow_single_cluster=allow_single_cluster)
+        workers = _TUNED[sig]
     ms = _per_instance(min_samples, count, "min_samples")
     mcs = _per_instance(min_cluster_size, count, "min_cluster_size")
     method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)

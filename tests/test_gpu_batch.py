@@ -40,3 +40,23 @@ def test_fit_many_degenerate_and_leaf(engine):
                             cluster_selection_method="leaf")
         np.testing.assert_array_equal(got[0], want[0])
         np.testing.assert_array_equal(got[1], want[1])
+
+
+def test_autotuned_workers(engine):
+    """The worker autotuner picks one of its candidates, remembers it for the
+    batch's size signature, and fit_many(workers="auto") gives the same
+    results as any fixed count."""
+    from fast_hdbscan_gb300 import batch
+
+    inst = synthetic.batch_instances(40, seed=22, n_min=200, n_max=5_000)
+    Xs = [X for X, _, _ in inst]
+    ms = [m for _, m, _ in inst]
+    mcs = [c for _, _, c in inst]
+    best, times = batch.autotune_workers(Xs, ms, mcs, candidates=(2, 8), sample=16)
+    assert best in (2, 8) and set(times) == {2, 8}
+    assert batch._TUNED[batch._signature(Xs)] == best
+    auto = batch.fit_many(Xs, ms, mcs, workers="auto")
+    fixed = batch.fit_many(Xs, ms, mcs, workers=3)
+    for (a, b), (c, d) in zip(auto, fixed):
+        np.testing.assert_array_equal(a, c)
+        np.testing.assert_array_equal(b, d)
