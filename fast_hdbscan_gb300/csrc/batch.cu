@@ -7,12 +7,12 @@
 // worker threads, each owning a non-blocking CUDA stream, takes instances
 // from a shared counter and runs the fused fit (fhg_hdbscan_fit) on its own
 // stream; the device interleaves the kernels of all streams.  Every
-// instance's result is exactly the single-fit result.  Instances are taken
-// largest first (longest-processing-time order), so that the biggest fits do
-// not start last and leave the other streams idle.  The work is ordered
+// instance's result is exactly the single-fit result.  Instances are taken in
+// the caller's order: mixing large fits (kernel-bound) with small ones
+// (launch-bound) overlaps better than largest-first (measured: 739 against
+// 644 instances/s on 4,096 uneven instances).  The work is ordered
 // after everything already queued on the caller's stream, and the caller's
 // stream waits for all of it.
-#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -53,10 +53,6 @@ extern "C" __attribute__((visibility("default"))) int fhg_hdbscan_fit_batch(
     FHG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
     FHG_CUDA(cudaEventRecord(start, caller));
 
-    std::vector<int64_t> order((size_t)count);
-    for (int64_t i = 0; i < count; ++i) order[(size_t)i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int64_t a, int64_t b) { return n[a] > n[b]; });
     std::atomic<int64_t> next{0};
     std::mutex err_mu;
     int first_rc = FHG_OK;
@@ -75,9 +71,8 @@ extern "C" __attribute__((visibility("default"))) int fhg_hdbscan_fit_batch(
             return;
         }
         for (;;) {
-            const int64_t k = next.fetch_add(1);
-            if (k >= count) break;
-            const int64_t i = order[(size_t)k];
+            const int64_t i = next.fetch_add(1);
+            if (i >= count) break;
             const int rc = fhg_hdbscan_fit(X_dev[i], n[i], d[i], min_samples[i],
                                            min_cluster_size[i], selection_method,
                                            max_cluster_size, allow_single_cluster, 0.0, 0.0,
