@@ -139,17 +139,20 @@ __device__ __forceinline__ int hd_cut(unsigned long long* buf, int cnt, int keep
     return cnt < keep ? cnt : keep;
 }
 
-// KB: k-blocks of 16 in the operand depth 3 * dp; W warps of 16 queries.
+// KB: k-blocks of 16 in the operand depth 3 * dp; W warps of MT m-tiles of
+// 16 queries (every staged B fragment feeds MT tensor-core ops).
 // cap: candidate buffer entries per query (L + kHdChunk rounded up, <= kHdCap):
 // after a cut to L a buffer always has room for one chunk's estimates.
-template <int KB, int W>
+template <int KB, int W, int MT>
 __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
     int64_t n, int L, int cap, const __nv_bfloat16* __restrict__ A,
     const __nv_bfloat16* __restrict__ B, const float* __restrict__ ny, int32_t* __restrict__ cand,
     float* __restrict__ T) {
-    constexpr int kHdQ = W * kHdRows;
+    constexpr int kWRows = kHdRows * MT;  // queries per warp (<= 32)
+    constexpr int kHdQ = W * kWRows;
     constexpr int KW = KB * 16;
     constexpr int RS = KW + 8;  // shared row stride (bf16): conflict-free fragment loads
+    static_assert(kWRows <= 32, "one lane per warp row checks its buffer");
     extern __shared__ __align__(16) unsigned char hd_smem[];
     __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(hd_smem);  // [2][kHdChunk][RS]
     unsigned long long* bufs =
@@ -159,27 +162,37 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
     float* tau = reinterpret_cast<float*>(cnt + kHdQ);                  // [kHdQ]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int64_t q0 = (int64_t)blockIdx.x * kHdQ + warp * kHdRows;
-    if (threadIdx.x < kHdQ) {
-        cnt[threadIdx.x] = 0;
-        tau[threadIdx.x] = INFINITY;
+    const int64_t q0 = (int64_t)blockIdx.x * kHdQ + warp * kWRows;
+    for (int i = threadIdx.x; i < kHdQ; i += W * 32) {
+        cnt[i] = 0;
+        tau[i] = INFINITY;
     }
-    // this warp's 16 query rows as A fragments
-    uint32_t a[KB][4];
-    const int64_t ra = q0 + g, rb = q0 + g + 8;
+    // this warp's query rows as A fragments: m-tile mt holds rows 16 mt + g
+    // (index 0) and 16 mt + g + 8 (index 1)
+    uint32_t a[MT][KB][4];
+    float nq[MT][2], tq[MT][2];
+    unsigned long long* bq[MT][2];
+    int* cq[MT][2];
 #pragma unroll
-    for (int kb = 0; kb < KB; ++kb) {
-        const int c0 = kb * 16 + 2 * t;
-        a[kb][0] = ra < n ? *reinterpret_cast<const uint32_t*>(A + ra * KW + c0) : 0u;
-        a[kb][1] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0) : 0u;
-        a[kb][2] = ra < n ? *reinterpret_cast<const uint32_t*>(A + ra * KW + c0 + 8) : 0u;
-        a[kb][3] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0 + 8) : 0u;
+    for (int mt = 0; mt < MT; ++mt) {
+        const int64_t ra = q0 + 16 * mt + g, rb = ra + 8;
+#pragma unroll
+        for (int kb = 0; kb < KB; ++kb) {
+            const int c0 = kb * 16 + 2 * t;
+            a[mt][kb][0] = ra < n ? *reinterpret_cast<const uint32_t*>(A + ra * KW + c0) : 0u;
+            a[mt][kb][1] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0) : 0u;
+            a[mt][kb][2] = ra < n ? *reinterpret_cast<const uint32_t*>(A + ra * KW + c0 + 8) : 0u;
+            a[mt][kb][3] = rb < n ? *reinterpret_cast<const uint32_t*>(A + rb * KW + c0 + 8) : 0u;
+        }
+        nq[mt][0] = ra < n ? ny[ra] : 0.0f;
+        nq[mt][1] = rb < n ? ny[rb] : 0.0f;
+        tq[mt][0] = tq[mt][1] = INFINITY;
+        const int r0 = warp * kWRows + 16 * mt + g;
+        bq[mt][0] = bufs + r0 * cap;
+        bq[mt][1] = bufs + (r0 + 8) * cap;
+        cq[mt][0] = cnt + r0;
+        cq[mt][1] = cnt + r0 + 8;
     }
-    const float nqa = ra < n ? ny[ra] : 0.0f, nqb = rb < n ? ny[rb] : 0.0f;
-    unsigned long long* bufa = bufs + (warp * kHdRows + g) * cap;
-    unsigned long long* bufb = bufs + (warp * kHdRows + g + 8) * cap;
-    int* cnta = cnt + warp * kHdRows + g;
-    int* cntb = cnt + warp * kHdRows + g + 8;
 
     const int64_t nchunks = (n + kHdChunk - 1) / kHdChunk;
     constexpr int kSeg = KW * 2 / 16;  // 16-byte segments per point row
@@ -208,16 +221,18 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
         }
     };
     stage(0, 0);
-    float ta = INFINITY, tb = INFINITY;
     for (int64_t c = 0; c < nchunks; ++c) {
         const int slot = (int)(c & 1);
         asm volatile("cp.async.wait_group 0;\n" ::);
         __syncthreads();  // chunk c visible; every warp is done with chunk c - 1
         if (c + 1 < nchunks) stage(c + 1, slot ^ 1);
         const __nv_bfloat16* bs = Bs + slot * kHdChunk * RS;
-        float acc[8][4];
+        float acc[MT][8][4];
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+        for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+                acc[mt][nt][0] = acc[mt][nt][1] = acc[mt][nt][2] = acc[mt][nt][3] = 0.0f;
 #pragma unroll
         for (int kb = 0; kb < KB; ++kb) {
 #pragma unroll
@@ -225,7 +240,8 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
                 const __nv_bfloat16* row = bs + (nt * 8 + g) * RS + kb * 16 + 2 * t;
                 const uint32_t b0 = *reinterpret_cast<const uint32_t*>(row);
                 const uint32_t b1 = *reinterpret_cast<const uint32_t*>(row + 8);
-                hd_mma(acc[nt], a[kb], b0, b1);
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) hd_mma(acc[mt][nt], a[mt][kb], b0, b1);
             }
         }
         // estimates below the row's current L-th value join its buffer; a row
@@ -233,42 +249,50 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
         // back to its L smallest (which can only tighten its threshold)
         const int64_t jb = c * kHdChunk;
         const bool whole = jb + kHdChunk <= n;
-        int pa = 0, pb = 0;
+        int pc[MT][2];
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
+        for (int mt = 0; mt < MT; ++mt) {
+            pc[mt][0] = pc[mt][1] = 0;
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int col = nt * 8 + 2 * t + (e & 1);
-                const bool hi = e >= 2;
-                const float dd =
-                    (whole || jb + col < n)
-                        ? fmaxf(__fsub_rn(__fadd_rn(hi ? nqb : nqa, npj[slot * kHdChunk + col]),
-                                          __fmul_rn(2.0f, acc[nt][e])),
-                                0.0f)
-                        : INFINITY;
-                acc[nt][e] = dd;
-                if (hi) pb += dd < tb ? 1 : 0;
-                else pa += dd < ta ? 1 : 0;
+            for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int col = nt * 8 + 2 * t + (e & 1);
+                    const int h = e >> 1;
+                    const float dd =
+                        (whole || jb + col < n)
+                            ? fmaxf(__fsub_rn(__fadd_rn(nq[mt][h], npj[slot * kHdChunk + col]),
+                                              __fmul_rn(2.0f, acc[mt][nt][e])),
+                                    0.0f)
+                            : INFINITY;
+                    acc[mt][nt][e] = dd;
+                    pc[mt][h] += dd < tq[mt][h] ? 1 : 0;
+                }
             }
         }
-        pa += __shfl_xor_sync(0xffffffffu, pa, 1);
-        pa += __shfl_xor_sync(0xffffffffu, pa, 2);
-        pb += __shfl_xor_sync(0xffffffffu, pb, 1);
-        pb += __shfl_xor_sync(0xffffffffu, pb, 2);
-        // lane 4g answers for rows g (low half of the mask) and g + 8
-        const unsigned over_a = __ballot_sync(0xffffffffu, t == 0 && *cnta + pa > cap);
-        const unsigned over_b = __ballot_sync(0xffffffffu, t == 0 && *cntb + pb > cap);
-        unsigned rows = 0;
+        unsigned rows = 0;  // bit r: warp row r must be cut before inserting
+        int any = 0;
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            rows |= ((over_a >> (4 * r)) & 1u) << r;
-            rows |= ((over_b >> (4 * r)) & 1u) << (r + 8);
+        for (int mt = 0; mt < MT; ++mt) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                int v = pc[mt][h];
+                v += __shfl_xor_sync(0xffffffffu, v, 1);
+                v += __shfl_xor_sync(0xffffffffu, v, 2);
+                pc[mt][h] = v;
+                any += v;
+                // lane 4g answers for row 16 mt + 8 h + g
+                const unsigned over = __ballot_sync(0xffffffffu, t == 0 && *cq[mt][h] + v > cap);
+#pragma unroll
+                for (int r = 0; r < 8; ++r)
+                    rows |= ((over >> (4 * r)) & 1u) << (16 * mt + 8 * h + r);
+            }
         }
         if (rows) {
             while (rows) {
                 const int r = __ffs(rows) - 1;
                 rows &= rows - 1u;
-                const int qr = warp * kHdRows + r;
+                const int qr = warp * kWRows + r;
                 unsigned long long* b = bufs + qr * cap;
                 const int kept = hd_cut(b, cnt[qr], L, lane);
                 if (lane == 0) {
@@ -277,19 +301,25 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
                 }
                 __syncwarp();
             }
-            ta = tau[warp * kHdRows + g];
-            tb = tau[warp * kHdRows + g + 8];
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                tq[mt][0] = tau[warp * kWRows + 16 * mt + g];
+                tq[mt][1] = tau[warp * kWRows + 16 * mt + g + 8];
+            }
         }
-        if (pa + pb > 0) {  // quad-uniform: the quad's rows have passing estimates
+        if (any > 0) {  // quad-uniform: the quad's rows have passing estimates
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
+            for (int mt = 0; mt < MT; ++mt) {
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const bool hi = e >= 2;
-                    const float dd = acc[nt][e];
-                    if (dd < (hi ? tb : ta)) {
-                        const int p = atomicAdd(hi ? cntb : cnta, 1);
-                        (hi ? bufb : bufa)[p] = hd_key(dd, (int32_t)(jb + nt * 8 + 2 * t + (e & 1)));
+                for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int h = e >> 1;
+                        const float dd = acc[mt][nt][e];
+                        if (dd < tq[mt][h]) {
+                            const int p = atomicAdd(cq[mt][h], 1);
+                            bq[mt][h][p] = hd_key(dd, (int32_t)(jb + nt * 8 + 2 * t + (e & 1)));
+                        }
                     }
                 }
             }
@@ -297,8 +327,8 @@ __global__ void __launch_bounds__(W * 32) hd_cand_kernel(
         __syncwarp();
     }
     // final cut: the L smallest estimates of every row, and the L-th estimate
-    for (int r = 0; r < kHdRows; ++r) {
-        const int qr = warp * kHdRows + r;
+    for (int r = 0; r < kWRows; ++r) {
+        const int qr = warp * kWRows + r;
         const int64_t q = q0 + r;
         unsigned long long* b = bufs + qr * cap;
         const int kept = hd_cut(b, cnt[qr], L, lane);
@@ -449,37 +479,40 @@ __global__ void __launch_bounds__(128) hd_exact_kernel(
     }
 }
 
-size_t cand_smem(int kb, int warps, int cap) {
+size_t cand_smem(int kb, int queries, int cap) {
     const int rs = kb * 16 + 8;
-    const int q = warps * kHdRows;
     return (size_t)2 * kHdChunk * rs * sizeof(__nv_bfloat16) +
-           (size_t)q * cap * sizeof(unsigned long long) + 2 * kHdChunk * sizeof(float) +
-           q * (sizeof(int) + sizeof(float));
+           (size_t)queries * cap * sizeof(unsigned long long) + 2 * kHdChunk * sizeof(float) +
+           queries * (sizeof(int) + sizeof(float));
 }
 
-template <int KB, int W>
+template <int KB, int W, int MT>
 int launch_cand_w(int64_t n, int L, int cap, const __nv_bfloat16* A, const __nv_bfloat16* B,
                   const float* ny, int32_t* cand, float* T, cudaStream_t s) {
-    const size_t smem = cand_smem(KB, W, cap);
-    FHG_CUDA(cudaFuncSetAttribute(hd_cand_kernel<KB, W>,
+    constexpr int Q = W * kHdRows * MT;
+    const size_t smem = cand_smem(KB, Q, cap);
+    FHG_CUDA(cudaFuncSetAttribute(hd_cand_kernel<KB, W, MT>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t blocks = (n + W * kHdRows - 1) / (W * kHdRows);
+    const int64_t blocks = (n + Q - 1) / Q;
     Stage stage(s, "hd_cand_kernel");
     ::fhg::note_launch();
-    hd_cand_kernel<KB, W><<<(unsigned)blocks, W * 32, smem, s>>>(n, L, cap, A, B, ny, cand, T);
+    hd_cand_kernel<KB, W, MT><<<(unsigned)blocks, W * 32, smem, s>>>(n, L, cap, A, B, ny, cand,
+                                                                       T);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
 
-// Eight warps (128 queries share every staged chunk) when their buffers fit
-// in shared memory, else four.
+// 128 queries share every staged chunk when their buffers fit in shared
+// memory (64 otherwise), as 8 (4) warps of one m-tile: two m-tiles per warp
+// (each B fragment feeding two tensor-core ops, half the warps) measured
+// slower at 1M x 64-D (2.34 s against 1.92 s per kNN).
 template <int KB>
 int launch_cand(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
                 const float* ny, int32_t* cand, float* T, cudaStream_t s) {
     const int cap = std::min(kHdCap, (L + kHdChunk + 31) / 32 * 32);
-    if (cand_smem(KB, 8, cap) <= (size_t)kHdSmemMax)
-        return launch_cand_w<KB, 8>(n, L, cap, A, B, ny, cand, T, s);
-    return launch_cand_w<KB, 4>(n, L, cap, A, B, ny, cand, T, s);
+    if (cand_smem(KB, 128, cap) <= (size_t)kHdSmemMax)
+        return launch_cand_w<KB, 8, 1>(n, L, cap, A, B, ny, cand, T, s);
+    return launch_cand_w<KB, 4, 1>(n, L, cap, A, B, ny, cand, T, s);
 }
 
 }  // namespace
