@@ -5,8 +5,8 @@
 
 Every instance gets exactly the labels and probabilities of a single fit
 (fast_hdbscan(X, min_samples, min_cluster_size)); the fits run concurrently on
-a pool of worker streams inside the engine.  The number of streams can be tuned per batch size signature (autotune_workers,
-fit_many(workers="auto")).
+a pool of worker streams inside the engine.  The number of streams can be
+tuned per batch size signature (autotune_workers, fit_many(workers="auto")).
 """
 import ctypes
 import time
