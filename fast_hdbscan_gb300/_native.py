@@ -89,6 +89,8 @@ SIGNATURES = {
                                          _D, _P, _P, _P, _P, _P, _P, _P, _P,
                                          ctypes.POINTER(_I64), _P, _P, _P,
                                          ctypes.POINTER(_I64), _P]),
+    "fhg_core_graphs": (_INT, [_I64, _I32, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
+                               _P, _P, ctypes.POINTER(_I64), _P]),
     "fhg_core_graph_mst": (_INT, [_P, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), _P]),
     "fhg_knn_scan_count": (_INT, [_P, _I32, _P, ctypes.c_float, ctypes.POINTER(_I64),
                                   ctypes.POINTER(_I64), _P]),

@@ -160,6 +160,84 @@ def core_graph_forests(graphs):
     return out
 
 
+def core_graphs_and_forests(inputs):
+    """Core graphs and spanning forests of many clusters on the GPU: ``inputs``
+    is a list of ``(neighbors, core_distances, min_spanning_tree, lens)`` in
+    in-cluster ids; the graphs are laid out as one block CSR
+    (``fhg_core_graphs``), their forests built in one launch
+    (``fhg_core_graph_mst``).  Returns ``[(graph, n_components,
+    component_labels, forest), ...]`` as knn_mst_union and
+    core_graph_spanning_tree give them."""
+    torch = _native._torch()
+    sizes = np.array([len(c) for _, c, _, _ in inputs], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    P = int(offs[-1])
+    k = max([np.asarray(nb).reshape(len(c), -1).shape[1] if len(c) else 0
+             for nb, c, _, _ in inputs] + [0])
+    nb_block = np.full((P, k), -1, dtype=np.int32)
+    for i, (nb, c, _, _) in enumerate(inputs):
+        if len(c):
+            a = np.asarray(nb).reshape(len(c), -1)
+            nb_block[offs[i]:offs[i + 1], :a.shape[1]] = a
+    lens_block = np.concatenate([np.asarray(l, np.float64) for _, _, _, l in inputs] + [[]])
+    if np.any(np.isnan(lens_block)):
+        raise ValueError("lens values must not be NaN")
+    core_block = np.concatenate([np.asarray(c, np.float32) for _, c, _, _ in inputs] + [[]])
+    msts = [np.asarray(m, np.float64).reshape(-1, 3) for _, _, m, _ in inputs]
+    mparent = np.concatenate([m[:, 0].astype(np.int64) + offs[i] for i, m in enumerate(msts)]
+                             + [np.zeros(0, np.int64)]).astype(np.int32)
+    mchild = np.concatenate([m[:, 1] for m in msts] + [np.zeros(0)]).astype(np.int32)
+    mdist = np.concatenate([m[:, 2] for m in msts] + [np.zeros(0)])
+    M = len(mparent)
+    out_graphs = []
+    if P == 0:
+        return [(CoreGraph(np.zeros(0, np.float32), np.zeros(0, np.float32),
+                           np.zeros(0, np.int32), np.zeros(1, np.int32)), 0,
+                 np.zeros(0, np.int64), np.zeros((0, 3))) for _ in inputs]
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    V = _native.vptr
+    cap = P * k + M
+    d = dict(nb=T(nb_block), lens=T(lens_block.astype(np.float64)), core=T(core_block.astype(np.float32)),
+             bs=T(np.repeat(offs[:-1], sizes).astype(np.int32)),
+             be=T(np.repeat(offs[1:], sizes).astype(np.int32)),
+             mp=T(mparent), mc=T(mchild), md=T(mdist.astype(np.float64)))
+    indptr = torch.empty(P + 1, dtype=torch.int32, device="cuda")
+    il = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    ib = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
+    w = torch.empty(max(cap, 1), dtype=torch.float32, device="cuda")
+    dist = torch.empty(max(cap, 1), dtype=torch.float32, device="cuda")
+    seg = torch.empty(P, dtype=torch.int32, device="cuda")
+    nnz = ctypes.c_int64(0)
+    lib = _native.load()
+    s = _native.stream_ptr()
+    _native.check(lib.fhg_core_graphs(P, k, V(d["nb"]), V(d["lens"]), V(d["core"]), V(d["bs"]),
+                                      V(d["be"]), M, V(d["mp"]) if M else None,
+                                      V(d["mc"]) if M else None, V(d["md"]) if M else None,
+                                      V(indptr), V(il), V(ib), V(w), V(dist), V(seg),
+                                      ctypes.byref(nnz), s))
+    edges = torch.empty((max(P - 1, 1), 3), dtype=torch.float64, device="cuda")
+    m = ctypes.c_int64(0)
+    _native.check(lib.fhg_core_graph_mst(V(indptr), V(ib), V(w), V(seg), P, V(edges),
+                                         ctypes.byref(m), s))
+    z = int(nnz.value)
+    h_indptr = indptr.cpu().numpy()
+    h_il, h_w, h_d = il[:z].cpu().numpy(), w[:z].cpu().numpy(), dist[:z].cpu().numpy()
+    all_edges = edges[: m.value].cpu().numpy()
+    owner = np.searchsorted(offs, all_edges[:, 0].astype(np.int64), side="right") - 1
+    order = np.argsort(owner, kind="stable")
+    bounds = np.searchsorted(owner[order], np.arange(len(inputs) + 1))
+    for i, sz in enumerate(sizes):
+        a, b = int(h_indptr[offs[i]]), int(h_indptr[offs[i + 1]])
+        g = CoreGraph(h_w[a:b].copy(), h_d[a:b].copy(), h_il[a:b].copy(),
+                      (h_indptr[offs[i]:offs[i + 1] + 1] - a).astype(np.int32))
+        f = all_edges[order[bounds[i]:bounds[i + 1]]].copy()
+        f[:, :2] -= offs[i]
+        nc = int(sz) - len(f)
+        comp = np.zeros(int(sz), np.int64) if nc <= 1 else _root_labels(int(sz), f)
+        out_graphs.append((g, max(nc, 1) if sz > 0 else 0, comp, f))
+    return out_graphs
+
+
 def _clusters_of_forest(num_components, component_labels, lensed_mst, graph, **kwargs):
     from .hdbscan import clusters_from_spanning_tree
 

@@ -339,6 +339,30 @@ FHG_API int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices
                               n_edges_host, as_stream(stream));
 }
 
+FHG_API int fhg_core_graphs(int64_t P, int32_t k, const int32_t* nb_dev, const double* lens_dev,
+                            const float* core_dev, const int32_t* blk_start_dev,
+                            const int32_t* blk_end_dev, int64_t M, const int32_t* mparent_dev,
+                            const int32_t* mchild_dev, const double* mdist_dev,
+                            int32_t* indptr_dev, int32_t* idx_local_dev, int32_t* idx_block_dev,
+                            float* weights_dev, float* distances_dev, int32_t* seg_end_dev,
+                            int64_t* nnz_host, void* stream) {
+    if (!nnz_host || (P > 0 && (!nb_dev || !lens_dev || !core_dev || !blk_start_dev ||
+                                !blk_end_dev || !indptr_dev || !idx_local_dev || !idx_block_dev ||
+                                !weights_dev || !distances_dev || !seg_end_dev)) ||
+        (M > 0 && (!mparent_dev || !mchild_dev || !mdist_dev))) {
+        set_error("fhg_core_graphs: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    if (k < 0 || M < 0) {
+        set_error("fhg_core_graphs: negative size");
+        return FHG_ERR_INVALID;
+    }
+    return core_graphs_layout(P, k, nb_dev, lens_dev, core_dev, blk_start_dev, blk_end_dev, M,
+                              mparent_dev, mchild_dev, mdist_dev, indptr_dev, idx_local_dev,
+                              idx_block_dev, weights_dev, distances_dev, seg_end_dev, nnz_host,
+                              as_stream(stream));
+}
+
 FHG_API int fhg_index_boruvka(fhg_index* index, int32_t min_samples,
                               const float* sample_weights_dev, int32_t weighted_k,
                               double* edges_dev, int32_t* neighbors_dev, float* core_dev,

@@ -25,6 +25,7 @@
 // pos), find every cycle and its largest pos by pointer doubling, drop that
 // edge, emit the others in pos order (a scan over pos slots) and hook them
 // with the lock-free union-find.
+#include <algorithm>
 #include <utility>
 
 #include "fhg_common.cuh"
@@ -191,6 +192,124 @@ __global__ void cg_relabel_kernel(int64_t n, int32_t* __restrict__ comp, int32_t
     comp[p] = uf_find(par, comp[p]);
 }
 
+// ------------------------------------------------------------ layout
+// The core graphs of many clusters as one block CSR (core_graph.py:19
+// knn_mst_union + :47 flatten_to_csr + :70 sort_by_lens): row q is point q of
+// the block layout (clusters one after another, points in index order).  A
+// row holds its kNN children (in neighbour order, each once, those inside the
+// cluster) and then its MST children not already present (in MST order),
+// sorted by weight with ties in that order; weight = float32(max(lens)),
+// distance = float32(max(core)) for kNN children, the MST distance otherwise.
+
+// Row q's MST edges: [lower_bound(q), lower_bound(q + 1)) of the sorted parents.
+__device__ __forceinline__ int64_t lower_bound_u32(const uint32_t* a, int64_t m, uint32_t v) {
+    int64_t lo = 0, hi = m;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Whether the e-th MST child of row q is kept: not a kNN child of the row
+// and not an earlier MST child of it.
+__device__ __forceinline__ bool mst_kept(const int32_t* __restrict__ nbq, int k,
+                                         const int32_t* __restrict__ mchild,
+                                         const int32_t* __restrict__ order, int64_t b, int64_t e) {
+    const int32_t ch = mchild[order[e]];
+    for (int j = 0; j < k; ++j)
+        if (nbq[j] == ch) return false;
+    for (int64_t f = b; f < e; ++f)
+        if (mchild[order[f]] == ch) return false;
+    return true;
+}
+
+__device__ __forceinline__ bool knn_kept(const int32_t* __restrict__ nbq, int j) {
+    const int32_t ch = nbq[j];
+    if (ch < 0) return false;
+    for (int i = 0; i < j; ++i)
+        if (nbq[i] == ch) return false;
+    return true;
+}
+
+__global__ void cgl_count_kernel(int64_t P, int k, const int32_t* __restrict__ nb,
+                                 const uint32_t* __restrict__ mkey, int64_t M,
+                                 const int32_t* __restrict__ mchild,
+                                 const int32_t* __restrict__ order, uint32_t* __restrict__ len) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P) return;
+    const int32_t* nbq = nb + q * k;
+    uint32_t c = 0;
+    for (int j = 0; j < k; ++j) c += knn_kept(nbq, j) ? 1u : 0u;
+    const int64_t b = lower_bound_u32(mkey, M, (uint32_t)q);
+    const int64_t e1 = lower_bound_u32(mkey, M, (uint32_t)(q + 1));
+    for (int64_t e = b; e < e1; ++e) c += mst_kept(nbq, k, mchild, order, b, e) ? 1u : 0u;
+    len[q] = c;
+}
+
+__global__ void cgl_fill_kernel(int64_t P, int k, const int32_t* __restrict__ nb,
+                                const uint32_t* __restrict__ mkey, int64_t M,
+                                const int32_t* __restrict__ mchild,
+                                const double* __restrict__ mdist,
+                                const int32_t* __restrict__ order,
+                                const double* __restrict__ lens, const float* __restrict__ core,
+                                const int32_t* __restrict__ blk_start,
+                                const int32_t* __restrict__ blk_end,
+                                const uint32_t* __restrict__ off, int32_t* __restrict__ indptr,
+                                int32_t* __restrict__ idx_local, int32_t* __restrict__ idx_block,
+                                float* __restrict__ w, float* __restrict__ dist,
+                                int32_t* __restrict__ seg_end) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P) return;
+    const int32_t* nbq = nb + q * k;
+    const int32_t s0 = blk_start[q];
+    const int64_t r0 = off[q];
+    int64_t r = r0;
+    indptr[q] = (int32_t)r0;
+    seg_end[q] = blk_end[q];
+    const double lq = lens[q];
+    const float cq = core[q];
+    for (int j = 0; j < k; ++j) {
+        if (!knn_kept(nbq, j)) continue;
+        const int32_t ch = nbq[j];
+        idx_local[r] = ch;
+        idx_block[r] = s0 + ch;
+        w[r] = (float)fmax(lq, lens[s0 + ch]);
+        dist[r] = fmaxf(cq, core[s0 + ch]);
+        ++r;
+    }
+    const int64_t b = lower_bound_u32(mkey, M, (uint32_t)q);
+    const int64_t e1 = lower_bound_u32(mkey, M, (uint32_t)(q + 1));
+    for (int64_t e = b; e < e1; ++e) {
+        if (!mst_kept(nbq, k, mchild, order, b, e)) continue;
+        const int32_t ch = mchild[order[e]];
+        idx_local[r] = ch;
+        idx_block[r] = s0 + ch;
+        w[r] = (float)fmax(lq, lens[s0 + ch]);
+        dist[r] = (float)mdist[order[e]];
+        ++r;
+    }
+    if (q == P - 1) indptr[P] = (int32_t)r;
+    // stable insertion sort of the row by weight
+    for (int64_t i = r0 + 1; i < r; ++i) {
+        const float wi = w[i], di = dist[i];
+        const int32_t li = idx_local[i], bi = idx_block[i];
+        int64_t j = i;
+        while (j > r0 && w[j - 1] > wi) {
+            w[j] = w[j - 1];
+            dist[j] = dist[j - 1];
+            idx_local[j] = idx_local[j - 1];
+            idx_block[j] = idx_block[j - 1];
+            --j;
+        }
+        w[j] = wi;
+        dist[j] = di;
+        idx_local[j] = li;
+        idx_block[j] = bi;
+    }
+}
+
 }  // namespace
 
 int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
@@ -258,6 +377,43 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
         components -= added;
     }
     *n_edges = m;
+    return FHG_OK;
+}
+
+
+int core_graphs_layout(int64_t P, int k, const int32_t* nb, const double* lens, const float* core,
+                       const int32_t* blk_start, const int32_t* blk_end, int64_t M,
+                       const int32_t* mparent, const int32_t* mchild, const double* mdist,
+                       int32_t* indptr, int32_t* idx_local, int32_t* idx_block, float* w,
+                       float* dist, int32_t* seg_end, int64_t* nnz, cudaStream_t s) {
+    *nnz = 0;
+    if (P <= 0) return FHG_OK;
+    if (P + (int64_t)k * P + M > 0x7fffffffLL) {
+        set_error("core graphs: more than 2^31 - 1 entries");
+        return FHG_ERR_UNSUPPORTED;
+    }
+    Stage stage(s, "core_graph_layout");
+    Workspace ws(s);
+    uint32_t *mkey, *len, *off, *total;
+    int32_t* order;
+    FHG_TRY(ws.alloc(&mkey, (size_t)std::max<int64_t>(M, 1)));
+    FHG_TRY(ws.alloc(&order, (size_t)std::max<int64_t>(M, 1)));
+    FHG_TRY(ws.alloc(&len, (size_t)P));
+    FHG_TRY(ws.alloc(&off, (size_t)P));
+    FHG_TRY(ws.alloc(&total, 1));
+    if (M > 0) {
+        FHG_CUDA(cudaMemcpyAsync(mkey, mparent, sizeof(uint32_t) * M, cudaMemcpyDeviceToDevice, s));
+        FHG_TRY(fill_iota_i32(order, M, s));
+        if (M > 1) FHG_TRY(radix_sort_u32(ws, mkey, order, M, 0, 32));  // stable: MST order kept
+    }
+    LAUNCH(cgl_count_kernel, P, P, k, nb, mkey, M, mchild, order, len);
+    FHG_TRY(scan_exclusive_u32(ws, len, off, P, total));
+    LAUNCH(cgl_fill_kernel, P, P, k, nb, mkey, M, mchild, mdist, order, lens, core, blk_start,
+           blk_end, off, indptr, idx_local, idx_block, w, dist, seg_end);
+    uint32_t h = 0;
+    FHG_CUDA(cudaMemcpyAsync(&h, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    *nnz = h;
     return FHG_OK;
 }
 

@@ -41,6 +41,18 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
                        const float* weights, const int32_t* seg_end, double* edges,
                        int64_t* n_edges, cudaStream_t s);
 
+// Block CSR of many clusters' core graphs (rows = points, cluster after
+// cluster): nb (P x k local ids or -1), lens (P, float64), core (P), the
+// cluster block [blk_start, blk_end) of every row, M MST edges (parent row,
+// child local id, distance).  Outputs indptr (P + 1), per entry the local and
+// the block index of the child, weight and distance (room for P k + M
+// entries), seg_end per row; *nnz entries.
+int core_graphs_layout(int64_t P, int k, const int32_t* nb, const double* lens, const float* core,
+                       const int32_t* blk_start, const int32_t* blk_end, int64_t M,
+                       const int32_t* mparent, const int32_t* mchild, const double* mdist,
+                       int32_t* indptr, int32_t* idx_local, int32_t* idx_block, float* w,
+                       float* dist, int32_t* seg_end, int64_t* nnz, cudaStream_t s);
+
 // The same on kNN lists from the spatial index (index given) or from the
 // brute-force high-dimensional kNN of X (n x d, index NULL) -- the latter is
 // nndescent.py:179 compute_mst_from_knn_graph with an exact kNN graph.

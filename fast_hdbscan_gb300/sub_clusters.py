@@ -7,8 +7,8 @@ noise propagation and non-finite remapping -- follows the reference step for
 step."""
 import numpy as np
 
-from .core_graph import (_clusters_of_forest, core_graph_clusters, core_graph_forests,
-                         core_graph_to_edge_list, knn_mst_union)
+from .core_graph import (_clusters_of_forest, core_graph_clusters, core_graph_to_edge_list,
+                         core_graphs_and_forests)
 from .hdbscan import _BaseEstimator as BaseEstimator
 from .hdbscan import _check_sample_weight, to_numpy_rec_array
 from .hdbscan import _ClusterMixin as ClusterMixin
@@ -76,11 +76,12 @@ def compute_sub_clusters_per_cluster(data, labels, probabilities, neighbors, cor
         mst[:, :2] = local[mst[:, :2].astype(np.int64)]
         core = core_distances[points]
         lens_values = lens_callback(data, probabilities, nb_local, core, mst, points)
-        per.append((points, lens_values, knn_mst_union(nb_local, core, mst, lens_values)))
-    # every cluster's forest in one launch, then each cluster's hierarchy
-    forests = core_graph_forests([g for _, _, g in per])
+        per.append((points, lens_values, (nb_local, core, mst, lens_values)))
+    # every cluster's core graph and forest on the GPU in one pass each, then
+    # each cluster's hierarchy
+    built = core_graphs_and_forests([inp for _, _, inp in per])
     out = []
-    for (points, lens_values, graph), (nc, comp, forest) in zip(per, forests):
+    for (points, lens_values, _), (graph, nc, comp, forest) in zip(per, built):
         out.append((*_clusters_of_forest(
             nc, comp, forest, graph,
             sample_weights=(sample_weights[points] if sample_weights is not None else None),

@@ -367,6 +367,24 @@ int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices_dev,
                        const float* weights_dev, const int32_t* seg_end_dev, int64_t n,
                        double* edges_dev, int64_t* n_edges_host, void* stream);
 
+/* core_graph.py:19 knn_mst_union + :47 flatten_to_csr + :70 sort_by_lens for
+ * many clusters at once, as one block CSR of P rows (the clusters' points one
+ * cluster after another).  nb_dev: P x k in-cluster neighbour ids (-1: none);
+ * lens_dev (float64) and core_dev per row; blk_start/blk_end_dev: the row's
+ * cluster block; M MST edges (parent row, child in-cluster id, distance).
+ * A row holds its kNN children (each once, in neighbour order) then its MST
+ * children not already present (in MST order), stably sorted by weight =
+ * float32(max lens); distance = max core for kNN children, else the MST
+ * distance.  Outputs: indptr_dev (P + 1), children as in-cluster and as block
+ * ids, weights, distances (room for P k + M entries), seg_end_dev (P, the
+ * block end, for fhg_core_graph_mst); *nnz_host entries. */
+int fhg_core_graphs(int64_t P, int32_t k, const int32_t* nb_dev, const double* lens_dev,
+                    const float* core_dev, const int32_t* blk_start_dev,
+                    const int32_t* blk_end_dev, int64_t M, const int32_t* mparent_dev,
+                    const int32_t* mchild_dev, const double* mdist_dev, int32_t* indptr_dev,
+                    int32_t* idx_local_dev, int32_t* idx_block_dev, float* weights_dev,
+                    float* distances_dev, int32_t* seg_end_dev, int64_t* nnz_host, void* stream);
+
 /* fhg_hdbscan_fit, with the large outputs also copied to host memory while
  * the fit runs: each non-NULL *_host destination receives its output from a
  * side stream as soon as the fit has finished writing it (neighbours and

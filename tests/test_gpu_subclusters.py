@@ -126,3 +126,34 @@ def test_batched_forests_equal_single(engine):
         assert nc == nc1
         np.testing.assert_array_equal(forest, forest1)
         np.testing.assert_array_equal(comp, comp1)
+
+
+def test_gpu_core_graph_layout_equals_host(engine):
+    """The block-CSR layout on the GPU (fhg_core_graphs) equals the host
+    knn_mst_union row for row (duplicates, self entries, empty rows, tied
+    weights), and its forests equal the single forests."""
+    from fast_hdbscan_gb300.core_graph import (core_graph_spanning_tree,
+                                               core_graphs_and_forests, knn_mst_union)
+
+    inputs = []
+    for seed, kind, n in [(9, "float", 800), (10, "int", 600), (11, "sparse", 300),
+                          (12, "neg", 1), (13, "int", 2)]:
+        nb, core, mst, lens = _random_core_graph_inputs(seed, max(n, 3), kind)
+        nb, core, lens = nb[:n], core[:n], lens[:n]
+        nb = np.where(nb < n, nb, -1).astype(np.int32)
+        mst = mst[(mst[:, 0] < n) & (mst[:, 1] < n)]
+        if n > 3:
+            nb[-2:] = -1
+            mst = mst[~np.isin(mst[:, 0], [n - 1, n - 2])]
+        inputs.append((nb, core, mst, lens))
+    built = core_graphs_and_forests(inputs)
+    for (nb, core, mst, lens), (g, nc, comp, forest) in zip(inputs, built):
+        h = knn_mst_union(nb, core, mst, lens)
+        np.testing.assert_array_equal(g.indptr, h.indptr)
+        np.testing.assert_array_equal(g.indices, h.indices)
+        np.testing.assert_array_equal(g.weights, h.weights)
+        np.testing.assert_array_equal(g.distances, h.distances)
+        nc1, comp1, forest1, _ = core_graph_spanning_tree(nb, core, mst, lens)
+        assert nc == nc1
+        np.testing.assert_array_equal(forest, forest1)
+        np.testing.assert_array_equal(comp, comp1)
