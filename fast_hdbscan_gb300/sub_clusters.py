@@ -5,8 +5,12 @@ and cluster hierarchy on the GPU), and the per-cluster results are merged
 into one labelling.  The host side -- the per-cluster loop, label merging,
 noise propagation and non-finite remapping -- follows the reference step for
 step."""
+import concurrent.futures
+import threading
+
 import numpy as np
 
+from . import _native
 from .core_graph import (_clusters_of_forest, core_graph_clusters, core_graph_to_edge_list,
                          core_graphs_and_forests)
 from .hdbscan import _BaseEstimator as BaseEstimator
@@ -80,13 +84,29 @@ def compute_sub_clusters_per_cluster(data, labels, probabilities, neighbors, cor
     # every cluster's core graph and forest on the GPU in one pass each, then
     # each cluster's hierarchy
     built = core_graphs_and_forests([inp for _, _, inp in per])
-    out = []
-    for (points, lens_values, _), (graph, nc, comp, forest) in zip(per, built):
-        out.append((*_clusters_of_forest(
-            nc, comp, forest, graph,
-            sample_weights=(sample_weights[points] if sample_weights is not None else None),
-            **kwargs), lens_values, points))
-    return out
+
+    # the clusters' hierarchies are independent: worker threads, each on its
+    # own CUDA stream, overlap their short launches and copies
+    torch = _native._torch()
+    tls = threading.local()
+
+    def hierarchy(i):
+        (points, lens_values, _), (graph, nc, comp, forest) = per[i], built[i]
+        if not hasattr(tls, "stream"):
+            tls.stream = torch.cuda.Stream()
+        with torch.cuda.stream(tls.stream):
+            res = _clusters_of_forest(
+                nc, comp, forest, graph,
+                sample_weights=(sample_weights[points] if sample_weights is not None else None),
+                **kwargs)
+        tls.stream.synchronize()
+        return (*res, lens_values, points)
+
+    torch.cuda.current_stream().synchronize()
+    if len(per) <= 1:
+        return [hierarchy(i) for i in range(len(per))]
+    with concurrent.futures.ThreadPoolExecutor(min(8, len(per))) as ex:
+        return list(ex.map(hierarchy, range(len(per))))
 
 
 def update_labels(cluster_probabilities, sub_labels_list, sub_probabilities_list,
