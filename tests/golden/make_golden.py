@@ -471,6 +471,68 @@ def subcluster_fixtures(only=None):
               f"{time.time() - t0:.1f}s")
 
 
+def _cg_inputs(seed, n, kind):
+    """Random core-graph inputs in in-cluster ids: kNN rows without the point
+    itself or repeats (as a fit's neighbours), a random spanning tree over
+    part of the points, and lens values (float / integer ties / negative)."""
+    rng = np.random.default_rng(seed)
+    k = 5
+    nb = np.argsort(rng.random((n, n)), axis=1)[:, :k + 1]
+    nb = np.array([[c for c in row if c != i][:k] for i, row in enumerate(nb)], np.int32)
+    drop = {"sparse": 0.6, "disc": 0.93}.get(kind, 0.1)
+    nb[rng.random((n, k)) < drop] = -1
+    core = rng.random(n).astype(np.float32)
+    perm = rng.permutation(n)
+    parents = perm[rng.integers(0, np.arange(1, n))]
+    mst = np.c_[parents, perm[1:], rng.random(n - 1)].astype(np.float64)
+    if kind in ("sparse", "disc"):
+        mst = mst[rng.random(n - 1) < (0.3 if kind == "sparse" else 0.05)]
+    lens = {"float": rng.random(n), "int": rng.integers(0, 6, n).astype(np.float64),
+            "neg": rng.normal(0, 1, n), "sparse": rng.random(n),
+            "disc": rng.integers(0, 3, n).astype(np.float64)}[kind]
+    return nb, core, mst, lens
+
+
+CORE_GRAPH_CASES = {"cg_float_400": (1, 400, "float"), "cg_int_400": (2, 400, "int"),
+                    "cg_neg_300": (3, 300, "neg"), "cg_sparse_300": (4, 300, "sparse"),
+                    "cg_disconnected_300": (5, 300, "disc")}
+
+
+def core_graph_fixtures(only=None):
+    """The reference's core graph (core_graph.py:19, :47) and its Boruvka forest
+    (:198) on random inputs, including empty rows and tied weights.
+
+    sort_by_lens (:70) orders each row with np.argsort; under numba that is
+    numba's quicksort, an insertion sort (stable) below 16 elements, while
+    numpy's own argsort (which the shim falls back to) may order ties
+    differently.  Rows here stay below 16 entries and are ordered with a
+    stable argsort, as numba orders them."""
+    from fast_hdbscan.core_graph import CoreGraph, boruvka_mst, flatten_to_csr, knn_mst_union
+
+    def sort_rows_as_numba(graph):
+        w, d, ix = graph.weights.copy(), graph.distances.copy(), graph.indices.copy()
+        for p in range(len(graph.indptr) - 1):
+            a, b = graph.indptr[p], graph.indptr[p + 1]
+            assert b - a < 16, "row too long for numba's insertion-sort range"
+            o = np.argsort(graph.weights[a:b], kind="stable")
+            w[a:b], d[a:b], ix[a:b] = graph.weights[a:b][o], graph.distances[a:b][o], \
+                graph.indices[a:b][o]
+        return CoreGraph(w, d, ix, graph.indptr)
+
+    for name, (seed, n, kind) in CORE_GRAPH_CASES.items():
+        if only and name not in only:
+            continue
+        nb, core, mst, lens = _cg_inputs(seed, n, kind)
+        g = sort_rows_as_numba(flatten_to_csr(knn_mst_union(nb, core, mst, lens)))
+        nc, comp, edges = boruvka_mst(g)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), nb=nb, core=core, mst=mst,
+                            lens=lens, weights=g.weights, distances=g.distances,
+                            indices=g.indices, indptr=g.indptr, n_components=np.int64(nc),
+                            components=np.asarray(comp, np.int64),
+                            edges=np.asarray(edges, np.float64))
+        print(f"{name}: n={n} nnz={g.indptr[-1]} components={nc} edges={len(edges)}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -494,6 +556,7 @@ def main():
         return
     if args.subclusters_only:
         subcluster_fixtures(args.only)
+        core_graph_fixtures(args.only)
         return
     for name, (factory, kwargs) in CASES.items():
         if args.only and name not in args.only:
@@ -506,6 +569,7 @@ def main():
         kruskal_fixtures()
         precomputed_fixtures()
         subcluster_fixtures()
+        core_graph_fixtures()
 
 
 if __name__ == "__main__":

@@ -18,7 +18,7 @@ from oracle import oracle as O
 # fit fixtures; fn_*.npz hold function-level cases, kr_*.npz the kNN-graph
 # Kruskal back-end (algorithm="kruskal")
 FIXTURES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("fn_", "kr_", "pc_", "sc_")))
+                  if not os.path.basename(p).startswith(("fn_", "kr_", "pc_", "sc_", "cg_")))
 KRUSKAL = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "kr_*.npz")))
 # metric="precomputed" on sparse graphs (precomputed.py:410 Boruvka, :479 Kruskal)
 PRECOMPUTED = sorted(os.path.basename(p)[:-4]

@@ -48,3 +48,26 @@ def test_branch_threshold_and_label_merge():
     # three branches in the first cluster stay; one in the second merges to one label
     assert labels.tolist() == [1, 2, 3, 0, 4, 4, 4]
     assert np.allclose(p[4:], 0.8)
+
+
+CG_CASES = ["cg_float_400", "cg_int_400", "cg_neg_300", "cg_sparse_300", "cg_disconnected_300"]
+
+
+@pytest.mark.parametrize("name", CG_CASES)
+def test_core_graph_and_oracle_forest_match_reference(name):
+    """The host core graph and the restated Boruvka (the checker of the GPU
+    forest) against the reference's own graph and forest (core_graph.py:198),
+    including empty rows, integer lens (ties) and a disconnected graph."""
+    from fast_hdbscan_gb300.core_graph import knn_mst_union
+    from oracle import core_graph_boruvka as CB
+
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ours = knn_mst_union(g["nb"], g["core"], g["mst"], g["lens"])
+    np.testing.assert_array_equal(ours.indptr, g["indptr"])
+    np.testing.assert_array_equal(ours.indices, g["indices"])
+    np.testing.assert_array_equal(ours.weights, g["weights"])
+    np.testing.assert_array_equal(ours.distances, g["distances"])
+    nc, comp, edges = CB.boruvka_mst(g["weights"], g["indices"], g["indptr"])
+    assert nc == int(g["n_components"])
+    np.testing.assert_array_equal(edges, g["edges"])
+    np.testing.assert_array_equal(comp, g["components"])

@@ -157,3 +157,21 @@ def test_gpu_core_graph_layout_equals_host(engine):
         assert nc == nc1
         np.testing.assert_array_equal(forest, forest1)
         np.testing.assert_array_equal(comp, comp1)
+
+
+@pytest.mark.parametrize("name", ["cg_float_400", "cg_int_400", "cg_neg_300", "cg_sparse_300",
+                                  "cg_disconnected_300"])
+def test_gpu_forest_matches_reference_fixture(engine, name):
+    """The GPU core graph and forest against the reference's (core_graph.py:198)."""
+    from fast_hdbscan_gb300.core_graph import core_graph_spanning_tree, core_graphs_and_forests
+
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    nc, comp, forest, graph = core_graph_spanning_tree(g["nb"], g["core"], g["mst"], g["lens"])
+    assert nc == int(g["n_components"])
+    np.testing.assert_array_equal(forest, g["edges"])
+    np.testing.assert_array_equal(comp, np.unique(g["components"], return_inverse=True)[1])
+    (g2, nc2, comp2, forest2), = core_graphs_and_forests([(g["nb"], g["core"], g["mst"],
+                                                           g["lens"])])
+    np.testing.assert_array_equal(g2.indices, g["indices"])
+    np.testing.assert_array_equal(g2.weights, g["weights"])
+    np.testing.assert_array_equal(forest2, g["edges"])
