@@ -58,3 +58,11 @@ def test_bf16_forward_close_to_exact():
     y_bf, _ = R.forward(p, feat, bf=True)
     y_ex, _ = R.forward(p, feat, bf=False)
     assert np.max(np.abs(y_bf - y_ex)) < 0.05 * max(1.0, np.max(np.abs(y_ex)))
+
+
+def test_engine_layout_matches_oracle():
+    """The Python model's parameter layout is the oracle's (and the kernels')."""
+    from fast_hdbscan_gb300 import radius
+
+    assert radius.N_PARAMS == R.N_PARAMS and radius.N_TRAINED == R.N_TRAINED
+    assert radius.LAYOUT == R.LAYOUT
