@@ -71,3 +71,37 @@ def test_core_graph_and_oracle_forest_match_reference(name):
     assert nc == int(g["n_components"])
     np.testing.assert_array_equal(edges, g["edges"])
     np.testing.assert_array_equal(comp, g["components"])
+
+
+def test_root_labels_follow_union_by_rank():
+    """A disconnected core graph's component labels: the reference's union-by-
+    rank roots (disjoint_set.py:30) numbered in root order, from the forest's
+    edges in order -- the same roots the restated Boruvka keeps."""
+    from fast_hdbscan_gb300.core_graph import _root_labels
+    from oracle import core_graph_boruvka as CB
+
+    g = np.load(os.path.join(GOLDEN, "cg_disconnected_300.npz"))
+    labels = _root_labels(len(g["indptr"]) - 1, g["edges"])
+    np.testing.assert_array_equal(labels, np.unique(g["components"], return_inverse=True)[1])
+    _, comp, _ = CB.boruvka_mst(g["weights"], g["indices"], g["indptr"])
+    np.testing.assert_array_equal(comp, g["components"])
+
+
+def test_label_propagation_on_a_small_core_graph():
+    """sub_clusters.py:132: noise points take the label with the largest summed
+    inverse weight among labelled neighbours, sweep after sweep; a noise point
+    with no labelled path stays noise."""
+    from fast_hdbscan_gb300.core_graph import CoreGraph
+    from fast_hdbscan_gb300.sub_clusters import propagate_labels_per_cluster
+
+    # 0 - 1 (w 1), 1 - 2 (w 4), 2 - 3 (w 1), 3 - 4 (w 2); 5 isolated
+    rows = [[1], [2], [3], [4], [], []]
+    ws = [[1.0], [4.0], [1.0], [2.0], [], []]
+    indptr = np.cumsum([0] + [len(r) for r in rows]).astype(np.int32)
+    g = CoreGraph(np.array(sum(ws, []), np.float32), np.zeros(4, np.float32),
+                  np.array(sum(rows, []), np.int32), indptr)
+    sub = np.array([0, -1, -1, 1, -1, -1])
+    out = propagate_labels_per_cluster(g, sub.copy())
+    # 1: neighbour 0 (label 0, 1/1) beats 2 (noise); 2: neighbours 1 (0 after the
+    # sweep reaches it, 1/4) and 3 (label 1, 1/1) -> 1; 4: neighbour 3 -> 1
+    assert out.tolist() == [0, 0, 1, 1, 1, -1]
