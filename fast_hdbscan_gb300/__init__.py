@@ -5,7 +5,13 @@
 
 Every stage (spatial index, kNN core distances, Boruvka MST, linkage tree,
 condensed tree, cluster selection, labels) runs as hand-written sm_103a CUDA
-kernels in libfhg.so, called through the C ABI of include/fhg.h.
+kernels in libfhg.so, called through the C ABI of include/fhg.h -- as do the
+reference's other back-ends behind the same API: algorithm="kruskal" with a
+kNN graph, metric="precomputed" sparse graphs, the kNN-graph route for data
+above 30 dimensions (an exact tensor-core kNN), and sub-cluster / branch
+detection (SubClusterDetector, BranchDetector).  batch.fit_many runs many
+independent fits at once; radius.RadiusModel is an optional learned kNN
+search radius that leaves every result unchanged.
 """
 from .branches import BranchDetector, find_branch_sub_clusters  # noqa: F401
 from .hdbscan import HDBSCAN, fast_hdbscan  # noqa: F401
