@@ -18,7 +18,13 @@ the parameters and every intermediate of the fit path:
   labels, probabilities       final outputs
   kd_*                        the reference KD-tree arrays (small cases only)
 
+Other families: ``fn_*`` (function-level cases), ``kr_*`` (algorithm="kruskal"),
+``pc_*`` (metric="precomputed"), ``sc_*`` (BranchDetector / SubClusterDetector on
+the reference's own fits) and ``cg_*`` (the reference's core graph and its
+Boruvka forest, core_graph.py:19/:198).
+
 Run:  python tests/golden/make_golden.py [--only NAME ...]
+      (--kruskal-only / --precomputed-only / --subclusters-only for one family)
 """
 import argparse
 import os
