@@ -105,3 +105,68 @@ def test_label_propagation_on_a_small_core_graph():
     # 1: neighbour 0 (label 0, 1/1) beats 2 (noise); 2: neighbours 1 (0 after the
     # sweep reaches it, 1/4) and 3 (label 1, 1/1) -> 1; 4: neighbour 3 -> 1
     assert out.tolist() == [0, 0, 1, 1, 1, -1]
+
+
+def _cycle_rule_forest(weights, indices, indptr):
+    """The GPU forest's round, restated in Python: candidates by (weight,
+    point) per component, the functional graph of candidates, each cycle's
+    largest-order edge dropped, the rest emitted in order (coregraph.cu)."""
+    n = len(indptr) - 1
+    w, idx = np.asarray(weights, np.float32), np.asarray(indices)
+    comp, ptr = np.arange(n), np.array(indptr[:-1])
+    own = np.array([next((r for r in range(p, n) if indptr[r + 1] > indptr[r]), -1)
+                    for p in range(n)])
+    out, first = [], True
+    while True:
+        if not first:
+            for p in range(n):
+                while ptr[p] < indptr[p + 1] and comp[idx[ptr[p]]] == comp[p]:
+                    ptr[p] += 1
+        first = False
+        best, pos = {}, {}
+        for p in range(n):
+            r = own[p]
+            if r < 0 or ptr[r] >= indptr[r + 1]:
+                continue
+            c, key = comp[p], (w[ptr[r]], p)
+            if c not in best or key < best[c]:
+                best[c] = key
+            pos[c] = min(pos.get(c, n), p)
+        succ = {c: comp[idx[ptr[own[p]]]] for c, (_, p) in best.items()}
+        drop, seen = set(), {}
+        for c in best:
+            path, x = [], c
+            while x in succ and x not in seen:
+                seen[x] = c
+                path.append(x)
+                x = succ[x]
+            if x in succ and seen.get(x) == c:
+                cyc = path[path.index(x):]
+                drop.add(max(cyc, key=lambda v: pos[v]))
+        keep = sorted((c for c in best if c not in drop), key=lambda c: pos[c])
+        if not keep:
+            break
+        par = {}
+
+        def find(x):
+            while par.get(x, x) != x:
+                x = par[x]
+            return x
+
+        for c in keep:
+            p = best[c][1]
+            e = ptr[own[p]]
+            out.append((float(p), float(idx[e]), float(w[e])))
+            a, b = find(c), find(comp[idx[e]])
+            par[max(a, b)] = min(a, b)
+        comp = np.array([find(comp[p]) for p in range(n)])
+    return np.array(out, dtype=np.float64).reshape(-1, 3)
+
+
+@pytest.mark.parametrize("name", CG_CASES)
+def test_cycle_rule_equals_sequential_merge(name):
+    """Dropping each candidate cycle's largest-order edge (the GPU round) gives
+    the reference's sequential union-find merge edge for edge."""
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ours = _cycle_rule_forest(g["weights"], g["indices"], g["indptr"])
+    np.testing.assert_array_equal(ours, g["edges"])
