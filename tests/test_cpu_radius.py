@@ -1,6 +1,6 @@
 """The learned-radius network's CPU restatement (oracle/radius_mlp.py): the
 bfloat16 rounding it emulates and a finite-difference check of its analytic
-gradient, which then judges the GPU backward kernels."""
+gradient, which then checks the GPU backward kernels."""
 import numpy as np
 
 from oracle import radius_mlp as R
