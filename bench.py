@@ -13,8 +13,9 @@ tree, EOM selection, labels and membership strengths).
          back to host inside the timed region.
 
 --impl reference times the CPU restatement of the reference algorithm
-(oracle/, OpenMP over the reference's parallel loops) on all host cores, on
-a bounded sample of the same workload per step.
+(oracle/, OpenMP over the reference's parallel loops) on all host cores, each
+step one fit of the same seeded 10M-point input (about half a minute on 16
+cores); cpu_baseline in the default line is one such fit.
 
 Multi-GPU: one process per GPU, each fitting its own independent dataset
 (the fit does not shard without a per-round exchange): weak scaling,
@@ -67,7 +68,6 @@ OTHER_WORKLOADS = {
                     generator="50 anisotropic Gaussians (covariance A A^T, A_ij ~ N(0, 0.3^2)),"
                               " centres N(0, 4 I)"),
 }
-CPU_SAMPLE_N = 1_000_000
 
 
 def parse_args():
@@ -80,7 +80,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-radius", action="store_true", help="skip the learned-radius arm")
-    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE_N)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="points per CPU fit (default: the workload's own size)")
     ap.add_argument("--workload", default="fit", choices=["fit", "batched", *OTHER_WORKLOADS],
                     help="fit: the metric's 10M x 3-D fit; batched: many independent fits; "
                          "umap2m: the 2M x 5-D fit; kruskal10m: the 10M x 3-D fit on the "
@@ -184,8 +185,9 @@ def tree_nodes(n):
 
 
 def algorithmic_bytes(kernel, n, k, d_pad):
-    """Least HBM bytes one launch of each timed kernel must move (fixed
-    formulas; every other access of the walk is a cache-resident re-read)."""
+    """Least HBM bytes one launch of a timed kernel must move, counted narrowly
+    (every other access of the walk is a cache-resident re-read).  Reported as
+    a second, labelled figure beside the stage-level formulas below."""
     if kernel == "knn_kernel":
         # read every point once (padded coordinates + caller index); write the
         # Morton-order rows (squared distance + position), the caller-order
@@ -197,6 +199,32 @@ def algorithmic_bytes(kernel, n, k, d_pad):
         # (component, least core) word
         return n * (4 + 4 + 8 + 4 + 1) + tree_nodes(n) * 8
     return None
+
+
+def boruvka_round_bytes(n, k, d, components):
+    """Algorithmic HBM bytes of one Boruvka round (fixed formula): per point
+    its k kNN edges (destination i32 + weight f32 + the destination's gathered
+    component i32), its coordinates, core distance, component and packed
+    candidate (4d + 4 + 4 + 8), the relabel read + write (8); per component
+    its packed best edge (8)."""
+    return n * k * 12 + n * (4 * d + 16) + 8 * components + n * 8
+
+
+def knn_stage_bytes(n, k, d):
+    """Algorithmic HBM bytes of the kNN / core-distance stage (fixed formula):
+    read X (4d per point), the spatial sort's write + read of the permuted
+    points and keys ((4d + 8) x 2), the kNN rows written (distance + index, 8
+    per neighbour) and the core distance (4)."""
+    return n * 4 * d + n * (4 * d + 8) * 2 + n * k * 8 + n * 4
+
+
+# The high-dimensional candidate kernel: GEMM depth per point pair and the
+# instruction path (kept beside the algorithmic 2 n^2 d count).
+HD_KERNEL_NOTE = "mma.sync m16n8k16 bf16, two-term split (hi, lo): depth 3 x padded d"
+
+
+def hd_kernel_depth(d):
+    return 3 * (32 if d <= 32 else (64 if d <= 64 else 96))
 
 
 def traffic_per_point(kernel):
@@ -318,7 +346,7 @@ def run_gb300(args):
     # per-stage share and the dominant kernel's roofline
     # kernel records nest inside the stage records: shares are over stages
     nested = ("knn_kernel", "search_kernel", "hd_cand_kernel", "hd_rerank_kernel",
-              "hd_exact_kernel", "highd_knn")
+              "hd_exact_kernel", "highd_knn", "boruvka_components")
     total_stage = sum(v[0] for k, v in stages.items() if k not in nested) or 1.0
     kernel_stages = {k: v for k, v in stages.items()
                      if k in ("knn_kernel", "search_kernel", "hd_cand_kernel")}
@@ -330,14 +358,16 @@ def run_gb300(args):
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
     roofline = None
-    rounds = max(1, stages.get("boruvka_search", [0, 1])[1] // max(args.steps, 1))
+    rounds = stages.get("boruvka_components", [0, 0])[1] // max(args.steps, 1)
     if dom == "hd_cand_kernel":
         # tensor-bound: 2 n^2 K flops per launch, K = 3 x 64 (two-term bf16
         # split) for d = 64; against the measured cuBLAS bf16 burst peak
         tot_ms, cnt = kernel_stages[dom]
         per_launch_ms = tot_ms / cnt
-        kdepth = 3 * (32 if d <= 32 else (64 if d <= 64 else 96))
-        flops = 2.0 * n * n * kdepth
+        # the candidate GEMM's algorithmic count, 2 n^2 d; the kernel's own
+        # depth (padding and a two-term split) is reported beside it
+        flops = 2.0 * n * n * d
+        kdepth = hd_kernel_depth(d)
         achieved = flops / (per_launch_ms / 1e3) / 1e12
         try:
             tpeak, tsrc = float(peaks["bf16_tflops"]), "measured cuBLAS bf16 burst"
@@ -347,25 +377,74 @@ def run_gb300(args):
                     "peak": tpeak, "peak_source": tsrc, "unit": "TFLOP/s",
                     "frac": round(achieved / tpeak, 5), "traffic": None,
                     "algorithmic_flops_per_launch": flops,
+                    "kernel_depth": kdepth,
+                    "issued_tflops": round(2.0 * n * n * kdepth / (per_launch_ms / 1e3) / 1e12,
+                                           2),
                     "launches_per_step": cnt // max(args.steps, 1),
                     "ms_per_launch": round(per_launch_ms, 4),
                     "kernel_share_of_stage_time": round(tot_ms / total_stage, 4),
-                    "note": "mma.sync m16n8k16 bf16 (legacy tensor path)"}
+                    "note": HD_KERNEL_NOTE}
     elif dom:
-        tot_ms, cnt = kernel_stages[dom]
-        per_launch_ms = tot_ms / cnt
-        alg = algorithmic_bytes(dom, n, (max(knn_k, ms) if kruskal else ms) + 1,
-                                4 if d <= 4 else 8)
-        achieved = alg / (per_launch_ms / 1e3) / 1e9
-        # the ncu traffic per point was measured for the Boruvka fit's kNN (k = 16)
-        tpp = None if kruskal else traffic_per_point(dom)
-        traffic = round(tpp * n) if tpp is not None else None
-        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peak,
-                    "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 5),
-                    "traffic": traffic, "algorithmic_bytes_per_launch": alg,
-                    "launches_per_step": cnt // max(args.steps, 1),
-                    "ms_per_launch": round(per_launch_ms, 4),
-                    "kernel_share_of_stage_time": round(tot_ms / total_stage, 4)}
+        kq = (max(knn_k, ms) if kruskal else ms) + 1
+        comps = stages.get("boruvka_components")
+        bor_ms = sum(stages.get(k, [0.0])[0] for k in
+                     ("boruvka_search", "boruvka_merge", "boruvka_nodes")) / args.steps
+        if comps and comps[1] > 0 and bor_ms > 0 and not kruskal:
+            # the Boruvka stage: every round's seed, search, merge and node
+            # passes, against the per-round formula summed over the rounds
+            rounds_f = comps[1] / args.steps
+            total = (rounds_f * boruvka_round_bytes(n, kq, d, 0)
+                     + 8 * comps[0] / args.steps)
+            achieved = total / (bor_ms / 1e3) / 1e9
+            tpp = traffic_per_point("boruvka_stage")
+            s_tot, s_cnt = kernel_stages.get("search_kernel", (0.0, 0))
+            s_alg = algorithmic_bytes("search_kernel", n, kq, 4 if d <= 4 else 8)
+            roofline = {
+                "bound": "hbm", "kernel": "boruvka_round (seed + search + merge + node passes)",
+                "achieved": round(achieved, 2), "peak": peak, "peak_source": peak_src,
+                "unit": "GB/s", "frac": round(achieved / peak, 5),
+                "traffic": round(tpp * n * rounds_f) if tpp is not None else None,
+                "traffic_note": "DRAM bytes of all kernels of the Boruvka rounds, per fit, "
+                                "scaled from an ncu capture on a 4M-point fit",
+                "algorithmic_bytes_per_fit": round(total),
+                "formula": "sum over rounds of n*k*12 + n*(4d+16) + 8*C_r + 8n",
+                "rounds_per_step": round(rounds_f, 2),
+                "components_per_step": round(comps[0] / args.steps),
+                "ms_per_step": round(bor_ms, 4),
+                "ms_per_round": round(bor_ms / max(rounds_f, 1), 4),
+                "stage_share": round(bor_ms * args.steps / total_stage, 4),
+                "search_kernel_narrow": None if not s_cnt else {
+                    "algorithmic_bytes_per_launch": s_alg,
+                    "ms_per_launch": round(s_tot / s_cnt, 4),
+                    "achieved": round(s_alg / (s_tot / s_cnt / 1e3) / 1e9, 2),
+                    "launches_per_step": s_cnt // max(args.steps, 1),
+                    "traffic": (round(traffic_per_point("search_kernel") * n)
+                                if traffic_per_point("search_kernel") else None)},
+            }
+        else:
+            tot_ms, cnt = kernel_stages[dom]
+            per_launch_ms = tot_ms / cnt
+            alg = algorithmic_bytes(dom, n, kq, 4 if d <= 4 else 8)
+            achieved = alg / (per_launch_ms / 1e3) / 1e9
+            # the ncu traffic per point was measured for the Boruvka fit's kNN (k = 16)
+            tpp = None if kruskal else traffic_per_point(dom)
+            traffic = round(tpp * n) if tpp is not None else None
+            roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
+                        "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+                        "frac": round(achieved / peak, 5), "traffic": traffic,
+                        "algorithmic_bytes_per_launch": alg,
+                        "launches_per_step": cnt // max(args.steps, 1),
+                        "ms_per_launch": round(per_launch_ms, 4),
+                        "kernel_share_of_stage_time": round(tot_ms / total_stage, 4)}
+        knn_ms = stages.get("knn", [0.0])[0] / args.steps
+        if knn_ms > 0 and not kruskal:
+            kb = knn_stage_bytes(n, kq, d)
+            roofline["knn_stage"] = {
+                "algorithmic_bytes_per_fit": kb, "ms_per_step": round(knn_ms, 4),
+                "achieved": round(kb / (knn_ms / 1e3) / 1e9, 2),
+                "frac": round(kb / (knn_ms / 1e3) / 1e9 / peak, 5),
+                "formula": "n*4d + n*(4d+8)*2 + n*k*8 + n*4",
+                "note": "issue-bound (list insertion and box tests), not HBM-bound"}
 
     # e2e through the public estimator, pinned host input, outputs to host
     e2e = None
@@ -445,7 +524,7 @@ def run_gb300(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(args.cpu_sample)
+        cpu = cpu_baseline_sample(_cpu_sample_n(args))
 
     if rank == 0:
         line = {
@@ -458,7 +537,8 @@ def run_gb300(args):
                        "l2": "inputs and working set (several GB) larger than the 129 MB L2"},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": int(launches),
             "clocks": clock_info,
-            "stages_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in stages.items()},
+            "stages_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in stages.items()
+                                   if k != "boruvka_components"},
             "stage_share": {k: round(v[0] / total_stage, 4) for k, v in stages.items()
                             if k not in nested},
             "boruvka_rounds": rounds,
@@ -470,10 +550,12 @@ def run_gb300(args):
 
 
 # ---------------------------------------------------------- CPU baseline
-def _oracle_fit_time(n, nthreads):
+def _oracle_fit_time(X, nthreads):
+    """Wall time of one fit of X by the oracle (the C/OpenMP restatement of
+    the reference's path), the reference's tie behaviour (mode 0)."""
     from oracle import oracle as O
 
-    X = make_data(n, WORKLOAD["seed"])
+    n = X.shape[0]
     t0 = time.perf_counter()
     if WORKLOAD.get("metric") == "precomputed":  # hdbscan.py:306 on the kNN graph
         import scipy.sparse
@@ -500,37 +582,60 @@ def _oracle_fit_time(n, nthreads):
     return time.perf_counter() - t0
 
 
+def _cpu_sample_n(args):
+    """Points per CPU fit: the workload's own size unless a workload's
+    brute-force reference path (the kNN-graph route, O(n^2)) needs a sample."""
+    if args.cpu_sample:
+        return args.cpu_sample
+    return WORKLOAD.get("cpu_sample", args.n)
+
+
 def cpu_baseline_sample(n_sample):
     cores = os.cpu_count() or 1
-    t = _oracle_fit_time(n_sample, cores)
+    X = make_data(n_sample, WORKLOAD["seed"])
+    t = _oracle_fit_time(X, cores)
+    whole = n_sample == WORKLOAD["n"]
     return {"value": round(n_sample / t, 1), "unit": "points/s", "cores": cores, "kind": "port",
-            "sample": f"{n_sample} points of the same generator, one fit, {t:.2f} s",
+            "sample": (f"the full workload ({n_sample} points, the same seeded input), one fit, "
+                       f"{t:.2f} s" if whole else
+                       f"{n_sample} points of the same generator, one fit, {t:.2f} s"),
+            "same_config": whole,
             "what": "C/OpenMP restatement of the reference fit path (oracle/), reference "
                     "tie mode; numba is not installed on this machine"}
 
 
 def run_reference(args):
+    """The reference's algorithm (the oracle's restatement, numba being absent
+    on the GPU host) on all host cores.  Each timed step fits the workload's
+    own input (the same seeded points as the GPU arm).  The untimed warm-up
+    steps fit a 1M-point draw of the generator: a compiled CPU path has no JIT
+    to warm, and a full-size warm-up would only double the run time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    n_sample = args.cpu_sample
+    n_fit = _cpu_sample_n(args)
+    X = make_data(n_fit, WORKLOAD["seed"])
+    Xw = make_data(min(n_fit, 1_000_000), WORKLOAD["seed"] + 1)
     for _ in range(args.warmup):
-        _oracle_fit_time(n_sample, cores)
-    times = [_oracle_fit_time(n_sample, cores) for _ in range(args.steps)]
+        _oracle_fit_time(Xw, cores)
+    times = [_oracle_fit_time(X, cores) for _ in range(args.steps)]
     s = sum(times) / len(times)
-    value = n_sample / s
+    value = n_fit / s
+    whole = n_fit == WORKLOAD["n"]
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": "points/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(s * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator of the benchmark workload)",
-        "config": {**{k: v for k, v in WORKLOAD.items() if k != "n"}, "n": n_sample,
-                   "sample_of_n": WORKLOAD["n"]},
+        "config": {**{k: v for k, v in WORKLOAD.items() if k != "n"}, "n": n_fit,
+                   **({} if whole else {"sample_of_n": WORKLOAD["n"]})},
         "cpu_baseline": {"value": round(value, 1), "unit": "points/s", "cores": cores,
-                         "kind": "port",
-                         "sample": f"{n_sample}-point sample of the workload per step"},
+                         "kind": "port", "same_config": whole,
+                         "sample": ("the full workload per step (the GPU arm's seeded input); "
+                                    "warm-up steps on a 1M-point draw" if whole else
+                                    f"{n_fit}-point sample of the workload per step")},
         "e2e": {"value": round(value, 1), "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -629,8 +734,6 @@ def main():
             METRIC += f" (algorithm='kruskal', knn_k={WORKLOAD['knn_k']})"
         elif WORKLOAD.get("algorithm") == "knn_graph":
             METRIC += f" (kNN-graph route, exact tensor-core kNN, knn_k={WORKLOAD['knn_k']})"
-        if args.cpu_sample == CPU_SAMPLE_N and "cpu_sample" in WORKLOAD:
-            args.cpu_sample = WORKLOAD["cpu_sample"]
         args.workload = "fit"
     if args.impl == "reference":
         run_reference(args)

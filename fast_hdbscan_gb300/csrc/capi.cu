@@ -8,6 +8,7 @@
 #include "highd.cuh"
 #include "mst.cuh"
 #include "radius.cuh"
+#include "reftree.cuh"
 #include "trees.cuh"
 
 #include <initializer_list>
@@ -40,7 +41,16 @@ struct StageRec {
 std::atomic<bool> g_prof_on{false};
 std::mutex g_prof_mu;
 std::vector<StageRec> g_prof;
+std::map<std::string, std::pair<double, int64_t>> g_counts;  // name -> (sum, samples)
 }  // namespace
+
+void profile_count(const char* name, double value) {
+    if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    auto& e = g_counts[name];
+    e.first += value;
+    e.second += 1;
+}
 
 Stage::Stage(cudaStream_t s, const char* name) : s_(s), name_(name) {
     if (!g_prof_on.load(std::memory_order_relaxed)) return;
@@ -112,6 +122,14 @@ FHG_API int fhg_release_cached_memory(void) {
     return FHG_OK;
 }
 
+FHG_API int fhg_set_tie_rule(int rule) {
+    if (rule != FHG_TIES_CANONICAL && rule != FHG_TIES_REFERENCE) {
+        set_error("fhg_set_tie_rule: unknown rule %d", rule);
+        return -1;
+    }
+    return set_tie_rule(rule);
+}
+
 FHG_API int fhg_profile_enable(int on) {
     g_prof_on.store(on != 0);
     return FHG_OK;
@@ -119,11 +137,12 @@ FHG_API int fhg_profile_enable(int on) {
 
 FHG_API int fhg_profile_report(char* buf, int64_t cap) {
     std::vector<StageRec> recs;
+    std::map<std::string, std::pair<double, int64_t>> agg;
     {
         std::lock_guard<std::mutex> lk(g_prof_mu);
         recs.swap(g_prof);
+        agg.swap(g_counts);
     }
-    std::map<std::string, std::pair<double, int64_t>> agg;
     int rc = FHG_OK;
     for (auto& r : recs) {
         float ms = 0.0f;
@@ -163,6 +182,28 @@ FHG_API int fhg_index_build(const float* X_dev, int64_t n, int32_t d, void* stre
         return FHG_ERR_INVALID;
     }
     return index_build(X_dev, n, d, as_stream(stream), out);
+}
+
+FHG_API int32_t fhg_reference_kdtree_levels(int64_t n) { return ref_tree_levels(n); }
+
+FHG_API int fhg_reference_kdtree(const float* X_dev, int64_t n, int32_t d, int32_t* idx_array_dev,
+                                 float* node_bounds_dev, void* stream) {
+    if (!X_dev || (!idx_array_dev && !node_bounds_dev)) {
+        set_error("fhg_reference_kdtree: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    fhg_index* ix = nullptr;
+    FHG_TRY(index_build(X_dev, n, d, s, &ix));
+    int rc;
+    {
+        Workspace ws(s);
+        RefTree t;
+        rc = ref_tree_build(ws, *ix, &t);
+        if (rc == FHG_OK) rc = ref_tree_export(t, idx_array_dev, node_bounds_dev, s);
+    }
+    const int rc2 = index_free(ix, s);
+    return rc != FHG_OK ? rc : rc2;
 }
 
 FHG_API int fhg_index_free(fhg_index* index, void* stream) {
@@ -337,6 +378,23 @@ FHG_API int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices
     }
     return core_graph_boruvka(n, indptr_dev, indices_dev, weights_dev, seg_end_dev, edges_dev,
                               n_edges_host, as_stream(stream));
+}
+
+FHG_API int fhg_propagate_labels(int64_t n_clusters, const int32_t* noise_first_dev,
+                                 const int32_t* noise_pt_dev, const int32_t* adj_ptr_dev,
+                                 const int32_t* adj_other_dev, const double* adj_w_dev,
+                                 int32_t* labels_dev, void* stream) {
+    if (n_clusters < 0) {
+        set_error("fhg_propagate_labels: negative cluster count");
+        return FHG_ERR_INVALID;
+    }
+    if (n_clusters > 0 && (!noise_first_dev || !noise_pt_dev || !adj_ptr_dev || !adj_other_dev ||
+                           !adj_w_dev || !labels_dev)) {
+        set_error("fhg_propagate_labels: null pointer");
+        return FHG_ERR_INVALID;
+    }
+    return propagate_labels(n_clusters, noise_first_dev, noise_pt_dev, adj_ptr_dev, adj_other_dev,
+                            adj_w_dev, labels_dev, as_stream(stream));
 }
 
 FHG_API int fhg_core_graphs(int64_t P, int32_t k, const int32_t* nb_dev, const double* lens_dev,

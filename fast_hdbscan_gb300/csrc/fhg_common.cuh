@@ -34,6 +34,10 @@ class Stage {
     cudaEvent_t a_ = nullptr;
 };
 
+// With profiling on, adds `value` to the named counter; fhg_profile_report
+// lists it beside the stages as [sum, samples].
+void profile_count(const char* name, double value);
+
 // A status carried through the host driver code.  Device kernels never trap:
 // bounded loops report through a device status word instead.
 struct Status {
