@@ -598,6 +598,10 @@ int64_t orc_parallel_boruvka(const orc_kdtree* t, int64_t min_samples, int mode,
                              float* core_out, int64_t* n_rounds) {
     int64_t n = t->n;
     int64_t k = weights ? wk : (min_samples > 1 ? min_samples + 1 : 2);
+    /* mode 2: mode 0's rules with a private search bound per point (see
+     * oracle.h); everything else runs as mode 0 */
+    const int private_bound = mode == 2;
+    if (mode == 2) mode = 0;
     float* kd = (float*)malloc(sizeof(float) * (size_t)(n * k));
     int32_t* ki = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n * k));
     orc_tree_query(t, k, mode, nthreads, kd, ki);
@@ -653,8 +657,9 @@ int64_t orc_parallel_boruvka(const orc_kdtree* t, int64_t min_samples, int mode,
 #endif
         for (int64_t i = 0; i < n; ++i) {
             const float* pt = ROW(t, i);
+            float own = INFINITY;
             cq_rec(&ctx, 0, pt, &cd[i], &cix[i], core[i], pc[i], node_lb(t, 0, pt),
-                   &cnnd[pc[i]]);
+                   private_bound ? &own : &cnnd[pc[i]]);
         }
         if (mode)
             for (int64_t i = 0; i < n; ++i)

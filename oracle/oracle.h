@@ -16,7 +16,16 @@
  *          (weight, index), a component's edge by (weight, min idx, max idx).
  *          The result does not depend on the spatial index, and is what the
  *          GPU engine reproduces bit for bit.
- * On tie-free input both modes give the same core distances and the same MST
+ *   mode 2 ("reference, parallel"): mode 0's result, computed with the
+ *          parallel loops running in parallel and deterministically.  In the
+ *          sequential reference a component's edge comes from its
+ *          lowest-index point attaining the component minimum w, and that
+ *          point's search is never cut short by the shared bound (the bound
+ *          only ever holds weights above w when it runs), so its candidate is
+ *          the first point at weight w in its KD-tree traversal.  Mode 2
+ *          therefore searches every point with a private bound and merges as
+ *          mode 0 does; the tests check it against mode 0 run on one thread.
+ * On tie-free input all modes give the same core distances and the same MST
  * weight multiset; they can differ only in which of several equal-weight MST
  * edges is kept.
  */

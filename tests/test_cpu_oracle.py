@@ -130,6 +130,39 @@ def test_oracle_parallel_threads_same_weights():
 
 
 @pytest.mark.parametrize("name", sorted(set(FIXTURES) - QUIRK))
+def test_oracle_parallel_reference_mode_fixtures(name):
+    """Mode 2 (the reference's sequential tie rules evaluated in parallel)
+    reproduces the reference's own fixtures bit for bit, on several threads."""
+    g = _load(name)
+    X = g["X"]
+    if X.shape[0] < 2:
+        pytest.skip("degenerate input handled in Python")
+    w = g["sample_weights"] if "sample_weights" in g.files else None
+    fit = O.fit(X, int(g["min_samples"]), int(g["min_cluster_size"]), mode=2, nthreads=4,
+                sample_weights=w, **_kw(g))
+    np.testing.assert_array_equal(fit.mst, g["mst_raw"])
+    np.testing.assert_array_equal(fit.labels, g["labels"])
+    np.testing.assert_array_equal(fit.probabilities, g["probabilities"])
+
+
+@pytest.mark.parametrize("gen,n,ms", [("varying_density", 60_000, 15),
+                                      ("blobs_2d", 60_000, 10),
+                                      ("umap_like", 30_000, 10),
+                                      ("varying_density", 40_000, 1)])
+def test_oracle_parallel_reference_mode_equals_sequential(gen, n, ms):
+    """Mode 2 on 8 threads equals mode 0 on one thread (the reference's loops
+    run in order) edge for edge, on inputs large enough for many tie choices."""
+    from fast_hdbscan_gb300 import synthetic
+
+    X = getattr(synthetic, gen)(n, seed=11)
+    tree = O.build_kdtree(X)
+    seq = O.parallel_boruvka(tree, ms, mode=0, nthreads=1)
+    par = O.parallel_boruvka(tree, ms, mode=2, nthreads=8)
+    np.testing.assert_array_equal(par[0], seq[0])
+    np.testing.assert_array_equal(par[2], seq[2])
+
+
+@pytest.mark.parametrize("name", sorted(set(FIXTURES) - QUIRK))
 def test_oracle_dbscan_cut_bitexact(name):
     """get_cluster_labelling_at_cut (cluster_trees.py:906) at several cuts of
     every fixture's reference linkage tree."""
