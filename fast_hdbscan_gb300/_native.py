@@ -4,6 +4,7 @@ The library is built in-tree by ``fast_hdbscan_gb300.build`` and loaded from
 ``fast_hdbscan_gb300/_lib/libfhg.so``.  There is no fallback: if the library
 or a CUDA device is missing, every engine call raises.
 """
+import contextlib
 import ctypes
 import os
 
@@ -29,8 +30,11 @@ _D = ctypes.c_double
 SIGNATURES = {
     "fhg_last_error": (ctypes.c_char_p, []),
     "fhg_abi_version": (_INT, []),
+    "fhg_set_tie_rule": (_INT, [_INT]),
     "fhg_release_cached_memory": (_INT, []),
     "fhg_index_build": (_INT, [_P, _I64, _I32, _P, ctypes.POINTER(_P)]),
+    "fhg_reference_kdtree_levels": (_I32, [_I64]),
+    "fhg_reference_kdtree": (_INT, [_P, _I64, _I32, _P, _P, _P]),
     "fhg_index_free": (_INT, [_P, _P]),
     "fhg_index_shape": (_INT, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I32)]),
     "fhg_index_knn": (_INT, [_P, _I32, _P, _P, _P]),
@@ -89,6 +93,7 @@ SIGNATURES = {
                                          _D, _P, _P, _P, _P, _P, _P, _P, _P,
                                          ctypes.POINTER(_I64), _P, _P, _P,
                                          ctypes.POINTER(_I64), _P]),
+    "fhg_propagate_labels": (_INT, [_I64, _P, _P, _P, _P, _P, _P, _P]),
     "fhg_core_graphs": (_INT, [_I64, _I32, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
                                _P, _P, ctypes.POINTER(_I64), _P]),
     "fhg_core_graph_mst": (_INT, [_P, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), _P]),
@@ -222,3 +227,17 @@ class Index:
             self.close()
         except Exception:
             pass
+
+
+@contextlib.contextmanager
+def tie_rule(reference):
+    """Runs the engine calls made inside the block, on this thread, with the
+    reference's Boruvka tie choices (``reference=True``: the ``reproducible``
+    flag) or the canonical total order (the default), then restores the
+    previous rule."""
+    lib = load()
+    old = lib.fhg_set_tie_rule(1 if reference else 0)
+    try:
+        yield
+    finally:
+        lib.fhg_set_tie_rule(old)

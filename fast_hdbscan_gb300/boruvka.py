@@ -22,9 +22,13 @@ def parallel_boruvka(tree, n_threads=None, min_samples=10,
 
     Returns ``(edges float64[n-1, 3], neighbors int32[n, k-1],
     core_distances float32[n])`` like the reference (k = min_samples + 1, at
-    least 2; with sample weights, weighted_knn_k).  ``n_threads`` and
-    ``reproducible`` are accepted for signature compatibility: the GPU result
-    is deterministic in every mode.
+    least 2; with sample weights, weighted_knn_k).  ``n_threads`` is accepted
+    for signature compatibility.  The GPU result is deterministic either way;
+    ``reproducible`` selects whose choices it makes among edges of equal
+    weight: False (default), a total order on point indices; True, the
+    reference's own -- its sequential rule and its KD-tree's traversal order
+    (fhg_set_tie_rule) -- so that the tree equals the reference's edge for
+    edge on data without tied distances.
     """
     torch = _native._torch()
     sample_weights = np.asarray(sample_weights, dtype=np.float32)
@@ -39,9 +43,10 @@ def parallel_boruvka(tree, n_threads=None, min_samples=10,
     d_w = torch.from_numpy(np.ascontiguousarray(sample_weights)).cuda() if weighted else None
     rounds = ctypes.c_int32(0)
     lib = _native.load()
-    _native.check(lib.fhg_index_boruvka(tree.index.handle, ms, _native.vptr(d_w), wk,
-                                        _native.dptr(edges), _native.vptr(nbrs),
-                                        _native.dptr(core), ctypes.byref(rounds),
-                                        _native.stream_ptr()))
+    with _native.tie_rule(bool(reproducible)):
+        _native.check(lib.fhg_index_boruvka(tree.index.handle, ms, _native.vptr(d_w), wk,
+                                            _native.dptr(edges), _native.vptr(nbrs),
+                                            _native.dptr(core), ctypes.byref(rounds),
+                                            _native.stream_ptr()))
     parallel_boruvka.last_rounds = rounds.value
     return edges.cpu().numpy(), nbrs.cpu().numpy(), core.cpu().numpy()

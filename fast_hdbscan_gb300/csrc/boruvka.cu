@@ -28,6 +28,7 @@
 #include "mst.cuh"
 #include "radius.cuh"
 #include "primitives.cuh"
+#include "reftree.cuh"
 #include "uf.cuh"
 
 #include <memory>
@@ -294,7 +295,8 @@ __global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
                             const float* __restrict__ knn_d, const float* __restrict__ core2,
                             const int32_t* __restrict__ comp, const int32_t* __restrict__ orig,
                             unsigned long long* keyA, float* __restrict__ cand_w,
-                            int32_t* __restrict__ cand_q, int8_t* __restrict__ exhausted) {
+                            int32_t* __restrict__ cand_q, int8_t* __restrict__ exhausted,
+                            int ref_ties) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int32_t c = comp[p];
@@ -335,7 +337,7 @@ __global__ void seed_kernel(int64_t n, int k, const int32_t* __restrict__ knn_s,
     cand_w[p] = bw;
     cand_q[p] = bq;
     if (bq >= 0) {
-        unsigned long long key = pack_key(bw, min(orig[p], bo));
+        unsigned long long key = pack_key(bw, ref_ties ? orig[p] : min(orig[p], bo));
         if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
     }
 }
@@ -359,7 +361,7 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     const float* __restrict__ core2, const int32_t* __restrict__ comp,
     const int2* __restrict__ nc, unsigned long long* keyA, float* __restrict__ cand_w,
     int32_t* __restrict__ cand_q, int lvl_lo, int lvl_hi, const int32_t* __restrict__ plist,
-    int64_t plen) {
+    int64_t plen, int ref_ties) {
     __shared__ int32_t s_stack[kSW][kStack];
     __shared__ float4 s_xyz[kSW][32 * (SP / 4)];
     __shared__ int2 s_cc[kSW][32];      // (component, core bits)
@@ -543,7 +545,7 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
     if (!valid || bq == seed_q) return;
     cand_w[p] = bw;
     cand_q[p] = bq;
-    unsigned long long key = pack_key(bw, min(ix.orig[p], bo));
+    unsigned long long key = pack_key(bw, ref_ties ? ix.orig[p] : min(ix.orig[p], bo));
     if (key < *(volatile unsigned long long*)&keyA[c]) atomicMin(&keyA[c], key);
 }
 
@@ -668,6 +670,174 @@ __global__ void merge_cmin_kernel(const int32_t* __restrict__ reps, int64_t nrep
     if (r != c) atomicMin(&cmin[r], cmin[c]);
 }
 
+// ------------------------------------------- reference tie mode, per round
+// The reference's choice of a component's edge (boruvka.py:34-60 over the
+// candidates of boruvka.py:290-331, its loops run in order): the point of
+// lowest caller index among those attaining the component's least weight w,
+// and that point's first candidate at weight w in its KD-tree walk.  (The
+// shared bound never cuts that point's search short: when it runs, the bound
+// only holds weights above w.)  With the component keys packed as (weight,
+// caller index of the choosing point), the key's low word is that point.
+__global__ void ref_winner_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                  const unsigned long long* __restrict__ keyA,
+                                  const int32_t* __restrict__ rank, int32_t* __restrict__ winner) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    const int32_t c = reps[i];
+    const unsigned long long key = keyA[c];
+    winner[c] = key == ~0ull ? -1 : rank[(uint32_t)(key & 0xffffffffu)];
+}
+
+// One warp per component: every point of another component at exactly the
+// winner's weight w (max(rdist, core, core) == w, the search's expression)
+// is found by a walk of the bucket tree limited to nodes that can hold one;
+// the reference's walk meets them in its own tree's depth-first order, and
+// the first of them in that order (ref_before) is the edge's far end.
+template <int DIM, int SP>
+__global__ void __launch_bounds__(kSW * 32) tie_walk_kernel(
+    IndexView ix, RefTreeView rt, const int32_t* __restrict__ reps, int64_t nrep,
+    const int32_t* __restrict__ comp, const float* __restrict__ core2,
+    const int2* __restrict__ nc, const int32_t* __restrict__ winner,
+    const float* __restrict__ cand_w, int32_t* __restrict__ cand_q, int32_t* __restrict__ tgt,
+    int* __restrict__ missing) {
+    __shared__ int32_t s_stack[kSW][kStack];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t i = (int64_t)blockIdx.x * kSW + warp;
+    if (i >= nrep) return;
+    const int32_t c = reps[i];
+    const int32_t p = winner[c];
+    if (p < 0) {
+        if (lane == 0) {
+            tgt[c] = -1;
+            atomicOr(missing, 1);
+        }
+        return;
+    }
+    const float w = cand_w[p], cp = core2[p];
+    float q[DIM];
+    {
+        float t[SP];
+        load_pt<SP>(ix.pts, p, t);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) q[j] = t[j];
+    }
+    int32_t best = -1;
+    int64_t best_pos = -1;
+    int32_t* st = s_stack[warp];
+    const int64_t first_leaf = ix.slots - 1;
+    auto wanted = [&](int64_t node) {
+        const int2 ncn = nc[node];
+        if (ncn.x == c || ncn.x == kEmpty || __int_as_float(ncn.y) > w) return false;
+        float b[2 * SP];
+        load_box<SP>(ix.box, node, b);
+        return box_lb_n<DIM, SP>(b, q) <= w;
+    };
+    int sp = 0;
+    if (wanted(0)) {
+        if (lane == 0) st[0] = 0;
+        sp = 1;
+    }
+    __syncwarp();
+    while (sp > 0) {
+        --sp;
+        const int32_t node = st[sp];
+        __syncwarp();
+        if (node >= first_leaf) {
+            const int64_t leaf = node - first_leaf;
+            const int64_t qp = leaf * kLeaf + lane;
+            int32_t my = -1;
+            int64_t mypos = -1;
+            if (leaf < ix.nleaves && qp < ix.n && comp[qp] != c) {
+                const float ck = core2[qp];
+                if (!(ck > w)) {
+                    float x[SP];
+                    load_pt<SP>(ix.pts, qp, x);
+                    const float wt = fmaxf(fmaxf(rdist_rn<DIM>(q, x), cp), ck);
+                    if (wt == w) {
+                        my = (int32_t)qp;
+                        mypos = rt.pos[ix.orig[qp]];
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const int32_t other = __shfl_xor_sync(kFull, my, o);
+                const int64_t opos = __shfl_xor_sync(kFull, mypos, o);
+                if (other >= 0 && (my < 0 || ref_before(rt, q, opos, mypos))) {
+                    my = other;
+                    mypos = opos;
+                }
+            }
+            if (my >= 0 && (best < 0 || ref_before(rt, q, mypos, best_pos))) {
+                best = my;
+                best_pos = mypos;
+            }
+            continue;
+        }
+        const int32_t l = 2 * node + 1, r = l + 1;
+        const bool wl = wanted(l), wr = wanted(r);
+        if (lane == 0) {
+            int t = sp;
+            if (wl) st[t++] = l;
+            if (wr) st[t] = r;
+        }
+        sp += (wl ? 1 : 0) + (wr ? 1 : 0);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (best < 0) {
+            tgt[c] = -1;
+            atomicOr(missing, 2);
+        } else {
+            cand_q[p] = best;
+            tgt[c] = comp[best];
+        }
+    }
+}
+
+// The reference adds the components' edges in its dict order (each
+// component's lowest caller index, cmin) and skips an edge whose ends are
+// already joined.  The edges form a functional graph on components; an edge
+// is skipped exactly when it closes its part's cycle, i.e. it is the cycle's
+// edge of largest cmin.  Pointer doubling finds every cycle's largest cmin.
+__global__ void crep_init_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                 const int32_t* __restrict__ tgt, const int32_t* __restrict__ cmin,
+                                 int32_t* __restrict__ nxt, int32_t* __restrict__ mx) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    const int32_t c = reps[i];
+    nxt[c] = tgt[c] >= 0 ? tgt[c] : c;
+    mx[c] = cmin[c];
+}
+__global__ void crep_step_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                 const int32_t* __restrict__ nxt, const int32_t* __restrict__ mx,
+                                 int32_t* __restrict__ nxt2, int32_t* __restrict__ mx2,
+                                 int* __restrict__ changed) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    const int32_t c = reps[i], x = nxt[c];
+    nxt2[c] = nxt[x];
+    const int32_t a = mx[c], b = mx[x];
+    mx2[c] = max(a, b);
+    if (changed && b > a) *changed = 1;
+}
+__global__ void crep_drop_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                 const int32_t* __restrict__ nxt, const int32_t* __restrict__ mx,
+                                 const int32_t* __restrict__ cmin, int32_t* __restrict__ tgt) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    const int32_t c = reps[i];
+    if (tgt[c] >= 0 && mx[nxt[c]] == cmin[c]) tgt[c] = -1;
+}
+__global__ void ref_emit_flags_kernel(const int32_t* __restrict__ reps, int64_t nrep,
+                                      const int32_t* __restrict__ tgt,
+                                      const int32_t* __restrict__ cmin, uint32_t* __restrict__ flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrep) return;
+    const int32_t c = reps[i];
+    if (tgt[c] >= 0) flag[cmin[c]] = 1u;
+}
+
 __global__ void finalize_edges_kernel(int64_t m, const int32_t* __restrict__ src,
                                       const int32_t* __restrict__ dst,
                                       const float* __restrict__ w2, double* __restrict__ edges) {
@@ -682,7 +852,7 @@ template <int DIM>
 int launch_search(const fhg_index& ix, const int8_t* knn_open,
                   const float* core2, const int32_t* comp, const int2* nc,
                   unsigned long long* keyA, float* cand_w, int32_t* cand_q, bool* try_sparse,
-                  cudaStream_t s) {
+                  int ref_ties, cudaStream_t s) {
     constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);  // as in the kNN kernel
     const int64_t n = ix.n;
     // When few points search (early rounds: most points' best edge is settled
@@ -716,7 +886,8 @@ int launch_search(const fhg_index& ix, const int8_t* knn_open,
             Stage stage(s, "search_kernel");
             ::fhg::note_launch();
             search_kernel<DIM, SP><<<grid_for((ns + 31) / 32, kSW), kSW * 32, 0, s>>>(
-                view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, 0, 64, list, ns);
+                view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, 0, 64, list, ns,
+                ref_ties);
             FHG_CUDA(cudaGetLastError());
             return FHG_OK;
         }
@@ -730,37 +901,74 @@ int launch_search(const fhg_index& ix, const int8_t* knn_open,
         ::fhg::note_launch();
         search_kernel<DIM, SP><<<grid_for(ix.nleaves, kSW), kSW * 32, 0, s>>>(
             view_of(ix), knn_open, core2, comp, nc, keyA, cand_w, cand_q, sp[0], sp[1],
-            nullptr, 0);
+            nullptr, 0, ref_ties);
         FHG_CUDA(cudaGetLastError());
     }
     return FHG_OK;
+}
+
+template <int DIM>
+int launch_tie_walk(const fhg_index& ix, const RefTree& rt, const int32_t* reps, int64_t nrep,
+                    const int32_t* comp, const float* core2, const int2* nc,
+                    const int32_t* winner, const float* cand_w, int32_t* cand_q, int32_t* tgt,
+                    int* missing, cudaStream_t s) {
+    constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);
+    if (nrep <= 0) return FHG_OK;
+    Stage stage(s, "tie_walk_kernel");
+    ::fhg::note_launch();
+    tie_walk_kernel<DIM, SP><<<grid_for(nrep, kSW), kSW * 32, 0, s>>>(
+        view_of(ix), view_of(rt), reps, nrep, comp, core2, nc, winner, cand_w, cand_q, tgt,
+        missing);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
+int tie_walk(const fhg_index& ix, const RefTree& rt, const int32_t* reps, int64_t nrep,
+             const int32_t* comp, const float* core2, const int2* nc, const int32_t* winner,
+             const float* cand_w, int32_t* cand_q, int32_t* tgt, int* missing, cudaStream_t s) {
+#define FHG_TW(D) launch_tie_walk<D>(ix, rt, reps, nrep, comp, core2, nc, winner, cand_w, cand_q, \
+                                     tgt, missing, s)
+    switch (ix.d) {
+        case 1: return FHG_TW(1);
+        case 2: return FHG_TW(2);
+        case 3: return FHG_TW(3);
+        case 4: return FHG_TW(4);
+        case 5: return FHG_TW(5);
+        case 6: return FHG_TW(6);
+        case 7: return FHG_TW(7);
+        case 8: return FHG_TW(8);
+        default:
+            if (ix.d <= 16) return FHG_TW(16);
+            return FHG_TW(32);
+    }
+#undef FHG_TW
 }
 
 int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* knn_d,
                  const int8_t* knn_open, int8_t* exhausted, const float* core2,
                  const int32_t* comp,
                  const int2* nc, unsigned long long* keyA, float* cand_w, int32_t* cand_q,
-                 bool* try_sparse, cudaStream_t s) {
+                 bool* try_sparse, int ref_ties, cudaStream_t s) {
     const int64_t n = ix.n;
     if (n > 0) {
         ::fhg::note_launch();
         seed_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, k, knn_s, knn_d, core2, comp, ix.orig,
-                                                       keyA, cand_w, cand_q, exhausted);
+                                                       keyA, cand_w, cand_q, exhausted, ref_ties);
         FHG_CUDA(cudaGetLastError());
     }
     switch (ix.d) {
-        case 1: return launch_search<1>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 2: return launch_search<2>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 3: return launch_search<3>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 4: return launch_search<4>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 5: return launch_search<5>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 6: return launch_search<6>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 7: return launch_search<7>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-        case 8: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+        case 1: return launch_search<1>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 2: return launch_search<2>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 3: return launch_search<3>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 4: return launch_search<4>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 5: return launch_search<5>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 6: return launch_search<6>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 7: return launch_search<7>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+        case 8: return launch_search<8>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
         default:
             if (ix.d <= 16)
-                return launch_search<16>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
-            return launch_search<32>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, s);
+                return launch_search<16>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
+            return launch_search<32>(ix, knn_open, core2, comp, nc, keyA, cand_w, cand_q, try_sparse, ref_ties, s);
     }
 }
 
@@ -775,6 +983,17 @@ int search_round(const fhg_index& ix, int k, const int32_t* knn_s, const float* 
 
 }  // namespace
 
+// The tie rule of the calling host thread (fhg_set_tie_rule).
+namespace {
+thread_local int t_tie_rule = FHG_TIES_CANONICAL;
+}
+int tie_rule() { return t_tie_rule; }
+int set_tie_rule(int rule) {
+    const int old = t_tie_rule;
+    t_tie_rule = rule;
+    return old;
+}
+
 int finalize_edges(const MstResult& r, double* edges, cudaStream_t s) {
     LAUNCH(finalize_edges_kernel, r.m, r.m, r.src, r.dst, r.w2, edges);
     return FHG_OK;
@@ -786,6 +1005,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     cudaStream_t s = ws.stream();
     const int64_t n = ix.n;
     const bool weighted = weights != nullptr && n > 1;
+    const int ref_ties = tie_rule() == FHG_TIES_REFERENCE ? 1 : 0;
     // the reference's k (boruvka.py:561-585)
     const int kq = weighted ? weighted_k : (min_samples > 1 ? min_samples + 1 : 2);
     const int k = (int)(kq < n ? kq : n);  // neighbours that exist
@@ -925,6 +1145,18 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&kpos, (size_t)n));
     FHG_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t) * n, s));
 
+    // the reference tie mode breaks ties in the order of the reference's own
+    // KD-tree, built here exactly; its pointer-doubling buffers
+    RefTree rt;
+    int32_t *cy_nxt = nullptr, *cy_mx = nullptr, *cy_nxt2 = nullptr, *cy_mx2 = nullptr;
+    if (ref_ties && ncomp > 1) {
+        FHG_TRY(ref_tree_build(ws, ix, &rt));
+        FHG_TRY(ws.alloc(&cy_nxt, (size_t)n));
+        FHG_TRY(ws.alloc(&cy_mx, (size_t)n));
+        FHG_TRY(ws.alloc(&cy_nxt2, (size_t)n));
+        FHG_TRY(ws.alloc(&cy_mx2, (size_t)n));
+    }
+
     int rounds = 0;
     bool try_sparse = true;  // until a round's global pass is dense
     while (ncomp > 1) {
@@ -933,6 +1165,7 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
                       (long long)ncomp);
             return FHG_ERR_NO_CONVERGENCE;
         }
+        profile_count("boruvka_components", (double)ncomp);  // C_r of the round
         {  // node_comp (boruvka.py:98-124), bottom-up
             Stage stage(s, "boruvka_nodes");
             LAUNCH(node_comp_leaf_kernel, ix.slots * 32, comp, core2, n, ix.nleaves, ix.slots, nc);
@@ -943,14 +1176,39 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         {
             Stage stage(s, "boruvka_search");
             FHG_TRY(search_round(ix, k, knn_s, knn_d, knn_open, exhausted, core2, comp, nc, keyA,
-                                 cand_w, cand_q, &try_sparse, s));
+                                 cand_w, cand_q, &try_sparse, ref_ties, s));
         }
         Stage merge_stage(s, "boruvka_merge");
-        LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);
-        LAUNCH(stage_c_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB, winner);
         FHG_CUDA(cudaMemsetAsync(iflag + 1, 0, sizeof(int), s));
-        LAUNCH(select_kernel, ncomp, reps, ncomp, winner, cand_q, comp, tgt, iflag + 1);
-        LAUNCH(emit_flags_kernel, ncomp, reps, ncomp, tgt, cmin, flag);
+        if (ref_ties) {
+            LAUNCH(ref_winner_kernel, ncomp, reps, ncomp, keyA, ix.rank, winner);
+            FHG_TRY(tie_walk(ix, rt, reps, ncomp, comp, core2, nc, winner, cand_w, cand_q, tgt,
+                             iflag + 1, s));
+            LAUNCH(crep_init_kernel, ncomp, reps, ncomp, tgt, cmin, cy_nxt, cy_mx);
+            const int R = bits_for(ncomp) + 1;
+            for (int r = 0; r < R; ++r) {
+                const bool check = (r & 3) == 3 && r + 1 < R;
+                if (check) FHG_CUDA(cudaMemsetAsync(iflag, 0, sizeof(int), s));
+                LAUNCH(crep_step_kernel, ncomp, reps, ncomp, cy_nxt, cy_mx, cy_nxt2, cy_mx2,
+                       check ? iflag : nullptr);
+                int32_t* t1 = cy_nxt; cy_nxt = cy_nxt2; cy_nxt2 = t1;
+                t1 = cy_mx; cy_mx = cy_mx2; cy_mx2 = t1;
+                if (check) {
+                    int h_changed = 1;
+                    FHG_CUDA(cudaMemcpyAsync(&h_changed, iflag, sizeof(int),
+                                             cudaMemcpyDeviceToHost, s));
+                    FHG_CUDA(cudaStreamSynchronize(s));
+                    if (!h_changed) break;
+                }
+            }
+            LAUNCH(crep_drop_kernel, ncomp, reps, ncomp, cy_nxt, cy_mx, cmin, tgt);
+            LAUNCH(ref_emit_flags_kernel, ncomp, reps, ncomp, tgt, cmin, flag);
+        } else {
+            LAUNCH(stage_b_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB);
+            LAUNCH(stage_c_kernel, n, n, comp, ix.orig, cand_w, cand_q, keyA, keyB, winner);
+            LAUNCH(select_kernel, ncomp, reps, ncomp, winner, cand_q, comp, tgt, iflag + 1);
+            LAUNCH(emit_flags_kernel, ncomp, reps, ncomp, tgt, cmin, flag);
+        }
         Workspace tmp(s);  // per-round scan scratch, released at the end of the round
         FHG_TRY(scan_exclusive_u32(tmp, flag, pos, n, cnt));
         LAUNCH(emit_write_kernel, ncomp, reps, ncomp, tgt, cmin, flag, pos, winner, cand_q, cand_w,

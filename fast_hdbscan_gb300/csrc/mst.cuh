@@ -41,6 +41,12 @@ int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
                        const float* weights, const int32_t* seg_end, double* edges,
                        int64_t* n_edges, cudaStream_t s);
 
+// Label propagation to noise points within clusters (sub_clusters.py:132),
+// every cluster in one launch; see fhg_propagate_labels in fhg.h.
+int propagate_labels(int64_t nclusters, const int32_t* noise_first, const int32_t* noise_pt,
+                     const int32_t* adj_ptr, const int32_t* adj_other, const double* adj_w,
+                     int32_t* labels, cudaStream_t s);
+
 // Block CSR of many clusters' core graphs (rows = points, cluster after
 // cluster): nb (P x k local ids or -1), lens (P, float64), core (P), the
 // cluster block [blk_start, blk_end) of every row, M MST edges (parent row,
@@ -80,6 +86,12 @@ int sorted_forest_edges(Workspace& ws, int64_t n, int64_t m, int kq, const int32
 int precomputed_mst(const int32_t* rows, const int32_t* cols, const double* data, int64_t nnz,
                     int64_t n, int min_samples, double* edges, int32_t* neighbors, double* core,
                     int64_t* n_components, cudaStream_t s);
+
+// The Boruvka tie rule of the calling host thread: FHG_TIES_CANONICAL (a
+// total order on indices) or FHG_TIES_REFERENCE (the reference's own choices,
+// from its KD-tree's traversal order).  set_tie_rule returns the old rule.
+int tie_rule();
+int set_tie_rule(int rule);
 
 int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* out,
                 float* core_o, int32_t* nbr_o, const float* weights = nullptr,

@@ -1,0 +1,468 @@
+// The reference's KD-tree, built exactly, on the GPU.
+//
+// The reference builds a median-split KD-tree (numba_kdtree.py:410-521):
+// node ranges halve an index array, each internal node splits on the axis of
+// largest spread (:129-158) by an introselect of its range around the
+// median (:372-413: median-of-three pivot :282, a Hoare partition :316,
+// insertion sort at 16 elements or fewer :186, heapsort after 2 log2(size)
+// partitions :247), and leaves keep the order those partitions leave behind.
+// The Boruvka search visits points in that tree's depth-first order, so
+// among candidates of equal weight the reference keeps the one this order
+// meets first.  The engine's own spatial index cannot reproduce that order;
+// this tree can, and the reference tie mode uses it as the tie-breaker.
+//
+// Every step of the build is reproduced, not just its result:
+//   * compare = (coordinate, index) lexicographic (:164-183), a total order;
+//     it is packed as one 64-bit key (order-preserving float bits << 32 |
+//     index), so one unsigned comparison decides;
+//   * a Hoare partition swaps the k-th element above the pivot counted from
+//     the left with the k-th element below it counted from the right, as long
+//     as the first lies left of the second, and puts the pivot at
+//     left + (elements below it).  That is a prefix count and a pairing, so a
+//     thread block runs each partition in parallel with the same result;
+//   * insertion sort and heapsort both leave their range in ascending order,
+//     which under a total order is unique: a block sorts the range instead.
+// One thread block per node of a level runs that node's whole introselect;
+// the levels run one after another.
+#include <cmath>
+
+#include "index.cuh"
+#include "primitives.cuh"
+#include "reftree.cuh"
+
+namespace fhg {
+namespace {
+
+constexpr int kSelThreads = 512;
+constexpr int kSelV = 8;                          // consecutive keys per thread and tile
+constexpr int kSelTile = kSelThreads * kSelV;     // keys per scan tile
+constexpr int kBlockSortMax = 4096;               // ranges a block sorts in shared memory
+
+#define LAUNCH(kernel, count, ...)                                                   \
+    do {                                                                             \
+        if ((count) > 0) {                                                           \
+            ::fhg::note_launch();                                                    \
+            kernel<<<grid_for((count), 256), 256, 0, s>>>(__VA_ARGS__);              \
+            FHG_CUDA(cudaGetLastError());                                            \
+        }                                                                            \
+    } while (0)
+
+// Order-preserving bits of a float (-0 and +0 compare equal, as in the
+// reference's `<` / `>` tests).
+__device__ __forceinline__ uint32_t ordered_bits(float f) {
+    uint32_t u = __float_as_uint(f);
+    if (u == 0x80000000u) u = 0u;
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void init_root_kernel(int64_t n, int32_t* __restrict__ idx, int32_t* __restrict__ nodeof,
+                                 int64_t* __restrict__ rs, int64_t* __restrict__ re) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) {
+        idx[p] = (int32_t)p;
+        nodeof[p] = 0;
+    }
+    if (p == 0) {
+        rs[0] = 0;
+        re[0] = n;
+    }
+}
+
+// Ranges of the next level: the left child takes the first half (rounded
+// down) of its parent's range (numba_kdtree.py:486-509).
+__global__ void child_ranges_kernel(int64_t first, int64_t count, int64_t* rs, int64_t* re) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t v = first + t;
+    const int64_t s = rs[v], e = re[v], mid = s + (e - s) / 2;
+    rs[2 * v + 1] = s;
+    re[2 * v + 1] = mid;
+    rs[2 * v + 2] = mid;
+    re[2 * v + 2] = e;
+}
+
+__global__ void box_init_kernel(int64_t first, int64_t count, int d, uint32_t* __restrict__ lo,
+                                uint32_t* __restrict__ hi) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count * d) return;
+    const int64_t v = first + t / d;
+    const int j = (int)(t % d);
+    lo[v * d + j] = 0xff800000u;  // ordered bits of +inf
+    hi[v * d + j] = 0x007fffffu;  // ordered bits of -inf
+}
+
+// Per node of the level: the bounding box of its points (_init_node,
+// numba_kdtree.py:67).  Positions of one node are contiguous; a warp whose 32
+// positions share one node reduces first, so a large node takes one atomic
+// per warp and dimension.
+__global__ void box_level_kernel(int64_t n, int d, int pad, const int32_t* __restrict__ idx,
+                                 const int32_t* __restrict__ nodeof,
+                                 const int32_t* __restrict__ rank, const float* __restrict__ pts,
+                                 uint32_t* lo, uint32_t* hi) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool valid = p < n;
+    const int32_t v = valid ? nodeof[p] : -1;
+    const int64_t row = valid ? (int64_t)rank[idx[p]] * pad : 0;
+    const int32_t v0 = __shfl_sync(kFull, v, 0);
+    const bool uniform = __all_sync(kFull, v == v0);
+    for (int j = 0; j < d; ++j) {
+        uint32_t a = valid ? ordered_bits(pts[row + j]) : 0xffffffffu;
+        uint32_t b = valid ? ordered_bits(pts[row + j]) : 0u;
+        if (uniform) {
+            a = __reduce_min_sync(kFull, a);
+            b = __reduce_max_sync(kFull, b);
+            if (lane == 0 && v0 >= 0) {
+                atomicMin(&lo[(int64_t)v0 * d + j], a);
+                atomicMax(&hi[(int64_t)v0 * d + j], b);
+            }
+        } else if (valid) {
+            atomicMin(&lo[(int64_t)v * d + j], a);
+            atomicMax(&hi[(int64_t)v * d + j], b);
+        }
+    }
+}
+
+// The split axis of every internal node of the level: the first dimension
+// of largest spread hi - lo, 0 when every spread is 0 (_find_node_split_dim,
+// numba_kdtree.py:129: `spread > max_spread`, max_spread starting at 0).
+// Also writes the node's box as float32 (lower then upper corner).
+__global__ void axis_level_kernel(int64_t first, int64_t count, int d,
+                                  const uint32_t* __restrict__ lo, const uint32_t* __restrict__ hi,
+                                  float* __restrict__ box, int32_t* __restrict__ axis) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t v = first + t;
+    float best = 0.0f;
+    int32_t a = 0;
+    for (int j = 0; j < d; ++j) {
+        const float l = from_ordered(lo[v * d + j]), h = from_ordered(hi[v * d + j]);
+        box[v * 2 * d + j] = l;
+        box[v * 2 * d + d + j] = h;
+        const float spread = __fsub_rn(h, l);
+        if (spread > best) {
+            best = spread;
+            a = j;
+        }
+    }
+    if (axis) axis[t] = a;
+}
+
+// key[p] = (ordered bits of the point's split coordinate) << 32 | index.
+__global__ void keys_level_kernel(int64_t n, int64_t first, int pad,
+                                  const int32_t* __restrict__ idx,
+                                  const int32_t* __restrict__ nodeof,
+                                  const int32_t* __restrict__ axis,
+                                  const int32_t* __restrict__ rank, const float* __restrict__ pts,
+                                  uint64_t* __restrict__ keys) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int32_t c = idx[p];
+    const float x = pts[(int64_t)rank[c] * pad + axis[nodeof[p] - first]];
+    keys[p] = ((uint64_t)ordered_bits(x) << 32) | (uint32_t)c;
+}
+
+__global__ void unpack_level_kernel(int64_t n, const uint64_t* __restrict__ keys,
+                                    const int64_t* __restrict__ rs, const int64_t* __restrict__ re,
+                                    int32_t* __restrict__ idx, int32_t* __restrict__ nodeof) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    idx[p] = (int32_t)(keys[p] & 0xffffffffu);
+    const int32_t v = nodeof[p];
+    const int64_t mid = rs[v] + (re[v] - rs[v]) / 2;
+    nodeof[p] = 2 * v + 1 + (p >= mid ? 1 : 0);
+}
+
+__global__ void inverse_kernel(int64_t n, const int32_t* __restrict__ idx, int32_t* __restrict__ pos) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) pos[idx[p]] = (int32_t)p;
+}
+
+__device__ __forceinline__ void swap_keys(uint64_t* k, int64_t a, int64_t b) {
+    const uint64_t t = k[a];
+    k[a] = k[b];
+    k[b] = t;
+}
+
+// Exclusive block prefix of one value per thread; returns the block total.
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* out, uint32_t* s_warp) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = lane < kSelThreads / 32 ? s_warp[lane] : 0u;
+        uint32_t y = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, y, o);
+            if (lane >= o) y += t;
+        }
+        if (lane < kSelThreads / 32) s_warp[32 + lane] = y - x;  // exclusive warp offsets
+        if (lane == 31) s_warp[64] = y;
+    }
+    __syncthreads();
+    *out = s_warp[32 + w] + incl - v;
+    const uint32_t total = s_warp[64];
+    __syncthreads();
+    return total;
+}
+
+// Sorts keys[l, r) ascending (r - l <= kBlockSortMax) in shared memory:
+// bitonic sort over the next power of two, padded with the largest key.
+__device__ void block_sort(uint64_t* keys, int64_t l, int64_t r, uint64_t* s_buf) {
+    const int m = (int)(r - l);
+    int m2 = 1;
+    while (m2 < m) m2 <<= 1;
+    for (int i = threadIdx.x; i < m2; i += blockDim.x) s_buf[i] = i < m ? keys[l + i] : ~0ull;
+    __syncthreads();
+    for (int size = 2; size <= m2; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < m2; i += blockDim.x) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const uint64_t a = s_buf[i], b = s_buf[j];
+                    if ((a > b) == up) {
+                        s_buf[i] = b;
+                        s_buf[j] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) keys[l + i] = s_buf[i];
+    __syncthreads();
+}
+
+// One block per internal node of the level: the reference's introselect of
+// the node's range around its median position (numba_kdtree.py:395
+// _introselect, :372 _introselect_impl).  pos_big / pos_small: per-node
+// scratch (the node's own range of two n-long arrays) pairing the swaps of a
+// partition.  A range that reaches the depth limit while longer than a block
+// can sort is recorded in big_sort (its bounds) for a device-wide sort after
+// the launch.
+__global__ void __launch_bounds__(kSelThreads) select_level_kernel(
+    int64_t first, const int64_t* __restrict__ rs, const int64_t* __restrict__ re,
+    int64_t n_nodes, uint64_t* keys, int32_t* __restrict__ pos_big,
+    int32_t* __restrict__ pos_small, int64_t* __restrict__ big_sort, int* big_sort_count) {
+    __shared__ uint64_t s_buf[kBlockSortMax];
+    __shared__ uint32_t s_warp[65];
+    __shared__ int64_t s_l, s_r, s_B;
+    __shared__ uint64_t s_pivot;
+    __shared__ int s_state;  // 0 partition, 1 sort in the block, 2 sort on the device, 3 done
+    __shared__ uint32_t s_K;
+    const int64_t v = first + blockIdx.x;
+    const int64_t s0 = rs[v], e0 = re[v];
+    // a node is a leaf when it has no children slots or fewer than 2 points
+    if (2 * v + 1 >= n_nodes || e0 - s0 < 2) return;
+    const int64_t nth = s0 + (e0 - s0) / 2;
+    if (threadIdx.x == 0) {
+        s_l = s0;
+        s_r = e0;
+    }
+    const int64_t size0 = e0 - s0;
+    // 2 * int(log2(size)) (numba_kdtree.py:411), exact for integers
+    int depth = size0 > 16 ? 2 * (63 - __clzll((unsigned long long)size0)) : 0;
+    __syncthreads();
+    while (true) {
+        if (threadIdx.x == 0) {
+            const int64_t l = s_l, r = s_r, m = r - l;
+            if (m <= 16 || depth == 0) {
+                // insertion sort (m <= 16) or the heapsort fallback: ascending
+                s_state = m <= kBlockSortMax ? 1 : 2;
+            } else {
+                s_state = 0;
+                // median of three (numba_kdtree.py:282), then the pivot to
+                // the end (:316)
+                const int64_t mid = (l + r - 1) / 2;
+                if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
+                if (keys[mid] > keys[r - 1]) {
+                    swap_keys(keys, mid, r - 1);
+                    if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
+                }
+                swap_keys(keys, mid, r - 1);
+                s_pivot = keys[r - 1];
+                s_K = 0;
+            }
+        }
+        if (depth > 0) --depth;
+        __syncthreads();
+        const int st = s_state;
+        if (st == 1) {
+            block_sort(keys, s_l, s_r, s_buf);
+            return;
+        }
+        if (st == 2) {
+            if (threadIdx.x == 0) {
+                const int slot = atomicAdd(big_sort_count, 1);
+                big_sort[2 * slot] = s_l;
+                big_sort[2 * slot + 1] = s_r;
+            }
+            return;
+        }
+        const int64_t l = s_l, r = s_r;
+        const uint64_t pivot = s_pivot;
+        // elements below the pivot in [l, r - 1)
+        uint32_t c_loc = 0;
+        for (int64_t p = l + threadIdx.x; p < r - 1; p += blockDim.x) c_loc += keys[p] < pivot;
+        uint32_t dummy;
+        const uint32_t c = block_exclusive(c_loc, &dummy, s_warp);
+        const int64_t B = l + c;
+        // pair the elements above the pivot left of B (ranked from the left)
+        // with those below it from B on (ranked from the right)
+        uint32_t carry = 0;
+        for (int64_t base = l; base < r - 1; base += kSelTile) {
+            const int64_t p0 = base + (int64_t)threadIdx.x * kSelV;
+            uint64_t kv[kSelV];
+            uint32_t cnt = 0;
+#pragma unroll
+            for (int j = 0; j < kSelV; ++j) {
+                const int64_t p = p0 + j;
+                kv[j] = p < r - 1 ? keys[p] : 0ull;
+                cnt += (p < r - 1 && kv[j] < pivot) ? 1u : 0u;
+            }
+            uint32_t before;
+            const uint32_t tile_total = block_exclusive(cnt, &before, s_warp);
+            before += carry;
+            uint32_t kb = 0;
+#pragma unroll
+            for (int j = 0; j < kSelV; ++j) {
+                const int64_t p = p0 + j;
+                if (p >= r - 1) break;
+                const bool small = kv[j] < pivot;
+                if (p < B && !small) {
+                    pos_big[l + (p - l) - before] = (int32_t)p;
+                    ++kb;
+                } else if (p >= B && small) {
+                    pos_small[l + (c - 1 - before)] = (int32_t)p;
+                }
+                before += small ? 1u : 0u;
+            }
+            if (kb) atomicAdd(&s_K, kb);
+            carry += tile_total;
+        }
+        __syncthreads();
+        const uint32_t K = s_K;
+        for (uint32_t k = threadIdx.x; k < K; k += blockDim.x)
+            swap_keys(keys, pos_big[l + k], pos_small[l + k]);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            swap_keys(keys, B, r - 1);
+            s_B = B;
+            if (nth < B) s_r = B;
+            else if (nth > B) s_l = B + 1;
+            else s_state = 3;
+        }
+        __syncthreads();
+        if (s_state == 3) return;
+    }
+}
+
+}  // namespace
+
+// [nodes][2][d] -> the reference's node_bounds layout [2][nodes][d]
+__global__ void bounds_layout_kernel(int64_t nodes, int d, const float* __restrict__ box,
+                                     float* __restrict__ out) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nodes * 2 * d) return;
+    const int64_t v = t / (2 * d);
+    const int side = (int)((t / d) % 2), j = (int)(t % d);
+    out[(int64_t)side * nodes * d + v * d + j] = box[t];
+}
+
+int ref_tree_export(const RefTree& t, int32_t* idx_array, float* node_bounds, cudaStream_t s) {
+    if (idx_array)
+        FHG_CUDA(cudaMemcpyAsync(idx_array, t.idx, sizeof(int32_t) * t.n,
+                                 cudaMemcpyDeviceToDevice, s));
+    if (node_bounds) LAUNCH(bounds_layout_kernel, t.nodes * 2 * t.d, t.nodes, t.d, t.box, node_bounds);
+    return FHG_OK;
+}
+
+int ref_tree_levels(int64_t n) {
+    // numba_kdtree.py:486: int(np.log2(max(1, (n - 1) / leaf_size)) + 1), leaf_size 40
+    double x = (double)(n - 1) / 40.0;
+    if (x < 1.0) x = 1.0;
+    return (int)(std::log2(x) + 1.0);
+}
+
+int ref_tree_build(Workspace& ws, const fhg_index& ix, RefTree* out) {
+    cudaStream_t s = ws.stream();
+    const int64_t n = ix.n;
+    const int d = ix.d, pad = ix.pad;
+    *out = RefTree();
+    out->n = n;
+    out->d = d;
+    out->levels = ref_tree_levels(n);
+    const int64_t nodes = ((int64_t)1 << out->levels) - 1;
+    out->nodes = nodes;
+    Stage stage(s, "ref_tree_build");
+    FHG_TRY(ws.alloc(&out->idx, (size_t)n));
+    FHG_TRY(ws.alloc(&out->pos, (size_t)n));
+    FHG_TRY(ws.alloc(&out->box, (size_t)(nodes * 2 * d)));
+    Workspace tmp(s);
+    int32_t *nodeof, *axis, *pos_big, *pos_small, *dummy;
+    int64_t *rs, *re, *big_sort;
+    uint32_t *lo, *hi;
+    uint64_t* keys;
+    int* big_count;
+    FHG_TRY(tmp.alloc(&nodeof, (size_t)n));
+    FHG_TRY(tmp.alloc(&axis, (size_t)((nodes + 1) / 2)));
+    FHG_TRY(tmp.alloc(&pos_big, (size_t)n));
+    FHG_TRY(tmp.alloc(&pos_small, (size_t)n));
+    FHG_TRY(tmp.alloc(&rs, (size_t)nodes));
+    FHG_TRY(tmp.alloc(&re, (size_t)nodes));
+    FHG_TRY(tmp.alloc(&lo, (size_t)(nodes * d)));
+    FHG_TRY(tmp.alloc(&hi, (size_t)(nodes * d)));
+    FHG_TRY(tmp.alloc(&keys, (size_t)n));
+    FHG_TRY(tmp.alloc(&big_count, 1));
+    const int64_t max_level_nodes = (nodes + 1) / 2;
+    FHG_TRY(tmp.alloc(&big_sort, (size_t)(2 * max_level_nodes)));
+    LAUNCH(init_root_kernel, n, n, out->idx, nodeof, rs, re);
+    for (int lvl = 0; lvl < out->levels; ++lvl) {
+        const int64_t first = ((int64_t)1 << lvl) - 1, count = (int64_t)1 << lvl;
+        LAUNCH(box_init_kernel, count * d, first, count, d, lo, hi);
+        LAUNCH(box_level_kernel, n, n, d, pad, out->idx, nodeof, ix.rank, ix.pts, lo, hi);
+        const bool last = lvl + 1 == out->levels;
+        LAUNCH(axis_level_kernel, count, first, count, d, lo, hi, out->box, last ? nullptr : axis);
+        if (last) break;
+        LAUNCH(child_ranges_kernel, count, first, count, rs, re);
+        LAUNCH(keys_level_kernel, n, n, first, pad, out->idx, nodeof, axis, ix.rank, ix.pts, keys);
+        FHG_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
+        ::fhg::note_launch();
+        select_level_kernel<<<(unsigned)count, kSelThreads, 0, s>>>(
+            first, rs, re, nodes, keys, pos_big, pos_small, big_sort, big_count);
+        FHG_CUDA(cudaGetLastError());
+        int h_big = 0;
+        FHG_CUDA(cudaMemcpyAsync(&h_big, big_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        if (h_big > 0) {
+            // ranges that hit the depth limit while longer than a block sorts:
+            // sorted ascending on the device (the heapsort's result)
+            std::vector<int64_t> h_ranges(2 * (size_t)h_big);
+            FHG_CUDA(cudaMemcpyAsync(h_ranges.data(), big_sort, sizeof(int64_t) * 2 * h_big,
+                                     cudaMemcpyDeviceToHost, s));
+            FHG_CUDA(cudaStreamSynchronize(s));
+            for (int i = 0; i < h_big; ++i) {
+                const int64_t l = h_ranges[2 * i], r = h_ranges[2 * i + 1];
+                Workspace one(s);
+                FHG_TRY(one.alloc(&dummy, (size_t)(r - l)));
+                FHG_TRY(radix_sort_u64(one, keys + l, dummy, r - l, 0, 64));
+            }
+        }
+        LAUNCH(unpack_level_kernel, n, n, keys, rs, re, out->idx, nodeof);
+    }
+    LAUNCH(inverse_kernel, n, n, out->idx, out->pos);
+    return FHG_OK;
+}
+
+}  // namespace fhg

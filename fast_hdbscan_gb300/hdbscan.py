@@ -537,10 +537,12 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
                              cluster_selection_epsilon, cluster_selection_persistence,
                              return_trees=return_trees, sample_weights=sample_weights)
     else:
-        fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
-                     max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
-                     cluster_selection_persistence, return_trees=return_trees,
-                     sample_weights=sample_weights, condensed_records=condensed_records)
+        # reproducible=True: the reference's own Boruvka tie choices
+        with _native.tie_rule(bool(reproducible)):
+            fr = gpu_fit(data, min_samples, min_cluster_size, cluster_selection_method,
+                         max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
+                         cluster_selection_persistence, return_trees=return_trees,
+                         sample_weights=sample_weights, condensed_records=condensed_records)
     result = (fr.labels, fr.probabilities, fr.linkage, fr.condensed, fr.sorted_mst,
               fr.neighbors, fr.core_distances)
     return result[: (None if return_trees else 2)]
@@ -581,9 +583,10 @@ def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, rep
                                                sample_weights=sample_weights,
                                                reproducible=reproducible)
     if sample_weights is None:
-        return parallel_boruvka(tree, 1, min_samples=min_samples)
+        return parallel_boruvka(tree, 1, min_samples=min_samples, reproducible=reproducible)
     return parallel_boruvka(tree, 1, min_samples=min_samples,
-                            sample_weights=np.asarray(sample_weights, dtype=np.float32))
+                            sample_weights=np.asarray(sample_weights, dtype=np.float32),
+                            reproducible=reproducible)
 
 
 def clusters_from_spanning_tree(minimum_spanning_tree, data_labels=None, semi_supervised=False,

@@ -44,11 +44,34 @@ int fhg_abi_version(void);
 /* Tracing (no counterpart in the reference, whose benchmark harness times
  * whole calls with perf_counter).  fhg_launch_count: kernels launched by this
  * library since load.  fhg_profile_enable(1): every stage records a pair of
- * CUDA events on its stream.  fhg_profile_report: waits for those events and
- * writes {"stage": [total_ms, count], ...} as JSON into buf, then clears them. */
+ * CUDA events on its stream, and counters add their values (for instance
+ * "boruvka_components": the component count at the start of every Boruvka
+ * round).  fhg_profile_report: waits for those events and writes
+ * {"stage": [total_ms, count], "counter": [sum, samples], ...} as JSON into
+ * buf, then clears them. */
 uint64_t fhg_launch_count(void);
 int fhg_profile_enable(int on);
 int fhg_profile_report(char* buf, int64_t cap);
+
+/* Boruvka tie rule of the calling host thread, for every later call from that
+ * thread (returns the previous rule).  Replaces the `reproducible` flag of
+ * boruvka.py:557 parallel_boruvka (hdbscan.py:343, :658):
+ *   FHG_TIES_CANONICAL (default): among equal mutual-reachability weights, a
+ *     total order on point indices -- a component's edge by (weight, min
+ *     endpoint, max endpoint).  The result does not depend on any thread
+ *     count or index layout.
+ *   FHG_TIES_REFERENCE: the reference's own choices, as its loops make them
+ *     when run in order: a component's edge comes from its point of lowest
+ *     index that attains the component's least weight, and goes to the first
+ *     point of that weight met by the depth-first walk of the reference's
+ *     KD-tree (built exactly, on the GPU, for this); edges that would close a
+ *     cycle are skipped in the reference's component order.  On data without
+ *     tied distances this reproduces the reference's MST, and so its labels
+ *     and probabilities, exactly.  It adds the tree build and one short walk
+ *     per component and round. */
+#define FHG_TIES_CANONICAL 0
+#define FHG_TIES_REFERENCE 1
+int fhg_set_tie_rule(int rule);
 
 /* Device scratch comes from one stream-ordered memory pool per device, owned
  * by this library, that keeps freed blocks cached for the next call (no
@@ -62,8 +85,22 @@ int fhg_release_cached_memory(void);
 typedef struct fhg_index fhg_index;
 
 /* Replaces numba_kdtree.py:478 build_kdtree(data, leaf_size=40).
- * X_dev: n x d float32, row-major, caller order.  1 <= d <= 8. */
+ * X_dev: n x d float32, row-major, caller order.  1 <= d <= 32. */
 int fhg_index_build(const float* X_dev, int64_t n, int32_t d, void* stream, fhg_index** out);
+/* numba_kdtree.py:478 build_kdtree(data, leaf_size=40) exactly: the
+ * reference's own median-split KD-tree, every introselect partition
+ * reproduced (GPU), for the reference tie mode (fhg_set_tie_rule) and for
+ * callers that need the reference's arrays.  X_dev: n x d float32 (1 <= d <=
+ * 32); levels = fhg_reference_kdtree_levels(n), nodes = 2^levels - 1.
+ *   idx_array_dev   n int32 (the reference's idx_array; nullable)
+ *   node_bounds_dev 2 x nodes x d float32 (node_bounds: lower corners, then
+ *                   upper corners; nullable)
+ * idx_start, idx_end and is_leaf follow from n alone (each node's range is
+ * halved, the left child taking the smaller half). */
+int32_t fhg_reference_kdtree_levels(int64_t n);
+int fhg_reference_kdtree(const float* X_dev, int64_t n, int32_t d, int32_t* idx_array_dev,
+                         float* node_bounds_dev, void* stream);
+
 /* Releases an index built by fhg_index_build. */
 int fhg_index_free(fhg_index* index, void* stream);
 /* Number of points and dimensions of an index. */
@@ -152,7 +189,11 @@ int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* str
  * sample_weights_dev (m + 1 float32, else NULL), :98
  * mst_to_linkage_tree_w_sample_weights: m x 4 float64 rows
  * [max(root_l, root_r), min(root_l, root_r), weight, size], size = points
- * (or the float32 sum of their weights) under the merge. */
+ * (or the float32 sum of their weights) under the merge.
+ * Precondition (as in the reference): the rows form a spanning tree of the
+ * points 0..m, so every endpoint is an integer in [0, m].  Endpoints outside
+ * that range are clamped into it (no memory outside the call's buffers is
+ * touched) and the resulting tree is meaningless. */
 int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m,
                             const float* sample_weights_dev, double* linkage_dev, void* stream);
 
@@ -165,9 +206,14 @@ int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m,
  * which every GPU that loads the library holds until the process exits.
  *   - m must not exceed FHG_NOALLOC_MAX_EDGES; larger inputs are rejected
  *     with FHG_ERR_INVALID (use fhg_mst_to_linkage_tree instead).
+ *   - The same endpoint precondition as fhg_mst_to_linkage_tree: every
+ *     endpoint in [0, m]; others are clamped into range.
  *   - The first call on each device looks up the array's device address
  *     (cudaGetSymbolAddress, with that device current); make that first call
- *     before any stream capture.
+ *     before any stream capture.  The address is cached per device for the
+ *     life of the process: after cudaDeviceReset (or anything else that
+ *     tears down and recreates the device's primary context) the cache is
+ *     stale, so do not call this entry point again in that process.
  *   - Every call shares the one array: calls that overlap on the GPU (for
  *     instance on two streams) race and corrupt each other's results.  Each
  *     call initialises what it reads, so back-to-back calls are safe. */
@@ -366,6 +412,23 @@ int fhg_hdbscan_fit_knn_graph(const float* X_dev, int64_t n, int32_t d, int32_t 
 int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices_dev,
                        const float* weights_dev, const int32_t* seg_end_dev, int64_t n,
                        double* edges_dev, int64_t* n_edges_host, void* stream);
+
+/* sub_clusters.py:132 propagate_labels_per_cluster for many clusters in one
+ * launch.  labels_dev: the sub-cluster labels of every cluster's points (any
+ * layout; -1 = noise), updated in place.  Cluster c's noise points are
+ * noise_pt_dev[noise_first_dev[c] .. noise_first_dev[c+1]) in increasing
+ * index order; noise point x's neighbours are adj_other_dev[adj_ptr_dev[x] ..
+ * adj_ptr_dev[x+1]) (indices into labels_dev) in the order of the reference's
+ * per-point dict, with the inverse weights adj_w_dev (float64).  Each cluster
+ * sweeps its noise points in order, giving each the label of largest summed
+ * inverse weight among its labelled neighbours (first label wins ties; later
+ * points of the same sweep see the new labels), until a sweep labels nothing.
+ * Unlike the reference, which loops forever when some noise point cannot be
+ * reached, such points stay -1. */
+int fhg_propagate_labels(int64_t n_clusters, const int32_t* noise_first_dev,
+                         const int32_t* noise_pt_dev, const int32_t* adj_ptr_dev,
+                         const int32_t* adj_other_dev, const double* adj_w_dev,
+                         int32_t* labels_dev, void* stream);
 
 /* core_graph.py:19 knn_mst_union + :47 flatten_to_csr + :70 sort_by_lens for
  * many clusters at once, as one block CSR of P rows (the clusters' points one
