@@ -163,12 +163,8 @@ def core_graph_forests(graphs):
 def core_graphs_and_forests(inputs):
     """Core graphs and spanning forests of many clusters on the GPU: ``inputs``
     is a list of ``(neighbors, core_distances, min_spanning_tree, lens)`` in
-    in-cluster ids; the graphs are laid out as one block CSR
-    (``fhg_core_graphs``), their forests built in one launch
-    (``fhg_core_graph_mst``).  Returns ``[(graph, n_components,
-    component_labels, forest), ...]`` as knn_mst_union and
-    core_graph_spanning_tree give them."""
-    torch = _native._torch()
+    in-cluster ids.  Returns ``[(graph, n_components, component_labels,
+    forest), ...]`` as knn_mst_union and core_graph_spanning_tree give them."""
     sizes = np.array([len(c) for _, c, _, _ in inputs], dtype=np.int64)
     offs = np.concatenate([[0], np.cumsum(sizes)])
     P = int(offs[-1])
@@ -180,27 +176,53 @@ def core_graphs_and_forests(inputs):
             a = np.asarray(nb).reshape(len(c), -1)
             nb_block[offs[i]:offs[i + 1], :a.shape[1]] = a
     lens_block = np.concatenate([np.asarray(l, np.float64) for _, _, _, l in inputs] + [[]])
-    if np.any(np.isnan(lens_block)):
-        raise ValueError("lens values must not be NaN")
     core_block = np.concatenate([np.asarray(c, np.float32) for _, c, _, _ in inputs] + [[]])
     msts = [np.asarray(m, np.float64).reshape(-1, 3) for _, _, m, _ in inputs]
-    mparent = np.concatenate([m[:, 0].astype(np.int64) + offs[i] for i, m in enumerate(msts)]
-                             + [np.zeros(0, np.int64)]).astype(np.int32)
-    mchild = np.concatenate([m[:, 1] for m in msts] + [np.zeros(0)]).astype(np.int32)
-    mdist = np.concatenate([m[:, 2] for m in msts] + [np.zeros(0)])
+    mst_bounds = np.concatenate([[0], np.cumsum([len(m) for m in msts])])
+    mst_local = np.concatenate(msts + [np.zeros((0, 3))])
+    return core_graphs_and_forests_block(sizes, nb_block, lens_block, core_block, mst_local,
+                                         mst_bounds)
+
+
+def core_graphs_and_forests_block(sizes, nb_block, lens_block, core_block, mst_local,
+                                  mst_bounds):
+    """Core graphs and spanning forests of many clusters laid out back to back
+    (cluster c's rows are the next sizes[c] rows of the blocks): nb_block
+    (rows x k in-cluster neighbour ids, -1 for none), lens_block (float64),
+    core_block, and the in-cluster MST edges mst_local[mst_bounds[c]:
+    mst_bounds[c+1]] (in-cluster ids, distance).  The graphs are laid out as
+    one block CSR (``fhg_core_graphs``) and their forests built in one launch
+    (``fhg_core_graph_mst``).  Returns ``[(graph, n_components,
+    component_labels, forest), ...]``."""
+    torch = _native._torch()
+    sizes = np.asarray(sizes, dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    P = int(offs[-1])
+    n_cl = len(sizes)
+    nb_block = np.asarray(nb_block, dtype=np.int32).reshape(P, -1)
+    k = nb_block.shape[1]
+    lens_block = np.asarray(lens_block, dtype=np.float64)
+    if np.any(np.isnan(lens_block)):
+        raise ValueError("lens values must not be NaN")
+    mst_local = np.asarray(mst_local, dtype=np.float64).reshape(-1, 3)
+    mst_bounds = np.asarray(mst_bounds, dtype=np.int64)
+    # parent rows as block rows; children stay in-cluster ids
+    m_owner = np.repeat(np.arange(n_cl), np.diff(mst_bounds))
+    mparent = (mst_local[:, 0].astype(np.int64) + offs[:-1][m_owner]).astype(np.int32)
+    mchild = mst_local[:, 1].astype(np.int32)
+    mdist = mst_local[:, 2]
     M = len(mparent)
-    out_graphs = []
     if P == 0:
         return [(CoreGraph(np.zeros(0, np.float32), np.zeros(0, np.float32),
                            np.zeros(0, np.int32), np.zeros(1, np.int32)), 0,
-                 np.zeros(0, np.int64), np.zeros((0, 3))) for _ in inputs]
+                 np.zeros(0, np.int64), np.zeros((0, 3))) for _ in range(n_cl)]
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
     V = _native.vptr
     cap = P * k + M
-    d = dict(nb=T(nb_block), lens=T(lens_block.astype(np.float64)), core=T(core_block.astype(np.float32)),
+    d = dict(nb=T(nb_block), lens=T(lens_block), core=T(np.asarray(core_block, np.float32)),
              bs=T(np.repeat(offs[:-1], sizes).astype(np.int32)),
              be=T(np.repeat(offs[1:], sizes).astype(np.int32)),
-             mp=T(mparent), mc=T(mchild), md=T(mdist.astype(np.float64)))
+             mp=T(mparent), mc=T(mchild), md=T(np.ascontiguousarray(mdist)))
     indptr = torch.empty(P + 1, dtype=torch.int32, device="cuda")
     il = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
     ib = torch.empty(max(cap, 1), dtype=torch.int32, device="cuda")
@@ -225,7 +247,8 @@ def core_graphs_and_forests(inputs):
     all_edges = edges[: m.value].cpu().numpy()
     owner = np.searchsorted(offs, all_edges[:, 0].astype(np.int64), side="right") - 1
     order = np.argsort(owner, kind="stable")
-    bounds = np.searchsorted(owner[order], np.arange(len(inputs) + 1))
+    bounds = np.searchsorted(owner[order], np.arange(n_cl + 1))
+    out_graphs = []
     for i, sz in enumerate(sizes):
         a, b = int(h_indptr[offs[i]]), int(h_indptr[offs[i + 1]])
         g = CoreGraph(h_w[a:b].copy(), h_d[a:b].copy(), h_il[a:b].copy(),

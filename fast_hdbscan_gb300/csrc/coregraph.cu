@@ -310,7 +310,89 @@ __global__ void cgl_fill_kernel(int64_t P, int k, const int32_t* __restrict__ nb
     }
 }
 
+// ------------------------------------------------------- label propagation
+// Noise points of a cluster take the label whose summed inverse lens weight
+// over their labelled core-graph neighbours is largest (sub_clusters.py:132).
+// The reference sweeps the cluster's noise points in index order, writing
+// each new label in place, so a point already sees the labels given earlier
+// in the same sweep; sweeps repeat while noise remains.  One thread runs that
+// sequence for its cluster, every cluster in parallel.  adj_*: for every
+// noise point (entries noise_first[c] .. noise_first[c+1] of cluster c, in
+// index order), its neighbours in the order the reference's per-point dict
+// holds them and their inverse weights; tab_*: per noise point, room for its
+// distinct neighbour labels (one slot per neighbour).  Label sums are
+// float64, in neighbour order; the first label reaching the largest sum
+// wins.  A sweep that labels nothing ends the cluster's work (points no
+// labelled point can reach stay noise).
+__global__ void propagate_kernel(int64_t nclusters, const int32_t* __restrict__ noise_first,
+                                 const int32_t* __restrict__ noise_pt,
+                                 const int32_t* __restrict__ adj_ptr,
+                                 const int32_t* __restrict__ adj_other,
+                                 const double* __restrict__ adj_w, int32_t* lab,
+                                 int32_t* __restrict__ tab_lab, double* __restrict__ tab_sum) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nclusters) return;
+    const int32_t a = noise_first[c], b = noise_first[c + 1];
+    // every sweep but the last labels at least one point
+    for (int32_t sweep = 0; sweep <= b - a; ++sweep) {
+        bool changed = false;
+        for (int32_t x = a; x < b; ++x) {
+            const int32_t p = noise_pt[x];
+            if (lab[p] != -1) continue;
+            const int32_t e0 = adj_ptr[x], e1 = adj_ptr[x + 1];
+            int32_t nd = 0;
+            for (int32_t e = e0; e < e1; ++e) {
+                const int32_t l = lab[adj_other[e]];
+                if (l == -1) continue;
+                int32_t t = 0;
+                while (t < nd && tab_lab[e0 + t] != l) ++t;
+                if (t == nd) {
+                    tab_lab[e0 + nd] = l;
+                    tab_sum[e0 + nd] = 0.0;
+                    ++nd;
+                }
+                tab_sum[e0 + t] = __dadd_rn(tab_sum[e0 + t], adj_w[e]);
+            }
+            if (nd == 0) continue;
+            double best = -INFINITY;
+            int32_t bl = -1;
+            for (int32_t t = 0; t < nd; ++t)
+                if (tab_sum[e0 + t] > best) {
+                    best = tab_sum[e0 + t];
+                    bl = tab_lab[e0 + t];
+                }
+            lab[p] = bl;
+            changed = true;
+        }
+        if (!changed) break;
+    }
+}
+
 }  // namespace
+
+int propagate_labels(int64_t nclusters, const int32_t* noise_first, const int32_t* noise_pt,
+                     const int32_t* adj_ptr, const int32_t* adj_other, const double* adj_w,
+                     int32_t* labels, cudaStream_t s) {
+    if (nclusters <= 0) return FHG_OK;
+    int32_t n_noise = 0, n_adj = 0;
+    FHG_CUDA(cudaMemcpyAsync(&n_noise, noise_first + nclusters, sizeof(int32_t),
+                             cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    if (n_noise <= 0) return FHG_OK;
+    FHG_CUDA(cudaMemcpyAsync(&n_adj, adj_ptr + n_noise, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    Workspace ws(s);
+    int32_t* tab_lab;
+    double* tab_sum;
+    FHG_TRY(ws.alloc(&tab_lab, (size_t)(n_adj > 0 ? n_adj : 1)));
+    FHG_TRY(ws.alloc(&tab_sum, (size_t)(n_adj > 0 ? n_adj : 1)));
+    ::fhg::note_launch();
+    propagate_kernel<<<grid_for(nclusters, 64), 64, 0, s>>>(
+        nclusters, noise_first, noise_pt, adj_ptr, adj_other, adj_w, labels, tab_lab, tab_sum);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
 
 int core_graph_boruvka(int64_t n, const int32_t* indptr, const int32_t* indices,
                        const float* weights, const int32_t* seg_end, double* edges,

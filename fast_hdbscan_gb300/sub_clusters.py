@@ -1,18 +1,22 @@
-"""Sub-cluster detection within fitted clusters (sub_clusters.py of the
-reference): every cluster's points get lens values (a callback or an array),
-their core graph is clustered on the lens (core_graph.py, the spanning forest
-and cluster hierarchy on the GPU), and the per-cluster results are merged
-into one labelling.  The host side -- the per-cluster loop, label merging,
-noise propagation and non-finite remapping -- follows the reference step for
-step."""
+"""Sub-cluster detection within fitted clusters (the reference's
+sub_clusters.py): every cluster's points get lens values (a callback or an
+array), their core graph is clustered on the lens (core_graph.py: the
+spanning forests and the cluster hierarchies on the GPU), and the
+per-cluster results are merged into one labelling.
+
+All clusters are handled together: one layout pass cuts every cluster's
+inputs out of the fit (cluster_layout), one GPU pass builds every core graph
+and forest, the label merge is a few vectorised passes over (cluster, label)
+pairs, and the optional propagation of labels to noise points runs on the
+GPU for every cluster in one launch.  The validation, the returned tuple and
+the fitted attributes are the reference's interface."""
 import concurrent.futures
 import threading
 
 import numpy as np
 
 from . import _native
-from .core_graph import (_clusters_of_forest, core_graph_clusters, core_graph_to_edge_list,
-                         core_graphs_and_forests)
+from .core_graph import _clusters_of_forest, core_graph_to_edge_list, core_graphs_and_forests_block
 from .hdbscan import _BaseEstimator as BaseEstimator
 from .hdbscan import _check_sample_weight, to_numpy_rec_array
 from .hdbscan import _ClusterMixin as ClusterMixin
@@ -30,156 +34,226 @@ def check_is_fitted(estimator, attributes, msg):
         raise NotFittedError(msg)
 
 
-def compute_sub_clusters_in_cluster(cluster, data, labels, probabilities, neighbors,
-                                    core_distances, min_spanning_tree, parent_labels,
-                                    child_labels, lens_callback, sample_weights=None,
-                                    **kwargs):
-    """sub_clusters.py:16: one cluster's sub-clusters, in in-cluster ids."""
-    points = np.nonzero(labels == cluster)[0]
-    in_cluster_ids = np.full(data.shape[0], -1, dtype=np.int32)
-    in_cluster_ids[points] = np.arange(len(points))
-    neighbors = in_cluster_ids[neighbors[points, :]]
-    core_distances = core_distances[points]
-    min_spanning_tree = min_spanning_tree[(parent_labels == cluster) & (child_labels == cluster)]
-    min_spanning_tree[:, :2] = in_cluster_ids[min_spanning_tree[:, :2].astype(np.int64)]
-    lens_values = lens_callback(data, probabilities, neighbors, core_distances,
-                                min_spanning_tree, points)
-    return (*core_graph_clusters(
-        lens_values, neighbors, core_distances, min_spanning_tree,
-        sample_weights=(sample_weights[points] if sample_weights is not None else None),
-        **kwargs), lens_values, points)
+def cluster_layout(labels, num_clusters, neighbors, min_spanning_tree):
+    """Every cluster's inputs in one pass, clusters back to back.
+
+    Returns (points, bounds, nb_local, mst_local, mst_bounds): the clustered
+    points grouped by cluster (cluster c at points[bounds[c]:bounds[c+1]], in
+    increasing index order), their kNN neighbours as in-cluster ids (-1 for
+    neighbours outside the cluster), and the MST edges with both ends in one
+    cluster, grouped by cluster in their original order with in-cluster ids
+    (cluster c's at mst_local[mst_bounds[c]:mst_bounds[c+1]]) -- the arrays
+    sub_clusters.py:16-61 cuts out for each cluster."""
+    labels = np.asarray(labels)
+    order = np.argsort(labels, kind="stable")
+    bounds = np.searchsorted(labels[order], np.arange(num_clusters + 1))
+    points = order[bounds[0]:]
+    bounds = bounds - bounds[0]
+    sizes = np.diff(bounds)
+    owner = np.repeat(np.arange(num_clusters), sizes)
+    local = np.full(len(labels), -1, dtype=np.int64)
+    local[points] = np.arange(len(points)) - np.repeat(bounds[:-1], sizes)
+    nb = np.asarray(neighbors)[points]
+    nb_c = np.maximum(nb, 0)
+    inside = (nb >= 0) & (labels[nb_c] == owner[:, None])
+    nb_local = np.where(inside, local[nb_c], -1).astype(np.int32)
+    mst = np.asarray(min_spanning_tree, dtype=np.float64)
+    pe = labels[mst[:, 0].astype(np.int64)]
+    ce = labels[mst[:, 1].astype(np.int64)]
+    kept = np.nonzero((pe == ce) & (pe >= 0))[0]
+    kept = kept[np.argsort(pe[kept], kind="stable")]
+    mst_bounds = np.searchsorted(pe[kept], np.arange(num_clusters + 1))
+    mst_local = mst[kept].copy()
+    mst_local[:, :2] = local[mst_local[:, :2].astype(np.int64)]
+    return points, bounds, nb_local, mst_local, mst_bounds
+
+
+def cluster_lens_values(lens, data, probabilities, points, bounds, nb_local, core, mst_local,
+                        mst_bounds):
+    """Lens values of every clustered point (clusters back to back): from an
+    array over the points, from a callback's all-clusters form in one call,
+    or from a per-cluster callback (sub_clusters.py:45) given each cluster's
+    slices."""
+    if isinstance(lens, np.ndarray):
+        return np.asarray(lens)[points]
+    all_clusters = getattr(lens, "all_clusters", None)
+    if all_clusters is not None:
+        return np.asarray(all_clusters(data, probabilities, points, bounds))
+    parts = [np.asarray(lens(data, probabilities, nb_local[bounds[c]:bounds[c + 1]],
+                             core[bounds[c]:bounds[c + 1]],
+                             mst_local[mst_bounds[c]:mst_bounds[c + 1]],
+                             points[bounds[c]:bounds[c + 1]]))
+             for c in range(len(bounds) - 1)]
+    return np.concatenate(parts + [np.zeros(0)])
 
 
 def compute_sub_clusters_per_cluster(data, labels, probabilities, neighbors, core_distances,
                                      min_spanning_tree, lens_callback, num_clusters,
                                      sample_weights=None, **kwargs):
-    """sub_clusters.py:64: compute_sub_clusters_in_cluster for every cluster.
-    The per-cluster inputs come from one grouping pass (points and in-cluster
-    MST edges in their original order, in-cluster ids in one array) instead
-    of a scan of all points and edges per cluster; they are the same arrays."""
-    labels = np.asarray(labels)
-    parent_labels = labels[min_spanning_tree[:, 0].astype(np.int64)]
-    child_labels = labels[min_spanning_tree[:, 1].astype(np.int64)]
-    order = np.argsort(labels, kind="stable")
-    bounds = np.searchsorted(labels[order], np.arange(num_clusters + 1))
-    same = parent_labels == child_labels
-    e_idx = np.nonzero(same)[0]
-    e_order = e_idx[np.argsort(parent_labels[e_idx], kind="stable")]
-    e_bounds = np.searchsorted(parent_labels[e_order], np.arange(num_clusters + 1))
-    local = np.empty(len(labels), dtype=np.int32)
-    for cluster in range(num_clusters):
-        pts = order[bounds[cluster]:bounds[cluster + 1]]
-        local[pts] = np.arange(len(pts), dtype=np.int32)
-    per = []
-    for cluster in range(num_clusters):
-        points = order[bounds[cluster]:bounds[cluster + 1]]
-        nb = neighbors[points, :]
-        cl_nb = np.where(nb >= 0, labels[np.maximum(nb, 0)], -2) == cluster
-        nb_local = np.where(cl_nb, local[np.maximum(nb, 0)], -1).astype(np.int32)
-        mst = min_spanning_tree[e_order[e_bounds[cluster]:e_bounds[cluster + 1]]].copy()
-        mst[:, :2] = local[mst[:, :2].astype(np.int64)]
-        core = core_distances[points]
-        lens_values = lens_callback(data, probabilities, nb_local, core, mst, points)
-        per.append((points, lens_values, (nb_local, core, mst, lens_values)))
-    # every cluster's core graph and forest on the GPU in one pass each, then
-    # each cluster's hierarchy
-    built = core_graphs_and_forests([inp for _, _, inp in per])
+    """sub_clusters.py:64: every cluster's sub-cluster hierarchy on its lens.
+    The clusters' inputs come from one layout pass (cluster_layout), their
+    core graphs and spanning forests from one GPU pass each, and their
+    hierarchies -- independent, a few short launches each -- run on worker
+    threads with a CUDA stream apiece.  Returns, per cluster, (labels,
+    probabilities, linkage tree, condensed tree, forest, core graph, lens
+    values, points)."""
+    points, bounds, nb_local, mst_local, mst_bounds = cluster_layout(
+        labels, num_clusters, neighbors, min_spanning_tree)
+    core = np.asarray(core_distances)[points]
+    lens = cluster_lens_values(lens_callback, data, probabilities, points, bounds, nb_local,
+                               core, mst_local, mst_bounds)
+    built = core_graphs_and_forests_block(np.diff(bounds), nb_local, lens, core, mst_local,
+                                          mst_bounds)
 
-    # the clusters' hierarchies are independent: worker threads, each on its
-    # own CUDA stream, overlap their short launches and copies
     torch = _native._torch()
     tls = threading.local()
 
-    def hierarchy(i):
-        (points, lens_values, _), (graph, nc, comp, forest) = per[i], built[i]
+    def hierarchy(c):
+        graph, nc, comp, forest = built[c]
+        pts = points[bounds[c]:bounds[c + 1]]
         if not hasattr(tls, "stream"):
             tls.stream = torch.cuda.Stream()
         with torch.cuda.stream(tls.stream):
             res = _clusters_of_forest(
                 nc, comp, forest, graph,
-                sample_weights=(sample_weights[points] if sample_weights is not None else None),
+                sample_weights=(sample_weights[pts] if sample_weights is not None else None),
                 **kwargs)
         tls.stream.synchronize()
-        return (*res, lens_values, points)
+        return (*res, lens[bounds[c]:bounds[c + 1]], pts)
 
     torch.cuda.current_stream().synchronize()
-    if len(per) <= 1:
-        return [hierarchy(i) for i in range(len(per))]
-    with concurrent.futures.ThreadPoolExecutor(min(8, len(per))) as ex:
-        return list(ex.map(hierarchy, range(len(per))))
+    if num_clusters <= 1:
+        return [hierarchy(c) for c in range(num_clusters)]
+    with concurrent.futures.ThreadPoolExecutor(min(8, num_clusters)) as ex:
+        return list(ex.map(hierarchy, range(num_clusters)))
+
+
+def _label_counts(sub_labels, points_list):
+    """Per cluster: the number of distinct sub-labels and whether -1 is one of
+    them, from one np.unique over (cluster, label) pairs.  Also returns the
+    clusters' points back to back, each point's cluster and its sub-label."""
+    n_cl = len(points_list)
+    sizes = np.array([len(p) for p in points_list], dtype=np.int64)
+    pts = (np.concatenate([np.asarray(p, dtype=np.int64) for p in points_list])
+           if n_cl else np.zeros(0, np.int64))
+    owner = np.repeat(np.arange(n_cl), sizes)
+    lab = np.asarray(sub_labels)[pts].astype(np.int64)
+    span = int(lab.max()) + 2 if lab.size else 1
+    pairs = np.unique(owner * span + (lab + 1))
+    distinct = np.bincount(pairs // span, minlength=n_cl)
+    noise = np.zeros(n_cl, dtype=np.int64)
+    noise[(pairs // span)[pairs % span == 0]] = 1
+    return distinct, noise, pts, owner, lab
 
 
 def update_labels(cluster_probabilities, sub_labels_list, sub_probabilities_list,
                   lens_values_list, points_list, data_size):
-    """sub_clusters.py:98: one labelling from the per-cluster results."""
+    """sub_clusters.py:98: one labelling from the per-cluster results.  Labels
+    are numbered cluster after cluster, every distinct sub-label (noise
+    included) taking one number and noise sharing the cluster's first;
+    probabilities are the mean of the cluster and sub-cluster probabilities
+    (float32: their sum, halved)."""
     labels = np.full(data_size, -1, dtype=np.int64)
     probabilities = cluster_probabilities.copy()
     sub_labels = np.zeros(data_size, dtype=np.int64)
     sub_probabilities = np.zeros(data_size, dtype=np.float32)
     lens_values = np.zeros(data_size, dtype=np.float32)
-    running_id = 0
-    for points, _labels, _probs, _lens in zip(points_list, sub_labels_list,
-                                              sub_probabilities_list, lens_values_list):
-        unique_labels = np.unique(_labels)
-        labels[points] = _labels + int(unique_labels[0] == -1) + running_id
-        sub_labels[points] = _labels
-        sub_probabilities[points] = _probs
-        probabilities[points] += _probs
-        probabilities[points] /= 2
-        lens_values[points] = _lens
-        running_id += len(unique_labels)
+    if len(points_list) == 0:
+        return labels, probabilities, sub_labels, sub_probabilities, lens_values
+    sub_labels[np.concatenate(points_list)] = np.concatenate(sub_labels_list)
+    distinct, noise, pts, owner, lab = _label_counts(sub_labels, points_list)
+    first = np.concatenate([[0], np.cumsum(distinct)[:-1]])
+    labels[pts] = lab + noise[owner] + first[owner]
+    sub_probabilities[pts] = np.concatenate(sub_probabilities_list)
+    merged = probabilities[pts]
+    merged += sub_probabilities[pts]
+    merged /= 2
+    probabilities[pts] = merged
+    lens_values[pts] = np.concatenate(lens_values_list)
     return labels, probabilities, sub_labels, sub_probabilities, lens_values
 
 
-def propagate_labels_per_cluster(graph, sub_labels):
-    """sub_clusters.py:132: noise points take the label of greatest summed
-    inverse lens weight among their labelled core-graph neighbours, repeated
-    until every point that can be reached is labelled."""
-    n = len(sub_labels)
-    undirected = [dict() for _ in range(n)]
-    for idx in range(n):
-        for i in range(graph.indptr[idx], graph.indptr[idx + 1]):
-            neighbor = int(graph.indices[i])
-            w = 1.0 / float(graph.weights[i])
-            if sub_labels[neighbor] == -1:
-                undirected[neighbor][idx] = w
-            if sub_labels[idx] == -1:
-                undirected[idx][neighbor] = w
-    while True:
-        noise_idx = np.nonzero(sub_labels == -1)[0]
-        if noise_idx.shape[0] == 0:
-            break
-        changed = False
-        for idx in noise_idx:
-            candidates = {}
-            for neighbor_idx, weight in undirected[idx].items():
-                label = sub_labels[neighbor_idx]
-                if label == -1:
-                    continue
-                candidates[label] = candidates.get(label, 0.0) + weight
-            if not candidates:
-                continue
-            max_weight, max_candidate = -np.inf, -1
-            for candidate, weight in candidates.items():
-                if weight > max_weight:
-                    max_weight, max_candidate = weight, candidate
-            sub_labels[idx] = max_candidate
-            changed = True
-        if not changed:  # unreachable noise stays noise (the reference loops forever)
-            break
-    return sub_labels
+def _noise_adjacency(graph, sub_labels, base):
+    """The neighbours of every noise point of one cluster's core graph, in the
+    order the reference's per-point dict (sub_clusters.py:134-142) holds
+    them: walking the CSR in row order, an entry (row -> col) first adds row
+    to col's dict if col is noise, then col to row's if row is noise; a
+    repeated pair keeps its first position and its last value.  Point ids
+    are offset by ``base``.  Returns (noise points ascending, their entry
+    counts, neighbours, inverse weights)."""
+    indptr = np.asarray(graph.indptr, dtype=np.int64)
+    n = len(indptr) - 1
+    rows = np.repeat(np.arange(n), np.diff(indptr))
+    cols = np.asarray(graph.indices, dtype=np.int64)
+    inv = 1.0 / np.asarray(graph.weights, dtype=np.float64)
+    noise = np.asarray(sub_labels) == -1
+    key = np.stack([cols, rows], axis=1).ravel()
+    other = np.stack([rows, cols], axis=1).ravel()
+    val = np.repeat(inv, 2)
+    ok = np.stack([noise[cols], noise[rows]], axis=1).ravel()
+    seq = np.nonzero(ok)[0]
+    key, other, val = key[seq], other[seq], val[seq]
+    pair = key * n + other
+    o = np.lexsort((seq, pair))
+    head = np.r_[True, pair[o][1:] != pair[o][:-1]]
+    tail = np.r_[head[1:], True]
+    first_seq = seq[o][head]
+    last_val = val[o][tail]
+    ukey, uother = key[o][head], other[o][head]
+    o2 = np.lexsort((first_seq, ukey))
+    noise_pts = np.nonzero(noise)[0]
+    counts = np.bincount(ukey[o2], minlength=n)[noise_pts]
+    return noise_pts + base, counts, uother[o2] + base, last_val[o2]
 
 
 def propagate_sub_cluster_labels(labels, sub_labels, graph_list, points_list):
-    """sub_clusters.py:170."""
-    running_id = 0
-    for points, core_graph in zip(points_list, graph_list):
-        unique_sub_labels = np.unique(sub_labels[points])
-        has_noise = unique_sub_labels[0] == -1 and len(unique_sub_labels) > 1
-        if has_noise:
-            sub_labels[points] = propagate_labels_per_cluster(core_graph, sub_labels[points])
-        labels[points] = sub_labels[points] + running_id
-        running_id += len(unique_sub_labels) - int(has_noise)
+    """sub_clusters.py:170: in every cluster that has both noise and
+    sub-clusters, noise points take labels by density-weighted majority votes
+    over the core graph, on the GPU for all such clusters in one launch
+    (``fhg_propagate_labels``, the reference's in-place sweeps,
+    sub_clusters.py:132); then labels are numbered cluster after cluster.
+    Noise that no labelled point can reach stays noise (the reference loops
+    forever there).  Updates and returns (labels, sub_labels)."""
+    if len(points_list) == 0:
+        return labels, sub_labels
+    distinct, noise, pts, owner, _ = _label_counts(sub_labels, points_list)
+    needs = np.nonzero((noise == 1) & (distinct > 1))[0]
+    if len(needs):
+        torch = _native._torch()
+        lab_parts, npt, cnt, adj_o, adj_w, nfirst = [], [], [], [], [], [0]
+        base = 0
+        for c in needs:
+            p = np.asarray(points_list[c], dtype=np.int64)
+            sl = np.asarray(sub_labels)[p]
+            a, b, o, w = _noise_adjacency(graph_list[c], sl, base)
+            lab_parts.append(sl)
+            npt.append(a)
+            cnt.append(b)
+            adj_o.append(o)
+            adj_w.append(w)
+            nfirst.append(nfirst[-1] + len(a))
+            base += len(p)
+        T = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).cuda()  # noqa
+        d_lab = T(np.concatenate(lab_parts), np.int32)
+        counts = np.concatenate(cnt)
+        d_first = T(nfirst, np.int32)
+        d_pts = T(np.concatenate(npt), np.int32)
+        d_ptr = T(np.concatenate([[0], np.cumsum(counts)]), np.int32)
+        d_oth = T(np.concatenate(adj_o + [np.zeros(0, np.int64)]), np.int32)
+        d_w = T(np.concatenate(adj_w + [np.zeros(0)]), np.float64)
+        V = _native.vptr
+        _native.check(_native.load().fhg_propagate_labels(
+            len(needs), V(d_first), V(d_pts), V(d_ptr), V(d_oth), V(d_w), V(d_lab),
+            _native.stream_ptr()))
+        new = d_lab.cpu().numpy().astype(np.asarray(sub_labels).dtype)
+        at = 0
+        for c in needs:
+            p = np.asarray(points_list[c], dtype=np.int64)
+            sub_labels[p] = new[at:at + len(p)]
+            at += len(p)
+    widths = distinct - ((noise == 1) & (distinct > 1))
+    first = np.concatenate([[0], np.cumsum(widths)[:-1]])
+    labels[pts] = np.asarray(sub_labels)[pts] + first[owner]
     return labels, sub_labels
 
 
@@ -275,8 +349,8 @@ def find_sub_clusters(clusterer, cluster_labels=None, cluster_probabilities=None
             raise ValueError(
                 "when providing values as lens_callback, they must have"
                 f"the same length as the data, {len(lens_callback)} != {data.shape[0]}")
-        lens_array = lens_callback[finite_index] if last_outlier > 0 else lens_callback
-        lens_callback = lambda a, b, c, d, e, pts: lens_array[pts]  # noqa: E731
+        lens_callback = np.asarray(lens_callback[finite_index] if last_outlier > 0
+                                   else lens_callback)
 
     num_clusters = np.max(cluster_labels) + 1
     (sub_labels, sub_probabilities, linkage_trees, condensed_trees, spanning_trees,

@@ -87,24 +87,48 @@ def test_root_labels_follow_union_by_rank():
     np.testing.assert_array_equal(comp, g["components"])
 
 
-def test_label_propagation_on_a_small_core_graph():
-    """sub_clusters.py:132: noise points take the label with the largest summed
-    inverse weight among labelled neighbours, sweep after sweep; a noise point
-    with no labelled path stays noise."""
-    from fast_hdbscan_gb300.core_graph import CoreGraph
-    from fast_hdbscan_gb300.sub_clusters import propagate_labels_per_cluster
+def reference_noise_dicts(graph, sub_labels):
+    """sub_clusters.py:134-142 restated as the test's checker: the per-point
+    dict of neighbours (insertion order, last value wins) of every noise
+    point."""
+    n = len(sub_labels)
+    und = [dict() for _ in range(n)]
+    for idx in range(n):
+        for i in range(graph.indptr[idx], graph.indptr[idx + 1]):
+            nb = int(graph.indices[i])
+            w = 1.0 / float(graph.weights[i])
+            if sub_labels[nb] == -1:
+                und[nb][idx] = w
+            if sub_labels[idx] == -1:
+                und[idx][nb] = w
+    return und
 
-    # 0 - 1 (w 1), 1 - 2 (w 4), 2 - 3 (w 1), 3 - 4 (w 2); 5 isolated
-    rows = [[1], [2], [3], [4], [], []]
-    ws = [[1.0], [4.0], [1.0], [2.0], [], []]
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_noise_adjacency_in_dict_order(seed):
+    """The propagation's host layout lists every noise point's neighbours in
+    the reference's dict order with the dict's values."""
+    from fast_hdbscan_gb300.core_graph import CoreGraph
+    from fast_hdbscan_gb300.sub_clusters import _noise_adjacency
+
+    rng = np.random.default_rng(seed)
+    n = 60
+    rows = [sorted(rng.choice(n, rng.integers(0, 6), replace=False).tolist()) for _ in range(n)]
+    if seed == 3:  # repeated pairs in both directions
+        rows = [r + r[:1] for r in rows]
+    ws = [rng.integers(1, 5, len(r)).astype(np.float32).tolist() for r in rows]
     indptr = np.cumsum([0] + [len(r) for r in rows]).astype(np.int32)
-    g = CoreGraph(np.array(sum(ws, []), np.float32), np.zeros(4, np.float32),
+    g = CoreGraph(np.array(sum(ws, []), np.float32), np.zeros(indptr[-1], np.float32),
                   np.array(sum(rows, []), np.int32), indptr)
-    sub = np.array([0, -1, -1, 1, -1, -1])
-    out = propagate_labels_per_cluster(g, sub.copy())
-    # 1: neighbour 0 (label 0, 1/1) beats 2 (noise); 2: neighbours 1 (0 after the
-    # sweep reaches it, 1/4) and 3 (label 1, 1/1) -> 1; 4: neighbour 3 -> 1
-    assert out.tolist() == [0, 0, 1, 1, 1, -1]
+    sub = rng.integers(-1, 3, n)
+    pts, counts, other, w = _noise_adjacency(g, sub, 100)
+    want = reference_noise_dicts(g, sub)
+    np.testing.assert_array_equal(pts - 100, np.nonzero(sub == -1)[0])
+    at = 0
+    for p, c in zip(pts - 100, counts):
+        got = list(zip((other[at:at + c] - 100).tolist(), w[at:at + c].tolist()))
+        assert got == list(want[p].items())
+        at += c
 
 
 def _cycle_rule_forest(weights, indices, indptr):

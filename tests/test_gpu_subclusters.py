@@ -175,3 +175,81 @@ def test_gpu_forest_matches_reference_fixture(engine, name):
     np.testing.assert_array_equal(g2.indices, g["indices"])
     np.testing.assert_array_equal(g2.weights, g["weights"])
     np.testing.assert_array_equal(forest2, g["edges"])
+
+
+def _reference_sweeps(graph, sub_labels):
+    """sub_clusters.py:145-166 restated as the checker: in-place sweeps over the
+    noise points in index order, until none is labelled (the reference would
+    loop forever on unreachable noise)."""
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_cpu_subclusters import reference_noise_dicts
+
+    lab = np.array(sub_labels).copy()
+    und = reference_noise_dicts(graph, lab)
+    while True:
+        changed = False
+        for idx in np.nonzero(lab == -1)[0]:
+            cand = {}
+            for nb, w in und[idx].items():
+                if lab[nb] == -1:
+                    continue
+                cand[lab[nb]] = cand.get(lab[nb], 0.0) + w
+            if not cand:
+                continue
+            best, bl = -np.inf, -1
+            for c, w in cand.items():
+                if w > best:
+                    best, bl = w, c
+            lab[idx] = bl
+            changed = True
+        if not changed:
+            return lab
+
+
+def _graph(rows, ws):
+    from fast_hdbscan_gb300.core_graph import CoreGraph
+
+    indptr = np.cumsum([0] + [len(r) for r in rows]).astype(np.int32)
+    return CoreGraph(np.array(sum(ws, []), np.float32), np.zeros(indptr[-1], np.float32),
+                     np.array(sum(rows, []), np.int32), indptr)
+
+
+def test_gpu_label_propagation_small_graph(engine):
+    """0 - 1 (w 1), 1 - 2 (w 4), 2 - 3 (w 1), 3 - 4 (w 2); 5 isolated: 1 takes 0's
+    label; 2 then weighs 1 (label 0, 1/4) against 3 (label 1, 1/1); 4 follows
+    3; 5 stays noise."""
+    from fast_hdbscan_gb300.sub_clusters import propagate_sub_cluster_labels
+
+    g = _graph([[1], [2], [3], [4], [], []], [[1.0], [4.0], [1.0], [2.0], [], []])
+    sub = np.array([0, -1, -1, 1, -1, -1], dtype=np.int64)
+    labels = np.zeros(6, dtype=np.int64)
+    propagate_sub_cluster_labels(labels, sub, [g], [np.arange(6)])
+    assert sub.tolist() == [0, 0, 1, 1, 1, -1]
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_gpu_label_propagation_matches_sweeps(engine, seed):
+    """Several clusters in one launch: every cluster's result equals the
+    reference's sequential sweeps; labels are renumbered cluster after
+    cluster."""
+    from fast_hdbscan_gb300.sub_clusters import propagate_sub_cluster_labels
+
+    rng = np.random.default_rng(seed)
+    graphs, subs, pts, at = [], [], [], 0
+    for c in range(5):
+        n = int(rng.integers(20, 120))
+        rows = [sorted(rng.choice(n, rng.integers(0, 5), replace=False).tolist())
+                for _ in range(n)]
+        ws = [rng.uniform(0.5, 3.0, len(r)).astype(np.float32).tolist() for r in rows]
+        graphs.append(_graph(rows, ws))
+        subs.append(rng.integers(-1, 3 if c != 2 else 1, n))  # cluster 2: noise + one label
+        pts.append(np.arange(at, at + n))
+        at += n
+    sub = np.concatenate(subs).astype(np.int64)
+    want = [_reference_sweeps(g, s) for g, s in zip(graphs, subs)]
+    labels = np.zeros(at, dtype=np.int64)
+    propagate_sub_cluster_labels(labels, sub, graphs, pts)
+    for p, w in zip(pts, want):
+        np.testing.assert_array_equal(sub[p], w)
