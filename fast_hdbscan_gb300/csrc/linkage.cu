@@ -74,7 +74,10 @@ struct __align__(32) NodeRec {
 // renumbered by the rank of their first edge, so a smaller label is an older
 // point).  A union links the younger root under the older one, so the points
 // a cluster absorbs within an interval link under the cluster's node -- each
-// its own record, no contended update -- and paths stay short.
+// its own record, no contended update -- and paths stay short.  The
+// renumbering only keeps the records an interval touches cache-resident: any
+// total age order gives a correct union-find, and the allocation-free entry
+// point runs on the raw point labels.
 __device__ __forceinline__ uint32_t age_key(int32_t x, int32_t n) {
     return x >= n ? (uint32_t)(x - n) : (uint32_t)x + 0x80000000u;
 }
@@ -527,8 +530,13 @@ __global__ void split_mst_kernel(int64_t m, const double* __restrict__ mst, int3
                                  int32_t* __restrict__ dst, double* __restrict__ w) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
-    src[i] = (int32_t)mst[3 * i + 0];
-    dst[i] = (int32_t)mst[3 * i + 1];
+    // Endpoints must be point ids in [0, m]; anything else (negative, too
+    // large, NaN) is clamped into range so that no node record outside the
+    // m + 1 points is ever addressed -- the tree is then meaningless, but
+    // memory stays safe.
+    const double a = mst[3 * i + 0], b = mst[3 * i + 1];
+    src[i] = (a >= 0.0 && a <= (double)m) ? (int32_t)a : 0;
+    dst[i] = (b >= 0.0 && b <= (double)m) ? (int32_t)b : 0;
     w[i] = mst[3 * i + 2];
 }
 __global__ void leaf_sizes_kernel(int64_t n, int32_t* __restrict__ size) {
