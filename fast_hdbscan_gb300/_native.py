@@ -31,6 +31,7 @@ SIGNATURES = {
     "fhg_last_error": (ctypes.c_char_p, []),
     "fhg_abi_version": (_INT, []),
     "fhg_set_tie_rule": (_INT, [_INT]),
+    "fhg_set_highd_kernel": (_INT, [_INT]),
     "fhg_release_cached_memory": (_INT, []),
     "fhg_index_build": (_INT, [_P, _I64, _I32, _P, ctypes.POINTER(_P)]),
     "fhg_reference_kdtree_levels": (_I32, [_I64]),

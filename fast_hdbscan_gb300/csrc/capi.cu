@@ -130,6 +130,14 @@ FHG_API int fhg_set_tie_rule(int rule) {
     return set_tie_rule(rule);
 }
 
+FHG_API int fhg_set_highd_kernel(int kernel) {
+    if (kernel != FHG_HD_TCGEN05 && kernel != FHG_HD_MMA_SYNC) {
+        set_error("fhg_set_highd_kernel: unknown kernel %d", kernel);
+        return -1;
+    }
+    return highd_use_legacy(kernel == FHG_HD_MMA_SYNC ? 1 : 0);
+}
+
 FHG_API int fhg_profile_enable(int on) {
     g_prof_on.store(on != 0);
     return FHG_OK;

@@ -31,11 +31,14 @@
 //    certified; the others (and none is assumed rare) are searched again.
 // 3. Fallback.  A warp per uncertified query scans every point in exact
 //    float32 with the same buffer-and-rank selection.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "highd.cuh"
+#include "tc.cuh"
 
 namespace fhg {
 namespace {
@@ -72,13 +75,18 @@ __global__ void __launch_bounds__(256) hd_mean_kernel(const float* __restrict__ 
 // Per point: the operand rows A = [hi, hi, lo] and B = [hi, lo, hi] (dp
 // columns each, zero-padded), |y|^2 (float32, dimension order), |c|, and the
 // running maxima of |y| and |c| (float bit patterns, non-negative).
-__global__ void hd_split_kernel(const float* __restrict__ X, int64_t n, int d, int dp,
+// Rows are kw >= 3 dp elements long (zero-padded: the tensor-core pipeline
+// takes whole 64-element row segments).
+__global__ void hd_split_kernel(const float* __restrict__ X, int64_t n, int d, int dp, int kw,
                                 const float* __restrict__ mu, __nv_bfloat16* __restrict__ A,
                                 __nv_bfloat16* __restrict__ B, float* __restrict__ ny,
                                 float* __restrict__ cn, unsigned* __restrict__ maxes) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int kw = 3 * dp;
+    for (int k = 3 * dp; k < kw; ++k) {
+        A[i * kw + k] = __float2bfloat16_rn(0.0f);
+        B[i * kw + k] = __float2bfloat16_rn(0.0f);
+    }
     float y2 = 0.0f, c2 = 0.0f;
     for (int k = 0; k < dp; ++k) {
         __nv_bfloat16 hi = __float2bfloat16_rn(0.0f), lo = hi;
@@ -353,6 +361,273 @@ __device__ __forceinline__ float hd_rdist(const float* __restrict__ q,
     return r;
 }
 
+// ------------------------------------------------- tcgen05 candidate GEMM
+// The same candidates as hd_cand_kernel, from a Blackwell pipeline: a CTA of
+// 128 queries holds their operand rows in shared memory (one TMA load), and
+// every point tile of 128 rows streams through a two-stage ring of shared
+// memory by TMA (cp.async.bulk.tensor, 128-byte swizzle); one thread issues
+// the 128 x 128 x 16 bf16 tcgen05.mma steps into a float32 accumulator in
+// tensor memory (two accumulators, so the next tile's products accumulate
+// while the last one is read); four warps read the accumulator rows
+// (tcgen05.ld, lane = query) and run the selection of hd_cand_kernel on them.
+//   warp 0  TMA producer        warp 1  MMA issuer (allocates TMEM)
+//   warps 4-7  epilogue: query row = 32 (warp - 4) + lane, the TMEM lane
+// Operand rows are padded to a multiple of 64 bf16 (KA atoms of 128 bytes).
+// The points' |y|^2 travel in their own four-slot ring, released by the
+// epilogue (the operand ring is released by the MMA, which runs ahead).
+constexpr int kTcBM = 128;       // queries per CTA (TMEM lanes)
+constexpr int kTcBN = 128;       // points per tile (accumulator columns)
+constexpr int kTcStages = 2;     // operand ring (gated by the MMA)
+constexpr int kTcNyStages = 4;   // |y|^2 ring (gated by the epilogue, which trails the MMA by
+                                 // at most two tiles: it never holds the producer back)
+constexpr int kTcSub = 8;        // estimates inserted between buffer checks
+constexpr int kTcThreads = 256;
+constexpr int kTcTmemCols = 2 * kTcBN;
+constexpr int kTcAtom = 128;     // bytes per swizzled operand row segment (64 bf16)
+
+__host__ __device__ constexpr int tc_cap(int L) { return (L + kTcSub + 7) / 8 * 8; }
+__host__ __device__ constexpr size_t tc_smem(int ka, int L) {
+    return (size_t)ka * kTcBM * kTcAtom                       // A
+           + (size_t)kTcStages * ka * kTcBN * kTcAtom         // B ring
+           + (size_t)kTcNyStages * kTcBN * sizeof(float)      // |y|^2 of the ring's points
+           + (size_t)kTcBM * tc_cap(L) * sizeof(unsigned long long)  // candidate buffers
+           + 1024;                                            // 1024-byte alignment slack
+}
+
+// hd_cut for buffers of up to 32 * PER entries (kept out of line: the
+// epilogue calls it rarely, from several places).
+template <int PER>
+__device__ __noinline__ int tc_cut(unsigned long long* buf, int cnt, int keep, int lane) {
+    unsigned long long mine[PER];
+    int rank[PER];
+#pragma unroll
+    for (int m = 0; m < PER; ++m) {
+        const int e = lane + 32 * m;
+        mine[m] = e < cnt ? buf[e] : ~0ull;
+        rank[m] = 0;
+    }
+    for (int e = 0; e < cnt; ++e) {
+        const unsigned long long o = buf[e];
+#pragma unroll
+        for (int m = 0; m < PER; ++m) rank[m] += o < mine[m] ? 1 : 0;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < PER; ++m)
+        if (lane + 32 * m < cnt && rank[m] < keep) buf[rank[m]] = mine[m];
+    __syncwarp();
+    return cnt < keep ? cnt : keep;
+}
+
+template <int KA, int PER>
+__global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
+    const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+    int64_t n, int L, int cap, const float* __restrict__ ny, int32_t* __restrict__ cand,
+    float* __restrict__ T, int* __restrict__ err) {
+    constexpr int kABytes = KA * kTcBM * kTcAtom;
+    constexpr int kBBytes = KA * kTcBN * kTcAtom;  // one stage
+    constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTcBM, kTcBN);
+    extern __shared__ unsigned char tc_smem_raw[];
+    // full: a stage's operand rows and |y|^2 landed; empty: the MMA read the
+    // stage's rows; nempty: the epilogue read a slot's |y|^2; tfull /
+    // tempty: an accumulator was written / read
+    __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], nempty[kTcNyStages],
+        tfull[2], tempty[2], afull, done;
+    __shared__ uint32_t tmem_slot;
+    unsigned char* base = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char* As = base;
+    unsigned char* Bs = As + kABytes;
+    float* nys = reinterpret_cast<float*>(Bs + kTcStages * kBBytes);
+    unsigned long long* bufs = reinterpret_cast<unsigned long long*>(nys + kTcNyStages * kTcBN);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t q0 = (int64_t)blockIdx.x * kTcBM;
+    const int64_t ntiles = (n + kTcBN - 1) / kTcBN;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTcStages; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int u = 0; u < kTcNyStages; ++u) tc::mbar_init(&nempty[u], 4 * 32);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 4 * 32);
+        }
+        tc::mbar_init(&afull, 1);
+        tc::mbar_init(&done, 1);
+        tc::fence_mbar_init();
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(&tmem_slot, kTcTmemCols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------------ TMA producer
+        if (tc::elect_one()) {
+            tc::prefetch_tmap(&mapA);
+            tc::prefetch_tmap(&mapB);
+            tc::mbar_arrive_expect_tx(&afull, kABytes);
+            for (int a = 0; a < KA; ++a)
+                tc::tma_load_2d(As + a * kTcBM * kTcAtom, &mapA, a * 64, (int32_t)q0, &afull);
+            int64_t issued = 0;
+            for (int64_t t = 0; t < ntiles; ++t) {
+                const int s = (int)(t % kTcStages);
+                const int u = (int)(t % kTcNyStages);
+                const uint32_t ph = (uint32_t)((t / kTcStages) & 1);
+                // the operand stage is free once the MMA has read tile
+                // t - kTcStages; the |y|^2 slot once the epilogue has read
+                // tile t - kTcNyStages
+                if (!tc::mbar_wait(&empty[s], ph ^ 1u, err, 1)) break;
+                if (!tc::mbar_wait(&nempty[u], (uint32_t)(((t / kTcNyStages) & 1) ^ 1), err, 7))
+                    break;
+                tc::mbar_arrive_expect_tx(&full[s], kBBytes + kTcBN * (uint32_t)sizeof(float));
+                unsigned char* dst = Bs + s * kBBytes;
+                for (int a = 0; a < KA; ++a)
+                    tc::tma_load_2d(dst + a * kTcBN * kTcAtom, &mapB, a * 64,
+                                    (int32_t)(t * kTcBN), &full[s]);
+                // |y|^2 of the tile's points (ny is padded to whole tiles)
+                tc::bulk_load(nys + u * kTcBN, ny + t * kTcBN, kTcBN * (uint32_t)sizeof(float),
+                              &full[s]);
+                issued = t + 1;
+            }
+            // no copy may still be in flight when the block exits
+            for (int64_t t = issued > kTcStages ? issued - kTcStages : 0; t < issued; ++t)
+                tc::mbar_drain(&full[t % kTcStages], (uint32_t)((t / kTcStages) & 1));
+            tc::mbar_drain(&afull, 0);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------- MMA issuer
+        if (tc::elect_one()) {
+            if (tc::mbar_wait(&afull, 0, err, 2)) {
+                for (int64_t t = 0; t < ntiles; ++t) {
+                    const int s = (int)(t % kTcStages);
+                    const int b = (int)(t & 1);
+                    if (!tc::mbar_wait(&full[s], (uint32_t)((t / kTcStages) & 1), err, 3)) break;
+                    if (!tc::mbar_wait(&tempty[b], (uint32_t)(((t >> 1) & 1) ^ 1), err, 4)) break;
+                    tc::tc_fence_after();
+                    const uint32_t d = tmem + (uint32_t)(b * kTcBN);
+                    const uint32_t a0 = tc::smem_u32(As), b0 = tc::smem_u32(Bs + s * kBBytes);
+#pragma unroll
+                    for (int a = 0; a < KA; ++a)
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)
+                            tc::mma_bf16(d,
+                                         tc::smem_desc_sw128(a0 + a * kTcBM * kTcAtom + kk * 32),
+                                         tc::smem_desc_sw128(b0 + a * kTcBN * kTcAtom + kk * 32),
+                                         kIdesc, (a | kk) != 0);
+                    tc::mma_commit(&empty[s]);
+                    tc::mma_commit(&tfull[b]);
+                }
+            }
+            // every issued product has landed before the accumulators are freed
+            tc::mma_commit(&done);
+            tc::mbar_drain(&done, 0);
+        }
+    } else if (warp >= 4) {
+        // -------------------------------------------------------- epilogue
+        const int quarter = warp & 3;
+        const int r = quarter * 32 + lane;
+        const int64_t q = q0 + r;
+        const float nq = q < n ? ny[q] : 0.0f;
+        unsigned long long* row = bufs + (size_t)r * cap;
+        float tq = INFINITY;
+        int cnt = 0;
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        for (int64_t t = 0; t < ntiles; ++t) {
+            const int b = (int)(t & 1);
+            if (!tc::mbar_wait(&tfull[b], (uint32_t)((t >> 1) & 1), err, 6)) break;
+            tc::tc_fence_after();
+            const int u = (int)(t % kTcNyStages);
+            const float* hy = nys + u * kTcBN;
+            const int64_t jb = t * kTcBN;
+            // 32 accumulator columns at a time; the accumulator is handed back
+            // to the MMA as soon as its last columns are in registers
+#pragma unroll 1
+            for (int c = 0; c < kTcBN / 32; ++c) {
+                uint32_t acc[32];
+                tc::tmem_ld32(tmem + lane_base + (uint32_t)(b * kTcBN + c * 32), acc);
+                tc::tmem_wait_ld();
+                if (c == kTcBN / 32 - 1) {
+                    tc::tc_fence_before();
+                    tc::mbar_arrive(&tempty[b]);
+                }
+                // estimates of 32 columns, 8 between buffer checks; only the
+                // last tile has columns past the points
+                auto columns = [&](auto whole_tag) {
+                    constexpr bool whole = decltype(whole_tag)::value;
+                    const float* h = hy + c * 32;
+                    const int64_t j0 = jb + c * 32;
+#pragma unroll
+                    for (int sub = 0; sub < 32 / kTcSub; ++sub) {
+                        float e[kTcSub];
+                        int pass = 0;
+#pragma unroll
+                        for (int i = 0; i < kTcSub; ++i) {
+                            const int col = sub * kTcSub + i;
+                            const float dot = __uint_as_float(acc[col]);
+                            e[i] = fmaxf(__fsub_rn(__fadd_rn(nq, h[col]), __fmul_rn(2.0f, dot)),
+                                         0.0f);
+                            if (!whole && j0 + col >= n) e[i] = INFINITY;
+                            pass += e[i] < tq ? 1 : 0;
+                        }
+                        // a row whose buffer cannot take these is first cut
+                        // back to its L smallest (which only tightens its
+                        // threshold)
+                        unsigned rows = __ballot_sync(0xffffffffu, cnt + pass > cap);
+                        if (rows) {
+                            __syncwarp();  // every lane's buffer writes visible to the warp
+                            do {
+                                const int rr = __ffs(rows) - 1;
+                                rows &= rows - 1u;
+                                const int cc = __shfl_sync(0xffffffffu, cnt, rr);
+                                unsigned long long* rb = bufs + (size_t)(quarter * 32 + rr) * cap;
+                                const int kept = tc_cut<PER>(rb, cc, L, lane);
+                                if (lane == rr) {
+                                    cnt = kept;
+                                    tq = kept >= L ? hd_dist(rb[L - 1]) : INFINITY;
+                                }
+                            } while (rows);
+                        }
+                        if (pass) {
+#pragma unroll
+                            for (int i = 0; i < kTcSub; ++i)
+                                if (e[i] < tq)
+                                    row[cnt++] = hd_key(e[i], (int32_t)(j0 + sub * kTcSub + i));
+                        }
+                    }
+                };
+                if (jb + kTcBN <= n) columns(std::true_type{});
+                else columns(std::false_type{});
+            }
+            tc::mbar_arrive(&nempty[u]);  // this tile's |y|^2 are read
+        }
+        // the L smallest estimates of every row, and its L-th estimate
+        __syncwarp();
+        for (int rr = 0; rr < 32; ++rr) {
+            const int cc = __shfl_sync(0xffffffffu, cnt, rr);
+            unsigned long long* rb = bufs + (size_t)(quarter * 32 + rr) * cap;
+            const int kept = tc_cut<PER>(rb, cc, L, lane);
+            const int64_t qq = q0 + quarter * 32 + rr;
+            if (qq < n) {
+                for (int e2 = lane; e2 < L; e2 += 32)
+                    cand[qq * L + e2] = e2 < kept ? (int32_t)(uint32_t)rb[e2] : -1;
+                if (lane == 0) T[qq] = kept >= L ? hd_dist(rb[L - 1]) : INFINITY;
+            }
+            __syncwarp();
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == 1) tc::tmem_dealloc(tmem, kTcTmemCols);
+}
+
 // Re-rank: a warp per query.  Writes the certified queries' k nearest (rows
 // of k, (distance, index) order) and lists the others.
 __global__ void __launch_bounds__(128) hd_rerank_kernel(
@@ -515,7 +790,91 @@ int launch_cand(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B
     return launch_cand_w<KB, 4, 1>(n, L, cap, A, B, ny, cand, T, s);
 }
 
+// cuTensorMapEncodeTiled from the driver, without linking libcuda.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+int tensor_map_rows(CUtensorMap* map, const __nv_bfloat16* base, int64_t rows, int kw,
+                    int box_rows) {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        FHG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                  cudaEnableDefault, &q));
+        if (!p || q != cudaDriverEntryPointSuccess) {
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return FHG_ERR_CUDA;
+        }
+        fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    const cuuint64_t gdim[2] = {(cuuint64_t)kw, (cuuint64_t)rows};
+    const cuuint64_t gstride[1] = {(cuuint64_t)kw * sizeof(__nv_bfloat16)};
+    const cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+    const cuuint32_t estride[2] = {1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                          const_cast<__nv_bfloat16*>(base), gdim, gstride, box, estride,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return FHG_ERR_CUDA;
+    }
+    return FHG_OK;
+}
+
+template <int KA, int PER>
+int launch_cand_tc(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
+                   const float* ny_padded, int32_t* cand, float* T, int* err, cudaStream_t s) {
+    CUtensorMap ma, mb;
+    FHG_TRY(tensor_map_rows(&ma, A, n, KA * 64, kTcBM));
+    FHG_TRY(tensor_map_rows(&mb, B, n, KA * 64, kTcBN));
+    const size_t smem = tc_smem(KA, L);
+    FHG_CUDA(cudaFuncSetAttribute(hd_cand_tc_kernel<KA, PER>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t blocks = (n + kTcBM - 1) / kTcBM;
+    Stage stage(s, "hd_cand_kernel");
+    ::fhg::note_launch();
+    hd_cand_tc_kernel<KA, PER><<<(unsigned)blocks, kTcThreads, smem, s>>>(
+        ma, mb, n, L, tc_cap(L), ny_padded, cand, T, err);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
+// The tensor-core pipeline's operand atoms for (dp, L), or 0 when the
+// mma.sync kernel must run (rows of 96 dimensions, or buffers too large for
+// shared memory).
+int tc_atoms(int dp, int L) {
+    const int ka = dp == 32 ? 2 : (dp == 64 ? 3 : 0);
+    if (ka == 0 || tc_cap(L) > 32 * 4 || tc_smem(ka, L) > (size_t)kHdSmemMax) return 0;
+    return ka;
+}
+
+int launch_cand_tc_any(int ka, int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
+                       const float* ny_padded, int32_t* cand, float* T, int* err,
+                       cudaStream_t s) {
+    const int per = (tc_cap(L) + 31) / 32;
+#define FHG_TC(KA, PER)                                                                     \
+    if (ka == KA && per == PER)                                                             \
+        return launch_cand_tc<KA, PER>(n, L, A, B, ny_padded, cand, T, err, s);
+    FHG_TC(2, 1) FHG_TC(2, 2) FHG_TC(2, 3) FHG_TC(2, 4)
+    FHG_TC(3, 1) FHG_TC(3, 2) FHG_TC(3, 3) FHG_TC(3, 4)
+#undef FHG_TC
+    set_error("tensor-core kNN: no pipeline for %d atoms, %d-entry buffers", ka, tc_cap(L));
+    return FHG_ERR_UNSUPPORTED;
+}
+
 }  // namespace
+
+// Which candidate kernel the calling thread's high-dimensional kNN uses: the
+// tcgen05 pipeline (default) or the mma.sync kernel.
+static thread_local int t_hd_legacy = 0;
+int highd_use_legacy(int on) {
+    const int old = t_hd_legacy;
+    t_hd_legacy = on;
+    return old;
+}
 
 int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_o,
               int64_t* fallbacks, cudaStream_t s) {
@@ -535,8 +894,10 @@ int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_
     if (n <= 0) return FHG_OK;
     Stage stage(s, "highd_knn");
     const int dp = d <= 32 ? 32 : (d <= 64 ? 64 : 96);
-    const int kw = 3 * dp;
     const int L = k + 32;
+    const int ka = t_hd_legacy ? 0 : tc_atoms(dp, L);
+    const int kw = ka ? 64 * ka : 3 * dp;
+    const int64_t n_pad = (n + kTcBN - 1) / kTcBN * kTcBN;
     Workspace ws(s);
     float *mu, *ny, *cn, *T;
     unsigned* maxes;
@@ -544,7 +905,7 @@ int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_
     int32_t *cand, *flist;
     unsigned long long* fcount;
     FHG_TRY(ws.alloc(&mu, (size_t)d));
-    FHG_TRY(ws.alloc(&ny, (size_t)n));
+    FHG_TRY(ws.alloc(&ny, (size_t)n_pad));  // whole point tiles for the bulk copies
     FHG_TRY(ws.alloc(&cn, (size_t)n));
     FHG_TRY(ws.alloc(&T, (size_t)n));
     FHG_TRY(ws.alloc(&maxes, 2));
@@ -555,15 +916,30 @@ int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_
     FHG_TRY(ws.alloc(&fcount, 1));
     FHG_CUDA(cudaMemsetAsync(maxes, 0, 2 * sizeof(unsigned), s));
     FHG_CUDA(cudaMemsetAsync(fcount, 0, sizeof(unsigned long long), s));
+    if (n_pad > n) FHG_CUDA(cudaMemsetAsync(ny + n, 0, sizeof(float) * (size_t)(n_pad - n), s));
     ::fhg::note_launch();
     hd_mean_kernel<<<d, 256, 0, s>>>(X, n, d, mu);
     ::fhg::note_launch();
-    hd_split_kernel<<<grid_for(n, 128), 128, 0, s>>>(X, n, d, dp, mu, A, B, ny, cn, maxes);
+    hd_split_kernel<<<grid_for(n, 128), 128, 0, s>>>(X, n, d, dp, kw, mu, A, B, ny, cn, maxes);
     FHG_CUDA(cudaGetLastError());
-    switch (dp) {
-        case 32: FHG_TRY(launch_cand<6>(n, L, A, B, ny, cand, T, s)); break;
-        case 64: FHG_TRY(launch_cand<12>(n, L, A, B, ny, cand, T, s)); break;
-        default: FHG_TRY(launch_cand<18>(n, L, A, B, ny, cand, T, s)); break;
+    if (ka) {
+        int* err;
+        FHG_TRY(ws.alloc(&err, 1));
+        FHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+        FHG_TRY(launch_cand_tc_any(ka, n, L, A, B, ny, cand, T, err, s));
+        int h_err = 0;
+        FHG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FHG_CUDA(cudaStreamSynchronize(s));
+        if (h_err) {
+            set_error("tensor-core kNN pipeline: a wait ran out (stage %d)", h_err);
+            return FHG_ERR_CUDA;
+        }
+    } else {
+        switch (dp) {
+            case 32: FHG_TRY(launch_cand<6>(n, L, A, B, ny, cand, T, s)); break;
+            case 64: FHG_TRY(launch_cand<12>(n, L, A, B, ny, cand, T, s)); break;
+            default: FHG_TRY(launch_cand<18>(n, L, A, B, ny, cand, T, s)); break;
+        }
     }
     {
         Stage st(s, "hd_rerank_kernel");

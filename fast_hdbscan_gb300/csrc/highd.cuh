@@ -13,5 +13,8 @@ constexpr int kHighdMaxDim = 96;
 // searched again exactly.
 int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_o,
               int64_t* fallbacks, cudaStream_t s);
+// Candidate kernel of the calling thread's later calls: 0 the tcgen05
+// pipeline (where its buffers fit), 1 the mma.sync kernel.  Returns the old.
+int highd_use_legacy(int on);
 
 }  // namespace fhg

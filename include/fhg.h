@@ -16,10 +16,12 @@
  *     message for the calling thread's last failure.
  *   - Scratch memory is taken with cudaMallocAsync on `stream` and released
  *     on the same stream before the call returns.
- *   - Ties are broken by a total order on point indices: kNN lists by
- *     (distance, index); a Boruvka component's outgoing edge by
+ *   - Ties are broken by a total order on point indices by default: kNN
+ *     lists by (distance, index); a Boruvka component's outgoing edge by
  *     (weight, min endpoint, max endpoint).  On tie-free input this yields the
- *     reference's core distances, kNN lists and MST weight multiset exactly.
+ *     reference's core distances, kNN lists and MST weight multiset exactly;
+ *     fhg_set_tie_rule(FHG_TIES_REFERENCE) makes the Boruvka edge choices the
+ *     reference's own as well.
  */
 #ifndef FHG_H
 #define FHG_H
@@ -116,8 +118,10 @@ int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t* idx_de
 
 /* Replaces boruvka.py:542 parallel_boruvka(tree, n_threads, min_samples,
  * sample_weights, reproducible): the minimum spanning tree of the
- * mutual-reachability graph.  The result does not depend on `reproducible`
- * or on any thread count: ties are broken by a total order on indices.
+ * mutual-reachability graph.  The result does not depend on any thread
+ * count; among equal weights it makes the choices of the calling thread's
+ * tie rule (fhg_set_tie_rule: a total order on indices, or the reference's
+ * own choices -- its `reproducible` flag in this library).
  *   sample_weights_dev NULL, or n float32 weights (caller order): the
  *                 reference's weighted path (boruvka.py:561-573), which queries
  *                 k = weighted_k = int(2 * min_samples / mean weight)
@@ -367,6 +371,19 @@ int fhg_hdbscan_fit_precomputed(const int32_t* rows_dev, const int32_t* cols_dev
                                 float* ct_lambda_dev, float* ct_size_dev, int64_t* ct_rows_host,
                                 int32_t* neighbors_dev, double* core_dev, int64_t* selected_dev,
                                 int64_t* n_selected_host, void* stream);
+
+/* Candidate kernel of the exact high-dimensional kNN (fhg_highd_knn and the
+ * d > 30 fits) for later calls from the calling thread; returns the previous
+ * choice.  No counterpart in the reference (its d > 30 route is pynndescent).
+ *   FHG_HD_TCGEN05 (default): a Blackwell pipeline -- TMA loads of the
+ *     operand tiles into shared memory, tcgen05.mma into tensor-memory
+ *     accumulators, candidate selection in the epilogue warps -- for padded
+ *     depths of 32 and 64 with k <= 32 (the others fall back);
+ *   FHG_HD_MMA_SYNC: the warp-level mma.sync kernel.
+ * Both give the same certified kNN. */
+#define FHG_HD_TCGEN05 0
+#define FHG_HD_MMA_SYNC 1
+int fhg_set_highd_kernel(int kernel);
 
 /* Exact kNN of every point of X (n x d float32, 1 <= d <= 96) by brute force:
  * bfloat16 tensor-core candidates (k + 32 per query, from a two-term bf16

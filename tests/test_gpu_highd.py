@@ -112,3 +112,30 @@ def test_knn_graph_fit_equals_oracle(engine):
     np.testing.assert_array_equal(est.labels_, labels)
     np.testing.assert_array_equal(est.probabilities_, probs)
     assert len(set(labels.tolist()) - {-1}) >= 2
+
+
+@pytest.mark.parametrize("n,d,k", [(100, 40, 5), (1000, 20, 31), (4999, 64, 31),
+                                   (20_000, 64, 16), (40_000, 48, 31)])
+def test_tcgen05_pipeline_equals_mma_sync_kernel(engine, n, d, k):
+    """The tcgen05 candidate pipeline (TMA, tensor memory, epilogue
+    selection) and the mma.sync kernel give the same certified kNN, equal to
+    the oracle's exact kNN -- on ragged last tiles and on fewer points than
+    one tile."""
+    from fast_hdbscan_gb300 import _native
+    from oracle import oracle as O
+
+    X = synthetic.aniso_highdim(n=n, seed=50 + d, dim=d, n_comp=7)
+    lib = _native.load()
+    assert lib.fhg_set_highd_kernel(0) == 0
+    rd_tc, ix_tc, fb_tc = _highd(X, k)
+    lib.fhg_set_highd_kernel(1)
+    try:
+        rd_ms, ix_ms, fb_ms = _highd(X, k)
+    finally:
+        lib.fhg_set_highd_kernel(0)
+    np.testing.assert_array_equal(ix_tc, ix_ms)
+    np.testing.assert_array_equal(rd_tc, rd_ms)
+    rd_o, ix_o = O.tree_query(O.build_kdtree(X), k, mode=1, nthreads=NTH)
+    np.testing.assert_array_equal(ix_tc, ix_o)
+    np.testing.assert_array_equal(rd_tc, rd_o)
+    print("n=%d d=%d k=%d: fallbacks tcgen05 %d, mma.sync %d" % (n, d, k, fb_tc, fb_ms))
