@@ -80,6 +80,10 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-radius", action="store_true", help="skip the learned-radius arm")
+    ap.add_argument("--no-ref-ties", action="store_true",
+                    help="skip the reference-tie-mode arm (reproducible=True)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-instances figure of the default line")
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="points per CPU fit (default: the workload's own size)")
     ap.add_argument("--workload", default="fit", choices=["fit", "batched", *OTHER_WORKLOADS],
@@ -220,11 +224,14 @@ def knn_stage_bytes(n, k, d):
 
 # The high-dimensional candidate kernel: GEMM depth per point pair and the
 # instruction path (kept beside the algorithmic 2 n^2 d count).
-HD_KERNEL_NOTE = "mma.sync m16n8k16 bf16, two-term split (hi, lo): depth 3 x padded d"
+HD_KERNEL_NOTE = ("tcgen05.mma 128x128x16 bf16 into tensor memory, TMA operand tiles, "
+                  "two-term split (hi, lo): depth 3 x padded d rounded up to 64")
 
 
 def hd_kernel_depth(d):
-    return 3 * (32 if d <= 32 else (64 if d <= 64 else 96))
+    if d <= 64:  # the tcgen05 pipeline's rows: whole 64-element segments
+        return -(-3 * (32 if d <= 32 else 64) // 64) * 64
+    return 3 * 96
 
 
 def traffic_per_point(kernel):
@@ -383,7 +390,8 @@ def run_gb300(args):
                     "launches_per_step": cnt // max(args.steps, 1),
                     "ms_per_launch": round(per_launch_ms, 4),
                     "kernel_share_of_stage_time": round(tot_ms / total_stage, 4),
-                    "note": HD_KERNEL_NOTE}
+                    "note": HD_KERNEL_NOTE if d <= 64 and knn_k + 1 <= 32 else
+                    "mma.sync m16n8k16 bf16, two-term split (hi, lo): depth 3 x padded d"}
     elif dom:
         kq = (max(knn_k, ms) if kruskal else ms) + 1
         comps = stages.get("boruvka_components")
@@ -522,6 +530,46 @@ def run_gb300(args):
                    "identical_labels": bool(torch.equal(labels, lab_plain)
                                             and torch.equal(probs, prob_plain))}
 
+    # the reference tie mode (reproducible=True): the same fit making the
+    # reference's own choices among equal-weight edges (its KD-tree built
+    # exactly on the GPU, a tie walk per component and round); the tests
+    # check its output against the reference's rules bit for bit
+    ref_ties = None
+    if not (pre or kruskal or kgraph or args.no_ref_ties):
+        old_rule = lib.fhg_set_tie_rule(1)
+        try:
+            for _ in range(args.warmup):
+                step()
+            barrier()
+            lib.fhg_profile_report(None, 0)
+            lib.fhg_profile_enable(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                step()
+            e1.record(stream)
+            barrier()
+            lib.fhg_profile_enable(0)
+            rbuf = ctypes.create_string_buffer(1 << 16)
+            lib.fhg_profile_report(rbuf, len(rbuf))
+            rst = json.loads(rbuf.value.decode() or "{}")
+        finally:
+            lib.fhg_set_tie_rule(old_rule)
+        ms_ref = max_over_ranks(e0.elapsed_time(e1) / args.steps, torch.device("cuda", local))
+        ref_ties = {"value": round(n * world / (ms_ref / 1e3), 1), "unit": "points/s",
+                    "ms_per_step": round(ms_ref, 3), "vs_plain": round(ms_step_max / ms_ref, 4),
+                    "stages_ms_per_step": {k: round(v[0] / args.steps, 3)
+                                           for k, v in rst.items()
+                                           if k in ("ref_tree_build", "tie_walk_kernel",
+                                                    "boruvka_search", "boruvka_merge")}}
+
+    # many independent fits of uneven size in one call (the batched
+    # executor), on the benchmark family's 4,096-instance batch
+    batched = None
+    if rank == 0 and not (pre or kruskal or kgraph or args.no_batched):
+        batched = batched_summary()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(_cpu_sample_n(args))
@@ -543,6 +591,8 @@ def run_gb300(args):
                             if k not in nested},
             "boruvka_rounds": rounds,
             "learned_radius": learned,
+            "reference_ties": ref_ties,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -643,6 +693,33 @@ def run_reference(args):
 
 
 # ------------------------------------------------ batched independent fits
+def batched_summary(instances=4096):
+    """One timed pass of fit_many over the 4,096-instance batch (sizes
+    log-uniform 200..200k, d 2..8, min_samples in {5, 10, 20},
+    min_cluster_size = max(10, n / 100)) after a warm-up on its first 64
+    instances; host arrays in, host labels and probabilities out."""
+    import torch
+    from fast_hdbscan_gb300 import synthetic
+    from fast_hdbscan_gb300.batch import fit_many
+
+    inst = synthetic.batch_instances(instances, seed=4)
+    Xs = [X for X, _, _ in inst]
+    ms = [m for _, m, _ in inst]
+    mcs = [c for _, _, c in inst]
+    total = sum(X.shape[0] for X in Xs)
+    fit_many(Xs[:64], ms[:64], mcs[:64], workers=16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fit_many(Xs, ms, mcs, workers=16)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    return {"value": round(len(Xs) / t, 2), "unit": "instances/s",
+            "points_per_s": round(total / t, 1), "s_total": round(t, 3),
+            "instances": len(Xs), "points": total, "workers": 16,
+            "workload": "batched_uneven_instances (bench.py --workload batched for the full "
+                        "report)"}
+
+
 def run_batched(args):
     """Many independent fits of uneven size (log-uniform 200..200k points, d
     2..8, 3-12 Gaussian blobs + 5 % noise, min_samples in {5, 10, 20},
