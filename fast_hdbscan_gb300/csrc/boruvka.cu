@@ -422,7 +422,23 @@ __global__ void __launch_bounds__(kSW * 32) search_kernel(
             co[lane] = ix.orig[base + lane];
         }
         __syncwarp();
-        for (int t = 0; t < cnt; ++t) {
+        // Only candidates that can matter to some needing lane are visited:
+        // a core distance within the largest needing threshold, and -- when
+        // every needing lane is in one component -- outside it.  The best
+        // edge is a minimum over (weight, index), so the order of the visits
+        // does not change it.
+        const unsigned needers = __ballot_sync(kFull, need);
+        const float mthr =
+            __uint_as_float(__reduce_max_sync(kFull, need ? __float_as_uint(thr) : 0u));
+        const int32_t c0 = __shfl_sync(kFull, c, __ffs(needers) - 1);
+        const bool one_comp = __all_sync(kFull, !need || c == c0);
+        bool relevant = false;
+        if (lane < cnt) {
+            const int2 mine = cc[lane];
+            relevant = !(__int_as_float(mine.y) > mthr) && !(one_comp && mine.x == c0);
+        }
+        for (unsigned todo = __ballot_sync(kFull, relevant); todo; todo &= todo - 1u) {
+            const int t = __ffs(todo) - 1;
             const int2 tcc = cc[t];
             const float tk = __int_as_float(tcc.y);
             if (need && tcc.x != c && tk <= thr) {
