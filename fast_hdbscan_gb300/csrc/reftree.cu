@@ -22,8 +22,10 @@
 //     thread block runs each partition in parallel with the same result;
 //   * insertion sort and heapsort both leave their range in ascending order,
 //     which under a total order is unique: a block sorts the range instead.
-// One thread block per node of a level runs that node's whole introselect;
-// the levels run one after another.
+// One thread block per node of a level runs that node's introselect; while a
+// node's active range is long (the top levels), its partition steps run on
+// the whole GPU instead, every such node of the level in the same launches.
+// The levels run one after another.
 #include <cmath>
 
 #include "index.cuh"
@@ -37,6 +39,16 @@ constexpr int kSelThreads = 512;
 constexpr int kSelV = 8;                          // consecutive keys per thread and tile
 constexpr int kSelTile = kSelThreads * kSelV;     // keys per scan tile
 constexpr int kBlockSortMax = 4096;               // ranges a block sorts in shared memory
+constexpr int64_t kWideMin = 32768;               // longer ranges partition device-wide
+
+// The saved introselect state of a node partitioned device-wide.
+constexpr int kWideActive = 0, kWideBlock = 1, kWideDone = 2;
+struct WideNode {
+    int64_t l, r, B;
+    uint64_t pivot;
+    int32_t depth, state;
+    uint32_t c, K;
+};
 
 #define LAUNCH(kernel, count, ...)                                                   \
     do {                                                                             \
@@ -244,6 +256,198 @@ __device__ void block_sort(uint64_t* keys, int64_t l, int64_t r, uint64_t* s_buf
     __syncthreads();
 }
 
+// ------------------------------------------------ device-wide partitions
+// A level with few nodes leaves most of the GPU idle while one block per
+// node partitions millions of keys.  While a node's active range is longer
+// than kWideMin, its partitions run on the whole GPU instead: the same
+// median-of-three, the same pairing of misplaced elements, with the prefix
+// counts taken over tiles of kSelTile keys, every such node of the level in
+// the same launches.  The block kernel then continues from the saved state.
+__device__ __forceinline__ int wide_node_of(const int64_t* __restrict__ tile_off, int count,
+                                            int64_t tile) {
+    int lo = 0, hi = count - 1;  // last node whose first tile <= tile
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tile_off[mid] <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One block: per node, start (init) or continue a partition step; tiles of
+// the step's range, their prefix over nodes, and in ctl the total of tiles
+// and the number of nodes partitioned in this step.
+__global__ void __launch_bounds__(kSelThreads) wide_setup_kernel(
+    int64_t first, int count, const int64_t* __restrict__ rs, const int64_t* __restrict__ re,
+    int64_t n_nodes, int init, uint64_t* keys, WideNode* wide, int64_t* __restrict__ tile_off,
+    int64_t* __restrict__ ctl) {
+    __shared__ uint32_t s_warp[65];
+    __shared__ int64_t s_carry;
+    __shared__ int s_active;
+    if (threadIdx.x == 0) {
+        s_carry = 0;
+        s_active = 0;
+    }
+    __syncthreads();
+    for (int base = 0; base < count; base += kSelThreads) {
+        const int t = base + threadIdx.x;
+        int64_t tiles = 0;
+        if (t < count) {
+            WideNode w = wide[t];
+            if (init) {
+                const int64_t v = first + t, s0 = rs[v], e0 = re[v], m = e0 - s0;
+                w.l = s0;
+                w.r = e0;
+                w.depth = m > 16 ? 2 * (63 - __clzll((unsigned long long)m)) : 0;
+                w.state = (2 * v + 1 >= n_nodes || m < 2) ? kWideDone : kWideActive;
+            }
+            if (w.state == kWideActive) {
+                const int64_t l = w.l, r = w.r, m = r - l;
+                if (m <= kWideMin || w.depth == 0) {
+                    w.state = kWideBlock;  // the block kernel takes over (or sorts)
+                } else {
+                    --w.depth;
+                    const int64_t mid = (l + r - 1) / 2;  // numba_kdtree.py:282
+                    if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
+                    if (keys[mid] > keys[r - 1]) {
+                        swap_keys(keys, mid, r - 1);
+                        if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
+                    }
+                    swap_keys(keys, mid, r - 1);
+                    w.pivot = keys[r - 1];
+                    w.K = 0;
+                    tiles = (m - 1 + kSelTile - 1) / kSelTile;
+                    atomicAdd(&s_active, 1);
+                }
+            }
+            wide[t] = w;
+        }
+        uint32_t before;
+        const uint32_t sum = block_exclusive((uint32_t)tiles, &before, s_warp);
+        if (t < count) tile_off[t] = s_carry + before;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += sum;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctl[0] = s_carry;   // tiles of this step, over all nodes
+        ctl[1] = s_active;  // nodes partitioned in this step
+    }
+}
+
+// Elements below the pivot in one tile of a node's step range [l, r - 1).
+__global__ void __launch_bounds__(kSelThreads) wide_count_kernel(
+    int count, const int64_t* __restrict__ tile_off, const WideNode* __restrict__ wide,
+    const uint64_t* __restrict__ keys, uint32_t* __restrict__ tile_small) {
+    __shared__ uint32_t s_warp[65];
+    const int64_t tile = blockIdx.x;
+    const int t = wide_node_of(tile_off, count, tile);
+    const WideNode w = wide[t];
+    const int64_t p0 = w.l + (tile - tile_off[t]) * kSelTile + (int64_t)threadIdx.x * kSelV;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int j = 0; j < kSelV; ++j) {
+        const int64_t p = p0 + j;
+        cnt += (p < w.r - 1 && keys[p] < w.pivot) ? 1u : 0u;
+    }
+    uint32_t dummy;
+    const uint32_t total = block_exclusive(cnt, &dummy, s_warp);
+    if (threadIdx.x == 0) tile_small[tile] = total;
+}
+
+// One block per node: the tiles' exclusive prefix of their counts, the
+// node's count c and the pivot's final place B = l + c.
+__global__ void __launch_bounds__(kSelThreads) wide_scan_kernel(
+    int count, const int64_t* __restrict__ tile_off, const int64_t* __restrict__ ctl,
+    WideNode* wide, const uint32_t* __restrict__ tile_small, uint32_t* __restrict__ tile_base) {
+    __shared__ uint32_t s_warp[65];
+    const int t = blockIdx.x;
+    const WideNode w = wide[t];
+    if (w.state != kWideActive) return;
+    const int64_t a = tile_off[t], b = t + 1 < count ? tile_off[t + 1] : ctl[0];
+    uint32_t carry = 0;
+    for (int64_t i0 = a; i0 < b; i0 += kSelThreads) {
+        const int64_t i = i0 + threadIdx.x;
+        uint32_t before;
+        const uint32_t sum = block_exclusive(i < b ? tile_small[i] : 0u, &before, s_warp);
+        if (i < b) tile_base[i] = carry + before;
+        carry += sum;
+    }
+    if (threadIdx.x == 0) {
+        wide[t].c = carry;
+        wide[t].B = w.l + carry;
+    }
+}
+
+// select_level_kernel's pairing, over tiles: elements above the pivot left
+// of B, ranked from the left, and elements below it from B on, ranked from
+// the right; K counts the pairs.
+__global__ void __launch_bounds__(kSelThreads) wide_rank_kernel(
+    int count, const int64_t* __restrict__ tile_off, WideNode* wide,
+    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ tile_base,
+    int32_t* __restrict__ pos_big, int32_t* __restrict__ pos_small) {
+    __shared__ uint32_t s_warp[65];
+    const int64_t tile = blockIdx.x;
+    const int t = wide_node_of(tile_off, count, tile);
+    const WideNode w = wide[t];
+    const int64_t l = w.l, r = w.r, B = w.B;
+    const uint32_t c = w.c;
+    const int64_t p0 = l + (tile - tile_off[t]) * kSelTile + (int64_t)threadIdx.x * kSelV;
+    uint64_t kv[kSelV];
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int j = 0; j < kSelV; ++j) {
+        const int64_t p = p0 + j;
+        kv[j] = p < r - 1 ? keys[p] : 0ull;
+        cnt += (p < r - 1 && kv[j] < w.pivot) ? 1u : 0u;
+    }
+    uint32_t before;
+    block_exclusive(cnt, &before, s_warp);
+    before += tile_base[tile];
+    uint32_t kb = 0;
+#pragma unroll
+    for (int j = 0; j < kSelV; ++j) {
+        const int64_t p = p0 + j;
+        if (p >= r - 1) break;
+        const bool small = kv[j] < w.pivot;
+        if (p < B && !small) {
+            pos_big[l + (p - l) - before] = (int32_t)p;
+            ++kb;
+        } else if (p >= B && small) {
+            pos_small[l + (c - 1 - before)] = (int32_t)p;
+        }
+        before += small ? 1u : 0u;
+    }
+    kb = __reduce_add_sync(kFull, kb);
+    if ((threadIdx.x & 31) == 0 && kb) atomicAdd(&wide[t].K, kb);
+}
+
+__global__ void __launch_bounds__(kSelThreads) wide_swap_kernel(
+    int count, const int64_t* __restrict__ tile_off, const WideNode* __restrict__ wide,
+    uint64_t* keys, const int32_t* __restrict__ pos_big, const int32_t* __restrict__ pos_small) {
+    const int64_t tile = blockIdx.x;
+    const int t = wide_node_of(tile_off, count, tile);
+    const WideNode w = wide[t];
+    const int64_t k0 = (tile - tile_off[t]) * kSelTile;
+    for (int64_t k = k0 + threadIdx.x; k < k0 + kSelTile && k < (int64_t)w.K; k += kSelThreads)
+        swap_keys(keys, pos_big[w.l + k], pos_small[w.l + k]);
+}
+
+// The pivot to its place; the range narrows to the side holding the median.
+__global__ void wide_finish_kernel(int count, WideNode* wide, uint64_t* keys, int64_t first,
+                                   const int64_t* __restrict__ rs, const int64_t* __restrict__ re) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    WideNode w = wide[t];
+    if (w.state != kWideActive) return;
+    swap_keys(keys, w.B, w.r - 1);
+    const int64_t v = first + t, nth = rs[v] + (re[v] - rs[v]) / 2;
+    if (nth < w.B) w.r = w.B;
+    else if (nth > w.B) w.l = w.B + 1;
+    else w.state = kWideDone;
+    wide[t] = w;
+}
+
 // One block per internal node of the level: the reference's introselect of
 // the node's range around its median position (numba_kdtree.py:395
 // _introselect, :372 _introselect_impl).  pos_big / pos_small: per-node
@@ -254,10 +458,11 @@ __device__ void block_sort(uint64_t* keys, int64_t l, int64_t r, uint64_t* s_buf
 __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
     int64_t first, const int64_t* __restrict__ rs, const int64_t* __restrict__ re,
     int64_t n_nodes, uint64_t* keys, int32_t* __restrict__ pos_big,
-    int32_t* __restrict__ pos_small, int64_t* __restrict__ big_sort, int* big_sort_count) {
+    int32_t* __restrict__ pos_small, int64_t* __restrict__ big_sort, int* big_sort_count,
+    const WideNode* __restrict__ wide) {
     __shared__ uint64_t s_buf[kBlockSortMax];
     __shared__ uint32_t s_warp[65];
-    __shared__ int64_t s_l, s_r, s_B;
+    __shared__ int64_t s_l, s_r;
     __shared__ uint64_t s_pivot;
     __shared__ int s_state;  // 0 partition, 1 sort in the block, 2 sort on the device, 3 done
     __shared__ uint32_t s_K;
@@ -273,6 +478,15 @@ __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
     const int64_t size0 = e0 - s0;
     // 2 * int(log2(size)) (numba_kdtree.py:411), exact for integers
     int depth = size0 > 16 ? 2 * (63 - __clzll((unsigned long long)size0)) : 0;
+    if (wide) {  // the device-wide partitions already ran the first steps
+        const WideNode w = wide[blockIdx.x];
+        if (w.state == kWideDone) return;
+        if (threadIdx.x == 0) {
+            s_l = w.l;
+            s_r = w.r;
+        }
+        depth = w.depth;
+    }
     __syncthreads();
     while (true) {
         if (threadIdx.x == 0) {
@@ -358,7 +572,6 @@ __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
         __syncthreads();
         if (threadIdx.x == 0) {
             swap_keys(keys, B, r - 1);
-            s_B = B;
             if (nth < B) s_r = B;
             else if (nth > B) s_l = B + 1;
             else s_state = 3;
@@ -427,21 +640,78 @@ int ref_tree_build(Workspace& ws, const fhg_index& ix, RefTree* out) {
     FHG_TRY(tmp.alloc(&big_count, 1));
     const int64_t max_level_nodes = (nodes + 1) / 2;
     FHG_TRY(tmp.alloc(&big_sort, (size_t)(2 * max_level_nodes)));
+    // device-wide partitions: saved node states, tile offsets, tile counts
+    int64_t wide_levels = 0;
+    while (wide_levels + 1 < out->levels && ((n + ((int64_t)1 << wide_levels) - 1) >> wide_levels) > kWideMin)
+        ++wide_levels;
+    WideNode* wide = nullptr;
+    int64_t *tile_off = nullptr, *ctl = nullptr;
+    uint32_t *tile_small = nullptr, *tile_base = nullptr;
+    if (wide_levels > 0) {
+        const int64_t wide_nodes = (int64_t)1 << (wide_levels - 1);
+        const size_t max_tiles = (size_t)(n / kSelTile + wide_nodes + 1);
+        FHG_TRY(tmp.alloc(&wide, (size_t)wide_nodes));
+        FHG_TRY(tmp.alloc(&tile_off, (size_t)wide_nodes));
+        FHG_TRY(tmp.alloc(&ctl, 2));
+        FHG_TRY(tmp.alloc(&tile_small, max_tiles));
+        FHG_TRY(tmp.alloc(&tile_base, max_tiles));
+    }
     LAUNCH(init_root_kernel, n, n, out->idx, nodeof, rs, re);
     for (int lvl = 0; lvl < out->levels; ++lvl) {
         const int64_t first = ((int64_t)1 << lvl) - 1, count = (int64_t)1 << lvl;
-        LAUNCH(box_init_kernel, count * d, first, count, d, lo, hi);
-        LAUNCH(box_level_kernel, n, n, d, pad, out->idx, nodeof, ix.rank, ix.pts, lo, hi);
         const bool last = lvl + 1 == out->levels;
-        LAUNCH(axis_level_kernel, count, first, count, d, lo, hi, out->box, last ? nullptr : axis);
+        {
+            Stage boxes(s, "ref_tree_boxes");
+            LAUNCH(box_init_kernel, count * d, first, count, d, lo, hi);
+            LAUNCH(box_level_kernel, n, n, d, pad, out->idx, nodeof, ix.rank, ix.pts, lo, hi);
+            LAUNCH(axis_level_kernel, count, first, count, d, lo, hi, out->box,
+                   last ? nullptr : axis);
+        }
         if (last) break;
-        LAUNCH(child_ranges_kernel, count, first, count, rs, re);
-        LAUNCH(keys_level_kernel, n, n, first, pad, out->idx, nodeof, axis, ix.rank, ix.pts, keys);
+        {
+            Stage kst(s, "ref_tree_keys");
+            LAUNCH(child_ranges_kernel, count, first, count, rs, re);
+            LAUNCH(keys_level_kernel, n, n, first, pad, out->idx, nodeof, axis, ix.rank, ix.pts,
+                   keys);
+        }
         FHG_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
-        ::fhg::note_launch();
-        select_level_kernel<<<(unsigned)count, kSelThreads, 0, s>>>(
-            first, rs, re, nodes, keys, pos_big, pos_small, big_sort, big_count);
-        FHG_CUDA(cudaGetLastError());
+        const bool wide_level = lvl < wide_levels;  // some node longer than kWideMin
+        if (wide_level) {
+            Stage sel(s, "ref_tree_select_wide");
+            for (int init = 1;; init = 0) {
+                ::fhg::note_launch();
+                wide_setup_kernel<<<1, kSelThreads, 0, s>>>(first, (int)count, rs, re, nodes, init,
+                                                           keys, wide, tile_off, ctl);
+                FHG_CUDA(cudaGetLastError());
+                int64_t h_ctl[2];
+                FHG_CUDA(cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, s));
+                FHG_CUDA(cudaStreamSynchronize(s));
+                if (h_ctl[1] == 0) break;
+                const unsigned tiles = (unsigned)h_ctl[0];
+                ::fhg::note_launch();
+                wide_count_kernel<<<tiles, kSelThreads, 0, s>>>((int)count, tile_off, wide, keys,
+                                                                tile_small);
+                ::fhg::note_launch();
+                wide_scan_kernel<<<(unsigned)count, kSelThreads, 0, s>>>((int)count, tile_off, ctl,
+                                                                         wide, tile_small, tile_base);
+                ::fhg::note_launch();
+                wide_rank_kernel<<<tiles, kSelThreads, 0, s>>>((int)count, tile_off, wide, keys,
+                                                               tile_base, pos_big, pos_small);
+                ::fhg::note_launch();
+                wide_swap_kernel<<<tiles, kSelThreads, 0, s>>>((int)count, tile_off, wide, keys,
+                                                               pos_big, pos_small);
+                FHG_CUDA(cudaGetLastError());
+                LAUNCH(wide_finish_kernel, count, (int)count, wide, keys, first, rs, re);
+            }
+        }
+        {
+            Stage sel(s, wide_level ? "ref_tree_select_top" : "ref_tree_select_deep");
+            ::fhg::note_launch();
+            select_level_kernel<<<(unsigned)count, kSelThreads, 0, s>>>(
+                first, rs, re, nodes, keys, pos_big, pos_small, big_sort, big_count,
+                wide_level ? wide : nullptr);
+            FHG_CUDA(cudaGetLastError());
+        }
         int h_big = 0;
         FHG_CUDA(cudaMemcpyAsync(&h_big, big_count, sizeof(int), cudaMemcpyDeviceToHost, s));
         FHG_CUDA(cudaStreamSynchronize(s));
