@@ -38,6 +38,7 @@
 #include <type_traits>
 
 #include "highd.cuh"
+#include "primitives.cuh"
 #include "tc.cuh"
 
 namespace fhg {
@@ -394,6 +395,28 @@ __host__ __device__ constexpr size_t tc_smem(int ka, int L) {
            + 1024;                                            // 1024-byte alignment slack
 }
 
+// Sort keys of the points by |y|^2 (non-negative: its float bits order it).
+__global__ void hd_norm_keys_kernel(int64_t n, const float* __restrict__ ny,
+                                    uint32_t* __restrict__ key, int32_t* __restrict__ perm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    key[i] = __float_as_uint(ny[i]);
+    perm[i] = (int32_t)i;
+}
+
+// Row r of Bp (vw 16-byte vectors) and nyp[r] from point perm[r].
+__global__ void hd_permute_kernel(int64_t n, int vw, const int32_t* __restrict__ perm,
+                                  const uint4* __restrict__ B, const float* __restrict__ ny,
+                                  uint4* __restrict__ Bp, float* __restrict__ nyp) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * vw) return;
+    const int64_t r = t / vw;
+    const int c = (int)(t - r * vw);
+    const int64_t j = perm[r];
+    Bp[t] = B[j * vw + c];
+    if (c == 0) nyp[r] = ny[j];
+}
+
 // hd_cut for buffers of up to 32 * PER entries (kept out of line: the
 // epilogue calls it rarely, from several places).
 template <int PER>
@@ -422,8 +445,9 @@ __device__ __noinline__ int tc_cut(unsigned long long* buf, int cnt, int keep, i
 template <int KA, int PER>
 __global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
     const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-    int64_t n, int L, int cap, const float* __restrict__ ny, int32_t* __restrict__ cand,
-    float* __restrict__ T, int* __restrict__ err) {
+    int64_t n, int L, int cap, const float* __restrict__ ny, const float* __restrict__ nyq,
+    const int32_t* __restrict__ perm, int32_t* __restrict__ cand, float* __restrict__ T,
+    int* __restrict__ err) {
     constexpr int kABytes = KA * kTcBM * kTcAtom;
     constexpr int kBBytes = KA * kTcBN * kTcAtom;  // one stage
     constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTcBM, kTcBN);
@@ -534,7 +558,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
         const int quarter = warp & 3;
         const int r = quarter * 32 + lane;
         const int64_t q = q0 + r;
-        const float nq = q < n ? ny[q] : 0.0f;
+        const float nq = q < n ? nyq[q] : 0.0f;
         unsigned long long* row = bufs + (size_t)r * cap;
         float tq = INFINITY;
         int cnt = 0;
@@ -602,8 +626,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
                         }
                     }
                 };
-                if (jb + kTcBN <= n) columns(std::true_type{});
-                else columns(std::false_type{});
+                if (jb + kTcBN <= n) {
+                    // the points run in increasing |y|^2, so h[c * 32] is the
+                    // least of the chunk and, rounding being monotone, no
+                    // estimate of the chunk is below
+                    // fl(fl(nq + h[c * 32]) - 2 max dot): a chunk whose bound
+                    // reaches every row's threshold holds no candidate
+                    float dmax = __uint_as_float(acc[0]);
+#pragma unroll
+                    for (int i = 1; i < 32; ++i) dmax = fmaxf(dmax, __uint_as_float(acc[i]));
+                    const float lb =
+                        __fsub_rn(__fadd_rn(nq, hy[c * 32]), __fmul_rn(2.0f, dmax));
+                    if (__any_sync(0xffffffffu, lb < tq)) columns(std::true_type{});
+                } else {
+                    columns(std::false_type{});
+                }
             }
             tc::mbar_arrive(&nempty[u]);  // this tile's |y|^2 are read
         }
@@ -616,7 +653,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
             const int64_t qq = q0 + quarter * 32 + rr;
             if (qq < n) {
                 for (int e2 = lane; e2 < L; e2 += 32)
-                    cand[qq * L + e2] = e2 < kept ? (int32_t)(uint32_t)rb[e2] : -1;
+                    cand[qq * L + e2] = e2 < kept ? perm[(uint32_t)rb[e2]] : -1;
                 if (lane == 0) T[qq] = kept >= L ? hd_dist(rb[L - 1]) : INFINITY;
             }
             __syncwarp();
@@ -826,7 +863,8 @@ int tensor_map_rows(CUtensorMap* map, const __nv_bfloat16* base, int64_t rows, i
 
 template <int KA, int PER>
 int launch_cand_tc(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
-                   const float* ny_padded, int32_t* cand, float* T, int* err, cudaStream_t s) {
+                   const float* ny_padded, const float* nyq, const int32_t* perm, int32_t* cand,
+                   float* T, int* err, cudaStream_t s) {
     CUtensorMap ma, mb;
     FHG_TRY(tensor_map_rows(&ma, A, n, KA * 64, kTcBM));
     FHG_TRY(tensor_map_rows(&mb, B, n, KA * 64, kTcBN));
@@ -837,7 +875,7 @@ int launch_cand_tc(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16
     Stage stage(s, "hd_cand_kernel");
     ::fhg::note_launch();
     hd_cand_tc_kernel<KA, PER><<<(unsigned)blocks, kTcThreads, smem, s>>>(
-        ma, mb, n, L, tc_cap(L), ny_padded, cand, T, err);
+        ma, mb, n, L, tc_cap(L), ny_padded, nyq, perm, cand, T, err);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
@@ -852,12 +890,12 @@ int tc_atoms(int dp, int L) {
 }
 
 int launch_cand_tc_any(int ka, int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
-                       const float* ny_padded, int32_t* cand, float* T, int* err,
-                       cudaStream_t s) {
+                       const float* ny_padded, const float* nyq, const int32_t* perm,
+                       int32_t* cand, float* T, int* err, cudaStream_t s) {
     const int per = (tc_cap(L) + 31) / 32;
 #define FHG_TC(KA, PER)                                                                     \
     if (ka == KA && per == PER)                                                             \
-        return launch_cand_tc<KA, PER>(n, L, A, B, ny_padded, cand, T, err, s);
+        return launch_cand_tc<KA, PER>(n, L, A, B, ny_padded, nyq, perm, cand, T, err, s);
     FHG_TC(2, 1) FHG_TC(2, 2) FHG_TC(2, 3) FHG_TC(2, 4)
     FHG_TC(3, 1) FHG_TC(3, 2) FHG_TC(3, 3) FHG_TC(3, 4)
 #undef FHG_TC
@@ -923,10 +961,32 @@ int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_
     hd_split_kernel<<<grid_for(n, 128), 128, 0, s>>>(X, n, d, dp, kw, mu, A, B, ny, cn, maxes);
     FHG_CUDA(cudaGetLastError());
     if (ka) {
+        // the points (B rows, |y|^2) in increasing |y|^2, for the chunk
+        // bound of the epilogue; candidates map back through perm
+        uint32_t* nkey;
+        int32_t* perm;
+        float* nyp;
+        __nv_bfloat16* Bp;
         int* err;
+        FHG_TRY(ws.alloc(&nkey, (size_t)n));
+        FHG_TRY(ws.alloc(&perm, (size_t)n));
+        FHG_TRY(ws.alloc(&nyp, (size_t)n_pad));
+        FHG_TRY(ws.alloc(&Bp, (size_t)(n * kw)));
         FHG_TRY(ws.alloc(&err, 1));
+        ::fhg::note_launch();
+        hd_norm_keys_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, ny, nkey, perm);
+        FHG_CUDA(cudaGetLastError());
+        FHG_TRY(radix_sort_u32(ws, nkey, perm, n, 0, 32));
+        const int64_t vecs = n * (kw / 8);
+        ::fhg::note_launch();
+        hd_permute_kernel<<<grid_for(vecs, 256), 256, 0, s>>>(
+            n, kw / 8, perm, reinterpret_cast<const uint4*>(B), ny,
+            reinterpret_cast<uint4*>(Bp), nyp);
+        FHG_CUDA(cudaGetLastError());
+        if (n_pad > n)
+            FHG_CUDA(cudaMemsetAsync(nyp + n, 0, sizeof(float) * (size_t)(n_pad - n), s));
         FHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-        FHG_TRY(launch_cand_tc_any(ka, n, L, A, B, ny, cand, T, err, s));
+        FHG_TRY(launch_cand_tc_any(ka, n, L, A, Bp, nyp, ny, perm, cand, T, err, s));
         int h_err = 0;
         FHG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
         FHG_CUDA(cudaStreamSynchronize(s));

@@ -107,31 +107,66 @@ __global__ void box_init_kernel(int64_t first, int64_t count, int d, uint32_t* _
 }
 
 // Per node of the level: the bounding box of its points (_init_node,
-// numba_kdtree.py:67).  Positions of one node are contiguous; a warp whose 32
-// positions share one node reduces first, so a large node takes one atomic
-// per warp and dimension.
-__global__ void box_level_kernel(int64_t n, int d, int pad, const int32_t* __restrict__ idx,
-                                 const int32_t* __restrict__ nodeof,
-                                 const int32_t* __restrict__ rank, const float* __restrict__ pts,
-                                 uint32_t* lo, uint32_t* hi) {
+// numba_kdtree.py:67).  Positions of one node are contiguous, so a warp
+// reduces each run of lanes that share a node (a segmented shuffle
+// reduction) and the run's first lane takes the atomics; a block whose
+// threads all share one node (the top levels) combines its warps first and
+// takes one atomic per dimension.  pts: the points in caller order, pad
+// floats per row.
+constexpr int kBoxThreads = 256;
+__global__ void __launch_bounds__(kBoxThreads) box_level_kernel(
+    int64_t n, int d, int pad, const int32_t* __restrict__ idx, const int32_t* __restrict__ nodeof,
+    const float* __restrict__ pts, uint32_t* lo, uint32_t* hi) {
+    __shared__ int32_t s_v0;
+    __shared__ uint32_t s_lo[kBoxThreads / 32][32], s_hi[kBoxThreads / 32][32];
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const bool valid = p < n;
     const int32_t v = valid ? nodeof[p] : -1;
-    const int64_t row = valid ? (int64_t)rank[idx[p]] * pad : 0;
-    const int32_t v0 = __shfl_sync(kFull, v, 0);
-    const bool uniform = __all_sync(kFull, v == v0);
+    const int64_t row = valid ? (int64_t)idx[p] * pad : 0;
+    if (threadIdx.x == 0) s_v0 = v;
+    __syncthreads();
+    const bool block_uniform = __syncthreads_and(valid && v == s_v0);
+    // lanes of the same node above this one, for each shuffle distance
+    unsigned same = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int32_t other = __shfl_down_sync(kFull, v, 1 << k);
+        if (lane + (1 << k) < 32 && other == v) same |= 1u << k;
+    }
+    const int32_t v_prev = __shfl_up_sync(kFull, v, 1);  // every lane takes part
+    const bool head = valid && (lane == 0 || v_prev != v);
     for (int j = 0; j < d; ++j) {
-        uint32_t a = valid ? ordered_bits(pts[row + j]) : 0xffffffffu;
-        uint32_t b = valid ? ordered_bits(pts[row + j]) : 0u;
-        if (uniform) {
-            a = __reduce_min_sync(kFull, a);
-            b = __reduce_max_sync(kFull, b);
-            if (lane == 0 && v0 >= 0) {
-                atomicMin(&lo[(int64_t)v0 * d + j], a);
-                atomicMax(&hi[(int64_t)v0 * d + j], b);
+        const uint32_t o = valid ? ordered_bits(pts[row + j]) : 0u;
+        uint32_t a = valid ? o : 0xffffffffu, b = o;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const uint32_t a2 = __shfl_down_sync(kFull, a, 1 << k);
+            const uint32_t b2 = __shfl_down_sync(kFull, b, 1 << k);
+            if (same & (1u << k)) {
+                a = min(a, a2);
+                b = max(b, b2);
             }
-        } else if (valid) {
+        }
+        if (block_uniform) {
+            if (lane == 0) {
+                s_lo[w][j] = a;
+                s_hi[w][j] = b;
+            }
+        } else if (head) {
+            atomicMin(&lo[(int64_t)v * d + j], a);
+            atomicMax(&hi[(int64_t)v * d + j], b);
+        }
+    }
+    if (block_uniform) {
+        __syncthreads();
+        if (threadIdx.x < d) {
+            const int j = threadIdx.x;
+            uint32_t a = s_lo[0][j], b = s_hi[0][j];
+            for (int k = 1; k < kBoxThreads / 32; ++k) {
+                a = min(a, s_lo[k][j]);
+                b = max(b, s_hi[k][j]);
+            }
             atomicMin(&lo[(int64_t)v * d + j], a);
             atomicMax(&hi[(int64_t)v * d + j], b);
         }
@@ -167,14 +202,22 @@ __global__ void axis_level_kernel(int64_t first, int64_t count, int d,
 __global__ void keys_level_kernel(int64_t n, int64_t first, int pad,
                                   const int32_t* __restrict__ idx,
                                   const int32_t* __restrict__ nodeof,
-                                  const int32_t* __restrict__ axis,
-                                  const int32_t* __restrict__ rank, const float* __restrict__ pts,
+                                  const int32_t* __restrict__ axis, const float* __restrict__ pts,
                                   uint64_t* __restrict__ keys) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int32_t c = idx[p];
-    const float x = pts[(int64_t)rank[c] * pad + axis[nodeof[p] - first]];
+    const float x = pts[(int64_t)c * pad + axis[nodeof[p] - first]];
     keys[p] = ((uint64_t)ordered_bits(x) << 32) | (uint32_t)c;
+}
+
+// The index's points (Morton order) back in caller order.
+__global__ void caller_order_kernel(int64_t n, int pad, const int32_t* __restrict__ orig,
+                                    const float* __restrict__ pts, float* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * pad) return;
+    const int64_t r = t / pad;
+    out[(int64_t)orig[r] * pad + (t - r * pad)] = pts[t];
 }
 
 __global__ void unpack_level_kernel(int64_t n, const uint64_t* __restrict__ keys,
@@ -448,23 +491,125 @@ __global__ void wide_finish_kernel(int count, WideNode* wide, uint64_t* keys, in
     wide[t] = w;
 }
 
+// The introselect of keys[l, r) around nth (l <= nth < r), continued in
+// shared memory once the active range fits (r - l <= kBlockSortMax): the
+// range is read once, every later partition and the final sort run on s_buf,
+// and it is written back once.  The pairing positions are 12-bit offsets in
+// s_big / s_small (a partition pairs at most (r - l - 1) / 2 elements).
+__device__ void select_in_smem(uint64_t* keys, int64_t l, int64_t r, int64_t nth, int depth,
+                               uint64_t* s_buf, uint16_t* s_big, uint16_t* s_small,
+                               uint32_t* s_warp, uint32_t* s_K) {
+    const int m = (int)(r - l), target = (int)(nth - l);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) s_buf[i] = keys[l + i];
+    __syncthreads();
+    int L = 0, R = m;
+    while (true) {
+        const int mm = R - L;
+        if (mm <= 16) {
+            // insertion sort (numba_kdtree.py:186): ascending, by ranks
+            uint64_t x = 0;
+            int rank = 0;
+            if (threadIdx.x < mm) {
+                x = s_buf[L + threadIdx.x];
+                for (int j = 0; j < mm; ++j) rank += s_buf[L + j] < x ? 1 : 0;
+            }
+            __syncthreads();
+            if (threadIdx.x < mm) s_buf[L + rank] = x;
+            __syncthreads();
+            break;
+        }
+        if (depth == 0) {
+            // the heapsort fallback (numba_kdtree.py:247): ascending
+            for (int i = threadIdx.x; i < m; i += blockDim.x) keys[l + i] = s_buf[i];
+            __syncthreads();
+            block_sort(keys, l + L, l + R, s_buf);
+            return;
+        }
+        --depth;
+        if (threadIdx.x == 0) {
+            // median of three (numba_kdtree.py:282), the pivot to the end
+            const int mid = (L + R - 1) / 2;
+            uint64_t a = s_buf[L], b = s_buf[mid], c = s_buf[R - 1], t;
+            if (a > b) { t = a; a = b; b = t; }
+            if (b > c) {
+                t = b; b = c; c = t;
+                if (a > b) { t = a; a = b; b = t; }
+            }
+            s_buf[L] = a;
+            s_buf[mid] = c;
+            s_buf[R - 1] = b;
+            *s_K = 0;
+        }
+        __syncthreads();
+        const uint64_t pivot = s_buf[R - 1];
+        const int p0 = L + (int)threadIdx.x * kSelV;
+        uint64_t kv[kSelV];
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int j = 0; j < kSelV; ++j) {
+            const int p = p0 + j;
+            kv[j] = p < R - 1 ? s_buf[p] : 0ull;
+            cnt += (p < R - 1 && kv[j] < pivot) ? 1u : 0u;
+        }
+        uint32_t before;
+        const uint32_t c = block_exclusive(cnt, &before, s_warp);
+        const int B = L + (int)c;
+        uint32_t kb = 0;
+#pragma unroll
+        for (int j = 0; j < kSelV; ++j) {
+            const int p = p0 + j;
+            if (p >= R - 1) break;
+            const bool small = kv[j] < pivot;
+            if (p < B && !small) {
+                s_big[(p - L) - before] = (uint16_t)p;
+                ++kb;
+            } else if (p >= B && small) {
+                s_small[c - 1 - before] = (uint16_t)p;
+            }
+            before += small ? 1u : 0u;
+        }
+        if (kb) atomicAdd(s_K, kb);
+        __syncthreads();
+        const uint32_t K = *s_K;
+        for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
+            const int a = s_big[k], b = s_small[k];
+            const uint64_t t = s_buf[a];
+            s_buf[a] = s_buf[b];
+            s_buf[b] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint64_t t = s_buf[B];
+            s_buf[B] = s_buf[R - 1];
+            s_buf[R - 1] = t;
+        }
+        __syncthreads();
+        if (target < B) R = B;
+        else if (target > B) L = B + 1;
+        else break;
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) keys[l + i] = s_buf[i];
+}
+
 // One block per internal node of the level: the reference's introselect of
 // the node's range around its median position (numba_kdtree.py:395
 // _introselect, :372 _introselect_impl).  pos_big / pos_small: per-node
 // scratch (the node's own range of two n-long arrays) pairing the swaps of a
-// partition.  A range that reaches the depth limit while longer than a block
-// can sort is recorded in big_sort (its bounds) for a device-wide sort after
-// the launch.
+// partition while the range is longer than a block holds.  A range that
+// reaches the depth limit while longer than a block can sort is recorded in
+// big_sort (its bounds) for a device-wide sort after the launch.  wide
+// (nullable): the state the device-wide partitions left for each node.
 __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
     int64_t first, const int64_t* __restrict__ rs, const int64_t* __restrict__ re,
     int64_t n_nodes, uint64_t* keys, int32_t* __restrict__ pos_big,
     int32_t* __restrict__ pos_small, int64_t* __restrict__ big_sort, int* big_sort_count,
     const WideNode* __restrict__ wide) {
     __shared__ uint64_t s_buf[kBlockSortMax];
+    __shared__ uint16_t s_big[kBlockSortMax / 2], s_small[kBlockSortMax / 2];
     __shared__ uint32_t s_warp[65];
     __shared__ int64_t s_l, s_r;
     __shared__ uint64_t s_pivot;
-    __shared__ int s_state;  // 0 partition, 1 sort in the block, 2 sort on the device, 3 done
+    __shared__ int s_done;
     __shared__ uint32_t s_K;
     const int64_t v = first + blockIdx.x;
     const int64_t s0 = rs[v], e0 = re[v];
@@ -474,6 +619,7 @@ __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
     if (threadIdx.x == 0) {
         s_l = s0;
         s_r = e0;
+        s_done = 0;
     }
     const int64_t size0 = e0 - s0;
     // 2 * int(log2(size)) (numba_kdtree.py:411), exact for integers
@@ -489,42 +635,36 @@ __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
     }
     __syncthreads();
     while (true) {
-        if (threadIdx.x == 0) {
-            const int64_t l = s_l, r = s_r, m = r - l;
-            if (m <= 16 || depth == 0) {
-                // insertion sort (m <= 16) or the heapsort fallback: ascending
-                s_state = m <= kBlockSortMax ? 1 : 2;
-            } else {
-                s_state = 0;
-                // median of three (numba_kdtree.py:282), then the pivot to
-                // the end (:316)
-                const int64_t mid = (l + r - 1) / 2;
-                if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
-                if (keys[mid] > keys[r - 1]) {
-                    swap_keys(keys, mid, r - 1);
-                    if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
-                }
-                swap_keys(keys, mid, r - 1);
-                s_pivot = keys[r - 1];
-                s_K = 0;
-            }
-        }
-        if (depth > 0) --depth;
-        __syncthreads();
-        const int st = s_state;
-        if (st == 1) {
-            block_sort(keys, s_l, s_r, s_buf);
+        const int64_t l = s_l, r = s_r;
+        if (r - l <= kBlockSortMax) {
+            select_in_smem(keys, l, r, nth, depth, s_buf, s_big, s_small, s_warp, &s_K);
             return;
         }
-        if (st == 2) {
+        if (depth == 0) {
+            // the heapsort fallback on a range longer than a block sorts:
+            // sorted ascending on the device after the launch
             if (threadIdx.x == 0) {
                 const int slot = atomicAdd(big_sort_count, 1);
-                big_sort[2 * slot] = s_l;
-                big_sort[2 * slot + 1] = s_r;
+                big_sort[2 * slot] = l;
+                big_sort[2 * slot + 1] = r;
             }
             return;
         }
-        const int64_t l = s_l, r = s_r;
+        --depth;
+        if (threadIdx.x == 0) {
+            // median of three (numba_kdtree.py:282), then the pivot to the
+            // end (:316)
+            const int64_t mid = (l + r - 1) / 2;
+            if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
+            if (keys[mid] > keys[r - 1]) {
+                swap_keys(keys, mid, r - 1);
+                if (keys[l] > keys[mid]) swap_keys(keys, l, mid);
+            }
+            swap_keys(keys, mid, r - 1);
+            s_pivot = keys[r - 1];
+            s_K = 0;
+        }
+        __syncthreads();
         const uint64_t pivot = s_pivot;
         // elements below the pivot in [l, r - 1)
         uint32_t c_loc = 0;
@@ -574,10 +714,10 @@ __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
             swap_keys(keys, B, r - 1);
             if (nth < B) s_r = B;
             else if (nth > B) s_l = B + 1;
-            else s_state = 3;
+            else s_done = 1;
         }
         __syncthreads();
-        if (s_state == 3) return;
+        if (s_done) return;
     }
 }
 
@@ -656,6 +796,9 @@ int ref_tree_build(Workspace& ws, const fhg_index& ix, RefTree* out) {
         FHG_TRY(tmp.alloc(&tile_small, max_tiles));
         FHG_TRY(tmp.alloc(&tile_base, max_tiles));
     }
+    float* ptsc;
+    FHG_TRY(tmp.alloc(&ptsc, (size_t)(n * pad)));
+    LAUNCH(caller_order_kernel, n * pad, n, pad, ix.orig, ix.pts, ptsc);
     LAUNCH(init_root_kernel, n, n, out->idx, nodeof, rs, re);
     for (int lvl = 0; lvl < out->levels; ++lvl) {
         const int64_t first = ((int64_t)1 << lvl) - 1, count = (int64_t)1 << lvl;
@@ -663,7 +806,7 @@ int ref_tree_build(Workspace& ws, const fhg_index& ix, RefTree* out) {
         {
             Stage boxes(s, "ref_tree_boxes");
             LAUNCH(box_init_kernel, count * d, first, count, d, lo, hi);
-            LAUNCH(box_level_kernel, n, n, d, pad, out->idx, nodeof, ix.rank, ix.pts, lo, hi);
+            LAUNCH(box_level_kernel, n, n, d, pad, out->idx, nodeof, ptsc, lo, hi);
             LAUNCH(axis_level_kernel, count, first, count, d, lo, hi, out->box,
                    last ? nullptr : axis);
         }
@@ -671,8 +814,7 @@ int ref_tree_build(Workspace& ws, const fhg_index& ix, RefTree* out) {
         {
             Stage kst(s, "ref_tree_keys");
             LAUNCH(child_ranges_kernel, count, first, count, rs, re);
-            LAUNCH(keys_level_kernel, n, n, first, pad, out->idx, nodeof, axis, ix.rank, ix.pts,
-                   keys);
+            LAUNCH(keys_level_kernel, n, n, first, pad, out->idx, nodeof, axis, ptsc, keys);
         }
         FHG_CUDA(cudaMemsetAsync(big_count, 0, sizeof(int), s));
         const bool wide_level = lvl < wide_levels;  // some node longer than kWideMin
