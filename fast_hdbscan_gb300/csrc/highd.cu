@@ -404,6 +404,50 @@ __global__ void hd_norm_keys_kernel(int64_t n, const float* __restrict__ ny,
     perm[i] = (int32_t)i;
 }
 
+// The nearest of `marks` landmarks (points 0, stride, 2 stride, ...) of every
+// point, in float32 (first landmark wins ties), with perm = identity.
+constexpr int kLandmarks = 256;
+__global__ void __launch_bounds__(256) hd_landmark_kernel(int64_t n, int d,
+                                                          const float* __restrict__ X, int marks,
+                                                          int64_t stride, uint32_t* __restrict__ key,
+                                                          int32_t* __restrict__ perm) {
+    __shared__ float lm[32][kHighdMaxDim];
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float best = INFINITY;
+    int bi = 0;
+    for (int c0 = 0; c0 < marks; c0 += 32) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < 32 * d; t += blockDim.x) {
+            const int l = t / d, j = t - (t / d) * d;
+            lm[l][j] = c0 + l < marks ? X[(int64_t)(c0 + l) * stride * d + j] : 0.0f;
+        }
+        __syncthreads();
+        if (p < n) {
+            float acc[32];
+#pragma unroll
+            for (int l = 0; l < 32; ++l) acc[l] = 0.0f;
+            for (int j = 0; j < d; ++j) {
+                const float x = X[p * d + j];
+#pragma unroll
+                for (int l = 0; l < 32; ++l) {
+                    const float t = x - lm[l][j];
+                    acc[l] = fmaf(t, t, acc[l]);
+                }
+            }
+#pragma unroll
+            for (int l = 0; l < 32; ++l)
+                if (c0 + l < marks && acc[l] < best) {
+                    best = acc[l];
+                    bi = c0 + l;
+                }
+        }
+    }
+    if (p < n) {
+        key[p] = (uint32_t)bi;
+        perm[p] = (int32_t)p;
+    }
+}
+
 // Row r of Bp (vw 16-byte vectors) and nyp[r] from point perm[r].
 __global__ void hd_permute_kernel(int64_t n, int vw, const int32_t* __restrict__ perm,
                                   const uint4* __restrict__ B, const float* __restrict__ ny,
@@ -446,8 +490,8 @@ template <int KA, int PER>
 __global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
     const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
     int64_t n, int L, int cap, const float* __restrict__ ny, const float* __restrict__ nyq,
-    const int32_t* __restrict__ perm, int32_t* __restrict__ cand, float* __restrict__ T,
-    int* __restrict__ err) {
+    const int32_t* __restrict__ perm, const int32_t* __restrict__ qperm,
+    int32_t* __restrict__ cand, float* __restrict__ T, int* __restrict__ err) {
     constexpr int kABytes = KA * kTcBM * kTcAtom;
     constexpr int kBBytes = KA * kTcBN * kTcAtom;  // one stage
     constexpr uint32_t kIdesc = tc::idesc_bf16_f32(kTcBM, kTcBN);
@@ -650,8 +694,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) hd_cand_tc_kernel(
             const int cc = __shfl_sync(0xffffffffu, cnt, rr);
             unsigned long long* rb = bufs + (size_t)(quarter * 32 + rr) * cap;
             const int kept = tc_cut<PER>(rb, cc, L, lane);
-            const int64_t qq = q0 + quarter * 32 + rr;
-            if (qq < n) {
+            const int64_t qr = q0 + quarter * 32 + rr;
+            if (qr < n) {
+                const int64_t qq = qperm[qr];
                 for (int e2 = lane; e2 < L; e2 += 32)
                     cand[qq * L + e2] = e2 < kept ? perm[(uint32_t)rb[e2]] : -1;
                 if (lane == 0) T[qq] = kept >= L ? hd_dist(rb[L - 1]) : INFINITY;
@@ -863,8 +908,8 @@ int tensor_map_rows(CUtensorMap* map, const __nv_bfloat16* base, int64_t rows, i
 
 template <int KA, int PER>
 int launch_cand_tc(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
-                   const float* ny_padded, const float* nyq, const int32_t* perm, int32_t* cand,
-                   float* T, int* err, cudaStream_t s) {
+                   const float* ny_padded, const float* nyq, const int32_t* perm,
+                   const int32_t* qperm, int32_t* cand, float* T, int* err, cudaStream_t s) {
     CUtensorMap ma, mb;
     FHG_TRY(tensor_map_rows(&ma, A, n, KA * 64, kTcBM));
     FHG_TRY(tensor_map_rows(&mb, B, n, KA * 64, kTcBN));
@@ -875,7 +920,7 @@ int launch_cand_tc(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16
     Stage stage(s, "hd_cand_kernel");
     ::fhg::note_launch();
     hd_cand_tc_kernel<KA, PER><<<(unsigned)blocks, kTcThreads, smem, s>>>(
-        ma, mb, n, L, tc_cap(L), ny_padded, nyq, perm, cand, T, err);
+        ma, mb, n, L, tc_cap(L), ny_padded, nyq, perm, qperm, cand, T, err);
     FHG_CUDA(cudaGetLastError());
     return FHG_OK;
 }
@@ -891,11 +936,13 @@ int tc_atoms(int dp, int L) {
 
 int launch_cand_tc_any(int ka, int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16* B,
                        const float* ny_padded, const float* nyq, const int32_t* perm,
-                       int32_t* cand, float* T, int* err, cudaStream_t s) {
+                       const int32_t* qperm, int32_t* cand, float* T, int* err,
+                       cudaStream_t s) {
     const int per = (tc_cap(L) + 31) / 32;
 #define FHG_TC(KA, PER)                                                                     \
     if (ka == KA && per == PER)                                                             \
-        return launch_cand_tc<KA, PER>(n, L, A, B, ny_padded, nyq, perm, cand, T, err, s);
+        return launch_cand_tc<KA, PER>(n, L, A, B, ny_padded, nyq, perm, qperm, cand, T, err, \
+                                       s);
     FHG_TC(2, 1) FHG_TC(2, 2) FHG_TC(2, 3) FHG_TC(2, 4)
     FHG_TC(3, 1) FHG_TC(3, 2) FHG_TC(3, 3) FHG_TC(3, 4)
 #undef FHG_TC
@@ -962,31 +1009,48 @@ int highd_knn(const float* X, int64_t n, int d, int k, float* rd_o, int32_t* ix_
     FHG_CUDA(cudaGetLastError());
     if (ka) {
         // the points (B rows, |y|^2) in increasing |y|^2, for the chunk
-        // bound of the epilogue; candidates map back through perm
-        uint32_t* nkey;
-        int32_t* perm;
-        float* nyp;
-        __nv_bfloat16* Bp;
+        // bound of the epilogue; candidates map back through perm.  The
+        // queries (A rows) grouped by their nearest landmark, so that the
+        // rows of a CTA tend to need the same chunks; results go back to
+        // the query's own row through qperm.
+        uint32_t *nkey, *qkey;
+        int32_t *perm, *qperm;
+        float *nyp, *nyq;
+        __nv_bfloat16 *Ap, *Bp;
         int* err;
         FHG_TRY(ws.alloc(&nkey, (size_t)n));
+        FHG_TRY(ws.alloc(&qkey, (size_t)n));
         FHG_TRY(ws.alloc(&perm, (size_t)n));
+        FHG_TRY(ws.alloc(&qperm, (size_t)n));
         FHG_TRY(ws.alloc(&nyp, (size_t)n_pad));
+        FHG_TRY(ws.alloc(&nyq, (size_t)n));
+        FHG_TRY(ws.alloc(&Ap, (size_t)(n * kw)));
         FHG_TRY(ws.alloc(&Bp, (size_t)(n * kw)));
         FHG_TRY(ws.alloc(&err, 1));
         ::fhg::note_launch();
         hd_norm_keys_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, ny, nkey, perm);
         FHG_CUDA(cudaGetLastError());
         FHG_TRY(radix_sort_u32(ws, nkey, perm, n, 0, 32));
+        const int marks = (int)std::min<int64_t>(kLandmarks, n);
+        ::fhg::note_launch();
+        hd_landmark_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, d, X, marks, n / marks, qkey,
+                                                             qperm);
+        FHG_CUDA(cudaGetLastError());
+        FHG_TRY(radix_sort_u32(ws, qkey, qperm, n, 0, 8));
         const int64_t vecs = n * (kw / 8);
         ::fhg::note_launch();
         hd_permute_kernel<<<grid_for(vecs, 256), 256, 0, s>>>(
             n, kw / 8, perm, reinterpret_cast<const uint4*>(B), ny,
             reinterpret_cast<uint4*>(Bp), nyp);
+        ::fhg::note_launch();
+        hd_permute_kernel<<<grid_for(vecs, 256), 256, 0, s>>>(
+            n, kw / 8, qperm, reinterpret_cast<const uint4*>(A), ny,
+            reinterpret_cast<uint4*>(Ap), nyq);
         FHG_CUDA(cudaGetLastError());
         if (n_pad > n)
             FHG_CUDA(cudaMemsetAsync(nyp + n, 0, sizeof(float) * (size_t)(n_pad - n), s));
         FHG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
-        FHG_TRY(launch_cand_tc_any(ka, n, L, A, Bp, nyp, ny, perm, cand, T, err, s));
+        FHG_TRY(launch_cand_tc_any(ka, n, L, Ap, Bp, nyp, nyq, perm, qperm, cand, T, err, s));
         int h_err = 0;
         FHG_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
         FHG_CUDA(cudaStreamSynchronize(s));
