@@ -382,6 +382,7 @@ constexpr int kTcStages = 2;     // operand ring (gated by the MMA)
 constexpr int kTcNyStages = 4;   // |y|^2 ring (gated by the epilogue, which trails the MMA by
                                  // at most two tiles: it never holds the producer back)
 constexpr int kTcSub = 8;        // estimates inserted between buffer checks
+constexpr int kTcStatic = 1024;  // room for the kernel's static shared memory (barriers)
 constexpr int kTcThreads = 256;
 constexpr int kTcTmemCols = 2 * kTcBN;
 constexpr int kTcAtom = 128;     // bytes per swizzled operand row segment (64 bf16)
@@ -930,7 +931,8 @@ int launch_cand_tc(int64_t n, int L, const __nv_bfloat16* A, const __nv_bfloat16
 // shared memory).
 int tc_atoms(int dp, int L) {
     const int ka = dp == 32 ? 2 : (dp == 64 ? 3 : 0);
-    if (ka == 0 || tc_cap(L) > 32 * 4 || tc_smem(ka, L) > (size_t)kHdSmemMax) return 0;
+    if (ka == 0 || tc_cap(L) > 32 * 4 || tc_smem(ka, L) + kTcStatic > (size_t)kHdSmemMax)
+        return 0;
     return ka;
 }
 
