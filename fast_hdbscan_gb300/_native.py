@@ -41,6 +41,9 @@ SIGNATURES = {
     "fhg_index_knn": (_INT, [_P, _I32, _P, _P, _P]),
     "fhg_index_boruvka": (_INT, [_P, _I32, _P, _I32, _P, _P, _P, ctypes.POINTER(_I32), _P]),
     "fhg_sort_mst": (_INT, [_P, _I64, _P, _P]),
+    "fhg_clusters_from_mst": (_INT, [_P, _I64, _I64, _I32, _D, _INT, _D, _D, _P, _P, _P, _P,
+                                     _P, _P, _P, _P, _P, ctypes.POINTER(_I64), _P,
+                                     ctypes.POINTER(_I64), _P]),
     "fhg_mst_to_linkage_tree": (_INT, [_P, _I64, _P, _P, _P]),
     "fhg_condense_tree": (_INT, [_P, _I64, _I64, _D, _P, _P, _P, _P, _P, ctypes.POINTER(_I64),
                                  _P]),

@@ -899,9 +899,9 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
              int64_t* selected_dev, int64_t* n_selected_host, void* stream,
              const FitExport& ex, int32_t knn_k = 0, int32_t query_k = 0,
              double* core64_dev = nullptr, const GraphInput* graph = nullptr,
-             bool brute_knn = false) {
+             bool brute_knn = false, const double* mst_in = nullptr) {
     FHG_TRY(check_ptrs("fhg_hdbscan_fit", {labels_dev, probs_dev}));
-    if (!graph) FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev}));
+    if (!graph && !mst_in) FHG_TRY(check_ptrs("fhg_hdbscan_fit", {X_dev}));
     if (min_samples < 1 || min_cluster_size < 1) {
         set_error("Min samples and min cluster size must be positive integers!");
         return FHG_ERR_INVALID;
@@ -918,14 +918,19 @@ int fit_impl(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
     SideCopies side(s);  // declared before the workspace: joins after its frees are queued
     Workspace ws(s);
     fhg_index* ix = nullptr;
-    if (!graph && !brute_knn) FHG_TRY(index_build(X_dev, n, d, s, &ix));
+    if (!graph && !brute_knn && !mst_in) FHG_TRY(index_build(X_dev, n, d, s, &ix));
     struct IndexGuard {
         fhg_index* p;
         cudaStream_t s;
         ~IndexGuard() { index_free(p, s); }
     } guard{ix, s};
     Linkage lk;
-    if (graph) {  // a precomputed sparse graph (precomputed.py:410 / :479)
+    if (mst_in) {  // a given spanning tree (hdbscan.py:497 clusters_from_spanning_tree)
+        int32_t *src, *dst;
+        double* w;
+        FHG_TRY(split_mst_f64(ws, mst_in, n - 1, &src, &dst, &w));
+        FHG_TRY(sort_and_link(ws, n, src, dst, w, nullptr, &lk, false));
+    } else if (graph) {  // a precomputed sparse graph (precomputed.py:410 / :479)
         double *kedges, *core64 = core64_dev;
         int32_t* nb = neighbors_dev;
         FHG_TRY(ws.alloc(&kedges, (size_t)(3 * (n - 1))));
@@ -1120,6 +1125,25 @@ FHG_API int fhg_hdbscan_fit_precomputed(
                     labels_dev, probs_dev, mst_dev, linkage_dev, ct_parent_dev, ct_child_dev,
                     ct_lambda_dev, ct_size_dev, ct_rows_host, neighbors_dev, nullptr,
                     selected_dev, n_selected_host, stream, FitExport(), 0, 0, core_dev, &g);
+}
+
+FHG_API int fhg_clusters_from_mst(const double* mst_dev, int64_t n, int64_t min_cluster_size,
+                                  int32_t selection_method, double max_cluster_size,
+                                  int allow_single_cluster, double epsilon, double persistence,
+                                  const float* sample_weights_dev, int64_t* labels_dev,
+                                  float* probs_dev, double* sorted_mst_dev, double* linkage_dev,
+                                  int64_t* ct_parent_dev, int64_t* ct_child_dev,
+                                  float* ct_lambda_dev, float* ct_size_dev, int64_t* ct_rows_host,
+                                  int64_t* selected_dev, int64_t* n_selected_host, void* stream) {
+    if (!mst_dev) {
+        set_error("fhg_clusters_from_mst: mst_dev is NULL");
+        return FHG_ERR_INVALID;
+    }
+    return fit_impl(nullptr, n, 0, 1, min_cluster_size, selection_method, max_cluster_size,
+                    allow_single_cluster, epsilon, persistence, sample_weights_dev, 0, labels_dev,
+                    probs_dev, sorted_mst_dev, linkage_dev, ct_parent_dev, ct_child_dev,
+                    ct_lambda_dev, ct_size_dev, ct_rows_host, nullptr, nullptr, selected_dev,
+                    n_selected_host, stream, FitExport(), 0, 0, nullptr, nullptr, false, mst_dev);
 }
 
 FHG_API int fhg_hdbscan_fit_export(

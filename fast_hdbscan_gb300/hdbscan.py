@@ -589,15 +589,65 @@ def compute_minimum_spanning_tree(data, min_samples=10, sample_weights=None, rep
                             reproducible=reproducible)
 
 
+def _clusters_from_mst(mst, method, min_cluster_size, max_cluster_size, allow_single_cluster,
+                       epsilon, persistence, sample_weights):
+    """clusters_from_spanning_tree's stages in one fhg_clusters_from_mst call."""
+    torch = _native._torch()
+    mst = np.ascontiguousarray(mst, dtype=np.float64).reshape(-1, 3)
+    m = mst.shape[0]
+    n = m + 1
+    d_mst = _native.to_device(mst, np.float64)
+    d_w = (_native.to_device(np.ascontiguousarray(sample_weights, dtype=np.float32), np.float32)
+           if sample_weights is not None else None)
+    E = _native.empty
+    labels, probs, sel = E(n, np.int64), E(n, np.float32), E(n, np.int64)
+    smst, linkage = E((m, 3), np.float64), E((m, 4), np.float64)
+    ctp, ctc = E(2 * n, np.int64), E(2 * n, np.int64)
+    ctl, cts = E(2 * n, np.float32), E(2 * n, np.float32)
+    rows, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
+    V = _native.vptr
+    lib = _native.load()
+    rc = lib.fhg_clusters_from_mst(
+        V(d_mst), n, int(min_cluster_size), method, float(max_cluster_size),
+        int(bool(allow_single_cluster)), float(epsilon), float(persistence), V(d_w), V(labels),
+        V(probs), V(smst), V(linkage), V(ctp), V(ctc), V(ctl), V(cts), ctypes.byref(rows),
+        V(sel), ctypes.byref(nsel), _native.stream_ptr())
+    if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
+        raise KeyError(lib.fhg_last_error().decode())
+    _native.check(rc)
+    r = rows.value
+    host = []
+    for t in (labels, probs, linkage, ctp[:r], ctc[:r], ctl[:r], cts[:r], smst):
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        host.append(h)
+    torch.cuda.current_stream().synchronize()
+    host = [h.numpy() for h in host]
+    ct = CondensedTree(host[3], host[4], host[5], host[6])
+    return host[0].astype(np.intp, copy=False), host[1], host[2], ct, host[7]
+
+
 def clusters_from_spanning_tree(minimum_spanning_tree, data_labels=None, semi_supervised=False,
                                 ss_algorithm="bc", min_cluster_size=10,
                                 cluster_selection_method="eom", max_cluster_size=np.inf,
                                 allow_single_cluster=False, cluster_selection_epsilon=0.0,
                                 cluster_selection_persistence=0.0, sample_weights=None):
-    """hdbscan.py:497: labels, probabilities, linkage, condensed tree, sorted MST."""
+    """hdbscan.py:497: labels, probabilities, linkage, condensed tree, sorted MST.
+
+    One call of fhg_clusters_from_mst (every stage on the GPU, one upload,
+    one batch of copies back); a single point goes through the step-by-step
+    functions."""
     if semi_supervised:
         raise NotImplementedError("semi-supervised selection is not on the GPU path")
     n_points = minimum_spanning_tree.shape[0] + 1
+    if n_points >= 2:
+        method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
+        if method is None:
+            raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
+        return _clusters_from_mst(minimum_spanning_tree, method, min_cluster_size,
+                                  max_cluster_size, allow_single_cluster,
+                                  cluster_selection_epsilon, cluster_selection_persistence,
+                                  sample_weights)
     sorted_mst = sort_mst(minimum_spanning_tree)
     if sample_weights is None:
         linkage_tree = mst_to_linkage_tree(sorted_mst)

@@ -185,6 +185,28 @@ int fhg_precomputed_mst(const int32_t* rows_dev, const int32_t* cols_dev, const 
                         double* edges_dev, int32_t* neighbors_dev, double* core_dev,
                         int64_t* n_components_host, void* stream);
 
+/* hdbscan.py:497 clusters_from_spanning_tree (unsupervised) in one call:
+ * the tree of n points given as n - 1 float64 rows (src, dst, weight) in any
+ * order is sorted by (weight, src, dst), turned into its linkage tree
+ * (sample_weights_dev: n float32 or NULL, as fhg_mst_to_linkage_tree),
+ * condensed with min_cluster_size, simplified with persistence > 0, and its
+ * clusters selected (selection_method 0 = eom with max_cluster_size and
+ * allow_single_cluster, 1 = leaf; epsilon > 0: cluster_epsilon_search), then
+ * every point labelled with its membership strength.  Outputs as
+ * fhg_hdbscan_fit: labels (int64), probabilities (float32), the sorted tree
+ * (n - 1 x 3 float64, nullable), the linkage tree (n - 1 x 4 float64,
+ * nullable), the condensed tree (capacity 2n rows, *ct_rows_host written),
+ * the selected clusters.  n >= 2; the endpoint precondition of
+ * fhg_mst_to_linkage_tree applies. */
+int fhg_clusters_from_mst(const double* mst_dev, int64_t n, int64_t min_cluster_size,
+                          int32_t selection_method, double max_cluster_size,
+                          int allow_single_cluster, double epsilon, double persistence,
+                          const float* sample_weights_dev, int64_t* labels_dev, float* probs_dev,
+                          double* sorted_mst_dev, double* linkage_dev, int64_t* ct_parent_dev,
+                          int64_t* ct_child_dev, float* ct_lambda_dev, float* ct_size_dev,
+                          int64_t* ct_rows_host, int64_t* selected_dev,
+                          int64_t* n_selected_host, void* stream);
+
 /* Replaces the np.lexsort((mst[:,1], mst[:,0], mst[:,2])) of hdbscan.py:511:
  * rows of an m x 3 float64 edge list ordered by (weight, src, dst). */
 int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream);

@@ -99,3 +99,65 @@ def test_weighted_linkage_and_condense_bitexact(engine, name):
     ct = condense_tree(g["linkage"], int(g["min_cluster_size"]), sample_weights=w)
     for a, b in zip(ct, _ct(g)):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", CASES + WEIGHTED)
+def test_clusters_from_spanning_tree_fused_bitexact(engine, name):
+    """hdbscan.py:497 clusters_from_spanning_tree in one fused call
+    (fhg_clusters_from_mst) on the reference's raw MST with the fixture's
+    selection options: labels, probabilities, linkage tree, condensed tree and
+    sorted MST equal the reference's arrays."""
+    from fast_hdbscan_gb300.hdbscan import clusters_from_spanning_tree
+
+    g = _golden(name)
+    w = g["sample_weights"] if "sample_weights" in g.files else None
+    labels, probs, linkage, ct, smst = clusters_from_spanning_tree(
+        g["mst_raw"], min_cluster_size=int(g["min_cluster_size"]),
+        cluster_selection_method=str(g["cluster_selection_method"]),
+        max_cluster_size=float(g["max_cluster_size"]),
+        allow_single_cluster=bool(g["allow_single_cluster"]),
+        cluster_selection_epsilon=float(g["cluster_selection_epsilon"]),
+        cluster_selection_persistence=float(g["cluster_selection_persistence"]),
+        sample_weights=w)
+    np.testing.assert_array_equal(smst, g["sorted_mst"])
+    np.testing.assert_array_equal(linkage, g["linkage"])
+    for a, b in zip(ct, _ct(g)):
+        np.testing.assert_array_equal(a, b)
+        assert a.dtype == b.dtype
+    np.testing.assert_array_equal(labels, g["labels"])
+    np.testing.assert_array_equal(probs, g["probabilities"])
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_clusters_from_spanning_tree_fused_vs_oracle(engine, seed):
+    """The fused call against the oracle's clusters_from_spanning_tree on
+    random trees with heavily tied integer weights (the sort's (weight, src,
+    dst) order decides), both selection methods, epsilon, persistence,
+    max_cluster_size, allow_single_cluster and sample weights."""
+    from fast_hdbscan_gb300.hdbscan import clusters_from_spanning_tree
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(50, 3000))
+    parent = np.array([rng.integers(0, i) for i in range(1, n)])
+    child = np.arange(1, n)
+    flip = rng.random(n - 1) < 0.5
+    src, dst = np.where(flip, child, parent), np.where(flip, parent, child)
+    wts = rng.integers(1, 12, size=n - 1).astype(np.float64) * 0.25
+    mst = np.stack([src, dst, wts], axis=1).astype(np.float64)[rng.permutation(n - 1)]
+    kw = dict(min_cluster_size=int(rng.integers(3, 40)),
+              cluster_selection_method=["eom", "leaf"][seed % 2],
+              max_cluster_size=[np.inf, float(n // 3)][(seed // 2) % 2],
+              allow_single_cluster=bool(seed % 3 == 0),
+              cluster_selection_epsilon=[0.0, 0.6][seed % 3 == 1],
+              cluster_selection_persistence=[0.0, 0.3][seed % 4 == 2])
+    w = (rng.integers(1, 5, size=n).astype(np.float32) if seed >= 4 else None)
+    labels, probs, linkage, ct, smst = clusters_from_spanning_tree(mst, sample_weights=w, **kw)
+    o_labels, o_probs, o_linkage, o_ct, o_smst, _ = O.clusters_from_spanning_tree(
+        mst, sample_weights=w, **kw)
+    np.testing.assert_array_equal(smst, o_smst)
+    np.testing.assert_array_equal(linkage, o_linkage)
+    for a, b in zip(ct, o_ct):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(labels, o_labels)
+    np.testing.assert_array_equal(probs, o_probs)
