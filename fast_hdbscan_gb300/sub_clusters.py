@@ -11,6 +11,7 @@ pairs, and the optional propagation of labels to noise points runs on the
 GPU for every cluster in one launch.  The validation, the returned tuple and
 the fitted attributes are the reference's interface."""
 import concurrent.futures
+import os
 import threading
 
 import numpy as np
@@ -34,7 +35,7 @@ def check_is_fitted(estimator, attributes, msg):
         raise NotFittedError(msg)
 
 
-def cluster_layout(labels, num_clusters, neighbors, min_spanning_tree):
+def cluster_layout(labels, num_clusters, neighbors, min_spanning_tree, device=None):
     """Every cluster's inputs in one pass, clusters back to back.
 
     Returns (points, bounds, nb_local, mst_local, mst_bounds): the clustered
@@ -43,29 +44,40 @@ def cluster_layout(labels, num_clusters, neighbors, min_spanning_tree):
     neighbours outside the cluster), and the MST edges with both ends in one
     cluster, grouped by cluster in their original order with in-cluster ids
     (cluster c's at mst_local[mst_bounds[c]:mst_bounds[c+1]]) -- the arrays
-    sub_clusters.py:16-61 cuts out for each cluster."""
-    labels = np.asarray(labels)
-    order = np.argsort(labels, kind="stable")
-    bounds = np.searchsorted(labels[order], np.arange(num_clusters + 1))
+    sub_clusters.py:16-61 cuts out for each cluster.  The passes (a stable
+    sort of the labels, the gathers) run as torch operations on ``device``
+    (the GPU when there is one); the results come back as NumPy arrays."""
+    import torch
+
+    if device is None:
+        device = "cuda" if torch.cuda.is_available() else "cpu"
+    lab = torch.as_tensor(np.ascontiguousarray(labels, dtype=np.int64), device=device)
+    n = lab.numel()
+    order = torch.sort(lab, stable=True).indices
+    marks = torch.arange(num_clusters + 1, dtype=torch.int64, device=device)
+    bounds = torch.searchsorted(lab[order].contiguous(), marks)
     points = order[bounds[0]:]
     bounds = bounds - bounds[0]
-    sizes = np.diff(bounds)
-    owner = np.repeat(np.arange(num_clusters), sizes)
-    local = np.full(len(labels), -1, dtype=np.int64)
-    local[points] = np.arange(len(points)) - np.repeat(bounds[:-1], sizes)
-    nb = np.asarray(neighbors)[points]
-    nb_c = np.maximum(nb, 0)
-    inside = (nb >= 0) & (labels[nb_c] == owner[:, None])
-    nb_local = np.where(inside, local[nb_c], -1).astype(np.int32)
-    mst = np.asarray(min_spanning_tree, dtype=np.float64)
-    pe = labels[mst[:, 0].astype(np.int64)]
-    ce = labels[mst[:, 1].astype(np.int64)]
-    kept = np.nonzero((pe == ce) & (pe >= 0))[0]
-    kept = kept[np.argsort(pe[kept], kind="stable")]
-    mst_bounds = np.searchsorted(pe[kept], np.arange(num_clusters + 1))
-    mst_local = mst[kept].copy()
-    mst_local[:, :2] = local[mst_local[:, :2].astype(np.int64)]
-    return points, bounds, nb_local, mst_local, mst_bounds
+    sizes = bounds[1:] - bounds[:-1]
+    owner = torch.repeat_interleave(marks[:-1], sizes)
+    local = torch.full((n,), -1, dtype=torch.int64, device=device)
+    local[points] = (torch.arange(points.numel(), dtype=torch.int64, device=device)
+                     - torch.repeat_interleave(bounds[:-1], sizes))
+    nb = torch.as_tensor(np.ascontiguousarray(neighbors), device=device)[points].long()
+    nb_c = nb.clamp(min=0)
+    inside = (nb >= 0) & (lab[nb_c] == owner[:, None])
+    nb_local = torch.where(inside, local[nb_c], torch.full_like(nb_c, -1)).to(torch.int32)
+    mst = torch.as_tensor(np.ascontiguousarray(min_spanning_tree, dtype=np.float64),
+                          device=device).reshape(-1, 3)
+    pe = lab[mst[:, 0].long()]
+    ce = lab[mst[:, 1].long()]
+    kept = torch.nonzero((pe == ce) & (pe >= 0)).flatten()
+    kept = kept[torch.sort(pe[kept], stable=True).indices]
+    mst_bounds = torch.searchsorted(pe[kept].contiguous(), marks)
+    mst_local = mst[kept].clone()
+    mst_local[:, :2] = local[mst_local[:, :2].long()].double()
+    return (points.cpu().numpy(), bounds.cpu().numpy(), nb_local.cpu().numpy(),
+            mst_local.cpu().numpy(), mst_bounds.cpu().numpy())
 
 
 def cluster_lens_values(lens, data, probabilities, points, bounds, nb_local, core, mst_local,
@@ -124,7 +136,8 @@ def compute_sub_clusters_per_cluster(data, labels, probabilities, neighbors, cor
     torch.cuda.current_stream().synchronize()
     if num_clusters <= 1:
         return [hierarchy(c) for c in range(num_clusters)]
-    with concurrent.futures.ThreadPoolExecutor(min(8, num_clusters)) as ex:
+    workers = min(16, os.cpu_count() or 8, num_clusters)
+    with concurrent.futures.ThreadPoolExecutor(workers) as ex:
         return list(ex.map(hierarchy, range(num_clusters)))
 
 

@@ -194,3 +194,32 @@ def test_cycle_rule_equals_sequential_merge(name):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     ours = _cycle_rule_forest(g["weights"], g["indices"], g["indptr"])
     np.testing.assert_array_equal(ours, g["edges"])
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_cluster_layout_equals_per_cluster_slices(seed):
+    """cluster_layout (torch passes; CPU tensors here) cuts every cluster's
+    points, in-cluster kNN ids and in-cluster MST edges exactly as slicing one
+    cluster at a time does (sub_clusters.py:16-61)."""
+    from fast_hdbscan_gb300.sub_clusters import cluster_layout
+
+    rng = np.random.default_rng(seed)
+    n, k, ncl = 3000, 7, 9
+    labels = rng.integers(-1, ncl, size=n)
+    nbrs = rng.integers(-1, n, size=(n, k)).astype(np.int32)
+    parent = np.array([rng.integers(0, i) for i in range(1, n)])
+    mst = np.stack([np.arange(1, n), parent, rng.random(n - 1)], axis=1)[rng.permutation(n - 1)]
+    points, bounds, nb_local, mst_local, mst_bounds = cluster_layout(labels, ncl, nbrs, mst,
+                                                                      device="cpu")
+    for c in range(ncl):
+        pts = np.nonzero(labels == c)[0]
+        np.testing.assert_array_equal(points[bounds[c]:bounds[c + 1]], pts)
+        local = {p: i for i, p in enumerate(pts)}
+        want = np.array([[local.get(q, -1) if q >= 0 else -1 for q in row] for row in nbrs[pts]],
+                        dtype=np.int32).reshape(-1, k)
+        np.testing.assert_array_equal(nb_local[bounds[c]:bounds[c + 1]], want)
+        rows = [(local[a], local[b], w) for a, b, w in mst
+                if labels[int(a)] == c and labels[int(b)] == c]
+        got = mst_local[mst_bounds[c]:mst_bounds[c + 1]]
+        np.testing.assert_array_equal(got, np.array(rows, dtype=np.float64).reshape(-1, 3))
+    assert nb_local.dtype == np.int32 and mst_local.dtype == np.float64
