@@ -86,14 +86,17 @@ def fit_many(instances, min_samples=10, min_cluster_size=10, cluster_selection_m
     method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
     if method is None:
         raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
-    Xs = [np.ascontiguousarray(X, dtype=np.float32) for X in instances]
+    Xs = [np.asarray(X) for X in instances]
+    bad = "every instance must be a finite n x d array with d <= 30"
     for X in Xs:
-        if X.ndim != 2 or X.shape[1] > 30 or not np.all(np.isfinite(X)):
-            raise ValueError("every instance must be a finite n x d array with d <= 30")
+        if X.ndim != 2 or X.shape[1] > 30:
+            raise ValueError(bad)
     results = [None] * count
     run = [i for i in range(count) if Xs[i].shape[0] >= 2]
     for i in range(count):
         if Xs[i].shape[0] < 2:  # hdbscan.py:278-304
+            if not np.all(np.isfinite(Xs[i])):
+                raise ValueError(bad)
             results[i] = (np.full(Xs[i].shape[0], -1, dtype=np.intp),
                           np.zeros(Xs[i].shape[0], dtype=np.float32))
     if not run:
@@ -102,8 +105,15 @@ def fit_many(instances, min_samples=10, min_cluster_size=10, cluster_selection_m
     offs = np.concatenate([[0], np.cumsum(sizes)])
     npts = np.array([Xs[i].shape[0] for i in run], dtype=np.int64)
     poffs = np.concatenate([[0], np.cumsum(npts)])
-    flat = torch.from_numpy(np.concatenate([Xs[i].ravel() for i in run])).pin_memory()
+    # every instance written once, as float32, straight into pinned memory;
+    # the finite check runs on the GPU
+    flat = torch.empty(int(offs[-1]), dtype=torch.float32, pin_memory=True)
+    fv = flat.numpy()
+    for j, i in enumerate(run):
+        fv[offs[j]:offs[j + 1]] = Xs[i].reshape(-1)
     d_x = flat.to("cuda", non_blocking=True)
+    if not bool(torch.isfinite(d_x).all()):
+        raise ValueError(bad)
     d_lab = torch.empty(int(poffs[-1]), dtype=torch.int64, device="cuda")
     d_prob = torch.empty(int(poffs[-1]), dtype=torch.float32, device="cuda")
     m = len(run)
@@ -126,8 +136,9 @@ def fit_many(instances, min_samples=10, min_cluster_size=10, cluster_selection_m
     lab.copy_(d_lab, non_blocking=True)
     prob.copy_(d_prob, non_blocking=True)
     torch.cuda.current_stream().synchronize()
-    lab, prob = lab.numpy(), prob.numpy()
+    # one copy out of pinned memory; each instance's results are views of it
+    lab, prob = lab.numpy().astype(np.intp, copy=True), prob.numpy().copy()
     for j, i in enumerate(run):
         a, b = int(poffs[j]), int(poffs[j + 1])
-        results[i] = (lab[a:b].astype(np.intp, copy=True), prob[a:b].copy())
+        results[i] = (lab[a:b], prob[a:b])
     return results

@@ -60,3 +60,26 @@ def test_autotuned_workers(engine):
     for (a, b), (c, d) in zip(auto, fixed):
         np.testing.assert_array_equal(a, c)
         np.testing.assert_array_equal(b, d)
+
+
+def test_fit_many_input_checks(engine):
+    """A non-finite instance is rejected (checked on the GPU after the one
+    upload), as is a row wider than 30; float64 instances give the float32
+    fits."""
+    import pytest as _pytest
+
+    from fast_hdbscan_gb300.batch import fit_many
+
+    X = synthetic.blobs_2d(2000, seed=5)
+    Y = X[:700].copy()
+    Y[13, 1] = np.nan
+    with _pytest.raises(ValueError):
+        fit_many([X, Y], min_samples=5, min_cluster_size=20)
+    with _pytest.raises(ValueError):
+        fit_many([np.zeros((10, 31), np.float32)], min_samples=5, min_cluster_size=5)
+    a = fit_many([X, X[:900]], min_samples=5, min_cluster_size=20)
+    b = fit_many([X.astype(np.float64), X[:900].astype(np.float64)], min_samples=5,
+                 min_cluster_size=20)
+    for (p, q), (r, s) in zip(a, b):
+        np.testing.assert_array_equal(p, r)
+        np.testing.assert_array_equal(q, s)
