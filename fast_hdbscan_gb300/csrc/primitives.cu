@@ -5,6 +5,8 @@
 // scatter kernel.  The scatter keeps LSD stability by letting each warp rank
 // its 512 items in order (warp match on the digit, per-warp running counters)
 // and adding the per-warp prefix of each digit.
+#include <algorithm>
+
 #include "primitives.cuh"
 
 namespace fhg {
@@ -194,6 +196,52 @@ __global__ void __launch_bounds__(kRsThreads) rs_scatter_kernel(
     }
 }
 
+// The same sort for n <= kRsTile in one launch: a bitonic sort in shared
+// memory of (digits, position) pairs, where digits are the key bits the LSD
+// passes cover ([begin, end) rounded up to whole 8-bit digits), so the order
+// is the stable one the passes give.
+constexpr int kRsSmallThreads = 1024;
+template <class K>
+__global__ void __launch_bounds__(kRsSmallThreads) rs_small_kernel(K* keys, int32_t* vals, int n,
+                                                                   int shift, int bits) {
+    __shared__ K sk[kRsTile];
+    __shared__ uint16_t si[kRsTile];
+    __shared__ int32_t sv[kRsTile];
+    const K mask = bits >= (int)(8 * sizeof(K)) ? ~K(0) : ((K(1) << bits) - K(1));
+    int m2 = 1;
+    while (m2 < n) m2 <<= 1;
+    for (int i = threadIdx.x; i < m2; i += blockDim.x) {
+        sk[i] = i < n ? keys[i] : ~K(0);
+        si[i] = i < n ? (uint16_t)i : (uint16_t)0xffffu;  // padding sorts last
+        if (i < n) sv[i] = vals ? vals[i] : 0;
+    }
+    __syncthreads();
+    for (int size = 2; size <= m2; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < m2; i += blockDim.x) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const K da = (sk[i] >> shift) & mask, db = (sk[j] >> shift) & mask;
+                    const bool greater = da > db || (da == db && si[i] > si[j]);
+                    if (greater == ((i & size) == 0)) {
+                        const K tk = sk[i];
+                        sk[i] = sk[j];
+                        sk[j] = tk;
+                        const uint16_t ti = si[i];
+                        si[i] = si[j];
+                        si[j] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        keys[i] = sk[i];
+        if (vals) vals[i] = sv[si[i]];
+    }
+}
+
 template <class K>
 int radix_sort(Workspace& ws, K* keys, int32_t* vals, int64_t n, int begin_bit, int end_bit) {
     if (n <= 1 || end_bit <= begin_bit) return FHG_OK;
@@ -202,6 +250,14 @@ int radix_sort(Workspace& ws, K* keys, int32_t* vals, int64_t n, int begin_bit, 
         return FHG_ERR_INVALID;
     }
     cudaStream_t s = ws.stream();
+    if (n <= kRsTile) {
+        const int bits = std::min(((end_bit - begin_bit + 7) / 8) * 8,
+                                  (int)(8 * sizeof(K)) - begin_bit);
+        ::fhg::note_launch();
+        rs_small_kernel<K><<<1, kRsSmallThreads, 0, s>>>(keys, vals, (int)n, begin_bit, bits);
+        FHG_CUDA(cudaGetLastError());
+        return FHG_OK;
+    }
     const int64_t tiles = (n + kRsTile - 1) / kRsTile;
     K* kalt;
     int32_t* valt;
