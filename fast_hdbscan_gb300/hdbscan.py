@@ -596,6 +596,9 @@ def _clusters_from_mst(mst, method, min_cluster_size, max_cluster_size, allow_si
     mst = np.ascontiguousarray(mst, dtype=np.float64).reshape(-1, 3)
     m = mst.shape[0]
     n = m + 1
+    if sample_weights is not None and np.shape(sample_weights) != (n,):
+        raise ValueError(f"sample_weights has shape {np.shape(sample_weights)}; a tree of "
+                         f"{m} edges needs one weight per point ({n})")
     d_mst = _native.to_device(mst, np.float64)
     d_w = (_native.to_device(np.ascontiguousarray(sample_weights, dtype=np.float32), np.float32)
            if sample_weights is not None else None)

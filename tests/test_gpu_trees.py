@@ -161,3 +161,17 @@ def test_clusters_from_spanning_tree_fused_vs_oracle(engine, seed):
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(labels, o_labels)
     np.testing.assert_array_equal(probs, o_probs)
+
+
+def test_clusters_from_spanning_tree_weight_shape(engine):
+    """A tree of m edges takes m + 1 sample weights; others are rejected
+    before any device work."""
+    from fast_hdbscan_gb300.hdbscan import clusters_from_spanning_tree
+
+    mst = np.array([[0, 1, 0.5], [1, 2, 0.7], [2, 3, 0.2]])
+    with pytest.raises(ValueError):
+        clusters_from_spanning_tree(mst, min_cluster_size=2,
+                                    sample_weights=np.ones(3, np.float32))
+    labels, probs, *_ = clusters_from_spanning_tree(mst, min_cluster_size=2,
+                                                    sample_weights=np.ones(4, np.float32))
+    assert labels.shape == (4,) and probs.shape == (4,)
