@@ -351,7 +351,8 @@ def gpu_fit(X, min_samples, min_cluster_size, cluster_selection_method="eom",
 def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_method="eom",
                     max_cluster_size=np.inf, allow_single_cluster=False,
                     cluster_selection_epsilon=0.0, cluster_selection_persistence=0.0,
-                    return_trees=True, sample_weights=None, knn_graph=False):
+                    return_trees=True, sample_weights=None, knn_graph=False,
+                    condensed_records=False):
     """One call of fhg_hdbscan_fit_kruskal: the kNN-graph Kruskal MST
     (kruskal.py:950) and the tree passes on the GPU, outputs copied back.
     knn_graph: fhg_hdbscan_fit_knn_graph instead, the d > 30 route
@@ -406,24 +407,51 @@ def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_m
     if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
         raise KeyError(lib.fhg_last_error().decode())
     _native.check(rc)
-    r, k = rows.value, nsel.value
-    labels_h = labels.cpu().numpy().astype(np.intp, copy=False)
+    return _fit_outputs_to_host(labels, probs, sel, nsel.value, trees, rows.value, linkage,
+                                ctp, ctc, ctl, cts, mst, nbrs, core, condensed_records)
+
+
+def _fit_outputs_to_host(labels, probs, sel, k, trees, r=0, linkage=None, ctp=None, ctc=None,
+                         ctl=None, cts=None, mst=None, nbrs=None, core=None, records=False):
+    """A fit's device outputs as a FitResult of NumPy arrays: every copy
+    queued at once into pinned host memory, one synchronisation.  With
+    records the condensed tree comes back as the record array HDBSCAN.fit
+    stores (hdbscan.py:93), laid out on the GPU."""
+    torch = _native._torch()
+    outs = [labels, probs, sel[:k]]
+    if trees:
+        if records:
+            rec = torch.empty(max(r, 1) * _REC_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+            if r > 0:
+                _native.check(_native.load().fhg_condensed_record_array(
+                    _native.vptr(ctp), _native.vptr(ctc), _native.vptr(ctl), _native.vptr(cts),
+                    r, _native.vptr(rec), _native.stream_ptr()))
+            cts_out = [rec[: r * _REC_DTYPE.itemsize]]
+        else:
+            cts_out = [ctp[:r], ctc[:r], ctl[:r], cts[:r]]
+        outs += [linkage, mst, nbrs, core] + cts_out
+    host = []
+    for t in outs:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        host.append(h)
+    torch.cuda.current_stream().synchronize()
+    host = [h.numpy() for h in host]
+    labels_h = host[0].astype(np.intp, copy=False)
     if not trees:
-        return FitResult(labels_h, probs.cpu().numpy(), None, None, None, None, None,
-                         sel[:k].cpu().numpy())
-    ct = CondensedTree(ctp[:r].cpu().numpy(), ctc[:r].cpu().numpy(), ctl[:r].cpu().numpy(),
-                       cts[:r].cpu().numpy())
-    return FitResult(labels_h, probs.cpu().numpy(), linkage.cpu().numpy(), ct,
-                     mst.cpu().numpy(), nbrs.cpu().numpy(), core.cpu().numpy(),
-                     sel[:k].cpu().numpy())
+        return FitResult(labels_h, host[1], None, None, None, None, None, host[2])
+    ct = host[7].view(_REC_DTYPE) if records else CondensedTree(*host[7:11])
+    return FitResult(labels_h, host[1], host[3], ct, host[4], host[5], host[6], host[2])
 
 
 def gpu_fit_precomputed(G, min_samples, min_cluster_size, algorithm="boruvka",
                         cluster_selection_method="eom", max_cluster_size=np.inf,
                         allow_single_cluster=False, cluster_selection_epsilon=0.0,
-                        cluster_selection_persistence=0.0, return_trees=True):
+                        cluster_selection_persistence=0.0, return_trees=True,
+                        condensed_records=False):
     """One call of fhg_hdbscan_fit_precomputed on a scipy sparse graph's COO
-    entries (metric="precomputed"), outputs copied back."""
+    entries (metric="precomputed"), outputs copied back (the condensed tree
+    as the record array with condensed_records)."""
     from .precomputed import validate_precomputed_sparse_graph
 
     validate_precomputed_sparse_graph(G)
@@ -459,16 +487,8 @@ def gpu_fit_precomputed(G, min_samples, min_cluster_size, algorithm="boruvka",
     if rc == _native.FHG_ERR_INVALID and "KeyError" in lib.fhg_last_error().decode():
         raise KeyError(lib.fhg_last_error().decode())
     _native.check(rc)
-    r, kk = rows_c.value, nsel.value
-    labels_h = labels.cpu().numpy().astype(np.intp, copy=False)
-    if not trees:
-        return FitResult(labels_h, probs.cpu().numpy(), None, None, None, None, None,
-                         sel[:kk].cpu().numpy())
-    ct = CondensedTree(ctp[:r].cpu().numpy(), ctc[:r].cpu().numpy(), ctl[:r].cpu().numpy(),
-                       cts[:r].cpu().numpy())
-    return FitResult(labels_h, probs.cpu().numpy(), linkage.cpu().numpy(), ct,
-                     mst.cpu().numpy(), nbrs.cpu().numpy(), core.cpu().numpy(),
-                     sel[:kk].cpu().numpy())
+    return _fit_outputs_to_host(labels, probs, sel, nsel.value, trees, rows_c.value, linkage,
+                                ctp, ctc, ctl, cts, mst, nbrs, core, condensed_records)
 
 
 def fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="bc",
@@ -523,19 +543,21 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
         fr = gpu_fit_precomputed(data, min_samples, min_cluster_size, algorithm,
                                  cluster_selection_method, max_cluster_size,
                                  allow_single_cluster, cluster_selection_epsilon,
-                                 cluster_selection_persistence, return_trees=return_trees)
+                                 cluster_selection_persistence, return_trees=return_trees,
+                                 condensed_records=condensed_records)
     elif _knn_graph_route(metric, data, sample_weights):  # hdbscan.py:446 -> nndescent.py:179
         ms = min_cluster_size if min_samples is None else min_samples
         fr = gpu_fit_kruskal(data, min_samples, min_cluster_size,
                              resolve_knn_graph_k(ms, knn_k), cluster_selection_method,
                              max_cluster_size, allow_single_cluster, cluster_selection_epsilon,
                              cluster_selection_persistence, return_trees=return_trees,
-                             knn_graph=True)
+                             knn_graph=True, condensed_records=condensed_records)
     elif algorithm == "kruskal":  # hdbscan.py:306-337 on the kNN-graph Kruskal MST
         fr = gpu_fit_kruskal(data, min_samples, min_cluster_size, knn_k,
                              cluster_selection_method, max_cluster_size, allow_single_cluster,
                              cluster_selection_epsilon, cluster_selection_persistence,
-                             return_trees=return_trees, sample_weights=sample_weights)
+                             return_trees=return_trees, sample_weights=sample_weights,
+                             condensed_records=condensed_records)
     else:
         # reproducible=True: the reference's own Boruvka tie choices
         with _native.tie_rule(bool(reproducible)):
@@ -735,7 +757,8 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
             kwargs = self.get_params()
             (self.labels_, self.probabilities_, self._single_linkage_tree,
              self._condensed_tree, self._min_spanning_tree, self._neighbors,
-             self._core_distances) = _fast_hdbscan(X, None, return_trees=True, **kwargs)
+             self._core_distances) = _fast_hdbscan(X, None, return_trees=True,
+                                                   condensed_records=True, **kwargs)
             self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
             return self
         if _is_tensor(X):

@@ -498,7 +498,7 @@ int fhg_core_graphs(int64_t P, int32_t k, const int32_t* nb_dev, const double* l
  * synchronise the stream before reading the host buffers.
  *   ct_records_dev (room for 2n records of 28 bytes, 4-byte aligned) receives
  *   the condensed tree as the record array HDBSCAN.fit stores (hdbscan.py:93,
- *   fields parent i8, child i8, lambda_val f4, child_size f4, packed), as
+ *   fields parent i8, child i8, lambda_val f8, child_size f4, packed), as
  *   fhg_condensed_record_array writes it; it needs the ct_* buffers.
  * Each exported output needs its device buffer (FHG_ERR_INVALID otherwise). */
 int fhg_hdbscan_fit_export(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
