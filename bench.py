@@ -491,7 +491,8 @@ def run_gb300(args):
         # condensed tree 28 B/row, neighbours n x ms i32, core distances f32 (Kruskal: f64)
         d2h = (n * 8 + n * 4 + (n - 1) * 24 + (n - 1) * 32 + rows_out * 28 + n * ms * 4
                + n * (8 if (kruskal or pre or kgraph) else 4))
-        h2d = n * WORKLOAD["graph_k"] * 16 if pre else n * d * 4  # graph: rows, cols, f64
+        # CSR graph: row pointers (int64), column indices (int32), weights (float64)
+        h2d = 8 * (n + 1) + 12 * n * WORKLOAD["graph_k"] if pre else n * d * 4
         e2e = {"value": round(n * world / e2e_s, 1), "unit": "points/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "s_per_step": round(e2e_s, 4),

@@ -452,20 +452,16 @@ def gpu_fit_precomputed(G, min_samples, min_cluster_size, algorithm="boruvka",
     """One call of fhg_hdbscan_fit_precomputed on a scipy sparse graph's COO
     entries (metric="precomputed"), outputs copied back (the condensed tree
     as the record array with condensed_records)."""
-    from .precomputed import validate_precomputed_sparse_graph
+    from .precomputed import graph_to_device, validate_precomputed_sparse_graph
 
-    validate_precomputed_sparse_graph(G)
-    coo = G.tocoo()
+    validate_precomputed_sparse_graph(G, check_values=False)
     n = G.shape[0]
     ms = min_cluster_size if min_samples is None else min_samples
     k = max(1, int(ms))
     method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)
     if method is None:
         raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
-    to_dev = _native.to_device
-    rows = to_dev(np.ascontiguousarray(coo.row, np.int32), np.int32)
-    cols = to_dev(np.ascontiguousarray(coo.col, np.int32), np.int32)
-    data = to_dev(np.ascontiguousarray(coo.data, np.float64), np.float64)
+    rows, cols, data = graph_to_device(G)
     E = _native.empty
     labels, probs, sel = E(n, np.int64), E(n, np.float32), E(n, np.int64)
     trees = return_trees
@@ -478,7 +474,7 @@ def gpu_fit_precomputed(G, min_samples, min_cluster_size, algorithm="boruvka",
     rows_c, nsel = ctypes.c_int64(0), ctypes.c_int64(0)
     V, lib = _native.vptr, _native.load()
     rc = lib.fhg_hdbscan_fit_precomputed(
-        V(rows), V(cols), V(data), int(coo.nnz), n, int(ms),
+        V(rows), V(cols), V(data), int(data.numel()), n, int(ms),
         1 if algorithm == "kruskal" else 0, int(min_cluster_size), method,
         float(max_cluster_size), int(bool(allow_single_cluster)),
         float(cluster_selection_epsilon), float(cluster_selection_persistence), V(labels),
@@ -748,7 +744,7 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
         if self.metric == "precomputed":  # hdbscan.py:688-697: a scipy sparse graph
             from .precomputed import validate_precomputed_sparse_graph
 
-            validate_precomputed_sparse_graph(X)
+            validate_precomputed_sparse_graph(X, check_values=False)  # weights: on the GPU
             if sample_weight is not None:
                 raise NotImplementedError(
                     "sample_weights is not supported with metric='precomputed'.")

@@ -7,9 +7,10 @@ import numpy as np
 from . import _native
 
 
-def validate_precomputed_sparse_graph(X):
+def validate_precomputed_sparse_graph(X, check_values=True):
     """precomputed.py:30: a square scipy sparse matrix with finite,
-    non-negative stored weights."""
+    non-negative stored weights (check_values=False: the shape only, the
+    weights being checked on the GPU by graph_to_device)."""
     import scipy.sparse
 
     if not scipy.sparse.issparse(X):
@@ -19,25 +20,52 @@ def validate_precomputed_sparse_graph(X):
     if X.ndim != 2 or X.shape[0] != X.shape[1]:
         raise ValueError("When metric='precomputed', X must be a square matrix. "
                          "Got shape: %s" % str(X.shape))
-    data = X.tocoo().data
+    if check_values:
+        _check_weights(np.asarray(X.data), np)
+
+
+def _check_weights(data, xp):
+    """The stored weights' checks of precomputed.py:30, on NumPy or torch
+    arrays."""
     if len(data) > 0:
-        if np.any(~np.isfinite(data)):
+        if bool(xp.any(~xp.isfinite(data))):
             raise ValueError("When metric='precomputed', all stored edge weights must be "
                              "finite. Found NaN or Inf values.")
-        if np.any(data < 0):
+        if bool(xp.any(data < 0)):
             raise ValueError("When metric='precomputed', all stored edge weights must be "
                              "non-negative. Found negative values.")
 
 
+def graph_to_device(X):
+    """The stored entries of a scipy sparse graph as device arrays (rows
+    int32, cols int32, weights float64) in the order X.tocoo() lists them:
+    row by row for CSR, column by column for CSC, as stored for COO.  The
+    compressed index of CSR / CSC is expanded on the GPU, and the weights are
+    checked there."""
+    torch = _native._torch()
+    dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dt)).cuda()  # noqa: E731
+    if X.format in ("csr", "csc"):
+        ptr = dev(X.indptr, np.int64)
+        major = torch.repeat_interleave(
+            torch.arange(X.shape[0] if X.format == "csr" else X.shape[1], dtype=torch.int32,
+                         device="cuda"), ptr[1:] - ptr[:-1])
+        minor = dev(X.indices, np.int32)
+        rows, cols = (major, minor) if X.format == "csr" else (minor, major)
+    else:
+        coo = X.tocoo()
+        rows, cols = dev(coo.row, np.int32), dev(coo.col, np.int32)
+        X = coo
+    data = dev(X.data, np.float64)
+    _check_weights(data, torch)
+    return rows.contiguous(), cols.contiguous(), data
+
+
 def _precomputed_mst(X, min_samples, algorithm):
     torch = _native._torch()
-    validate_precomputed_sparse_graph(X)
-    coo = X.tocoo()
+    validate_precomputed_sparse_graph(X, check_values=False)
     n = X.shape[0]
     k = max(1, int(min_samples))
-    rows = torch.from_numpy(np.ascontiguousarray(coo.row, np.int32)).cuda()
-    cols = torch.from_numpy(np.ascontiguousarray(coo.col, np.int32)).cuda()
-    data = torch.from_numpy(np.ascontiguousarray(coo.data, np.float64)).cuda()
+    rows, cols, data = graph_to_device(X)
     edges = torch.empty((max(n - 1, 0), 3), dtype=torch.float64, device="cuda")
     nbrs = torch.empty((n, k), dtype=torch.int32, device="cuda")
     core = torch.empty((n,), dtype=torch.float64, device="cuda")

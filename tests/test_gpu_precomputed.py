@@ -100,3 +100,30 @@ def test_precomputed_validation(engine):
     with pytest.raises(NotImplementedError):
         fast_hdbscan(scipy.sparse.csr_matrix(np.eye(5, k=1)), metric="precomputed",
                      sample_weights=np.ones(5))
+
+
+def test_graph_to_device_matches_tocoo(engine):
+    """The device entries of a CSR, CSC or COO graph (the compressed index
+    expanded on the GPU) list exactly what X.tocoo() lists, in its order; the
+    weight checks on the GPU raise the reference's errors."""
+    import scipy.sparse
+
+    from fast_hdbscan_gb300.hdbscan import HDBSCAN
+    from fast_hdbscan_gb300.precomputed import graph_to_device
+
+    rng = np.random.default_rng(3)
+    dense = rng.random((60, 60)) * (rng.random((60, 60)) < 0.2)
+    for X in (scipy.sparse.csr_matrix(dense), scipy.sparse.csc_matrix(dense),
+              scipy.sparse.coo_matrix(dense), scipy.sparse.csr_matrix(dense).tolil()):
+        rows, cols, data = graph_to_device(X)
+        coo = X.tocoo()
+        np.testing.assert_array_equal(rows.cpu().numpy(), coo.row)
+        np.testing.assert_array_equal(cols.cpu().numpy(), coo.col)
+        np.testing.assert_array_equal(data.cpu().numpy(), coo.data)
+    bad = scipy.sparse.csr_matrix(dense)
+    bad.data[3] = np.inf
+    with pytest.raises(ValueError, match="finite"):
+        HDBSCAN(metric="precomputed").fit(bad)
+    bad.data[3] = -1.0
+    with pytest.raises(ValueError, match="non-negative"):
+        HDBSCAN(metric="precomputed").fit(bad)
