@@ -772,6 +772,19 @@ class HDBSCAN(_ClusterMixin, _BaseEstimator):
             X = Xd.cpu().numpy()
         X = check_array(X, ensure_all_finite=False)
         self._raw_data = X
+        if sample_weight is None and X.ndim == 2 and X.shape[0] >= 2:
+            # upload first, check finiteness on the GPU: a finite input goes
+            # straight on from the device copy (the float32 the engine uses)
+            Xd = _native.to_device(np.ascontiguousarray(X, dtype=np.float32), np.float32)
+            if bool(_native._torch().isfinite(Xd).all().item()):
+                self._all_finite = True
+                kwargs = self.get_params()
+                (self.labels_, self.probabilities_, self._single_linkage_tree,
+                 self._condensed_tree, self._min_spanning_tree, self._neighbors,
+                 self._core_distances) = _fast_hdbscan(Xd, None, return_trees=True,
+                                                       condensed_records=True, **kwargs)
+                self._condensed_tree = to_numpy_rec_array(self._condensed_tree)
+                return self
         if sample_weight is not None:
             sample_weight = _check_sample_weight(sample_weight, X, dtype=np.float32)
         self._all_finite = bool(np.all(np.isfinite(X)))
