@@ -255,3 +255,25 @@ def test_fit_export_copies_match_device_outputs(engine):
         ctypes.byref(nsel), None, _native.hptr(h), None, None, None, None, _native.stream_ptr())
     assert rc == _native.FHG_ERR_INVALID
     assert "device buffer" in lib.fhg_last_error().decode()
+
+
+@pytest.mark.parametrize("seed,d,side,n,ms,mcs", [
+    (0, 2, 200, 20_000, 10, 20), (1, 3, 40, 30_000, 5, 10), (2, 5, 8, 20_000, 3, 5),
+    (3, 2, 120, 8_000, 1, 5), (4, 3, 25, 12_000, 15, 40), (5, 4, 12, 15_000, 7, 15),
+])
+def test_fit_vs_oracle_integer_grid(engine, seed, d, side, n, ms, mcs):
+    """Distinct points of an integer grid: squared distances and core
+    distances tie everywhere, so every tie rule of the canonical mode (kNN
+    lists by (distance, index), a point's candidate by (weight, index), a
+    component's edge by (weight, min index, max index), orientation, sort,
+    condensed tree) is exercised; every output equals the oracle's bit for
+    bit."""
+    from fast_hdbscan_gb300.hdbscan import fast_hdbscan
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(1000 + seed)
+    cells = rng.choice(side ** d, size=n, replace=False)
+    X = np.stack([(cells // side ** j) % side for j in range(d)], axis=1).astype(np.float32)
+    res = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs, return_trees=True)
+    orc = O.fit(X, ms, mcs, mode=1, nthreads=8)
+    _assert_fit_equal(res, orc)
