@@ -568,7 +568,7 @@ def run_gb300(args):
                     "ms_per_step": round(ms_ref, 3), "vs_plain": round(ms_step_max / ms_ref, 4),
                     "stages_ms_per_step": {k: round(v[0] / args.steps, 3)
                                            for k, v in rst.items()
-                                           if k.startswith(("ref_tree", "tie_walk", "boruvka"))}}
+                                           if k.startswith(("ref_tree", "ref_knn", "tie_walk", "boruvka"))}}
 
     # many independent fits of uneven size in one call (the batched
     # executor), on the benchmark family's 4,096-instance batch

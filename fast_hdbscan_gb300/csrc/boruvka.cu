@@ -1058,6 +1058,15 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         FHG_TRY(knn_with_radius(ix, k, *ru, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
     else
         FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
+    // the reference tie mode breaks ties in the order of the reference's own
+    // KD-tree, built here exactly; its kNN lists (and so round 0 and the
+    // neighbour matrix) list equal distances in the order of the reference's
+    // query and heap, and replace the engine's rows (the same distances)
+    RefTree rt;
+    if (ref_ties && n > 1) {
+        FHG_TRY(ref_tree_build(ws, ix, &rt));
+        FHG_TRY(ref_knn(rt, ix, kq, weighted, knn_open, knn_d, knn_s, nbr_o, kq - 1, s));
+    }
     FHG_TRY(ws.alloc(&core2, (size_t)n));
     if (weighted) {
         float* w_s;
@@ -1161,12 +1170,9 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     FHG_TRY(ws.alloc(&kpos, (size_t)n));
     FHG_CUDA(cudaMemsetAsync(flag, 0, sizeof(uint32_t) * n, s));
 
-    // the reference tie mode breaks ties in the order of the reference's own
-    // KD-tree, built here exactly; its pointer-doubling buffers
-    RefTree rt;
+    // the reference tie mode's pointer-doubling buffers
     int32_t *cy_nxt = nullptr, *cy_mx = nullptr, *cy_nxt2 = nullptr, *cy_mx2 = nullptr;
     if (ref_ties && ncomp > 1) {
-        FHG_TRY(ref_tree_build(ws, ix, &rt));
         FHG_TRY(ws.alloc(&cy_nxt, (size_t)n));
         FHG_TRY(ws.alloc(&cy_mx, (size_t)n));
         FHG_TRY(ws.alloc(&cy_nxt2, (size_t)n));

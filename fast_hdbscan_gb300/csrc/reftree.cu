@@ -721,7 +721,190 @@ __global__ void __launch_bounds__(kSelThreads) select_level_kernel(
     }
 }
 
+// ----------------------------------------------- the reference's kNN query
+constexpr int kRefKnnMax = 64;  // heap entries
+constexpr int kRefStack = 64;   // pending subtrees of the walk (<= levels + 1)
+
+// simple_heap_push (numba_kdtree.py:578): a max-heap of k entries whose root
+// is replaced by a smaller priority and sifted down, with its tie rules.
+__device__ __forceinline__ void ref_heap_push(float* pri, int32_t* ind, int size, float p,
+                                              int32_t x) {
+    if (p >= pri[0]) return;
+    int i = 0;
+    while (true) {
+        const int c1 = 2 * i + 1, c2 = c1 + 1;
+        int sw;
+        if (c1 >= size) break;
+        if (c2 >= size) {
+            if (pri[c1] > p) sw = c1;
+            else break;
+        } else if (pri[c1] >= pri[c2]) {
+            if (p < pri[c1]) sw = c1;
+            else break;
+        } else {
+            if (p < pri[c2]) sw = c2;
+            else break;
+        }
+        pri[i] = pri[sw];
+        ind[i] = ind[sw];
+        i = sw;
+    }
+    pri[i] = p;
+    ind[i] = x;
+}
+
+// One thread per caller point: tree_query_recursion (numba_kdtree.py:680)
+// with an explicit stack -- a subtree is pruned when its bound exceeds the
+// heap's largest entry at the time it is visited, a leaf pushes its points in
+// tree order, an internal node visits the child of smaller bound first (the
+// left one on equal bounds) -- then deheap_sort (:652, siftdown :630).
+__global__ void __launch_bounds__(128) ref_knn_kernel(
+    RefTreeView t, const int32_t* __restrict__ tidx, const float* __restrict__ pts, int pad,
+    const int32_t* __restrict__ rank, const int32_t* __restrict__ orig,
+    const int32_t* __restrict__ list, int64_t count, int k, int kk, int sqrt_order,
+    float* __restrict__ d_s, int32_t* __restrict__ s_s, int32_t* __restrict__ nbr_o,
+    int nbr_cols) {
+    const int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= count) return;
+    const int64_t c = orig[list[li]];  // the query, by caller index
+    const int d = t.d;
+    float q[32];
+    const float* qp = pts + (int64_t)rank[c] * pad;
+    for (int j = 0; j < d; ++j) q[j] = qp[j];
+    float pri[kRefKnnMax], rd[kRefKnnMax];
+    int32_t ind[kRefKnnMax];
+    for (int j = 0; j < k; ++j) {
+        pri[j] = INFINITY;
+        ind[j] = -1;
+    }
+    int32_t st_v[kRefStack], st_s[kRefStack], st_e[kRefStack];
+    float st_lb[kRefStack];
+    int sp = 0;
+    st_v[0] = 0;
+    st_s[0] = 0;
+    st_e[0] = (int32_t)t.n;
+    st_lb[0] = ref_node_lb(t, 0, q);
+    sp = 1;
+    while (sp > 0) {
+        --sp;
+        const int32_t v = st_v[sp], s0 = st_s[sp], e0 = st_e[sp];
+        if (st_lb[sp] > pri[0]) continue;
+        if (2 * (int64_t)v + 1 >= t.nodes || e0 - s0 < 2) {
+            for (int32_t i = s0; i < e0; ++i) {
+                const int32_t x = tidx[i];
+                const float* xp = pts + (int64_t)rank[x] * pad;
+                float r = 0.0f;
+                for (int j = 0; j < d; ++j) {
+                    const float df = __fsub_rn(q[j], xp[j]);
+                    r = __fadd_rn(r, __fmul_rn(df, df));
+                }
+                if (r < pri[0]) ref_heap_push(pri, ind, k, r, x);
+            }
+        } else if (sp + 2 <= kRefStack) {
+            const int32_t mid = s0 + (e0 - s0) / 2, l = 2 * v + 1, r = l + 1;
+            const float bl = ref_node_lb(t, l, q), br = ref_node_lb(t, r, q);
+            // the child visited first goes on top
+            const bool left_first = bl <= br;
+            st_v[sp] = left_first ? r : l;
+            st_s[sp] = left_first ? mid : s0;
+            st_e[sp] = left_first ? e0 : mid;
+            st_lb[sp] = left_first ? br : bl;
+            ++sp;
+            st_v[sp] = left_first ? l : r;
+            st_s[sp] = left_first ? s0 : mid;
+            st_e[sp] = left_first ? mid : e0;
+            st_lb[sp] = left_first ? bl : br;
+            ++sp;
+        }
+    }
+    // deheap_sort on the distances the query returns: squared, or their
+    // square roots; the squared values travel with their entries
+    for (int j = 0; j < k; ++j) {
+        rd[j] = pri[j];
+        if (sqrt_order) pri[j] = __fsqrt_rn(pri[j]);
+    }
+    for (int j = k - 1; j > 0; --j) {
+        float tp = pri[0]; pri[0] = pri[j]; pri[j] = tp;
+        float tr = rd[0]; rd[0] = rd[j]; rd[j] = tr;
+        int32_t ti = ind[0]; ind[0] = ind[j]; ind[j] = ti;
+        int e = 0;  // siftdown of [0, j)
+        while (e * 2 + 1 < j) {
+            const int lc = e * 2 + 1, rc = lc + 1;
+            int sw = e;
+            if (pri[sw] < pri[lc]) sw = lc;
+            if (rc < j && pri[sw] < pri[rc]) sw = rc;
+            if (sw == e) break;
+            tp = pri[e]; pri[e] = pri[sw]; pri[sw] = tp;
+            tr = rd[e]; rd[e] = rd[sw]; rd[sw] = tr;
+            ti = ind[e]; ind[e] = ind[sw]; ind[sw] = ti;
+            e = sw;
+        }
+    }
+    const int64_t p = rank[c];
+    for (int j = 0; j < kk; ++j) {
+        d_s[p * kk + j] = rd[j];
+        s_s[p * kk + j] = ind[j] >= 0 ? rank[ind[j]] : -1;
+        if (nbr_o && j >= 1 && j - 1 < nbr_cols) nbr_o[c * nbr_cols + j - 1] = ind[j];
+    }
+}
+
+// Rows whose order can differ from the reference's: two entries at the same
+// distance (the reference lists them in its query and heap order, the engine
+// by index; with sqrt_order, the same square root), or a point outside the
+// list at the k-th distance (tie, from the kNN kernel: the reference keeps
+// the first one its walk meets).  Elsewhere the k nearest and their order
+// are unique.
+__global__ void tie_rows_kernel(int64_t n, int kk, int sqrt_order,
+                                const float* __restrict__ d_s, const int8_t* __restrict__ tie,
+                                uint32_t* __restrict__ flag) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    bool f = tie && tie[p] != 0;
+    for (int j = 0; j + 1 < kk && !f; ++j) {
+        const float a = d_s[p * kk + j], b = d_s[p * kk + j + 1];
+        f = sqrt_order ? __fsqrt_rn(a) == __fsqrt_rn(b) : a == b;
+    }
+    flag[p] = f ? 1u : 0u;
+}
+__global__ void tie_list_kernel(int64_t n, const uint32_t* __restrict__ flag,
+                                const uint32_t* __restrict__ pos, int32_t* __restrict__ list) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n && flag[p]) list[pos[p]] = (int32_t)p;
+}
+
 }  // namespace
+
+int ref_knn(const RefTree& t, const fhg_index& ix, int k, bool sqrt_order, const int8_t* tie,
+            float* d_s, int32_t* s_s, int32_t* nbr_o, int nbr_cols, cudaStream_t s) {
+    if (k < 1 || k > kRefKnnMax || t.d > 32 || t.levels + 1 > kRefStack) {
+        set_error("reference kNN: k = %d, d = %d, %d levels out of range", k, t.d, t.levels);
+        return FHG_ERR_UNSUPPORTED;
+    }
+    const int64_t n = t.n;
+    const int kk = (int)(k < n ? k : n);
+    Stage stage(s, "ref_knn");
+    Workspace tmp(s);
+    uint32_t *flag, *pos, *cnt;
+    int32_t* list;
+    FHG_TRY(tmp.alloc(&flag, (size_t)n));
+    FHG_TRY(tmp.alloc(&pos, (size_t)n));
+    FHG_TRY(tmp.alloc(&cnt, 1));
+    FHG_TRY(tmp.alloc(&list, (size_t)n));
+    LAUNCH(tie_rows_kernel, n, n, kk, sqrt_order ? 1 : 0, d_s, tie, flag);
+    FHG_TRY(scan_exclusive_u32(tmp, flag, pos, n, cnt));
+    LAUNCH(tie_list_kernel, n, n, flag, pos, list);
+    uint32_t h_cnt = 0;
+    FHG_CUDA(cudaMemcpyAsync(&h_cnt, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    FHG_CUDA(cudaStreamSynchronize(s));
+    profile_count("ref_knn_rows", (double)h_cnt);
+    if (h_cnt == 0) return FHG_OK;
+    ::fhg::note_launch();
+    ref_knn_kernel<<<grid_for((int64_t)h_cnt, 128), 128, 0, s>>>(
+        view_of(t), t.idx, ix.pts, ix.pad, ix.rank, ix.orig, list, (int64_t)h_cnt, k, kk,
+        sqrt_order ? 1 : 0, d_s, s_s, nbr_o, nbr_cols);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
 
 // [nodes][2][d] -> the reference's node_bounds layout [2][nodes][d]
 __global__ void bounds_layout_kernel(int64_t nodes, int d, const float* __restrict__ box,

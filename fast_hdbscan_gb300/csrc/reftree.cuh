@@ -37,6 +37,21 @@ int ref_tree_build(Workspace& ws, const fhg_index& ix, RefTree* out);
 // node_bounds [2][nodes][d] (either may be null).
 int ref_tree_export(const RefTree& t, int32_t* idx_array, float* node_bounds, cudaStream_t s);
 
+// numba_kdtree.py:765 parallel_tree_query(tree, data, k) for every point, as
+// the reference computes it: its depth-first walk of this tree, its max-heap
+// of k (squared distance, index) entries and its heap sort, so that equal
+// distances come out in the reference's order.  With sqrt_order the sort
+// runs on the square roots (the query without output_rdist, boruvka.py:567).
+// d_s / s_s hold the engine's lists (Morton-order rows of kk = min(k, n)
+// squared distances and Morton positions, (distance, index) order) and tie
+// (nullable) its flags of a point outside the list at the k-th distance; the
+// rows that can differ from the reference's -- equal distances inside, or a
+// tie at the k-th -- are recomputed by the reference's query and written
+// over, with columns 1.. of the caller-order neighbour matrix nbr_o
+// (nullable, nbr_cols columns).  k <= 64, d <= 32.
+int ref_knn(const RefTree& t, const fhg_index& ix, int k, bool sqrt_order, const int8_t* tie,
+            float* d_s, int32_t* s_s, int32_t* nbr_o, int nbr_cols, cudaStream_t s);
+
 // numba_kdtree.py:549 point_to_node_lower_bound_rdist of node v's box, in
 // the reference's float32 operation order.
 __device__ __forceinline__ float ref_node_lb(const RefTreeView& t, int64_t v, const float* q) {

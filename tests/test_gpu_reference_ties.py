@@ -32,34 +32,20 @@ def _kw(g):
                 cluster_selection_persistence=float(g["cluster_selection_persistence"]))
 
 
-# Exact duplicate points put equal distances inside kNN lists, which the
-# reference orders by its heap and the engine by index: round 0 (built from
-# the lists) then differs, so the tie mode is exact only up to tie-broken
-# edges there.
-KNN_TIES = {"edge_dups"}
-
-
 @pytest.mark.parametrize("name", FIT_FIXTURES)
 def test_reference_ties_fixture(engine, name):
     from fast_hdbscan_gb300.hdbscan import compute_minimum_spanning_tree, fast_hdbscan
-    from parity import tie_report
-
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     X = g["X"]
     ms, mcs = int(g["min_samples"]), int(g["min_cluster_size"])
     w = g["sample_weights"] if "sample_weights" in g.files else None
-    if name in KNN_TIES:
-        mst, _, _ = compute_minimum_spanning_tree(X, min_samples=ms, reproducible=True)
-        labels, probs = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs,
-                                     reproducible=True, **_kw(g))
-        tie_report(labels, probs, mst, g["labels"], g["probabilities"], g["mst_raw"],
-                   max_share=1.0)
-        return
     if X.shape[1] <= 30 or w is not None:
         mst, nbrs, core = compute_minimum_spanning_tree(X, min_samples=ms, sample_weights=w,
                                                         reproducible=True)
         np.testing.assert_array_equal(mst, g["mst_raw"])
         np.testing.assert_array_equal(core, g["core"])
+        # the reference's query and heap order, equal distances included
+        np.testing.assert_array_equal(nbrs, g["neighbors"])
     labels, probs, _, _, smst, _, _ = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs,
                                                    sample_weights=w, reproducible=True,
                                                    return_trees=True, **_kw(g))
@@ -116,3 +102,29 @@ def test_tie_rule_is_restored(engine):
     b, _, _ = compute_minimum_spanning_tree(X, min_samples=10)
     np.testing.assert_array_equal(a, b)
     assert _native.load().fhg_set_tie_rule(0) == 0
+
+
+@pytest.mark.parametrize("seed,d,side,n,ms,mcs", [
+    (0, 2, 150, 12_000, 10, 20), (1, 3, 30, 15_000, 5, 10), (2, 4, 10, 6_000, 3, 5),
+])
+def test_reference_ties_integer_grid_vs_oracle(engine, seed, d, side, n, ms, mcs):
+    """Distinct points of an integer grid, plus exact duplicates of some of
+    them: equal distances inside every kNN list, which the reference orders
+    by its query and heap.  The reference tie mode lists them as the
+    reference does and equals the oracle's sequential reference semantics
+    (mode 0) bit for bit."""
+    from fast_hdbscan_gb300.hdbscan import compute_minimum_spanning_tree, fast_hdbscan
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(2000 + seed)
+    cells = rng.choice(side ** d, size=n, replace=False)
+    X = np.stack([(cells // side ** j) % side for j in range(d)], axis=1).astype(np.float32)
+    X = np.concatenate([X, X[rng.choice(n, n // 20, replace=False)]])
+    orc = O.fit(X, ms, mcs, mode=0, nthreads=1)
+    mst, nbrs, core = compute_minimum_spanning_tree(X, min_samples=ms, reproducible=True)
+    np.testing.assert_array_equal(core, orc.core)
+    np.testing.assert_array_equal(nbrs, orc.neighbors)
+    np.testing.assert_array_equal(mst, orc.mst)
+    labels, probs = fast_hdbscan(X, min_samples=ms, min_cluster_size=mcs, reproducible=True)
+    np.testing.assert_array_equal(labels, orc.labels)
+    np.testing.assert_array_equal(probs, orc.probabilities)
