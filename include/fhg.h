@@ -67,10 +67,12 @@ int fhg_profile_report(char* buf, int64_t cap);
  *     index that attains the component's least weight, and goes to the first
  *     point of that weight met by the depth-first walk of the reference's
  *     KD-tree (built exactly, on the GPU, for this); edges that would close a
- *     cycle are skipped in the reference's component order.  On data without
- *     tied distances this reproduces the reference's MST, and so its labels
- *     and probabilities, exactly.  It adds the tree build and one short walk
- *     per component and round. */
+ *     cycle are skipped in the reference's component order; kNN rows with
+ *     equal distances are listed as the reference's own query and heap list
+ *     them.  This reproduces the reference's MST, neighbour matrix, labels
+ *     and probabilities exactly, duplicates included.  It adds the tree
+ *     build, the re-query of tied kNN rows and one short walk per component
+ *     and round. */
 #define FHG_TIES_CANONICAL 0
 #define FHG_TIES_REFERENCE 1
 int fhg_set_tie_rule(int rule);
