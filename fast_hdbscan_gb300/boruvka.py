@@ -26,9 +26,10 @@ def parallel_boruvka(tree, n_threads=None, min_samples=10,
     for signature compatibility.  The GPU result is deterministic either way;
     ``reproducible`` selects whose choices it makes among edges of equal
     weight: False (default), a total order on point indices; True, the
-    reference's own -- its sequential rule and its KD-tree's traversal order
-    (fhg_set_tie_rule) -- so that the tree equals the reference's edge for
-    edge on data without tied distances.
+    reference's own -- its sequential rule, its KD-tree's traversal order and
+    its kNN query's order among equal distances (fhg_set_tie_rule) -- so that
+    the tree and the neighbour matrix equal the reference's, duplicates
+    included.
     """
     torch = _native._torch()
     sample_weights = np.asarray(sample_weights, dtype=np.float32)
