@@ -514,10 +514,12 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
                   condensed_records=False):
     """fast_hdbscan with one more option for HDBSCAN.fit: the condensed tree
     as the record array the estimator stores, laid out on the GPU."""
+    host_rows = False  # finiteness of a NumPy input still to check
     if _is_tensor(data):
         pass
     elif metric == "euclidean":
-        data = check_array(data)
+        data = check_array(data, ensure_all_finite=False)
+        host_rows = True
         if sample_weights is not None:
             sample_weights = _check_sample_weight(sample_weights, data, dtype=np.float32)
     elif metric != "precomputed":
@@ -532,9 +534,18 @@ def _fast_hdbscan(data, data_labels=None, semi_supervised=False, ss_algorithm="b
     if cluster_selection_method not in ("eom", "leaf"):
         raise ValueError(f"Invalid cluster_selection_method {cluster_selection_method}")
     if data.shape[0] < 2:
+        if host_rows:
+            check_array(data)
         return _degenerate(data.shape[0], return_trees)
     _unsupported_routes(metric, algorithm, sample_weights, semi_supervised, data, cannot_link,
                         cannot_link_groups, knn_k)
+    if host_rows:
+        # finiteness checked on the uploaded float32 copy, which every route
+        # takes from here; a copy that fails it gets the host check's error
+        Xd = _native.to_device(np.ascontiguousarray(data, dtype=np.float32), np.float32)
+        if not bool(_native._torch().isfinite(Xd).all().item()):
+            check_array(data)
+        data = Xd
     if metric == "precomputed":  # hdbscan.py:306-337 on a precomputed sparse graph
         fr = gpu_fit_precomputed(data, min_samples, min_cluster_size, algorithm,
                                  cluster_selection_method, max_cluster_size,

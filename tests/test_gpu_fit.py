@@ -14,6 +14,7 @@
   are identical at every point that is not an endpoint of a tie-broken edge.
 """
 import os
+import re
 
 import numpy as np
 import pytest
@@ -124,6 +125,26 @@ def test_missing_data_remap(engine):
     clean = list(range(1, 5)) + list(range(6, 200))
     clean_model = HDBSCAN().fit(Xm[clean])
     assert np.allclose(clean_model.labels_, model.labels_[clean])
+
+
+def test_fast_hdbscan_non_finite_raises(engine):
+    """hdbscan.py:233 check_array: the functional entry point rejects NaN and
+    infinity (checked on the device copy) with the host check's ValueError,
+    and a finite float64 input fits as its float32 copy."""
+    from fast_hdbscan_gb300.hdbscan import check_array, fast_hdbscan
+
+    X = _golden("blobs200")["X"].astype(np.float64)
+    for bad in (np.nan, np.inf, -np.inf):
+        Xb = X.copy()
+        Xb[7, 1] = bad
+        with pytest.raises(ValueError) as host:
+            check_array(Xb)
+        with pytest.raises(ValueError, match=re.escape(str(host.value).splitlines()[0][:20])):
+            fast_hdbscan(Xb)
+    a = fast_hdbscan(X)
+    b = fast_hdbscan(X.astype(np.float32))
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
 
 
 def test_cached_pool_release_between_fits(engine):
