@@ -37,7 +37,11 @@ extern "C" __attribute__((visibility("default"))) int fhg_hdbscan_fit_batch(
     const int32_t* min_samples, const int64_t* min_cluster_size, int32_t selection_method,
     double max_cluster_size, int allow_single_cluster, int64_t* const* labels_dev,
     float* const* probs_dev, int32_t n_workers, int32_t* status_host, void* stream) {
-    if (count <= 0) return FHG_OK;
+    if (count < 0) {
+        set_error("fhg_hdbscan_fit_batch: negative instance count (%lld)", (long long)count);
+        return FHG_ERR_INVALID;
+    }
+    if (count == 0) return FHG_OK;
     if (!X_dev || !n || !d || !min_samples || !min_cluster_size || !labels_dev || !probs_dev ||
         !status_host) {
         set_error("fhg_hdbscan_fit_batch: null pointer argument");

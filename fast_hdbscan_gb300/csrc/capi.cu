@@ -27,6 +27,16 @@ void set_error(const char* fmt, ...) {
 }
 const char* last_error() { return g_last_error.c_str(); }
 
+// Sizes and counts: zero is an empty input, a negative value a caller error.
+int check_counts(const char* fn, std::initializer_list<int64_t> cs) {
+    for (int64_t c : cs)
+        if (c < 0) {
+            set_error("%s: negative size or count (%lld)", fn, (long long)c);
+            return FHG_ERR_INVALID;
+        }
+    return FHG_OK;
+}
+
 int finalize_edges(const MstResult& r, double* edges, cudaStream_t s);
 
 // ---------------------------------------------------------------- tracing
@@ -380,6 +390,7 @@ FHG_API int fhg_knn_graph_mst(const float* X_dev, int64_t n, int32_t d, int32_t 
 FHG_API int fhg_core_graph_mst(const int32_t* indptr_dev, const int32_t* indices_dev,
                                const float* weights_dev, const int32_t* seg_end_dev, int64_t n,
                                double* edges_dev, int64_t* n_edges_host, void* stream) {
+    FHG_TRY(check_counts("fhg_core_graph_mst", {n}));
     if (!n_edges_host || (n > 1 && (!indptr_dev || !indices_dev || !weights_dev || !edges_dev))) {
         set_error("fhg_core_graph_mst: null pointer");
         return FHG_ERR_INVALID;
@@ -535,7 +546,8 @@ int check_ptrs(const char* fn, std::initializer_list<const void*> ps) {
 using namespace fhg::capi;
 
 FHG_API int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, void* stream) {
-    if (m <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_sort_mst", {m}));
+    if (m == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_sort_mst", {mst_dev, sorted_dev}));
     cudaStream_t s = as_stream(stream);
     Workspace ws(s);
@@ -550,7 +562,8 @@ FHG_API int fhg_sort_mst(const double* mst_dev, int64_t m, double* sorted_dev, v
 FHG_API int fhg_mst_to_linkage_tree(const double* sorted_mst_dev, int64_t m,
                                     const float* sample_weights_dev, double* linkage_dev,
                                     void* stream) {
-    if (m <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_mst_to_linkage_tree", {m}));
+    if (m == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_mst_to_linkage_tree", {sorted_mst_dev, linkage_dev}));
     cudaStream_t s = as_stream(stream);
     Workspace ws(s);
@@ -569,7 +582,8 @@ FHG_API int fhg_condense_tree(const double* linkage_dev, int64_t m, int64_t min_
                               float* child_size_dev, int64_t* n_rows_host, void* stream) {
     FHG_TRY(check_ptrs("fhg_condense_tree", {n_rows_host}));
     *n_rows_host = 0;
-    if (m <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_condense_tree", {m}));
+    if (m == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_condense_tree",
                        {linkage_dev, parent_dev, child_dev, lambda_dev, child_size_dev}));
     if (min_cluster_size <= 0) {
@@ -599,7 +613,8 @@ FHG_API int fhg_extract_eom_clusters(const int64_t* parent_dev, const int64_t* c
                                      int64_t* n_sel_host, void* stream) {
     FHG_TRY(check_ptrs("fhg_extract_eom_clusters", {n_sel_host}));
     *n_sel_host = 0;
-    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_extract_eom_clusters", {rows}));
+    if (rows == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_extract_eom_clusters",
                        {parent_dev, child_dev, lambda_dev, child_size_dev, sel_dev}));
     cudaStream_t s = as_stream(stream);
@@ -624,10 +639,11 @@ FHG_API int fhg_label_points(const int64_t* parent_dev, const int64_t* child_dev
                              const int64_t* sel_dev, int64_t n_sel, double epsilon,
                              int64_t n_samples, int64_t* labels_dev, float* probs_dev,
                              void* stream) {
-    if (n_samples <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_label_points", {rows, n_sel, n_samples}));
+    if (n_samples == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_label_points", {labels_dev, probs_dev}));
     cudaStream_t s = as_stream(stream);
-    if (rows <= 0 || n_sel <= 0) {
+    if (rows == 0 || n_sel == 0) {
         ::fhg::note_launch();
         fill_labels_kernel<<<grid_for(n_samples, 256), 256, 0, s>>>(n_samples, labels_dev, probs_dev);
         FHG_CUDA(cudaGetLastError());
@@ -657,7 +673,8 @@ FHG_API int fhg_cluster_tree_leaves(const int64_t* parent_dev, const int64_t* ch
                                     void* stream) {
     FHG_TRY(check_ptrs("fhg_cluster_tree_leaves", {n_sel_host}));
     *n_sel_host = 0;
-    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_cluster_tree_leaves", {rows}));
+    if (rows == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_cluster_tree_leaves",
                        {parent_dev, child_dev, lambda_dev, child_size_dev, sel_dev}));
     cudaStream_t s = as_stream(stream);
@@ -682,11 +699,12 @@ FHG_API int fhg_membership_strengths(const int64_t* parent_dev, const int64_t* c
                                      int64_t rows, const int64_t* sel_dev, int64_t n_sel,
                                      const int64_t* labels_dev, int64_t n_samples,
                                      float* probs_dev, void* stream) {
-    if (n_samples <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_membership_strengths", {rows, n_sel, n_samples}));
+    if (n_samples == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_membership_strengths", {labels_dev, probs_dev}));
     cudaStream_t s = as_stream(stream);
     FHG_CUDA(cudaMemsetAsync(probs_dev, 0, sizeof(float) * n_samples, s));
-    if (rows <= 0 || n_sel <= 0) return FHG_OK;
+    if (rows == 0 || n_sel == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_membership_strengths",
                        {parent_dev, child_dev, lambda_dev, child_size_dev, sel_dev}));
     Workspace ws(s);
@@ -735,7 +753,8 @@ __global__ void condensed_records_kernel(int64_t rows, const int64_t* __restrict
 FHG_API int fhg_condensed_record_array(const int64_t* parent_dev, const int64_t* child_dev,
                                        const float* lambda_dev, const float* child_size_dev,
                                        int64_t rows, void* records_dev, void* stream) {
-    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_condensed_record_array", {rows}));
+    if (rows == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_condensed_record_array",
                        {parent_dev, child_dev, lambda_dev, child_size_dev, records_dev}));
     if (reinterpret_cast<uintptr_t>(records_dev) % 4 != 0) {
@@ -759,7 +778,8 @@ FHG_API int fhg_simplify_hierarchy(int64_t* parent_dev, int64_t* child_dev, floa
                                    int64_t* out_rows_host, void* stream) {
     FHG_TRY(check_ptrs("fhg_simplify_hierarchy", {out_rows_host}));
     *out_rows_host = 0;
-    if (rows <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_simplify_hierarchy", {rows}));
+    if (rows == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_simplify_hierarchy",
                        {parent_dev, child_dev, lambda_dev, child_size_dev, out_parent_dev,
                         out_child_dev, out_lambda_dev, out_child_size_dev}));
@@ -784,10 +804,11 @@ FHG_API int fhg_cluster_epsilon_search(const int64_t* parent_dev, const int64_t*
                                        int64_t* n_out_host, void* stream) {
     FHG_TRY(check_ptrs("fhg_cluster_epsilon_search", {n_out_host}));
     *n_out_host = 0;
-    if (n_clusters <= 0) return FHG_OK;
+    FHG_TRY(check_counts("fhg_cluster_epsilon_search", {rows, n_clusters}));
+    if (n_clusters == 0) return FHG_OK;
     FHG_TRY(check_ptrs("fhg_cluster_epsilon_search",
                        {parent_dev, child_dev, lambda_dev, child_size_dev, clusters_dev, out_dev}));
-    if (rows <= 0) {
+    if (rows == 0) {
         set_error("fhg_cluster_epsilon_search: empty cluster tree");
         return FHG_ERR_INVALID;
     }

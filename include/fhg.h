@@ -14,6 +14,9 @@
  *   - Every call is stream-ordered on `stream` (NULL = legacy default stream)
  *     and returns an FHG_* status; FHG_OK = 0.  fhg_last_error() returns a
  *     message for the calling thread's last failure.
+ *   - A size or count of zero is an empty input, not an error; a negative
+ *     one, or a null pointer where data is needed, is FHG_ERR_INVALID,
+ *     reported before any CUDA call.
  *   - Scratch memory is taken with cudaMallocAsync on `stream` and released
  *     on the same stream before the call returns.
  *   - Ties are broken by a total order on point indices by default: kNN

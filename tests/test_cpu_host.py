@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
+from fast_hdbscan_gb300 import _native
 
 
 def _declared_functions():
@@ -54,6 +55,44 @@ def test_library_error_reporting_without_gpu():
                                                     ctypes.c_void_p, ctypes.c_void_p]
     rc = lib.fhg_mst_to_linkage_tree_noalloc(None, 65537, None, None)
     assert rc == 1 and b"FHG_NOALLOC_MAX_EDGES" in lib.fhg_last_error()
+
+
+# entry points that take no data (status, switches, sizes, the last call's
+# fallback count) or for which a null argument is a valid request (freeing no
+# index, switching the radius off)
+_NO_DATA = {"fhg_last_error", "fhg_abi_version", "fhg_set_tie_rule", "fhg_set_highd_kernel",
+            "fhg_release_cached_memory", "fhg_reference_kdtree_levels", "fhg_index_free",
+            "fhg_radius_param_count", "fhg_radius_use", "fhg_radius_fallbacks"}
+
+
+@pytest.mark.parametrize("name", [n for n in _native.SIGNATURES if n not in _NO_DATA])
+def test_entry_point_rejects_null_and_negative_arguments(name):
+    """Every data entry point answers null pointers and negative sizes with
+    FHG_ERR_INVALID and a message, before any CUDA call (a negative size is
+    never taken for an empty input).  Host out-parameters are given, so that
+    the checks after them are reached too."""
+    from fast_hdbscan_gb300 import build
+
+    lib = ctypes.CDLL(build.build())
+    lib.fhg_last_error.restype = ctypes.c_char_p
+    restype, argtypes = _native.SIGNATURES[name]
+    fn = getattr(lib, name)
+    fn.restype, fn.argtypes = restype, argtypes
+    keep, args = [], []
+    for a in argtypes:
+        if isinstance(a, type) and issubclass(a, ctypes._Pointer):
+            keep.append(a._type_(0))
+            args.append(ctypes.pointer(keep[-1]))
+        elif a in (ctypes.c_void_p,):
+            args.append(None)
+        elif a in (ctypes.c_double, ctypes.c_float):
+            args.append(0.0)
+        elif a is ctypes.c_uint64:
+            args.append(0)
+        else:
+            args.append(-1)
+    assert fn(*args) == _native.FHG_ERR_INVALID
+    assert lib.fhg_last_error()
 
 
 def test_badargs_raise_before_the_engine():
