@@ -1,12 +1,13 @@
-"""The reference's own estimator tests (fast_hdbscan/tests/test_hdbscan.py),
-restated against the GPU engine on the same inputs.
+"""The reference's own estimator and edge-case tests
+(fast_hdbscan/tests/test_hdbscan.py, test_edge_cases.py), restated against
+the GPU engine.
 
 The reference's module-level data -- make_blobs(n_samples=200,
 random_state=10), shuffled with random_state=7 and standardised, with
 n_clusters = 3 -- is the committed fixture ``blobs200`` (written by the
-unmodified reference's generator; scikit-learn is not needed here), and its
-blob labels are the fixture ``blobs200_w_labels``' weights.  Every other
-input is made with NumPy exactly as the reference's test makes it.
+reference's generator; scikit-learn is not needed here).  The other inputs
+are made with NumPy as the reference's tests make them, except the three
+blobs of the epsilon edge cases, which NumPy draws in place of make_blobs.
 """
 import os
 
@@ -168,3 +169,39 @@ def test_issue_63_no_spurious_noise(engine):
                          allow_single_cluster=True).fit_predict(data)
         assert len(set(labels.tolist()) - {-1}) >= 1, seed
         assert np.sum(labels == -1) / len(labels) < 0.9, seed
+
+
+def _three_blobs(seed=42):
+    """200 points around three centres in 2-D (the reference's edge-case
+    tests draw theirs from scikit-learn's make_blobs)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-10, 10, size=(3, 2))
+    return np.vstack([rng.normal(c, 1.0, size=(67 if i < 2 else 66, 2))
+                      for i, c in enumerate(centres)])
+
+
+def test_edge_case_inputs(engine):
+    """test_edge_cases.py:8-69: a single point, two points, 50 identical
+    points, min_cluster_size above n, 1-D data, min_samples near n, and
+    epsilon 0 or very large with a single cluster allowed."""
+    from fast_hdbscan_gb300 import HDBSCAN
+
+    assert HDBSCAN(min_cluster_size=2).fit_predict(np.array([[1.0, 2.0]]))[0] == -1
+    two = HDBSCAN(min_cluster_size=2).fit_predict(np.array([[0.0, 0.0], [0.1, 0.0]]))
+    assert len(set(two.tolist()) - {-1}) <= 1
+    assert len(HDBSCAN(min_cluster_size=5).fit_predict(np.full((50, 3), 1.0))) == 50
+    np.random.seed(42)
+    assert np.all(HDBSCAN(min_cluster_size=100).fit_predict(np.random.rand(10, 2)) == -1)
+    np.random.seed(42)
+    X1 = np.concatenate([np.random.normal(0, 0.1, 50),
+                         np.random.normal(5, 0.1, 50)]).reshape(-1, 1)
+    assert len(set(HDBSCAN(min_cluster_size=10).fit_predict(X1).tolist()) - {-1}) >= 1
+    np.random.seed(42)
+    assert len(HDBSCAN(min_cluster_size=5, min_samples=18).fit_predict(
+        np.random.rand(20, 2))) == 20
+    X = _three_blobs()
+    labels = HDBSCAN(min_cluster_size=10, cluster_selection_epsilon=0.0).fit_predict(X)
+    assert len(set(labels.tolist()) - {-1}) >= 1
+    labels = HDBSCAN(min_cluster_size=10, cluster_selection_epsilon=1000.0,
+                     allow_single_cluster=True).fit_predict(X)
+    assert len(set(labels.tolist()) - {-1}) <= 1
