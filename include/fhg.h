@@ -136,7 +136,8 @@ int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t* idx_de
  *                 point index), src inside the component that chose the edge.
  *   neighbors_dev n x (k-1) int32: kNN without the point itself
  *                 (neighbors[:, 1:]; k = min_samples + 1, at least 2, or
- *                 weighted_k).
+ *                 weighted_k).  min(k, n) <= 64, else FHG_ERR_UNSUPPORTED
+ *                 (the same limit holds for every fit entry point).
  *   core_dev      n float32: sqrt of the core value (boruvka.py:647).
  *   n_rounds_host optional: Boruvka rounds after the kNN-seeded round. */
 int fhg_index_boruvka(fhg_index* index, int32_t min_samples, const float* sample_weights_dev,
