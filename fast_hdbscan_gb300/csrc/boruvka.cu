@@ -1030,11 +1030,16 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
         set_error("weighted kNN: k = %d (2 * min_samples / mean weight) is below 1", kq);
         return FHG_ERR_INVALID;
     }
-    if (k > 64) {
+    // lists of up to 64 live in registers (and the reference tie mode's
+    // re-query takes no more); longer ones in shared memory
+    const int k_max = ref_ties ? 64 : kKnnMaxK;
+    if (k > k_max) {
         if (weighted)
-            set_error("weighted kNN: k = %d (2 * min_samples / mean weight) exceeds 64", kq);
+            set_error("weighted kNN: k = %d (2 * min_samples / mean weight) exceeds %d%s", kq,
+                      k_max, ref_ties ? " in the reference tie mode" : "");
         else
-            set_error("min_samples must be at most 63 (got %d)", min_samples);
+            set_error("min_samples must be at most %d (got %d)%s", k_max - 1, min_samples,
+                      ref_ties ? " in the reference tie mode" : "");
         return FHG_ERR_UNSUPPORTED;
     }
     const int64_t m_cap = n > 1 ? n - 1 : 1;
@@ -1054,7 +1059,8 @@ int boruvka_mst(Workspace& ws, const fhg_index& ix, int min_samples, MstResult* 
     int8_t* knn_open;  // the kNN kernel's tie flags, then "seed not provably final"
     FHG_TRY(ws.alloc(&knn_open, (size_t)n));
     // the neighbours[:, 1:] matrix (kq - 1 columns) straight from the kNN kernel
-    if (const RadiusUse* ru = radius_in_use())
+    const RadiusUse* ru = k <= 64 ? radius_in_use() : nullptr;  // (radius passes: k <= 64)
+    if (ru)
         FHG_TRY(knn_with_radius(ix, k, *ru, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));
     else
         FHG_TRY(index_knn(ix, k, knn_d, knn_s, knn_d_o, nbr_o, s, knn_open, kq - 1, 1));

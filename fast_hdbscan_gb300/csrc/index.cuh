@@ -126,6 +126,9 @@ struct KnnCap {
     unsigned long long* fail_count = nullptr;
     unsigned long long* scan_count = nullptr;
 };
+// Longest kNN list: lists of up to 64 are kept in registers, longer ones (a
+// warp per query) in shared memory.
+constexpr int kKnnMaxK = 2048;
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
               cudaStream_t s, int8_t* tie_s = nullptr, int io_stride = 0, int io_skip = 0,
               const KnnCap& cap = KnnCap());

@@ -255,6 +255,188 @@ __global__ void __launch_bounds__(kKnnWarps * 32, knn_min_blocks<DIM, K>()) knn_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Lists longer than 64: one warp per query, its sorted list in shared memory.
+//
+// The list (k keys in (squared distance, caller index) order, unfilled slots
+// (+inf, INT32_MAX)) and a merge buffer take 2 * kpad 64-bit words of
+// dynamic shared memory (kpad = k rounded up to 32, at most kKnnMaxK), the
+// sorted candidates of one bucket 32 more.  The walk is knn_kernel's for a
+// single query: the home bucket, then every ancestor's sibling subtree,
+// entered while its box bound is within the k-th distance.  A bucket's 32
+// candidates are the warp's lanes; those below the k-th key are sorted across
+// the warp (bitonic) and merged into the list by rank (each entry's place =
+// its own index + the entries of the other sequence below it; no key occurs
+// twice, so the places are distinct).  The list is the k smallest keys of all
+// points and the tie flag has knn_kernel's meaning, so both kernels give the
+// same outputs bit for bit.
+
+// Ascending bitonic sort of 32 keys, one per lane.
+__device__ __forceinline__ unsigned long long warp_sort_u64(unsigned long long v, int lane) {
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(kFull, v, stride);
+            const bool ascending = (lane & size) == 0;
+            const bool lower = (lane & stride) == 0;
+            v = (lower == ascending) ? (o < v ? o : v) : (o > v ? o : v);
+        }
+    }
+    return v;
+}
+
+// Number of entries of the ascending a[0, len) below key.
+__device__ __forceinline__ int count_below(const unsigned long long* a, int len,
+                                           unsigned long long key) {
+    int lo = 0, hi = len;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int DIM, int SP>
+__global__ void __launch_bounds__(32) knn_large_kernel(IndexView ix, int k, float* __restrict__ d_s,
+                                                       int32_t* __restrict__ i_s,
+                                                       float* __restrict__ d_o,
+                                                       int32_t* __restrict__ i_o,
+                                                       int8_t* __restrict__ tie_s, int io_stride,
+                                                       int io_skip,
+                                                       unsigned long long* scan_count) {
+    extern __shared__ unsigned long long s_lists[];  // [kpad] list, [kpad] buffer, [32] bucket
+    __shared__ int32_t st[kStack];
+    const int lane = threadIdx.x;
+    const int64_t qi = blockIdx.x;
+    if (qi >= ix.n) return;
+    const int kpad = (k + 31) & ~31;
+    unsigned long long* A = s_lists;
+    unsigned long long* B = s_lists + kpad;
+    unsigned long long* S = s_lists + 2 * kpad;
+    const unsigned long long kEmptyKey = pack_entry(INFINITY, INT32_MAX);
+    for (int j = lane; j < kpad; j += 32) A[j] = kEmptyKey;
+    float q[DIM];
+    {
+        float t[SP];
+        load_pt<SP>(ix.pts, qi, t);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) q[j] = t[j];
+    }
+    __syncwarp();
+    float rejmin = INFINITY;  // least distance of an examined point left out
+    int scans = 0;
+    auto scan_leaf = [&](int64_t lf) {
+        ++scans;
+        const int64_t base = lf * kLeaf;
+        const int cnt = (int)(ix.n - base < kLeaf ? ix.n - base : kLeaf);
+        unsigned long long key = ~0ull;
+        float dd = INFINITY;
+        if (lane < cnt) {
+            float c[SP];
+            load_pt<SP>(ix.pts, base + lane, c);
+            dd = rdist_rn<DIM>(q, c);
+            key = pack_entry(dd, __ldg(ix.orig + base + lane));
+        }
+        const bool keep = lane < cnt && key < A[k - 1];
+        if (lane < cnt && !keep) rejmin = fminf(rejmin, dd);
+        const unsigned kmask = __ballot_sync(kFull, keep);
+        if (kmask == 0u) return;
+        const int ns = __popc(kmask);
+        const unsigned long long sv = warp_sort_u64(keep ? key : ~0ull, lane);
+        S[lane] = sv;
+        __syncwarp();
+        for (int j = lane; j < k; j += 32) {
+            const unsigned long long e = A[j];
+            const int at = j + count_below(S, ns, e);
+            if (at < k) B[at] = e;
+            else if (entry_orig(e) != INT32_MAX) rejmin = fminf(rejmin, entry_dist(e));
+        }
+        if (lane < ns) {
+            const int at = lane + count_below(A, k, sv);
+            if (at < k) B[at] = sv;
+            else rejmin = fminf(rejmin, entry_dist(sv));
+        }
+        __syncwarp();
+        unsigned long long* t = A;
+        A = B;
+        B = t;
+    };
+
+    const int64_t leaf = qi / kLeaf;
+    scan_leaf(leaf);
+    const int64_t first_leaf_node = ix.slots - 1;
+    int64_t x = first_leaf_node + leaf;
+    while (x > 0) {
+        const int32_t sib = (int32_t)((x & 1) ? x + 1 : x - 1);
+        const bool right_side = (x & 1) != 0;
+        int sp = 1;
+        if (lane == 0) st[0] = sib;
+        __syncwarp();
+        while (sp > 0) {
+            --sp;
+            const int32_t node = st[sp];
+            __syncwarp();
+            float b[2 * SP];
+            load_box<SP>(ix.box, node, b);
+            const float lb = box_lb_n<DIM, SP>(b, q);
+            if (!(lb <= entry_dist(A[k - 1]))) continue;
+            if (node >= first_leaf_node) {
+                scan_leaf(node - first_leaf_node);
+            } else {
+                const int32_t l = 2 * node + 1, r = l + 1;
+                const int32_t near = right_side ? l : r, far = right_side ? r : l;
+                if (lane == 0) {
+                    st[sp] = far;
+                    st[sp + 1] = near;
+                }
+                sp += 2;
+                __syncwarp();
+            }
+        }
+        x = (x - 1) >> 1;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rejmin = fminf(rejmin, __shfl_xor_sync(kFull, rejmin, o));
+    if (scan_count && lane == 0) atomicAdd(scan_count, (unsigned long long)scans);
+    if (tie_s && lane == 0) tie_s[qi] = rejmin == entry_dist(A[k - 1]) ? 1 : 0;
+    const int64_t o_row = ix.orig[qi];
+    for (int j = lane; j < k; j += 32) {
+        const unsigned long long e = A[j];
+        const float dj = entry_dist(e);
+        const int32_t oj = entry_orig(e);
+        const int32_t o = oj == INT32_MAX ? -1 : oj;  // k > n leaves slots empty
+        if (d_s) {
+            d_s[qi * k + j] = dj;
+            i_s[qi * k + j] = o >= 0 ? __ldg(ix.rank + o) : -1;
+        }
+        if (d_o) d_o[o_row * k + j] = dj;
+        if (i_o && j >= io_skip) i_o[o_row * io_stride + j - io_skip] = o;
+    }
+}
+
+template <int DIM>
+int launch_knn_large(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o,
+                     int32_t* i_o, int8_t* tie_s, int io_stride, int io_skip, const KnnCap& cap,
+                     cudaStream_t s) {
+    constexpr int SP = DIM <= 4 ? 4 : (DIM <= 8 ? 8 : DIM);
+    if (cap.cap2 || cap.redo) {
+        set_error("knn: a search radius takes k <= 64 (got %d)", k);
+        return FHG_ERR_UNSUPPORTED;
+    }
+    if (ix.n <= 0) return FHG_OK;
+    const int kpad = (k + 31) & ~31;
+    const size_t smem = sizeof(unsigned long long) * (size_t)(2 * kpad + 32);
+    Stage stage(s, "knn_kernel");
+    ::fhg::note_launch();
+    knn_large_kernel<DIM, SP><<<(unsigned)ix.n, 32, smem, s>>>(view_of(ix), k, d_s, i_s, d_o, i_o,
+                                                               tie_s, io_stride, io_skip,
+                                                               cap.scan_count);
+    FHG_CUDA(cudaGetLastError());
+    return FHG_OK;
+}
+
 template <int DIM, int K>
 int launch_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
                int8_t* tie_s, int io_stride, int io_skip, const KnnCap& cap, cudaStream_t s) {
@@ -287,9 +469,9 @@ int dispatch_k(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o,
 int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, int32_t* i_o,
               cudaStream_t s, int8_t* tie_s, int io_stride, int io_skip, const KnnCap& cap) {
     if (io_stride <= 0) io_stride = k;
-    if (k < 1 || k > 64) {
-        set_error("knn: k must be in [1, 64] (got %d)", k);
-        return FHG_ERR_INVALID;
+    if (k < 1 || k > kKnnMaxK) {
+        set_error("knn: k must be in [1, %d] (got %d)", kKnnMaxK, k);
+        return k < 1 ? FHG_ERR_INVALID : FHG_ERR_UNSUPPORTED;
     }
     if ((d_s == nullptr) != (i_s == nullptr) || (d_o != nullptr && i_o == nullptr) ||
         (d_o != nullptr && (io_stride != k || io_skip != 0))) {
@@ -297,6 +479,21 @@ int index_knn(const fhg_index& ix, int k, float* d_s, int32_t* i_s, float* d_o, 
         return FHG_ERR_INVALID;
     }
     Stage stage(s, "knn");
+    if (k > 64) {  // the list no longer fits in registers
+#define FHG_LARGE(D) launch_knn_large<D>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s)
+        switch (ix.d) {
+            case 1: return FHG_LARGE(1);
+            case 2: return FHG_LARGE(2);
+            case 3: return FHG_LARGE(3);
+            case 4: return FHG_LARGE(4);
+            case 5: return FHG_LARGE(5);
+            case 6: return FHG_LARGE(6);
+            case 7: return FHG_LARGE(7);
+            case 8: return FHG_LARGE(8);
+            default: return ix.d <= 16 ? FHG_LARGE(16) : FHG_LARGE(32);
+        }
+#undef FHG_LARGE
+    }
     switch (ix.d) {
         case 1: return dispatch_k<1>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);
         case 2: return dispatch_k<2>(ix, k, d_s, i_s, d_o, i_o, tie_s, io_stride, io_skip, cap, s);

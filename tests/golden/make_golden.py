@@ -100,6 +100,12 @@ CASES = {
                 dict(min_samples=15, min_cluster_size=25)),
     "vd3d_20k": (lambda: synthetic.varying_density(20000, seed=13),
                  dict(min_samples=15, min_cluster_size=50)),
+    # kNN lists longer than 64 (min_samples >= 64; the estimator's default
+    # min_samples is min_cluster_size)
+    "blobs2d_2k_ms100": (lambda: synthetic.blobs_2d(2000, seed=10),
+                         dict(min_samples=100, min_cluster_size=100)),
+    "vd3d_3k_mcs120": (lambda: synthetic.varying_density(3000, seed=14),
+                       dict(min_cluster_size=120)),
     # sample weights (hdbscan.py:199 sample_weights; boruvka.py:527-573;
     # cluster_trees.py:98, :205)
     "blobs200_w_labels": (_blobs200, dict(min_cluster_size=5, sample_weights=_blobs200_labels)),

@@ -29,7 +29,7 @@ GOLDEN_FIT = ["ka150", "ka150_eps", "blobs200", "blobs200_ms1", "blobs200_leaf",
               "blobs200_maxcs", "blobs200_single", "blobs200_persist", "blobs2d_2k",
               "blobs2d_20k", "umap5d_5k", "vd3d_5k", "vd3d_20k", "edge_two", "edge_1d",
               "edge_highms", "edge_dups", "edge_mcs_gt_n", "blobs200_w_labels", "blobs2d_2k_w",
-              "vd3d_5k_w", "hd12_2k", "hd24_1k"]
+              "vd3d_5k_w", "hd12_2k", "hd24_1k", "blobs2d_2k_ms100", "vd3d_3k_mcs120"]
 
 
 def _golden(name):

@@ -47,42 +47,28 @@ def test_hdbscan_dbscan_clustering(engine):
     assert _n_clusters(labels) == N_CLUSTERS
 
 
-# The engine keeps each point's kNN list in registers: min_samples (which
-# the estimator defaults to min_cluster_size) is at most MAX_MIN_SAMPLES,
-# and a larger one raises NotImplementedError instead of fitting.
-MAX_MIN_SAMPLES = 63
-
-
 def test_hdbscan_no_clusters(engine):
-    """test_hdbscan.py:103 (the estimator's default min_samples would be
-    n + 1 here, above the engine's limit: that call raises, and the
-    estimator runs with fast_hdbscan's min_samples of 10)."""
+    """test_hdbscan.py:103 (the estimator's min_samples is then n + 1:
+    every core distance is infinite)."""
     from fast_hdbscan_gb300 import HDBSCAN, fast_hdbscan
 
     X = _X()
     labels, p = fast_hdbscan(X, min_cluster_size=len(X) + 1)
     assert _n_clusters(labels) == 0
-    with pytest.raises(NotImplementedError, match="min_samples"):
-        HDBSCAN(min_cluster_size=len(X) + 1).fit(X)
-    est = HDBSCAN(min_cluster_size=len(X) + 1, min_samples=10).fit(X)
-    assert _n_clusters(est.labels_) == 0
+    assert _n_clusters(HDBSCAN(min_cluster_size=len(X) + 1).fit(X).labels_) == 0
 
 
 def test_hdbscan_min_cluster_size(engine):
     """test_hdbscan.py:120: every min_cluster_size from 2 to n, through both
     entry points; no cluster is smaller than min_cluster_size.
-    fast_hdbscan's min_samples defaults to 10, the estimator's to
-    min_cluster_size; above the engine's min_samples limit the estimator's
-    default raises, and it runs with min_samples at the limit instead."""
+    (fast_hdbscan's min_samples defaults to 10, the estimator's to
+    min_cluster_size, so the estimator's kNN lists grow to the whole set.)"""
     from fast_hdbscan_gb300 import HDBSCAN, fast_hdbscan
 
     X = _X()
-    with pytest.raises(NotImplementedError, match="min_samples"):
-        HDBSCAN(min_cluster_size=MAX_MIN_SAMPLES + 1).fit(X)
     for mcs in range(2, len(X) + 1):
-        ms = None if mcs <= MAX_MIN_SAMPLES else MAX_MIN_SAMPLES
         for labels in (fast_hdbscan(X, min_cluster_size=mcs)[0],
-                       HDBSCAN(min_cluster_size=mcs, min_samples=ms).fit(X).labels_):
+                       HDBSCAN(min_cluster_size=mcs).fit(X).labels_):
             kept = labels[labels != -1]
             if kept.size:
                 assert np.bincount(kept).min() >= mcs

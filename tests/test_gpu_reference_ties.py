@@ -104,6 +104,21 @@ def test_tie_rule_is_restored(engine):
     assert _native.load().fhg_set_tie_rule(0) == 0
 
 
+def test_reference_ties_take_at_most_63_min_samples(engine):
+    """The tie mode re-queries tied kNN rows with lists of up to 64; a larger
+    min_samples raises there (the default rule takes it) and leaves the
+    default rule in place."""
+    from fast_hdbscan_gb300 import _native
+    from fast_hdbscan_gb300.hdbscan import compute_minimum_spanning_tree
+
+    X = synthetic.varying_density(3_000, seed=24)
+    with pytest.raises(NotImplementedError, match="reference tie mode"):
+        compute_minimum_spanning_tree(X, min_samples=64, reproducible=True)
+    mst, _, _ = compute_minimum_spanning_tree(X, min_samples=64)
+    assert mst.shape == (X.shape[0] - 1, 3)
+    assert _native.load().fhg_set_tie_rule(0) == 0
+
+
 @pytest.mark.parametrize("seed,d,side,n,ms,mcs", [
     (0, 2, 150, 12_000, 10, 20), (1, 3, 30, 15_000, 5, 10), (2, 4, 10, 6_000, 3, 5),
 ])
