@@ -116,7 +116,8 @@ int fhg_index_shape(const fhg_index* index, int64_t* n, int32_t* d);
 /* Replaces numba_kdtree.py:765 parallel_tree_query(tree, tree.data, k,
  * output_rdist=True): for every point its k nearest points (itself included)
  * by squared float32 distance, ascending.  rdist_dev: n x k float32,
- * idx_dev: n x k int32, rows in caller order.  1 <= k <= 64; entries past the
+ * idx_dev: n x k int32, rows in caller order.  1 <= k <= 2048 (lists longer
+ * than 64 are kept in shared memory, a warp per query); entries past the
  * n-th neighbour are (+inf, -1). */
 int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t* idx_dev,
                   void* stream);
@@ -136,8 +137,9 @@ int fhg_index_knn(fhg_index* index, int32_t k, float* rdist_dev, int32_t* idx_de
  *                 point index), src inside the component that chose the edge.
  *   neighbors_dev n x (k-1) int32: kNN without the point itself
  *                 (neighbors[:, 1:]; k = min_samples + 1, at least 2, or
- *                 weighted_k).  min(k, n) <= 64, else FHG_ERR_UNSUPPORTED
- *                 (the same limit holds for every fit entry point).
+ *                 weighted_k).  min(k, n) <= 2048 (64 in the reference tie
+ *                 mode), else FHG_ERR_UNSUPPORTED; the same holds for every
+ *                 Boruvka fit entry point.
  *   core_dev      n float32: sqrt of the core value (boruvka.py:647).
  *   n_rounds_host optional: Boruvka rounds after the kNN-seeded round. */
 int fhg_index_boruvka(fhg_index* index, int32_t min_samples, const float* sample_weights_dev,
