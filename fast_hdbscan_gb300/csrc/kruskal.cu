@@ -248,9 +248,12 @@ int kruskal_mst_of_lists(int64_t n, int min_samples, int query_k, const float* w
                          cudaStream_t s) {
     const int kq = query_k;
     const int64_t kk = kq - 1;
-    if (kq < 2 || kq > 64) {
-        set_error("kruskal: the kNN query size must be in [2, 64] (got %d)", kq);
-        return kq > 64 ? FHG_ERR_UNSUPPORTED : FHG_ERR_INVALID;
+    // the spatial index's kNN takes lists of up to kKnnMaxK; the
+    // high-dimensional kNN graph is used here with lists of up to 64
+    const int kq_max = index ? kKnnMaxK : 64;
+    if (kq < 2 || kq > kq_max) {
+        set_error("kruskal: the kNN query size must be in [2, %d] (got %d)", kq_max, kq);
+        return kq > kq_max ? FHG_ERR_UNSUPPORTED : FHG_ERR_INVALID;
     }
     if (n * kk > 0x7fffffffLL) {
         set_error("kruskal: %lld kNN edges exceed the int32 edge index", (long long)(n * kk));

@@ -369,9 +369,10 @@ def gpu_fit_kruskal(X, min_samples, min_cluster_size, knn_k, cluster_selection_m
     ms = min_cluster_size if min_samples is None else min_samples
     w = None if sample_weights is None else np.ascontiguousarray(sample_weights, np.float32)
     kq = int(knn_k) + 1 if knn_graph else kruskal_query_k(int(ms), int(knn_k), w)
-    if kq > (96 if knn_graph else 64):
+    kq_max = 64 if knn_graph else 2048  # the kNN graph's lists; the spatial index's
+    if kq > kq_max:
         raise NotImplementedError(f"a kNN query of {kq} neighbours exceeds the GPU kNN's "
-                                  f"{96 if knn_graph else 64}")
+                                  f"{kq_max}")
     d_w = _native.to_device(w, np.float32) if w is not None else None
     cols = kq - 1 if w is not None else (ms if ms > 1 else 1)
     method = {"eom": 0, "leaf": 1}.get(cluster_selection_method)

@@ -45,8 +45,8 @@ def kruskal_mst_from_feature_matrix(numba_tree, min_samples, knn_k=None, sample_
     if sample_weights is not None:
         w = np.ascontiguousarray(sample_weights, dtype=np.float32)
     kq = kruskal_query_k(ms, knn_k, w)
-    if kq > 64:
-        raise NotImplementedError(f"a kNN query of {kq} neighbours exceeds the GPU kNN's 64")
+    if kq > 2048:  # kNN lists of the spatial index: up to 64 in registers, longer in shared memory
+        raise NotImplementedError(f"a kNN query of {kq} neighbours exceeds the GPU kNN's 2048")
     cols = kq - 1 if w is not None else (ms if ms > 1 else 1)
     edges = torch.empty((max(n - 1, 0), 3), dtype=torch.float64, device="cuda")
     nbrs = torch.empty((n, cols), dtype=torch.int32, device="cuda")

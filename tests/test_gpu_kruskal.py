@@ -50,6 +50,8 @@ def test_kruskal_vs_reference(engine, name):
     ("blobs_2d", 60_000, 1, 4, False),
     ("umap_like", 40_000, 8, 12, False),
     ("varying_density", 50_000, 6, 10, True),
+    ("varying_density", 30_000, 70, 16, False),  # kNN lists longer than 64
+    ("blobs_2d", 20_000, 10, 150, False),
 ])
 def test_kruskal_vs_oracle_synthetic(engine, gen, n, ms, knn_k, weighted):
     from fast_hdbscan_gb300.hdbscan import compute_minimum_spanning_tree
