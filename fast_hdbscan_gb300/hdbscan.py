@@ -3,10 +3,12 @@
 ``HDBSCAN(...).fit`` / ``fit_predict``, ``fast_hdbscan``,
 ``compute_minimum_spanning_tree`` and ``clusters_from_spanning_tree`` keep the
 reference's signatures, validation, error types and return conventions; the
-work runs in the GB300 engine (libfhg.so) with no CPU fallback.  Paths the
-reference routes elsewhere (non-Euclidean metrics, precomputed graphs,
-Kruskal back-ends, semi-supervised selection, sample weights) raise
-NotImplementedError.
+work runs in the GB300 engine (libfhg.so) with no CPU fallback.  On the GPU:
+the Euclidean Boruvka fit (with or without sample weights, either tie rule),
+algorithm="kruskal" with an integer knn_k, metric="precomputed" sparse
+graphs and the d > 30 kNN-graph route.  The rest (other metrics, the
+full-pairwise Kruskal, cannot-link constraints, semi-supervised selection)
+raises NotImplementedError.
 """
 import ctypes
 import numbers
