@@ -158,7 +158,7 @@ int fhg_index_boruvka(fhg_index* index, int32_t min_samples, const float* sample
  *                 reference computes it: max(knn_k, min_samples) + 1
  *                 (knn_k + 1 when min_samples == 1; with sample weights
  *                 max(knn_k, int(2 * min_samples / float(np.mean(w)))) + 1).
- *                 2 <= query_k <= 64.
+ *                 2 <= query_k <= 2048.
  *   sample_weights_dev NULL, or n float32 weights: the weighted core
  *                 distance (boruvka.py:528) and float32 edge lengths.
  *   edges_dev     (n-1) x 3 float64: src, dst, weight.
@@ -432,7 +432,8 @@ int fhg_highd_knn(const float* X_dev, int64_t n, int32_t d, int32_t k, float* rd
  * max(3 min_samples, 15), then max(knn_k, min_samples)): float64 core
  * distances (the min_samples-th neighbour; 0 for min_samples 1), neighbours
  * n x min_samples, the Kruskal forest of the mutual-reachability kNN edges
- * with +inf bridges (edges (n-1) x 3 float64). */
+ * with +inf bridges (edges (n-1) x 3 float64).  knn_k <= 63, else
+ * FHG_ERR_UNSUPPORTED. */
 int fhg_knn_graph_mst(const float* X_dev, int64_t n, int32_t d, int32_t min_samples,
                       int32_t knn_k, double* edges_dev, int32_t* neighbors_dev, double* core_dev,
                       int64_t* n_components_host, void* stream);
