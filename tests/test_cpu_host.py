@@ -205,3 +205,45 @@ def test_bench_max_over_ranks_gloo():
         p.join(120)
     got = dict(q.get(timeout=10) for _ in range(2))
     assert got == {0: 20.0, 1: 20.0}
+
+
+def _c_kind(decl):
+    """Kind of one C parameter or return declaration: 'ptr' or its integer /
+    floating type ('int' is int32 on every supported platform)."""
+    decl = decl.strip()
+    if "*" in decl:
+        return "ptr"
+    base = decl.replace("const", " ").split()[0]
+    return {"int32_t": "i32", "int": "i32", "int64_t": "i64", "uint64_t": "u64", "double": "f64",
+            "float": "f32"}.get(base, "?" + base)
+
+
+def _ctypes_kind(t):
+    if t is ctypes.c_void_p or t is ctypes.c_char_p or (
+            isinstance(t, type) and issubclass(t, ctypes._Pointer)):
+        return "ptr"
+    for ct, kind in ((ctypes.c_int32, "i32"), (ctypes.c_int, "i32"), (ctypes.c_int64, "i64"),
+                     (ctypes.c_uint64, "u64"), (ctypes.c_double, "f64"), (ctypes.c_float, "f32")):
+        if t is ct:
+            return kind
+    return "?"
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every entry point's ctypes argtypes and restype (fast_hdbscan_gb300/_native.py)
+    have the count and kinds (pointer, int32, int64, uint64, float, double) of
+    its prototype in include/fhg.h, so no argument is passed with the wrong width."""
+    text = open(os.path.join(ROOT, "include", "fhg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    protos = re.findall(r"([A-Za-z_][\w \*]*?)\b(fhg_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text,
+                        flags=re.S)
+    checked = 0
+    for ret, name, params in protos:
+        if name not in _native.SIGNATURES:
+            continue
+        restype, argtypes = _native.SIGNATURES[name]
+        decls = [p for p in params.split(",") if p.strip() not in ("", "void")]
+        assert [_c_kind(p) for p in decls] == [_ctypes_kind(a) for a in argtypes], name
+        assert _c_kind(ret + " x") == _ctypes_kind(restype), name
+        checked += 1
+    assert checked == len(_native.SIGNATURES)
